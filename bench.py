@@ -1,0 +1,309 @@
+"""Benchmark: cells/s meshed at 512^3 (MarchingCubes::new(513) on the seeded
+64-sphere union over [-1,1]^3).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one MarchingCubes extraction of the whole 512 x 512 x 513-cell
+grid (the reference's traversal visits 513 cell layers): sampling, cell
+classification + scan, vertex/index emission.  `value` is timed with CUDA
+events on the library's stream with the program already resident and the
+mesh left on the device; `e2e` times the public C ABI with host buffers
+(program upload H2D, mesh download D2H into pinned memory) on the host clock.
+L2 is flushed (a 256 MiB write) before every timed step.
+
+--impl reference times the oracle (the C++ restatement of the reference's
+single-threaded Rust CPU path; Rust does not build here) on all host cores,
+each step a bounded slab of the same grid.
+
+Multi-GPU: one process per GPU under torchrun runs an independent replica of
+the workload (the extraction has no cross-GPU exchange); value sums them.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SIZE = 513
+CELLS = (SIZE - 1) * (SIZE - 1) * SIZE
+METRIC = "cells/s meshed at 512^3"
+WORKLOAD = {"workload": "MarchingCubes::new(513), hard-min union of 64 spheres (seed 1234), [-1,1]^3",
+            "cells": CELLS, "samples": SIZE * SIZE * (SIZE + 1), "l2": "flushed (256 MiB write) before each step"}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return d["hbm_gbs"], "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline_port(src_bytes, budget_s=12.0, threads=1):
+    """The oracle's MarchingCubes over a bounded middle slab of the same grid."""
+    import oracle
+    prog = oracle.Program(src_bytes)
+    mid = SIZE // 2
+    secs, cells, _ = prog.mc_timed(SIZE, mid, mid + 2 * threads, threads)
+    per_layer = secs / (2 * threads)
+    layers = max(threads, int(budget_s / max(per_layer, 1e-6)) * threads)
+    layers = min(layers, SIZE - 1)
+    z0 = max(0, mid - layers // 2)
+    secs, cells, tris = prog.mc_timed(SIZE, z0, z0 + layers, threads)
+    return {"value": cells / secs, "unit": "cells/s", "cores": threads, "kind": "port",
+            "sample": "oracle MarchingCubes over cell layers [%d, %d) of the 512^3 grid (%d cells, %.1f s)"
+                      % (z0, z0 + layers, cells, secs)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from isosurface_gb300 import scenes
+    from isosurface_gb300 import source as S
+    import oracle
+    threads = os.cpu_count() or 1
+    prog = oracle.Program(S.lower(scenes.sphere_union()))
+    # size each step to a few seconds of work
+    mid = SIZE // 2
+    secs, _, _ = prog.mc_timed(SIZE, mid, mid + threads, threads)
+    layers = max(threads, int(3.0 / max(secs, 1e-6)) * threads)
+    layers = min(layers, SIZE - 1)
+    z0 = max(0, mid - layers // 2)
+    for _ in range(args.warmup):
+        prog.mc_timed(SIZE, z0, z0 + layers, threads)
+    total_s, total_cells = 0.0, 0
+    for _ in range(args.steps):
+        s, c, _ = prog.mc_timed(SIZE, z0, z0 + layers, threads)
+        total_s += s
+        total_cells += c
+    value = total_cells / total_s
+    out = {"metric": METRIC, "value": value, "unit": "cells/s", "impl": "reference", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": dict(WORKLOAD, sample_layers=[z0, z0 + layers]),
+           "cpu_baseline": {"value": value, "unit": "cells/s", "cores": threads, "kind": "port",
+                            "sample": "oracle (C++ restatement of the reference's CPU path) over cell layers "
+                                      "[%d, %d) per step, split across %d threads" % (z0, z0 + layers, threads)},
+           "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from isosurface_gb300 import build as gbuild
+    gbuild.build()
+    from isosurface_gb300 import Context, scenes
+    from isosurface_gb300 import source as S
+    from isosurface_gb300._capi import lib
+
+    src = scenes.sphere_union()
+    src_bytes = S.lower(src)
+    ctx = Context(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        info = ctx.mc_extract(src, SIZE)
+    import ctypes
+    ms_buf = (ctypes.c_double * 8)()
+    ln_buf = (ctypes.c_uint64 * 8)()
+    lib().iso_ctx_stage_times(ctx.h, ms_buf, ln_buf)  # reset
+    lib().iso_ctx_enable_stage_timing(ctx.h, 1)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = ctx.kernel_launches
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xFF)
+            starts[k].record(stream)
+        info = ctx.mc_extract(src, SIZE)
+        ends[k].record(stream)
+    barrier()
+    launches = ctx.kernel_launches - launches0
+    clk = clocks.stop()
+    lib().iso_ctx_stage_times(ctx.h, ms_buf, ln_buf)
+    lib().iso_ctx_enable_stage_timing(ctx.h, 0)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = sum(step_ms) / len(step_ms)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * CELLS / (ms / 1e3)
+
+    # per-stage device time (CUDA events on the launching stream) and roofline
+    stages = {"sample": 0, "classify_scan": 1, "emit": 2}
+    nv, nt = info.num_vertices, info.num_triangles
+    samples = SIZE * SIZE * (SIZE + 1)
+    words = (SIZE + 31) // 32
+    algo_bytes = {
+        # f32 field written once + one sign bit per sample
+        "sample": 4 * samples + 4 * words * SIZE * (SIZE + 1),
+        # sign-bit volume read once + two u32 offsets per cell row
+        "classify_scan": 4 * words * SIZE * (SIZE + 1) + 8 * (SIZE - 1) * SIZE,
+        # mesh written (12 B per vertex, 12 B per triangle) + 2 field samples read per vertex
+        "emit": 12 * nv + 12 * nt + 8 * nv,
+    }
+    per_stage = {}
+    for name, i in stages.items():
+        n = max(int(ln_buf[i]), 1)
+        per_stage[name] = {"ms_per_launch": ms_buf[i] / n, "launches": int(ln_buf[i]),
+                           "share": ms_buf[i] / max(sum(ms_buf[j] for j in stages.values()), 1e-9)}
+    dom = max(stages, key=lambda s: ms_buf[stages[s]])
+    peak, peak_kind = peaks()
+    achieved = algo_bytes[dom] / (per_stage[dom]["ms_per_launch"] / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        traffic = json.load(open(tpath)).get(dom)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                "algorithmic_bytes": algo_bytes[dom]}
+
+    # e2e through the public C ABI with host buffers
+    from isosurface_gb300._capi import MeshInfo, check
+    vbuf = torch.empty((nv * 3 + 1024,), dtype=torch.float32, pin_memory=True)
+    ibuf = torch.empty((nt * 3 + 1024,), dtype=torch.int32, pin_memory=True)
+    f32p, u32p = ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_uint32)
+
+    def e2e_step():
+        ph = ctypes.c_void_p()
+        check(lib().iso_program_create(ctx.h, src_bytes, len(src_bytes), ctypes.byref(ph)), ctx.h)
+        mi = MeshInfo()
+        check(lib().iso_mc_extract(ctx.h, ph, SIZE, 0, ctypes.byref(mi)), ctx.h)
+        check(lib().iso_mesh_download(ctx.h, ctypes.cast(vbuf.data_ptr(), f32p), vbuf.numel(),
+                                      ctypes.cast(ibuf.data_ptr(), u32p), ibuf.numel(), None, 0), ctx.h)
+        lib().iso_program_destroy(ph)
+        return mi
+
+    for _ in range(args.warmup):
+        e2e_step()
+    barrier()
+    e2e_times = []
+    for k in range(args.steps):
+        flush.fill_(k & 0xFF)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        mi = e2e_step()
+        e2e_times.append(time.perf_counter() - t0)
+    barrier()
+    e2e_s = sum(e2e_times) / len(e2e_times)
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * CELLS / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": len(src_bytes),
+           "d2h_bytes_per_step": 12 * mi.num_vertices + 12 * mi.num_triangles, "ms_per_step": 1e3 * e2e_s}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_port(src_bytes)
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+               "config": dict(WORKLOAD, parallelism="replicas" if world > 1 else "single", vertices=nv,
+                              triangles=nt),
+               "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "stages": per_stage,
+               "cpu_baseline": cpu, "clocks": clk}
+        print(json.dumps(out))
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

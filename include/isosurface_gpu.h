@@ -1,0 +1,226 @@
+/*
+ * isosurface_gpu.h -- C ABI of the GB300 isosurface extraction library.
+ *
+ * The library replaces the extraction hot path of swiftcoder/isosurface
+ * (a Rust crate).  Each extraction entry point below stands in for one
+ * reference call; the reference's Rust wrapper would bind these functions
+ * through `extern "C"` and replay the resulting mesh into
+ * the caller's Extractor, so the reference API
+ *
+ *     MarchingCubes::new(n).extract(&source, &mut extractor)
+ *
+ * stays as it is.  Plain pointers and sizes only; no CUDA, torch or C++ types
+ * cross this boundary (CUDA streams are passed as `void*`).
+ *
+ * Threading: one iso_ctx per host thread; calls on one context are not
+ * thread-safe.  Every function returns an iso_status and never aborts.
+ *
+ * Output convention (IndexedVertices, src/extractor.rs:72-93): vertices are
+ * f32 x,y,z triples in the reference's [0,1]^3 sample frame, indices are u32
+ * triangles.  For MarchingCubes and DualContouring the library produces the
+ * vertex and index buffers that the reference produces, in the same order.
+ * LinearHashedMarchingCubes walks a HashMap in RandomState order in the
+ * reference, so only its triangle set is defined; the library emits it in a
+ * deterministic order.
+ */
+#ifndef ISOSURFACE_GPU_H
+#define ISOSURFACE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define ISO_API __attribute__((visibility("default")))
+#else
+#define ISO_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Status codes                                                              */
+/* ------------------------------------------------------------------------ */
+typedef int iso_status;
+#define ISO_OK 0
+#define ISO_ERR_INVALID_ARG 1   /* null pointer, size out of range, ...       */
+#define ISO_ERR_CAPACITY 2      /* caller buffer too small; see *_required    */
+#define ISO_ERR_CUDA 3          /* a CUDA runtime call failed                 */
+#define ISO_ERR_TIMEOUT 4       /* a bounded device-side wait gave up         */
+#define ISO_ERR_BAD_PROGRAM 5   /* source program failed validation           */
+#define ISO_ERR_NO_DEVICE 6     /* no CUDA device / wrong device index        */
+#define ISO_ERR_OUT_OF_MEMORY 7 /* device allocation failed                   */
+#define ISO_ERR_TOO_LARGE 8     /* mesh does not fit u32 indices              */
+#define ISO_ERR_UNSUPPORTED 9   /* source lacks what the call needs (normals) */
+
+/* Human-readable name of a status code (static string). */
+ISO_API const char* iso_status_str(iso_status s);
+
+/* Message of the last error raised on this context ("" if none). */
+ISO_API const char* iso_ctx_last_error(const struct iso_ctx* ctx);
+
+/* ------------------------------------------------------------------------ */
+/* Contexts                                                                  */
+/* ------------------------------------------------------------------------ */
+typedef struct iso_ctx iso_ctx;
+
+/* Create a context on CUDA device `device`.  The context owns a CUDA stream,
+ * its device work buffers (grown on demand and reused) and the device copy of
+ * the last extracted mesh. */
+ISO_API iso_status iso_ctx_create(int device, iso_ctx** out);
+ISO_API iso_status iso_ctx_destroy(iso_ctx* ctx);
+
+/* The cudaStream_t every kernel of this context is launched on. */
+ISO_API iso_status iso_ctx_get_stream(iso_ctx* ctx, void** stream);
+
+/* Launch on a caller-owned cudaStream_t instead (NULL restores the context's
+ * own stream).  The caller keeps the stream alive while the context uses it. */
+ISO_API iso_status iso_ctx_set_stream(iso_ctx* ctx, void* stream);
+
+/* Number of kernels this context has launched since creation. */
+ISO_API uint64_t iso_ctx_kernel_launches(const iso_ctx* ctx);
+
+/* Per-stage device timing: when enabled, every kernel the context launches is
+ * bracketed by CUDA events on its stream.  iso_ctx_stage_times synchronises,
+ * writes the accumulated milliseconds and launch counts of each stage
+ * (ISO_STAGE_COUNT entries each) and resets them. */
+#define ISO_STAGE_SAMPLE 0      /* grid sampler (field + sign bits)            */
+#define ISO_STAGE_CLASSIFY 1    /* cell classification + count + scan          */
+#define ISO_STAGE_EMIT 2        /* vertex / index emission                     */
+#define ISO_STAGE_SIGNS 3       /* sign bits of a caller-supplied field        */
+#define ISO_STAGE_PLACE 4       /* dual-contouring vertex placement            */
+#define ISO_STAGE_OCTREE 5      /* octree build / dual-cube gather             */
+#define ISO_STAGE_MLP 6         /* surrogate network                           */
+#define ISO_STAGE_OTHER 7
+#define ISO_STAGE_COUNT 8
+ISO_API iso_status iso_ctx_enable_stage_timing(iso_ctx* ctx, int enable);
+ISO_API iso_status iso_ctx_stage_times(iso_ctx* ctx, double* ms, uint64_t* launches);
+
+/* ------------------------------------------------------------------------ */
+/* Source programs                                                           */
+/* ------------------------------------------------------------------------ */
+/*
+ * An implicit source (a Sampler over a Source tree: src/sampler.rs,
+ * src/source.rs, src/implicit/*.rs) is handed to the library as a program:
+ *
+ *   u32 magic     = 0x314F5349 ("ISO1" little-endian)
+ *   u32 n_ops
+ *   u32 n_consts
+ *   u32 flags     = 0
+ *   u32 ops[n_ops]        op = word & 0xFF, a = word >> 8 (a constant index)
+ *   f32 consts[n_consts]
+ *
+ * Ops run in postfix order over a value stack and a point stack; the point
+ * stack starts with the sample point p.  Each point op opens a scope that
+ * ends at its PT_POP and must leave one value.
+ *
+ *   0x01 PT_DOMAIN     k[a..a+6] = scale xyz, offset xyz  push q = p*scale + offset
+ *   0x02 PT_TRANSLATE  k[a..a+3] = centre                 push q = p - centre
+ *   0x03 PT_RIGID      k[a..a+12] = t xyz, M (row-major)  push q = M (p - t)
+ *   0x04 PT_POP                                           end the innermost scope
+ *   0x10 SPHERE        k[a]   = radius                    sphere.rs:35-63
+ *   0x11 BOX           k[a..a+3] = half extent            rectangular_prism.rs:36-80
+ *   0x12 CYLINDER      k[a..a+2] = radius, half length    cylinder.rs:41-85
+ *   0x13 TORUS         k[a..a+2] = radius, tube radius    torus.rs:40-108
+ *   0x20 UNION         min(a, b)                          csg.rs:35-51
+ *   0x21 INTERSECTION  max(a, b)                          csg.rs:68-72
+ *   0x22 DIFFERENCE    max(b, -a)  (b minus a)            csg.rs:96-100
+ *   0x23 SMOOTH_UNION  k[a] = k; min(a,b) - h*h*k/4, h = max(k-|a-b|,0)/k
+ *   0x30 SPHERE_SET    k[a] = n, k[a+1] = 0 hard / 1 smooth, k[a+2] = k,
+ *                      then n x (cx, cy, cz, r): a left fold of UNION (or
+ *                      SMOOTH_UNION) over spheres translated to their centres
+ *   0x40 CD_BEGIN      k[a] = epsilon; normals of the scope up to the matching
+ *   0x41 CD_END        CD_END by central differences (source.rs:52-95)
+ *
+ * Normals (HermiteSource::sample_normal, unnormalised): primitives as in the
+ * reference; UNION takes the component-wise min of the operands' normals
+ * (csg.rs:47-51); INTERSECTION, DIFFERENCE and SMOOTH_UNION (which have no
+ * normal in the reference) take the normal of the operand that decides the
+ * value; PT_RIGID rotates the normal back by M^T; PT_DOMAIN and PT_TRANSLATE
+ * pass it through.
+ */
+typedef struct iso_program iso_program;
+
+ISO_API iso_status iso_program_create(iso_ctx* ctx, const uint8_t* bytes, size_t len, iso_program** out);
+ISO_API iso_status iso_program_destroy(iso_program* prog);
+
+/* ------------------------------------------------------------------------ */
+/* Mesh results                                                              */
+/* ------------------------------------------------------------------------ */
+typedef struct iso_mesh_info {
+    uint64_t num_vertices;
+    uint64_t num_triangles;
+    uint64_t num_cells;       /* cells (or dual cubes / octree cubes) visited */
+} iso_mesh_info;
+
+/* Copy the context's last mesh to host buffers (pageable or pinned).
+ * vertices: 3*num_vertices floats (6 with normals, x y z nx ny nz interleaved
+ *           as IndexedInterleavedNormals, extractor.rs:97-127)
+ * indices:  3*num_triangles u32
+ * keys:     optional, 2 u64 per vertex: the vertex's dedup key (MC/DC: the
+ *           lattice edge id of GridKey, index_cache.rs:48-61, in the second
+ *           word 0; LHMC: the MortonKey pair, index_cache.rs:63-73)
+ * Capacities are element counts; ISO_ERR_CAPACITY if any is short. */
+ISO_API iso_status iso_mesh_download(iso_ctx* ctx, float* vertices, uint64_t vertex_floats_cap,
+                             uint32_t* indices, uint64_t index_cap,
+                             uint64_t* keys, uint64_t key_cap);
+
+/* Device pointers of the context's last mesh (valid until the next
+ * extraction on this context).  keys is NULL unless requested. */
+ISO_API iso_status iso_mesh_device(iso_ctx* ctx, const float** vertices, const uint32_t** indices,
+                           const uint64_t** keys, iso_mesh_info* info);
+
+/* Extraction flags */
+#define ISO_FLAG_KEYS 1u      /* also produce per-vertex dedup keys          */
+#define ISO_FLAG_NORMALS 2u   /* IndexedInterleavedNormals: per-vertex source normal */
+
+/* ------------------------------------------------------------------------ */
+/* Grid sampling (PrimalGrid, src/traversal/primal_grid.rs:39-89)            */
+/* ------------------------------------------------------------------------ */
+/* Sample the source at the points of MarchingCubes::new(size):
+ * (x/(size-1), y/(size-1), z/(size-1)) in f32, x,y < size, z <= size
+ * (the reference samples one layer past z = 1).  The field is written to
+ * `field` (device memory, row pitch `pitch` floats >= size, x fastest, then
+ * y, then z: size+1 layers of size rows). */
+ISO_API iso_status iso_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t size,
+                           float* field, uint64_t pitch);
+
+/* ------------------------------------------------------------------------ */
+/* MarchingCubes (src/marching_cubes.rs:59-82)                               */
+/* ------------------------------------------------------------------------ */
+/* MarchingCubes::<Signed>::new(size).extract(&Sampler::new(&source), &mut e).
+ * The mesh stays on the device in the context; `info` receives its size. */
+ISO_API iso_status iso_mc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t flags,
+                          iso_mesh_info* info);
+
+/* Marching cubes over a caller-supplied device field laid out as
+ * iso_sample_grid writes it (nx x ny x nz samples, row pitch `pitch` floats,
+ * vertex positions (x/(nx-1)... ) as the reference computes them with
+ * one_over_size = 1/(nx-1); nx == ny). */
+ISO_API iso_status iso_mc_extract_field(iso_ctx* ctx, const float* field, uint32_t nx, uint32_t ny, uint32_t nz,
+                                uint64_t pitch, uint32_t flags, iso_mesh_info* info);
+
+/* Case index of every cell of MarchingCubes::new(size) (the bits of
+ * classify_corners, marching_cubes_impl.rs:26-37) into host memory:
+ * size x (size-1) x (size-1) bytes, traversal order (z, y, x). */
+ISO_API iso_status iso_mc_cases(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint8_t* cases_host);
+
+/* ------------------------------------------------------------------------ */
+/* PointCloud (src/point_cloud.rs:50-63)                                      */
+/* ------------------------------------------------------------------------ */
+ISO_API iso_status iso_point_cloud_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size,
+                                   iso_mesh_info* info);
+
+/* ------------------------------------------------------------------------ */
+/* Host-side sampling helpers                                                */
+/* ------------------------------------------------------------------------ */
+/* Evaluate the source (scalar, and normal when normals != NULL) at n host
+ * points (x,y,z triples).  Used to check the device evaluator. */
+ISO_API iso_status iso_sample_points(iso_ctx* ctx, const iso_program* prog, const float* points, uint64_t n,
+                             float* values, float* normals);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ISOSURFACE_GPU_H */

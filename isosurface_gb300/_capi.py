@@ -1,0 +1,91 @@
+"""ctypes binding of the C ABI in include/isosurface_gpu.h.
+
+The shared library is the in-tree build (isosurface_gb300/_build/libisosurface_gpu.so,
+made by isosurface_gb300/build.py).  There is no CPU fallback: if the library
+is missing or no CUDA device is visible, every entry point raises.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libisosurface_gpu.so")
+
+ISO_OK = 0
+STATUS = {
+    0: "ISO_OK", 1: "ISO_ERR_INVALID_ARG", 2: "ISO_ERR_CAPACITY", 3: "ISO_ERR_CUDA", 4: "ISO_ERR_TIMEOUT",
+    5: "ISO_ERR_BAD_PROGRAM", 6: "ISO_ERR_NO_DEVICE", 7: "ISO_ERR_OUT_OF_MEMORY", 8: "ISO_ERR_TOO_LARGE",
+    9: "ISO_ERR_UNSUPPORTED",
+}
+ISO_FLAG_KEYS = 1
+ISO_FLAG_NORMALS = 2
+
+
+class IsoError(RuntimeError):
+    def __init__(self, status, message=""):
+        self.status = status
+        super().__init__("%s%s" % (STATUS.get(status, "ISO_ERR_%d" % status), (": " + message) if message else ""))
+
+
+class MeshInfo(ctypes.Structure):
+    _fields_ = [("num_vertices", ctypes.c_uint64), ("num_triangles", ctypes.c_uint64),
+                ("num_cells", ctypes.c_uint64)]
+
+
+_lib = None
+
+vp = ctypes.c_void_p
+u8p = ctypes.POINTER(ctypes.c_uint8)
+f32p = ctypes.POINTER(ctypes.c_float)
+u32p = ctypes.POINTER(ctypes.c_uint32)
+u64p = ctypes.POINTER(ctypes.c_uint64)
+i32 = ctypes.c_int
+u32 = ctypes.c_uint32
+u64 = ctypes.c_uint64
+
+# name -> (restype, argtypes); every symbol include/isosurface_gpu.h declares
+SIGNATURES = {
+    "iso_status_str": (ctypes.c_char_p, [i32]),
+    "iso_ctx_last_error": (ctypes.c_char_p, [vp]),
+    "iso_ctx_create": (i32, [i32, ctypes.POINTER(vp)]),
+    "iso_ctx_destroy": (i32, [vp]),
+    "iso_ctx_get_stream": (i32, [vp, ctypes.POINTER(vp)]),
+    "iso_ctx_set_stream": (i32, [vp, vp]),
+    "iso_ctx_kernel_launches": (u64, [vp]),
+    "iso_ctx_enable_stage_timing": (i32, [vp, i32]),
+    "iso_ctx_stage_times": (i32, [vp, ctypes.POINTER(ctypes.c_double), u64p]),
+    "iso_program_create": (i32, [vp, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(vp)]),
+    "iso_program_destroy": (i32, [vp]),
+    "iso_mesh_download": (i32, [vp, f32p, u64, u32p, u64, u64p, u64]),
+    "iso_mesh_device": (i32, [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp),
+                              ctypes.POINTER(MeshInfo)]),
+    "iso_sample_grid": (i32, [vp, vp, u32, vp, u64]),
+    "iso_mc_extract": (i32, [vp, vp, u32, u32, ctypes.POINTER(MeshInfo)]),
+    "iso_mc_extract_field": (i32, [vp, vp, u32, u32, u32, u64, u32, ctypes.POINTER(MeshInfo)]),
+    "iso_mc_cases": (i32, [vp, vp, u32, u8p]),
+    "iso_point_cloud_extract": (i32, [vp, vp, u32, ctypes.POINTER(MeshInfo)]),
+    "iso_sample_points": (i32, [vp, vp, f32p, u64, f32p, f32p]),
+}
+
+
+def lib():
+    """Load the library (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise IsoError(6, "CUDA library not built: run isosurface_gb300/build.py (%s missing)" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status, ctx=None):
+    if status != ISO_OK:
+        msg = ""
+        if ctx:
+            raw = lib().iso_ctx_last_error(ctx)
+            msg = raw.decode() if raw else ""
+        raise IsoError(status, msg)

@@ -1,0 +1,270 @@
+"""The reference's extraction API over the GPU library.
+
+    mc = MarchingCubes(size)
+    mc.extract(Sampler(source), IndexedVertices(vertices, indices))
+
+mirrors ``MarchingCubes::new(size).extract(&sampler, &mut extractor)``
+(src/marching_cubes.rs:46-82); DualContouring, LinearHashedMarchingCubes and
+PointCloud follow their reference constructors in the same way.  The mesh is
+extracted on the GPU and then replayed into the extractor: bulk for the
+extractors defined here, one ``extract_vertex`` / ``extract_index`` call per
+element for any other object with those methods (the reference's Extractor
+trait, src/extractor.rs:17-20).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _capi
+from ._capi import ISO_FLAG_KEYS, ISO_FLAG_NORMALS, IsoError, MeshInfo, check, lib
+from .source import Sampler, Source, lower
+
+__all__ = [
+    "Context", "Program", "Mesh", "default_context", "MarchingCubes", "PointCloud",
+    "OnlyVertices", "IndexedVertices", "OnlyInterleavedNormals", "IndexedInterleavedNormals",
+]
+
+
+class Program:
+    """A source program uploaded to a context."""
+
+    def __init__(self, ctx, source_or_bytes):
+        self.ctx = ctx
+        data = source_or_bytes if isinstance(source_or_bytes, (bytes, bytearray)) else lower(source_or_bytes)
+        self.bytes = bytes(data)
+        h = ctypes.c_void_p()
+        check(lib().iso_program_create(ctx.h, self.bytes, len(self.bytes), ctypes.byref(h)), ctx.h)
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().iso_program_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Mesh:
+    """A mesh copied back from the device: vertices (n, 3) or (n, 6) f32,
+    triangles (m, 3) u32, keys (n, 2) u64 when requested."""
+
+    def __init__(self, vertices, indices, keys=None, cells=0):
+        self.vertices = vertices
+        self.indices = indices
+        self.keys = keys
+        self.cells = cells
+
+    @property
+    def triangles(self):
+        return self.indices.reshape(-1, 3)
+
+
+class Context:
+    """One iso_ctx: a CUDA stream plus reusable device buffers."""
+
+    def __init__(self, device=0):
+        h = ctypes.c_void_p()
+        check(lib().iso_ctx_create(device, ctypes.byref(h)))
+        self.h = h
+        self.device = device
+        self._programs = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            for p in self._programs.values():
+                p.close()
+            self._programs.clear()
+            lib().iso_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self):
+        s = ctypes.c_void_p()
+        check(lib().iso_ctx_get_stream(self.h, ctypes.byref(s)), self.h)
+        return s.value
+
+    def set_stream(self, stream_handle):
+        check(lib().iso_ctx_set_stream(self.h, ctypes.c_void_p(stream_handle)), self.h)
+
+    @property
+    def kernel_launches(self):
+        return lib().iso_ctx_kernel_launches(self.h)
+
+    def program(self, source):
+        """Upload (once per distinct program) and return a Program."""
+        data = source if isinstance(source, (bytes, bytearray)) else lower(source)
+        data = bytes(data)
+        p = self._programs.get(data)
+        if p is None:
+            p = Program(self, data)
+            self._programs[data] = p
+        return p
+
+    # -- extraction ---------------------------------------------------------
+    def mc_extract(self, source, size, keys=False):
+        info = MeshInfo()
+        flags = ISO_FLAG_KEYS if keys else 0
+        check(lib().iso_mc_extract(self.h, self.program(source).h, size, flags, ctypes.byref(info)), self.h)
+        return info
+
+    def mc_extract_field(self, field_ptr, nx, ny, nz, pitch, keys=False):
+        info = MeshInfo()
+        flags = ISO_FLAG_KEYS if keys else 0
+        check(lib().iso_mc_extract_field(self.h, ctypes.c_void_p(field_ptr), nx, ny, nz, pitch, flags,
+                                         ctypes.byref(info)), self.h)
+        return info
+
+    def mc_cases(self, source, size):
+        out = np.empty((size, size - 1, size - 1), np.uint8)
+        check(lib().iso_mc_cases(self.h, self.program(source).h, size,
+                                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))), self.h)
+        return out
+
+    def point_cloud_extract(self, source, size):
+        info = MeshInfo()
+        check(lib().iso_point_cloud_extract(self.h, self.program(source).h, size, ctypes.byref(info)), self.h)
+        return info
+
+    def sample_grid(self, source, size, field_ptr, pitch):
+        check(lib().iso_sample_grid(self.h, self.program(source).h, size, ctypes.c_void_p(field_ptr), pitch), self.h)
+
+    def sample_points(self, source, points, normals=False):
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+        vals = np.empty(len(pts), np.float32)
+        nrm = np.empty((len(pts), 3), np.float32) if normals else None
+        f32p = ctypes.POINTER(ctypes.c_float)
+        check(lib().iso_sample_points(self.h, self.program(source).h, pts.ctypes.data_as(f32p), len(pts),
+                                      vals.ctypes.data_as(f32p),
+                                      nrm.ctypes.data_as(f32p) if normals else None), self.h)
+        return (vals, nrm) if normals else vals
+
+    def download(self, info, keys=False, vertex_floats=3, out=None):
+        """Copy the last mesh to host numpy arrays (or into `out` = (vertices, indices))."""
+        nv, nt = info.num_vertices, info.num_triangles
+        if out is not None:
+            v, i = out
+        else:
+            v = np.empty((nv, vertex_floats), np.float32)
+            i = np.empty(3 * nt, np.uint32)
+        k = np.empty((nv, 2), np.uint64) if keys else None
+        check(lib().iso_mesh_download(
+            self.h, v.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), v.size,
+            i.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), i.size,
+            k.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)) if keys else None, 0 if k is None else k.size), self.h)
+        return Mesh(v, i, k, info.num_cells)
+
+    def device_mesh(self):
+        v, i, k = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        info = MeshInfo()
+        check(lib().iso_mesh_device(self.h, ctypes.byref(v), ctypes.byref(i), ctypes.byref(k), ctypes.byref(info)),
+              self.h)
+        return v.value, i.value, k.value, info
+
+
+_default = {}
+
+
+def default_context(device=0):
+    ctx = _default.get(device)
+    if ctx is None:
+        ctx = Context(device)
+        _default[device] = ctx
+    return ctx
+
+
+# ---------------------------------------------------------------------------
+# Extractors (src/extractor.rs)
+# ---------------------------------------------------------------------------
+class _Extractor:
+    with_normals = False
+    with_indices = True
+
+    def take(self, vertices, indices):
+        raise NotImplementedError
+
+
+class OnlyVertices(_Extractor):
+    """Vertices as a flat f32 list, faces discarded (extractor.rs:24-42)."""
+    with_indices = False
+
+    def __init__(self, vertices):
+        self.vertices = vertices
+
+    def take(self, vertices, indices):
+        self.vertices.extend(vertices.reshape(-1).tolist())
+
+
+class IndexedVertices(_Extractor):
+    """Vertices as a flat f32 list plus u32 indices (extractor.rs:72-93)."""
+
+    def __init__(self, vertices, indices):
+        self.vertices, self.indices = vertices, indices
+
+    def take(self, vertices, indices):
+        self.vertices.extend(vertices.reshape(-1).tolist())
+        self.indices.extend(indices.tolist())
+
+
+class OnlyInterleavedNormals(OnlyVertices):
+    """x y z nx ny nz per vertex, faces discarded (extractor.rs:46-69)."""
+    with_normals = True
+
+
+class IndexedInterleavedNormals(IndexedVertices):
+    """x y z nx ny nz per vertex plus indices (extractor.rs:97-127)."""
+    with_normals = True
+
+
+def _replay(extractor, mesh):
+    if isinstance(extractor, _Extractor):
+        extractor.take(mesh.vertices, mesh.indices)
+        return
+    for v in mesh.vertices:
+        extractor.extract_vertex(tuple(float(c) for c in v))
+    for i in mesh.indices:
+        extractor.extract_index(int(i))
+
+
+def _source_of(sampler):
+    return sampler.source if isinstance(sampler, Sampler) else sampler
+
+
+class MarchingCubes:
+    """MarchingCubes::<Signed>::new(size) (src/marching_cubes.rs:46-50)."""
+
+    def __init__(self, size, context=None):
+        if size < 1:
+            raise ValueError("size must be at least 1")
+        self.size = size
+        self.context = context
+
+    def extract(self, sampler, extractor):
+        ctx = self.context or default_context()
+        source = _source_of(sampler)
+        if getattr(extractor, "with_normals", False):
+            raise IsoError(9, "per-vertex normals are not available for MarchingCubes yet")
+        info = ctx.mc_extract(source, self.size)
+        _replay(extractor, ctx.download(info))
+
+
+class PointCloud:
+    """PointCloud::<Signed>::new(size) (src/point_cloud.rs:38-48)."""
+
+    def __init__(self, size, context=None):
+        self.size = size
+        self.context = context
+
+    def extract(self, sampler, extractor):
+        ctx = self.context or default_context()
+        info = ctx.point_cloud_extract(_source_of(sampler), self.size)
+        _replay(extractor, ctx.download(info))

@@ -1,0 +1,68 @@
+"""Build the CUDA library in-tree:  isosurface_gb300/_build/libisosurface_gpu.so
+
+    python -m isosurface_gb300.build [--force]
+
+One nvcc per translation unit, in parallel, for sm_103a only, then one link.
+The translation units whose arithmetic must match the reference's f32 order
+are compiled with -fmad=false (no a*b+c contraction; IEEE sqrt and division
+are nvcc's defaults and stay on).
+"""
+import concurrent.futures as cf
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OUT_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT_DIR, "libisosurface_gpu.so")
+NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+# translation unit -> extra flags
+UNITS = {
+    "ctx.cu": ["-fmad=false"],
+    "sample.cu": ["-fmad=false"],
+    "mc.cu": ["-fmad=false"],
+}
+HEADERS = ["internal.h", "vm.cuh", "mc_tables.h"]
+
+
+def _deps():
+    paths = [os.path.join(CSRC, u) for u in UNITS] + [os.path.join(CSRC, h) for h in HEADERS]
+    paths.append(os.path.join(ROOT, "include", "isosurface_gpu.h"))
+    paths.append(os.path.abspath(__file__))
+    return [p for p in paths if os.path.exists(p)]
+
+
+def _compile(unit, flags):
+    src = os.path.join(CSRC, unit)
+    obj = os.path.join(OUT_DIR, unit + ".o")
+    cmd = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+           "-I", os.path.join(ROOT, "include"), "-c", src, "-o", obj, *flags]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (unit, " ".join(cmd), r.stderr))
+    return obj
+
+
+def build(force=False, verbose=False):
+    os.makedirs(OUT_DIR, exist_ok=True)
+    if not force and os.path.exists(LIB):
+        if os.path.getmtime(LIB) >= max(os.path.getmtime(p) for p in _deps()):
+            return LIB
+    with cf.ThreadPoolExecutor(max_workers=min(8, len(UNITS))) as ex:
+        objs = list(ex.map(lambda kv: _compile(*kv), UNITS.items()))
+    cmd = [NVCC, *ARCH, "-shared", "-cudart", "shared", "-o", LIB + ".tmp", *objs]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    os.replace(LIB + ".tmp", LIB)
+    if verbose:
+        print(LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv, verbose=True)

@@ -1,0 +1,520 @@
+// Contexts, programs, buffers and the C ABI entry points (include/isosurface_gpu.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "internal.h"
+
+namespace iso {
+
+iso_status fail(iso_ctx* ctx, iso_status s, const std::string& msg) {
+    if (ctx) ctx->last_error = msg;
+    return s;
+}
+
+iso_status cuda_fail(iso_ctx* ctx, cudaError_t e, const char* what) {
+    if (ctx) ctx->last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return (e == cudaErrorMemoryAllocation) ? ISO_ERR_OUT_OF_MEMORY : ISO_ERR_CUDA;
+}
+
+iso_status set_device(iso_ctx* ctx) {
+    cudaError_t e = cudaSetDevice(ctx->device);
+    return e == cudaSuccess ? ISO_OK : cuda_fail(ctx, e, "cudaSetDevice");
+}
+
+iso_status ensure(iso_ctx* ctx, DevBuf& b, size_t bytes) {
+    if (bytes <= b.bytes) return ISO_OK;
+    if (b.p) {
+        // the buffer may still be read by queued work of this context
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "sync before regrow");
+        cudaFree(b.p);
+        b.p = nullptr;
+        b.bytes = 0;
+    }
+    size_t want = bytes + bytes / 8 + 256;
+    cudaError_t e = cudaMalloc(&b.p, want);
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        cudaGetLastError();
+        return cuda_fail(ctx, e, "cudaMalloc");
+    }
+    b.bytes = want;
+    return ISO_OK;
+}
+
+iso_status check_launch(iso_ctx* ctx, const char* what) {
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? ISO_OK : cuda_fail(ctx, e, what);
+}
+
+iso_status read_device_errors(iso_ctx* ctx) {
+    uint32_t h = 0;
+    cudaError_t e = cudaMemcpy(&h, ctx->d_err, 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "read error flags");
+    if (h == 0) return ISO_OK;
+    cudaMemset(ctx->d_err, 0, 4);
+    if (h & DERR_SCAN_TIMEOUT) return fail(ctx, ISO_ERR_TIMEOUT, "scan look-back wait gave up");
+    if (h & DERR_QUEUE_TIMEOUT) return fail(ctx, ISO_ERR_TIMEOUT, "work-queue wait gave up");
+    if (h & DERR_SVD_ITER) return fail(ctx, ISO_ERR_TIMEOUT, "QR iteration bound reached");
+    return fail(ctx, ISO_ERR_CAPACITY, "device output capacity exceeded");
+}
+
+static cudaEvent_t take_event(iso_ctx* ctx) {
+    if (!ctx->event_pool.empty()) {
+        cudaEvent_t e = ctx->event_pool.back();
+        ctx->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return e;
+}
+
+StageTimer::StageTimer(iso_ctx* c, int s) : ctx(c), stage(s) {
+    ctx->stage_launches[stage]++;
+    if (!ctx->timing) return;
+    a = take_event(ctx);
+    if (a) cudaEventRecord(a, ctx->stream);
+}
+
+StageTimer::~StageTimer() {
+    if (!a) return;
+    cudaEvent_t b = take_event(ctx);
+    if (!b) {
+        ctx->event_pool.push_back(a);
+        return;
+    }
+    cudaEventRecord(b, ctx->stream);
+    ctx->pending.push_back({stage, a, b});
+}
+
+}  // namespace iso
+
+using namespace iso;
+
+namespace {
+
+enum : uint32_t {
+    OP_PT_DOMAIN = 0x01, OP_PT_TRANSLATE = 0x02, OP_PT_RIGID = 0x03, OP_PT_POP = 0x04,
+    OP_SPHERE = 0x10, OP_BOX = 0x11, OP_CYLINDER = 0x12, OP_TORUS = 0x13,
+    OP_UNION = 0x20, OP_INTERSECTION = 0x21, OP_DIFFERENCE = 0x22, OP_SMOOTH_UNION = 0x23,
+    OP_SPHERE_SET = 0x30, OP_CD_BEGIN = 0x40, OP_CD_END = 0x41,
+};
+
+// Validates a program and fills the jump table; mirrors the device evaluator's limits.
+bool validate(iso_program* p, std::string* err) {
+    const uint32_t nops = (uint32_t)p->ops.size(), nk = (uint32_t)p->consts.size();
+    p->jump.assign(nops, 0);
+    struct Scope {
+        uint32_t op, pc;
+        int vdepth;
+    };
+    std::vector<Scope> scopes;
+    int vsp = 0, psp = 0, cd_depth = 0;
+    auto need = [&](uint32_t a, uint64_t n) { return (uint64_t)a + n <= nk; };
+    for (uint32_t pc = 0; pc < nops; ++pc) {
+        uint32_t op = p->ops[pc] & 0xFF, a = p->ops[pc] >> 8;
+        switch (op) {
+        case OP_PT_DOMAIN: case OP_PT_TRANSLATE: case OP_PT_RIGID: {
+            uint32_t n = op == OP_PT_DOMAIN ? 6 : op == OP_PT_TRANSLATE ? 3 : 12;
+            if (!need(a, n)) { *err = "constant index out of range"; return false; }
+            if (psp + 1 >= PSTACK) { *err = "point scopes nested too deeply"; return false; }
+            ++psp;
+            scopes.push_back({op, pc, vsp});
+            break;
+        }
+        case OP_PT_POP:
+            if (scopes.empty() || scopes.back().op == OP_CD_BEGIN) { *err = "PT_POP without a point scope"; return false; }
+            if (vsp != scopes.back().vdepth + 1) { *err = "point scope must leave exactly one value"; return false; }
+            scopes.pop_back();
+            --psp;
+            break;
+        case OP_CD_BEGIN:
+            if (!need(a, 1)) { *err = "constant index out of range"; return false; }
+            if (cd_depth > 0) { *err = "nested CD_BEGIN is not supported"; return false; }
+            ++cd_depth;
+            scopes.push_back({op, pc, vsp});
+            break;
+        case OP_CD_END:
+            if (scopes.empty() || scopes.back().op != OP_CD_BEGIN) { *err = "CD_END without CD_BEGIN"; return false; }
+            if (vsp != scopes.back().vdepth + 1) { *err = "CD scope must leave exactly one value"; return false; }
+            p->jump[scopes.back().pc] = (int32_t)pc;
+            scopes.pop_back();
+            --cd_depth;
+            break;
+        case OP_SPHERE: case OP_BOX: case OP_CYLINDER: case OP_TORUS: {
+            uint32_t n = op == OP_SPHERE ? 1 : op == OP_BOX ? 3 : 2;
+            if (!need(a, n)) { *err = "constant index out of range"; return false; }
+            if (++vsp > VSTACK) { *err = "value stack deeper than 16"; return false; }
+            break;
+        }
+        case OP_UNION: case OP_INTERSECTION: case OP_DIFFERENCE: case OP_SMOOTH_UNION:
+            if (op == OP_SMOOTH_UNION && !need(a, 1)) { *err = "constant index out of range"; return false; }
+            if (op == OP_SMOOTH_UNION && !(p->consts[a] > 0.0f)) { *err = "smooth union needs k > 0"; return false; }
+            if (vsp - (scopes.empty() ? 0 : scopes.back().vdepth) < 2) { *err = "binary op needs two operands"; return false; }
+            --vsp;
+            break;
+        case OP_SPHERE_SET: {
+            if (!need(a, 3)) { *err = "constant index out of range"; return false; }
+            float fn = p->consts[a];
+            if (!(fn >= 1.0f) || fn != std::floor(fn) || fn > 16777216.0f) { *err = "bad sphere count"; return false; }
+            if (!need(a + 3, 4ull * (uint64_t)fn)) { *err = "sphere data out of range"; return false; }
+            if (p->consts[a + 1] != 0.0f && !(p->consts[a + 2] > 0.0f)) { *err = "smooth set needs k > 0"; return false; }
+            if (++vsp > VSTACK) { *err = "value stack deeper than 16"; return false; }
+            break;
+        }
+        default:
+            *err = "unknown opcode";
+            return false;
+        }
+    }
+    if (!scopes.empty()) { *err = "unclosed scope"; return false; }
+    if (vsp != 1) { *err = "program must leave exactly one value"; return false; }
+    return true;
+}
+
+void classify(iso_program* p) {
+    const auto& o = p->ops;
+    auto op = [&](size_t i) { return o[i] & 0xFF; };
+    auto arg = [&](size_t i) { return o[i] >> 8; };
+    p->kind = PK_GENERIC;
+    size_t set_pc = SIZE_MAX;
+    if (o.size() == 1 && op(0) == OP_SPHERE_SET) {
+        set_pc = 0;
+        p->has_domain = false;
+    } else if (o.size() == 3 && op(0) == OP_PT_DOMAIN && op(1) == OP_SPHERE_SET && op(2) == OP_PT_POP) {
+        set_pc = 1;
+        p->has_domain = true;
+        for (int i = 0; i < 6; ++i) p->domain[i] = p->consts[arg(0) + i];
+    }
+    if (set_pc != SIZE_MAX && p->consts[arg(set_pc) + 1] == 0.0f) {
+        p->kind = PK_SPHERE_SET_HARD;
+        p->set_at = arg(set_pc);
+        p->set_n = (uint32_t)p->consts[p->set_at];
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* iso_status_str(iso_status s) {
+    switch (s) {
+    case ISO_OK: return "ISO_OK";
+    case ISO_ERR_INVALID_ARG: return "ISO_ERR_INVALID_ARG";
+    case ISO_ERR_CAPACITY: return "ISO_ERR_CAPACITY";
+    case ISO_ERR_CUDA: return "ISO_ERR_CUDA";
+    case ISO_ERR_TIMEOUT: return "ISO_ERR_TIMEOUT";
+    case ISO_ERR_BAD_PROGRAM: return "ISO_ERR_BAD_PROGRAM";
+    case ISO_ERR_NO_DEVICE: return "ISO_ERR_NO_DEVICE";
+    case ISO_ERR_OUT_OF_MEMORY: return "ISO_ERR_OUT_OF_MEMORY";
+    case ISO_ERR_TOO_LARGE: return "ISO_ERR_TOO_LARGE";
+    case ISO_ERR_UNSUPPORTED: return "ISO_ERR_UNSUPPORTED";
+    default: return "ISO_ERR_UNKNOWN";
+    }
+}
+
+const char* iso_ctx_last_error(const iso_ctx* ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+iso_status iso_ctx_create(int device, iso_ctx** out) {
+    if (!out) return ISO_ERR_INVALID_ARG;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return ISO_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= count) return ISO_ERR_NO_DEVICE;
+    iso_ctx* ctx = new (std::nothrow) iso_ctx();
+    if (!ctx) return ISO_ERR_OUT_OF_MEMORY;
+    ctx->device = device;
+    iso_status s = set_device(ctx);
+    cudaError_t e = cudaSuccess;
+    if (s == ISO_OK) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+    if (s == ISO_OK && e == cudaSuccess) e = cudaMallocHost(&ctx->h_pinned, 4096);
+    if (s == ISO_OK && e == cudaSuccess) e = cudaMalloc(&ctx->d_err, 256);
+    if (s == ISO_OK && e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, 256);
+    if (s != ISO_OK || e != cudaSuccess) {
+        iso_status r = s != ISO_OK ? s : cuda_fail(ctx, e, "context setup");
+        iso_ctx_destroy(ctx);
+        return r;
+    }
+    ctx->stream = ctx->own_stream;
+    *out = ctx;
+    return ISO_OK;
+}
+
+iso_status iso_ctx_destroy(iso_ctx* ctx) {
+    if (!ctx) return ISO_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    DevBuf* bufs[] = {&ctx->field, &ctx->bits, &ctx->rowtri, &ctx->rowvert, &ctx->scan, &ctx->aux,
+                      &ctx->aux2, &ctx->aux3, &ctx->mesh_v, &ctx->mesh_i, &ctx->mesh_k};
+    for (DevBuf* b : bufs)
+        if (b->p) cudaFree(b->p);
+    if (ctx->d_err) cudaFree(ctx->d_err);
+    if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+    for (auto& p : ctx->pending) {
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    for (cudaEvent_t ev : ctx->event_pool) cudaEventDestroy(ev);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+    return ISO_OK;
+}
+
+iso_status iso_ctx_get_stream(iso_ctx* ctx, void** stream) {
+    if (!ctx || !stream) return ISO_ERR_INVALID_ARG;
+    *stream = (void*)ctx->stream;
+    return ISO_OK;
+}
+
+iso_status iso_ctx_set_stream(iso_ctx* ctx, void* stream) {
+    if (!ctx) return ISO_ERR_INVALID_ARG;
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return ISO_OK;
+}
+
+uint64_t iso_ctx_kernel_launches(const iso_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+iso_status iso_ctx_enable_stage_timing(iso_ctx* ctx, int enable) {
+    if (!ctx) return ISO_ERR_INVALID_ARG;
+    ctx->timing = enable != 0;
+    return ISO_OK;
+}
+
+iso_status iso_ctx_stage_times(iso_ctx* ctx, double* ms, uint64_t* launches) {
+    if (!ctx) return ISO_ERR_INVALID_ARG;
+    iso_status s = set_device(ctx);
+    if (s != ISO_OK) return s;
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "stage times");
+    for (auto& p : ctx->pending) {
+        float t = 0.0f;
+        if (cudaEventElapsedTime(&t, p.a, p.b) == cudaSuccess) ctx->stage_ms[p.stage] += t;
+        else cudaGetLastError();
+        ctx->event_pool.push_back(p.a);
+        ctx->event_pool.push_back(p.b);
+    }
+    ctx->pending.clear();
+    for (int i = 0; i < ISO_STAGE_COUNT; ++i) {
+        if (ms) ms[i] = ctx->stage_ms[i];
+        if (launches) launches[i] = ctx->stage_launches[i];
+        ctx->stage_ms[i] = 0.0;
+        ctx->stage_launches[i] = 0;
+    }
+    return ISO_OK;
+}
+
+iso_status iso_program_create(iso_ctx* ctx, const uint8_t* bytes, size_t len, iso_program** out) {
+    if (!ctx || !bytes || !out) return ISO_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (len < 16) return fail(ctx, ISO_ERR_BAD_PROGRAM, "program shorter than its header");
+    uint32_t h[4];
+    std::memcpy(h, bytes, 16);
+    if (h[0] != 0x314F5349u) return fail(ctx, ISO_ERR_BAD_PROGRAM, "bad magic");
+    if ((uint64_t)16 + 4ull * h[1] + 4ull * h[2] != len) return fail(ctx, ISO_ERR_BAD_PROGRAM, "length does not match header");
+    if (h[1] == 0) return fail(ctx, ISO_ERR_BAD_PROGRAM, "empty program");
+    iso_program* p = new (std::nothrow) iso_program();
+    if (!p) return ISO_ERR_OUT_OF_MEMORY;
+    p->ctx = ctx;
+    p->ops.resize(h[1]);
+    p->consts.resize(h[2]);
+    std::memcpy(p->ops.data(), bytes + 16, 4ull * h[1]);
+    if (h[2]) std::memcpy(p->consts.data(), bytes + 16 + 4ull * h[1], 4ull * h[2]);
+    std::string err;
+    if (!validate(p, &err)) {
+        delete p;
+        return fail(ctx, ISO_ERR_BAD_PROGRAM, err);
+    }
+    classify(p);
+    iso_status s = set_device(ctx);
+    if (s != ISO_OK) {
+        delete p;
+        return s;
+    }
+    // sphere data of the fast path is re-based to a 16-byte boundary for float4 loads
+    const size_t nk = p->consts.size() + 4;
+    cudaError_t e = cudaMalloc(&p->d_ops, 4 * p->ops.size());
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_consts, 4 * nk);
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_jump, 4 * p->jump.size());
+    if (e == cudaSuccess) e = cudaMemcpy(p->d_ops, p->ops.data(), 4 * p->ops.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !p->consts.empty())
+        e = cudaMemcpy(p->d_consts, p->consts.data(), 4 * p->consts.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(p->d_jump, p->jump.data(), 4 * p->jump.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && p->kind == PK_SPHERE_SET_HARD) {
+        float* d_set = nullptr;
+        e = cudaMalloc(&d_set, 16ull * p->set_n);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(d_set, p->consts.data() + p->set_at + 3, 16ull * p->set_n, cudaMemcpyHostToDevice);
+        p->d_set = d_set;
+    }
+    if (e != cudaSuccess) {
+        iso_status r = cuda_fail(ctx, e, "program upload");
+        iso_program_destroy(p);
+        return r;
+    }
+    *out = p;
+    return ISO_OK;
+}
+
+iso_status iso_program_destroy(iso_program* p) {
+    if (!p) return ISO_ERR_INVALID_ARG;
+    if (p->ctx) cudaSetDevice(p->ctx->device);
+    if (p->d_ops) cudaFree(p->d_ops);
+    if (p->d_consts) cudaFree(p->d_consts);
+    if (p->d_jump) cudaFree(p->d_jump);
+    if (p->d_set) cudaFree(p->d_set);
+    delete p;
+    return ISO_OK;
+}
+
+iso_status iso_mesh_download(iso_ctx* ctx, float* vertices, uint64_t vertex_floats_cap, uint32_t* indices,
+                             uint64_t index_cap, uint64_t* keys, uint64_t key_cap) {
+    if (!ctx) return ISO_ERR_INVALID_ARG;
+    iso_status s = set_device(ctx);
+    if (s != ISO_OK) return s;
+    const uint64_t nvf = ctx->last.num_vertices * (uint64_t)ctx->last_vertex_floats;
+    const uint64_t ni = 3 * ctx->last.num_triangles;
+    if ((vertices && vertex_floats_cap < nvf) || (indices && index_cap < ni))
+        return fail(ctx, ISO_ERR_CAPACITY, "host buffers too small for the mesh");
+    if (keys) {
+        if (!(ctx->last_flags & ISO_FLAG_KEYS)) return fail(ctx, ISO_ERR_INVALID_ARG, "mesh was extracted without keys");
+        if (key_cap < 2 * ctx->last.num_vertices) return fail(ctx, ISO_ERR_CAPACITY, "key buffer too small");
+    }
+    cudaError_t e = cudaSuccess;
+    if (vertices && nvf) e = cudaMemcpyAsync(vertices, ctx->mesh_v.p, 4 * nvf, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess && indices && ni)
+        e = cudaMemcpyAsync(indices, ctx->mesh_i.p, 4 * ni, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess && keys && ctx->last.num_vertices)
+        e = cudaMemcpyAsync(keys, ctx->mesh_k.p, 16 * ctx->last.num_vertices, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return e == cudaSuccess ? ISO_OK : cuda_fail(ctx, e, "mesh download");
+}
+
+iso_status iso_mesh_device(iso_ctx* ctx, const float** vertices, const uint32_t** indices, const uint64_t** keys,
+                           iso_mesh_info* info) {
+    if (!ctx) return ISO_ERR_INVALID_ARG;
+    if (vertices) *vertices = (const float*)ctx->mesh_v.p;
+    if (indices) *indices = (const uint32_t*)ctx->mesh_i.p;
+    if (keys) *keys = (ctx->last_flags & ISO_FLAG_KEYS) ? (const uint64_t*)ctx->mesh_k.p : nullptr;
+    if (info) *info = ctx->last;
+    return ISO_OK;
+}
+
+static iso_status sample_into_ctx(iso_ctx* ctx, const iso_program* prog, uint32_t size, Lattice* L) {
+    const uint32_t nx = size, ny = size, nz = size + 1;
+    const uint64_t pitch = default_pitch(nx);
+    const uint32_t W = words_per_row(nx);
+    iso_status s;
+    if ((s = ensure(ctx, ctx->field, 4ull * pitch * ny * nz)) != ISO_OK) return s;
+    if ((s = ensure(ctx, ctx->bits, 4ull * W * ny * nz)) != ISO_OK) return s;
+    const float inv = 1.0f / (float)(size - 1);
+    if ((s = launch_sample_grid(ctx, prog, nx, ny, nz, inv, (float*)ctx->field.p, pitch, (uint32_t*)ctx->bits.p)) != ISO_OK)
+        return s;
+    *L = Lattice{nx, ny, nz, pitch, (const float*)ctx->field.p, (const uint32_t*)ctx->bits.p, W, inv, nullptr};
+    return ISO_OK;
+}
+
+static iso_status check_size(iso_ctx* ctx, const iso_program* prog, uint32_t size) {
+    if (!ctx || !prog) return ISO_ERR_INVALID_ARG;
+    if (prog->ctx != ctx) return fail(ctx, ISO_ERR_INVALID_ARG, "program belongs to another context");
+    if (size == 0) return fail(ctx, ISO_ERR_INVALID_ARG, "size must be at least 1");
+    if (size > 65536) return fail(ctx, ISO_ERR_INVALID_ARG, "size above 65536");
+    return set_device(ctx);
+}
+
+iso_status iso_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t size, float* field, uint64_t pitch) {
+    iso_status s = check_size(ctx, prog, size);
+    if (s != ISO_OK) return s;
+    if (!field || pitch < size) return fail(ctx, ISO_ERR_INVALID_ARG, "field null or pitch < size");
+    const uint32_t W = words_per_row(size);
+    if ((s = ensure(ctx, ctx->bits, 4ull * W * size * (size + 1))) != ISO_OK) return s;
+    const float inv = size > 1 ? 1.0f / (float)(size - 1) : 0.0f;
+    if ((s = launch_sample_grid(ctx, prog, size, size, size + 1, inv, field, pitch, (uint32_t*)ctx->bits.p)) != ISO_OK)
+        return s;
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    return e == cudaSuccess ? ISO_OK : cuda_fail(ctx, e, "sample grid");
+}
+
+iso_status iso_mc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t flags, iso_mesh_info* info) {
+    iso_status s = check_size(ctx, prog, size);
+    if (s != ISO_OK) return s;
+    if (flags & ~(uint32_t)(ISO_FLAG_KEYS | ISO_FLAG_NORMALS)) return fail(ctx, ISO_ERR_INVALID_ARG, "unknown flags");
+    if (flags & ISO_FLAG_NORMALS) return fail(ctx, ISO_ERR_UNSUPPORTED, "normals flag not available for MC yet");
+    if (size == 1) {
+        ctx->last = iso_mesh_info{};
+        ctx->last_flags = flags;
+        if (info) *info = ctx->last;
+        return ISO_OK;
+    }
+    Lattice L;
+    if ((s = sample_into_ctx(ctx, prog, size, &L)) != ISO_OK) return s;
+    return mc_extract_lattice(ctx, L, flags, info);
+}
+
+iso_status iso_mc_extract_field(iso_ctx* ctx, const float* field, uint32_t nx, uint32_t ny, uint32_t nz, uint64_t pitch,
+                                uint32_t flags, iso_mesh_info* info) {
+    if (!ctx || !field) return ISO_ERR_INVALID_ARG;
+    if (nx != ny || nx < 2 || nz < 2 || pitch < nx || nx > 65536 || nz > 65537)
+        return fail(ctx, ISO_ERR_INVALID_ARG, "need nx == ny >= 2, nz >= 2, pitch >= nx");
+    if (flags & ~(uint32_t)ISO_FLAG_KEYS) return fail(ctx, ISO_ERR_INVALID_ARG, "unknown flags");
+    iso_status s = set_device(ctx);
+    if (s != ISO_OK) return s;
+    const uint32_t W = words_per_row(nx);
+    if ((s = ensure(ctx, ctx->bits, 4ull * W * ny * nz)) != ISO_OK) return s;
+    if ((s = launch_sign_bits(ctx, field, nx, ny, nz, pitch, (uint32_t*)ctx->bits.p)) != ISO_OK) return s;
+    Lattice L{nx, ny, nz, pitch, field, (const uint32_t*)ctx->bits.p, W, 1.0f / (float)(nx - 1), nullptr};
+    return mc_extract_lattice(ctx, L, flags, info);
+}
+
+iso_status iso_mc_cases(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint8_t* cases_host) {
+    iso_status s = check_size(ctx, prog, size);
+    if (s != ISO_OK) return s;
+    if (!cases_host) return fail(ctx, ISO_ERR_INVALID_ARG, "null output");
+    if (size < 2) return ISO_OK;
+    Lattice L;
+    if ((s = sample_into_ctx(ctx, prog, size, &L)) != ISO_OK) return s;
+    const uint64_t ncells = (uint64_t)(size - 1) * (size - 1) * size;
+    if ((s = ensure(ctx, ctx->aux, ncells)) != ISO_OK) return s;
+    if ((s = mc_cases_lattice(ctx, L, (uint8_t*)ctx->aux.p)) != ISO_OK) return s;
+    cudaError_t e = cudaMemcpyAsync(cases_host, ctx->aux.p, ncells, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return e == cudaSuccess ? ISO_OK : cuda_fail(ctx, e, "mc cases");
+}
+
+iso_status iso_sample_points(iso_ctx* ctx, const iso_program* prog, const float* points, uint64_t n, float* values,
+                             float* normals) {
+    if (!ctx || !prog || (!points && n) || (!values && n)) return ISO_ERR_INVALID_ARG;
+    iso_status s = set_device(ctx);
+    if (s != ISO_OK) return s;
+    if (n == 0) return ISO_OK;
+    if ((s = ensure(ctx, ctx->aux, 28 * n)) != ISO_OK) return s;
+    float* d_pts = (float*)ctx->aux.p;
+    float* d_vals = d_pts + 3 * n;
+    float* d_nrm = d_vals + n;
+    cudaError_t e = cudaMemcpyAsync(d_pts, points, 12 * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "upload points");
+    if ((s = launch_sample_points(ctx, prog, d_pts, n, d_vals, normals ? d_nrm : nullptr)) != ISO_OK) return s;
+    e = cudaMemcpyAsync(values, d_vals, 4 * n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess && normals) e = cudaMemcpyAsync(normals, d_nrm, 12 * n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return e == cudaSuccess ? ISO_OK : cuda_fail(ctx, e, "sample points");
+}
+
+iso_status iso_point_cloud_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, iso_mesh_info* info) {
+    (void)prog;
+    (void)size;
+    (void)info;
+    return fail(ctx, ISO_ERR_UNSUPPORTED, "point cloud not built yet");
+}
+
+}  // extern "C"

@@ -1,0 +1,148 @@
+"""Write the marching-cubes table headers used by the CUDA library and by the oracle.
+
+    python isosurface_gb300/csrc/gen_mc_tables.py [tests/golden/mc_tables.json]
+
+Input is the JSON copy of the reference's tables (marching_cubes_tables.rs:16-331
+of swiftcoder/isosurface, Apache-2.0) that tests/golden/make_golden.py extracts.
+The tables are data that must match the reference entry for entry, so they are
+carried over unchanged; everything else in the headers is derived here:
+
+* ``iso_tri_count[case]``      number of triangles of a case (<= 5)
+* ``iso_tri_edges[case]``      the case's triangle edge list, 4 bits per edge,
+                               edge k of the list in bits [4k, 4k+4)
+* ``iso_edge_order[case]``     the case's distinct edges in order of first use
+                               by the triangle list (again 4 bits each)
+* ``iso_edge_mask[case]``      12-bit mask of the edges whose corners differ in
+                               sign; equal to EDGE_CROSSING_MASK (checked here)
+
+The generator also checks that every crossing edge of a case is used by one of
+its triangles and that no triangle uses a non-crossing edge: the GPU's
+vertex-ownership rule relies on it.
+"""
+import json
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+
+LICENSE = """// Marching-cubes tables of swiftcoder/isosurface (src/marching_cubes_tables.rs),
+// Copyright 2021 Tristam MacDonald, licensed under the Apache License, Version 2.0
+// (http://www.apache.org/licenses/LICENSE-2.0).  Carried over entry for entry
+// because the extracted meshes must match the reference's; the derived tables
+// below them are generated.  Generated by isosurface_gb300/csrc/gen_mc_tables.py
+// -- do not edit.
+"""
+
+
+def derive(t):
+    ec = t["EDGE_CONNECTION"]
+    tri = t["TRIANGLE_CONNECTION"]
+    counts, packed, order, nord, masks = [], [], [], [], []
+    for case in range(256):
+        row = tri[case]
+        n = 0
+        while n < 5 and row[3 * n] >= 0:
+            n += 1
+        edges = row[: 3 * n]
+        assert all(0 <= e < 12 for e in edges)
+        assert all(v == -1 for v in row[3 * n:]), case
+        mask = 0
+        for e, (u, v) in enumerate(ec):
+            if ((case >> u) & 1) != ((case >> v) & 1):
+                mask |= 1 << e
+        assert mask == t["EDGE_CROSSING_MASK"][case], case
+        used = 0
+        for e in edges:
+            used |= 1 << e
+        assert used == mask, (case, used, mask)
+        w = 0
+        for k, e in enumerate(edges):
+            w |= e << (4 * k)
+        firsts = []
+        for e in edges:
+            if e not in firsts:
+                firsts.append(e)
+        o = 0
+        for k, e in enumerate(firsts):
+            o |= e << (4 * k)
+        counts.append(n)
+        packed.append(w)
+        order.append(o)
+        nord.append(len(firsts))
+        masks.append(mask)
+    return counts, packed, order, nord, masks
+
+
+def fmt_rows(vals, per, fmt):
+    lines = []
+    for i in range(0, len(vals), per):
+        lines.append("    " + ", ".join(fmt(v) for v in vals[i: i + per]) + ",")
+    return "\n".join(lines)
+
+
+def write_device_header(t, path):
+    counts, packed, order, nord, masks = derive(t)
+    s = [LICENSE, "#pragma once", "#include <stdint.h>", "",
+         "// Storage class of the tables; a CUDA translation unit defines it as",
+         "// `static __device__ const` (or __constant__) before including this header.",
+         "#ifndef ISO_TABLE",
+         "#define ISO_TABLE static const",
+         "#endif", "",
+         "// Corner offsets of a cell (CORNERS, marching_cubes_tables.rs:16-25).",
+         "ISO_TABLE uint8_t iso_corners[8][3] = {" + ", ".join("{%d, %d, %d}" % tuple(c) for c in t["CORNERS"]) + "};",
+         "// Corners joined by each cell edge (EDGE_CONNECTION, marching_cubes_tables.rs:32-45).",
+         "ISO_TABLE uint8_t iso_edge_connection[12][2] = {" + ", ".join("{%d, %d}" % tuple(e) for e in t["EDGE_CONNECTION"]) + "};",
+         "// Morton-cube to marching-cubes corner remap (REMAP_CUBE, marching_cubes_tables.rs:29).",
+         "ISO_TABLE uint8_t iso_remap_cube[8] = {" + ", ".join(str(v) for v in t["REMAP_CUBE"]) + "};",
+         "",
+         "// Triangles per case.",
+         "ISO_TABLE uint8_t iso_tri_count[256] = {",
+         fmt_rows(counts, 32, str),
+         "};",
+         "// Triangle edge lists (TRIANGLE_CONNECTION, marching_cubes_tables.rs:74-331), 4 bits per edge.",
+         "ISO_TABLE uint64_t iso_tri_edges[256] = {",
+         fmt_rows(packed, 4, lambda v: "0x%015xull" % v),
+         "};",
+         "// Distinct edges of each case in order of first use, 4 bits per edge.",
+         "ISO_TABLE uint64_t iso_edge_order[256] = {",
+         fmt_rows(order, 4, lambda v: "0x%012xull" % v),
+         "};",
+         "// Number of distinct edges of each case.",
+         "ISO_TABLE uint8_t iso_edge_count[256] = {",
+         fmt_rows(nord, 32, str),
+         "};",
+         "// Crossing-edge masks (equal to EDGE_CROSSING_MASK, marching_cubes_tables.rs:49-70).",
+         "ISO_TABLE uint16_t iso_edge_mask[256] = {",
+         fmt_rows(masks, 16, lambda v: "0x%03x" % v),
+         "};", ""]
+    open(path, "w").write("\n".join(s))
+
+
+def write_oracle_header(t, path):
+    s = [LICENSE, "#pragma once", "#include <stdint.h>", "",
+         "namespace ref_tables {",
+         "static const int CORNERS[8][3] = {" + ", ".join("{%d, %d, %d}" % tuple(c) for c in t["CORNERS"]) + "};",
+         "static const int REMAP_CUBE[8] = {" + ", ".join(str(v) for v in t["REMAP_CUBE"]) + "};",
+         "static const int EDGE_CONNECTION[12][2] = {" + ", ".join("{%d, %d}" % tuple(e) for e in t["EDGE_CONNECTION"]) + "};",
+         "static const uint16_t EDGE_CROSSING_MASK[256] = {",
+         fmt_rows(t["EDGE_CROSSING_MASK"], 13, lambda v: "0x%03x" % v),
+         "};",
+         "static const int8_t TRIANGLE_CONNECTION[256][16] = {"]
+    for row in t["TRIANGLE_CONNECTION"]:
+        s.append("    {" + ", ".join(str(v) for v in row) + "},")
+    s.append("};")
+    s.append("}  // namespace ref_tables")
+    open(path, "w").write("\n".join(s) + "\n")
+
+
+def main():
+    src = sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "tests", "golden", "mc_tables.json")
+    t = json.load(open(src))
+    write_device_header(t, os.path.join(HERE, "mc_tables.h"))
+    write_oracle_header(t, os.path.join(ROOT, "oracle", "ref_tables.h"))
+    print("wrote mc_tables.h and oracle/ref_tables.h")
+
+
+if __name__ == "__main__":
+    main()

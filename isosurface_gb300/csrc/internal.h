@@ -1,0 +1,135 @@
+// Internal declarations shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/isosurface_gpu.h"
+
+namespace iso {
+
+// Device-side error bits (ctx->d_err), read back after each call.
+enum : uint32_t {
+    DERR_SCAN_TIMEOUT = 1u,      // decoupled look-back gave up waiting
+    DERR_CAPACITY = 2u,          // a kernel found its output buffer too small
+    DERR_SVD_ITER = 4u,          // QR sweeps hit their bound
+    DERR_QUEUE_TIMEOUT = 8u,     // work-queue wait gave up
+};
+
+// Program kinds with a dedicated sampler.
+enum ProgramKind : int {
+    PK_GENERIC = 0,
+    PK_SPHERE_SET_HARD = 1,  // [PT_DOMAIN] SPHERE_SET(hard) [PT_POP]
+};
+
+// Device limits of the program evaluator
+constexpr int VSTACK = 16;
+constexpr int PSTACK = 8;
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+struct ProgView {
+    const uint32_t* ops;
+    const float* k;
+    const int32_t* jump;  // CD_BEGIN -> index of its CD_END (others 0)
+    uint32_t n_ops;
+};
+
+}  // namespace iso
+
+struct iso_ctx {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    // work buffers (grow-only, reused across calls)
+    iso::DevBuf field, bits, rowtri, rowvert, scan, aux, aux2, aux3;
+    // last mesh
+    iso::DevBuf mesh_v, mesh_i, mesh_k;
+    iso_mesh_info last{};
+    uint32_t last_flags = 0;
+    int last_vertex_floats = 3;
+    // pinned host scratch
+    uint64_t* h_pinned = nullptr;
+    uint32_t* d_err = nullptr;
+    uint64_t launches = 0;
+    std::string last_error;
+    // per-stage event timing (iso_ctx_enable_stage_timing)
+    bool timing = false;
+    std::vector<cudaEvent_t> event_pool;
+    struct Pending {
+        int stage;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pending;
+    double stage_ms[ISO_STAGE_COUNT] = {};
+    uint64_t stage_launches[ISO_STAGE_COUNT] = {};
+};
+
+namespace iso {
+// Brackets the kernels launched in its scope with events when timing is on.
+struct StageTimer {
+    iso_ctx* ctx;
+    int stage;
+    cudaEvent_t a = nullptr;
+    StageTimer(iso_ctx* c, int s);
+    ~StageTimer();
+};
+}  // namespace iso
+
+struct iso_program {
+    iso_ctx* ctx = nullptr;
+    std::vector<uint32_t> ops;
+    std::vector<float> consts;
+    std::vector<int32_t> jump;
+    uint32_t* d_ops = nullptr;
+    float* d_consts = nullptr;
+    int32_t* d_jump = nullptr;
+    float* d_set = nullptr;  // PK_SPHERE_SET_HARD: n float4 spheres, 16-byte aligned
+    int kind = iso::PK_GENERIC;
+    bool has_normal = true;
+    // PK_SPHERE_SET_HARD
+    bool has_domain = false;
+    float domain[6] = {0, 0, 0, 0, 0, 0};
+    uint32_t set_at = 0, set_n = 0;
+    iso::ProgView view() const { return iso::ProgView{d_ops, d_consts, d_jump, (uint32_t)ops.size()}; }
+};
+
+namespace iso {
+
+iso_status fail(iso_ctx* ctx, iso_status s, const std::string& msg);
+iso_status cuda_fail(iso_ctx* ctx, cudaError_t e, const char* what);
+iso_status ensure(iso_ctx* ctx, DevBuf& b, size_t bytes);
+iso_status check_launch(iso_ctx* ctx, const char* what);
+iso_status read_device_errors(iso_ctx* ctx);
+iso_status set_device(iso_ctx* ctx);
+
+// sample.cu
+iso_status launch_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t nx, uint32_t ny, uint32_t nz,
+                              float inv, float* field, uint64_t pitch, uint32_t* bits);
+iso_status launch_sign_bits(iso_ctx* ctx, const float* field, uint32_t nx, uint32_t ny, uint32_t nz,
+                            uint64_t pitch, uint32_t* bits);
+iso_status launch_sample_points(iso_ctx* ctx, const iso_program* prog, const float* d_pts, uint64_t n,
+                                float* d_vals, float* d_normals);
+
+// mc.cu -- marching cubes over a lattice of samples (sign bits + values)
+struct Lattice {
+    uint32_t nx, ny, nz;     // sample points along each axis
+    uint64_t pitch;          // floats per row of `values`
+    const float* values;     // nz x ny rows of `pitch` floats
+    const uint32_t* bits;    // nz x ny rows of words_per_row words, bit set iff !(v > 0)
+    uint32_t words_per_row;
+    float inv;               // point position = (x*inv, y*inv, z*inv)
+    const float4* positions; // DC: explicit xyz per point (w unused); null = regular grid
+};
+iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, iso_mesh_info* info);
+iso_status mc_cases_lattice(iso_ctx* ctx, const Lattice& L, uint8_t* d_cases);
+
+inline uint32_t words_per_row(uint32_t nx) { return (nx + 31) / 32; }
+inline uint64_t default_pitch(uint32_t nx) { return ((uint64_t)nx + 7) & ~7ull; }
+
+}  // namespace iso

@@ -1,0 +1,549 @@
+// Marching cubes over a lattice of samples: MarchingCubes::extract
+// (src/marching_cubes.rs:59-82) with PrimalGrid's traversal order
+// (src/traversal/primal_grid.rs:39-89), and the dual-cube pass of
+// DualContouring (src/dual_contouring.rs:88-101), which is the same cell
+// kernel over the dual lattice.
+//
+// The reference visits cells in (z, y, x) order, emits each vertex the first
+// time a triangle references its lattice edge (IndexCache,
+// src/mesh.rs:240-251) and then writes the faces in visit order.  This file
+// reproduces that output exactly, without a hash table:
+//
+// * The first cell to reference a lattice edge is determined by the edge's
+//   position alone (every crossing edge of a cell is used by one of the
+//   cell's triangles -- checked when the tables are generated), so each cell
+//   knows which of its crossing edges it "owns": interior cells own the three
+//   edges at their far corner; cells on the x=0 / y=0 / z=0 faces own more.
+// * Pass 1 (mc_count_scan) classifies every cell from packed sign bits and
+//   scans, per x-row of cells, the triangle count and the owned-vertex count
+//   with a single-pass decoupled look-back scan: rowtri[r], rowvert[r] are the
+//   exclusive output offsets of row r (r = z*(ny-1) + y).
+// * Pass 2 (mc_emit) re-derives, for a strip of rows of one z layer and the
+//   rows at y-1 and z-1 that own the strip's other edges, each cell's case and
+//   in-row prefix of owned vertices in shared memory.  A vertex id is then the
+//   owner row's offset + the owner cell's in-row prefix + the edge's rank in
+//   the owner's first-use order.  The owner computes the crossing with its
+//   own edge direction, as the reference's first visitor does, so positions
+//   are bit-identical.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "internal.h"
+#define ISO_TABLE static __device__ const
+#include "mc_tables.h"
+
+namespace iso {
+namespace {
+
+constexpr int WARPS = 8;
+constexpr uint32_t FULL = 0xFFFFFFFFu;
+constexpr uint64_t FLAG_A = 1ull << 62;
+constexpr uint64_t FLAG_P = 2ull << 62;
+constexpr uint64_t FLAG_MASK = 3ull << 62;
+constexpr uint64_t F31 = (1ull << 31) - 1;
+constexpr uint32_t SPIN_LIMIT = 1u << 20;
+
+// Lower endpoint (relative to the cell origin) and axis of each cell edge,
+// from CORNERS and EDGE_CONNECTION (marching_cubes_tables.rs:16-45).
+__device__ __constant__ uint8_t c_edge_lo[12][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 0}, {0, 0, 1}, {1, 0, 1},
+                                                    {0, 1, 1}, {0, 0, 1}, {0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}};
+__device__ __constant__ uint8_t c_edge_axis[12] = {0, 1, 0, 1, 0, 1, 0, 1, 2, 2, 2, 2};
+// Local edge by axis and the lower endpoint's two off-axis offsets (d1 + 2*d2):
+// x: (dy, dz), y: (dx, dz), z: (dx, dy).
+__device__ __constant__ uint8_t c_local_edge[3][4] = {{0, 2, 4, 6}, {3, 1, 7, 5}, {8, 9, 11, 10}};
+
+// Owned-edge masks by boundary class (x==0) | (y==0)<<1 | (z==0)<<2.  An edge
+// whose lower endpoint sits at offset d on an off-axis is owned by the cell
+// iff d == 1 or the cell is on the low face of that axis.
+__host__ __device__ inline uint32_t owned_mask(int cls) {
+    const int lo[12][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 0}, {0, 0, 1}, {1, 0, 1},
+                           {0, 1, 1}, {0, 0, 1}, {0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}};
+    const int axis[12] = {0, 1, 0, 1, 0, 1, 0, 1, 2, 2, 2, 2};
+    uint32_t m = 0;
+    for (int e = 0; e < 12; ++e) {
+        bool own = true;
+        for (int a = 0; a < 3; ++a) {
+            if (a == axis[e]) continue;
+            bool low_face = (cls >> a) & 1;
+            if (!(lo[e][a] == 1 || low_face)) own = false;
+        }
+        if (own) m |= 1u << e;
+    }
+    return m;
+}
+
+struct Tables {
+    uint8_t tri_count[256];
+    uint8_t edge_count[256];
+    uint16_t edge_mask[256];
+    uint64_t tri_edges[256];
+    uint64_t edge_order[256];
+    uint16_t owned[8];
+};
+
+__device__ void load_tables(Tables* t, bool full) {
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+        t->tri_count[i] = iso_tri_count[i];
+        t->edge_mask[i] = iso_edge_mask[i];
+        if (full) {
+            t->edge_count[i] = iso_edge_count[i];
+            t->tri_edges[i] = iso_tri_edges[i];
+            t->edge_order[i] = iso_edge_order[i];
+        }
+    }
+    if (threadIdx.x < 8) t->owned[threadIdx.x] = (uint16_t)owned_mask(threadIdx.x);
+}
+
+// Case of cell (32*c + lane) of the row whose corner rows are a, b (y+1), c_ (z+1), d (y+1,z+1).
+__device__ __forceinline__ uint32_t cell_case(const uint32_t* a, const uint32_t* b, const uint32_t* cz,
+                                              const uint32_t* d, uint32_t c, uint32_t W, int lane) {
+    uint32_t nxt = c + 1 < W;
+    uint32_t va = __funnelshift_r(a[c], nxt ? a[c + 1] : 0u, lane);
+    uint32_t vb = __funnelshift_r(b[c], nxt ? b[c + 1] : 0u, lane);
+    uint32_t vc = __funnelshift_r(cz[c], nxt ? cz[c + 1] : 0u, lane);
+    uint32_t vd = __funnelshift_r(d[c], nxt ? d[c + 1] : 0u, lane);
+    // CORNERS order: 0 (x,y,z) 1 (x+1,y,z) 2 (x+1,y+1,z) 3 (x,y+1,z) 4..7 the same at z+1
+    return (va & 1u) | ((va >> 1) & 1u) << 1 | ((vb >> 1) & 1u) << 2 | (vb & 1u) << 3 | (vc & 1u) << 4 |
+           ((vc >> 1) & 1u) << 5 | ((vd >> 1) & 1u) << 6 | (vd & 1u) << 7;
+}
+
+__device__ __forceinline__ uint32_t warp_sum(uint32_t v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    return v;
+}
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane) {
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(FULL, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+__device__ __forceinline__ uint64_t pack(uint64_t flag, uint64_t t, uint64_t v) { return flag | (t << 31) | v; }
+__device__ __forceinline__ uint64_t unpack_t(uint64_t s) { return (s >> 31) & F31; }
+__device__ __forceinline__ uint64_t unpack_v(uint64_t s) { return s & F31; }
+
+struct CountArgs {
+    const uint32_t* bits;
+    uint32_t W, nx, ny, nz;
+    uint32_t rows;          // (ny-1)*(nz-1)
+    uint32_t* rowtri;       // rows+1
+    uint32_t* rowvert;      // rows+1
+    uint64_t* status;       // one word per block
+    uint32_t* ticket;
+    uint64_t* totals;       // [0] triangles [1] vertices
+    uint32_t* err;
+};
+
+// Pass 1: per-row counts + decoupled look-back exclusive scan (one warp per row).
+__global__ void __launch_bounds__(WARPS * 32) mc_count_scan(CountArgs A) {
+    __shared__ Tables tb;
+    __shared__ uint32_t s_bid;
+    __shared__ uint32_t s_t[WARPS], s_v[WARPS];
+    __shared__ uint64_t s_excl_t, s_excl_v;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    load_tables(&tb, false);
+    if (threadIdx.x == 0) s_bid = atomicAdd(A.ticket, 1u);
+    __syncthreads();
+    const uint32_t bid = s_bid;
+    const uint32_t row = bid * WARPS + warp;
+    uint32_t tri = 0, vert = 0;
+    if (row < A.rows) {
+        const uint32_t ncy = A.ny - 1;
+        const uint32_t y = row % ncy, z = row / ncy;
+        const uint32_t* a = A.bits + ((uint64_t)z * A.ny + y) * A.W;
+        const uint32_t* b = a + A.W;
+        const uint32_t* cz = a + (uint64_t)A.ny * A.W;
+        const uint32_t* d = cz + A.W;
+        const int cls_yz = (y == 0 ? 2 : 0) | (z == 0 ? 4 : 0);
+        for (uint32_t c = 0; c < A.W; ++c) {
+            uint32_t x = 32 * c + lane;
+            uint32_t cs = cell_case(a, b, cz, d, c, A.W, lane);
+            if (x + 1 < A.nx) {
+                tri += tb.tri_count[cs];
+                vert += __popc((uint32_t)tb.edge_mask[cs] & tb.owned[cls_yz | (x == 0 ? 1 : 0)]);
+            }
+        }
+        tri = warp_sum(tri);
+        vert = warp_sum(vert);
+    }
+    if (lane == 0) {
+        s_t[warp] = tri;
+        s_v[warp] = vert;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t t = lane < WARPS ? s_t[lane] : 0u, v = lane < WARPS ? s_v[lane] : 0u;
+        uint32_t ti = warp_incl_scan(t, lane), vi = warp_incl_scan(v, lane);
+        uint64_t agg_t = __shfl_sync(FULL, ti, WARPS - 1), agg_v = __shfl_sync(FULL, vi, WARPS - 1);
+        volatile uint64_t* st = A.status;
+        if (lane == 0) {
+            __threadfence();
+            st[bid] = pack(bid == 0 ? FLAG_P : FLAG_A, agg_t, agg_v);
+        }
+        uint64_t ex_t = 0, ex_v = 0;
+        if (bid > 0) {
+            int64_t base = (int64_t)bid - 1;
+            while (true) {
+                int64_t j = base - lane;
+                uint64_t s = FLAG_P;
+                if (j >= 0) {
+                    uint32_t it = 0;
+                    s = st[j];
+                    while ((s & FLAG_MASK) == 0 && it < SPIN_LIMIT) {
+                        __nanosleep(64);
+                        s = st[j];
+                        ++it;
+                    }
+                    if ((s & FLAG_MASK) == 0) {
+                        atomicOr(A.err, DERR_SCAN_TIMEOUT);
+                        s = FLAG_P;
+                    }
+                }
+                uint32_t pmask = __ballot_sync(FULL, (s & FLAG_MASK) == FLAG_P);
+                int first = pmask ? __ffs(pmask) - 1 : 32;
+                uint64_t ct = lane <= first ? unpack_t(s) : 0, cv = lane <= first ? unpack_v(s) : 0;
+                for (int o = 16; o > 0; o >>= 1) {
+                    ct += __shfl_xor_sync(FULL, ct, o);
+                    cv += __shfl_xor_sync(FULL, cv, o);
+                }
+                ex_t += ct;
+                ex_v += cv;
+                if (pmask) break;
+                base -= 32;
+            }
+            if (lane == 0) {
+                uint64_t it_ = ex_t + agg_t, iv_ = ex_v + agg_v;
+                if (it_ > F31 || iv_ > F31) atomicOr(A.err, DERR_CAPACITY);
+                __threadfence();
+                st[bid] = pack(FLAG_P, it_ & F31, iv_ & F31);
+            }
+        }
+        if (lane < WARPS) {
+            s_t[lane] = ti - t;
+            s_v[lane] = vi - v;
+        }
+        if (lane == 0) {
+            s_excl_t = ex_t;
+            s_excl_v = ex_v;
+            if (bid == gridDim.x - 1) {
+                A.totals[0] = ex_t + agg_t;
+                A.totals[1] = ex_v + agg_v;
+                A.rowtri[A.rows] = (uint32_t)(ex_t + agg_t);
+                A.rowvert[A.rows] = (uint32_t)(ex_v + agg_v);
+            }
+        }
+    }
+    __syncthreads();
+    if (row < A.rows && lane == 0) {
+        A.rowtri[row] = (uint32_t)(s_excl_t + s_t[warp]);
+        A.rowvert[row] = (uint32_t)(s_excl_v + s_v[warp]);
+    }
+}
+
+struct EmitArgs {
+    const uint32_t* bits;
+    const float* values;
+    const float4* positions;  // null: regular grid
+    uint64_t pitch;
+    uint32_t W, nx, ny, nz;
+    float inv;
+    int rb;                   // rows per block
+    const uint32_t* rowtri;
+    const uint32_t* rowvert;
+    float* out_v;             // 3 floats per vertex
+    uint32_t* out_i;          // 3 per triangle
+    uint64_t* out_k;          // 2 per vertex (nullable)
+    uint64_t cap_v, cap_t;
+    uint32_t* err;
+};
+
+// rank of edge e among the owned edges of a cell, in first-use order
+__device__ __forceinline__ uint32_t owned_rank(const Tables& tb, uint32_t cs, uint32_t owned, uint32_t e) {
+    uint64_t ord = tb.edge_order[cs];
+    uint32_t n = tb.edge_count[cs], r = 0;
+    for (uint32_t k = 0; k < n; ++k) {
+        uint32_t f = (uint32_t)(ord >> (4 * k)) & 15u;
+        if (f == e) break;
+        r += (owned >> f) & 1u;
+    }
+    return r;
+}
+
+// Pass 2: write vertices and triangles of rows [y0, y0+rb) of layer z.
+__global__ void __launch_bounds__(WARPS * 32) mc_emit(EmitArgs A) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    Tables& tb = *reinterpret_cast<Tables*>(smem);
+    const uint32_t ncx = A.nx - 1, ncy = A.ny - 1;
+    const int rb = A.rb;
+    const int nrows = 2 * (rb + 1);
+    uint8_t* s_case = smem + sizeof(Tables);                                  // nrows * ncx
+    uint16_t* s_vpre = reinterpret_cast<uint16_t*>(s_case + ((nrows * ncx + 15) & ~15u));  // nrows * ncx
+    uint32_t* s_rowv = reinterpret_cast<uint32_t*>(s_vpre + ((nrows * ncx + 7) & ~7u));    // nrows
+    uint16_t* s_lx = reinterpret_cast<uint16_t*>(s_rowv + ((nrows + 3) & ~3));            // rb * ncx
+    uint32_t* s_lt = reinterpret_cast<uint32_t*>(s_lx + ((rb * ncx + 7) & ~7u));          // rb * ncx
+    __shared__ uint32_t s_nact[32];
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t z = blockIdx.y;
+    const uint32_t y0 = blockIdx.x * rb;
+    const int rows_here = (int)min((uint32_t)rb, ncy - y0);
+    const uint32_t r0 = z * ncy + y0;
+    if (A.rowtri[r0 + rows_here] == A.rowtri[r0]) return;  // no triangle in the strip
+    load_tables(&tb, true);
+    __syncthreads();
+
+    // smem row (kz, jy) <-> lattice cell row (y0-1+jy, z-1+kz)
+    for (int sr = warp; sr < nrows; sr += WARPS) {
+        const int kz = sr / (rb + 1), jy = sr % (rb + 1);
+        const int64_t yy = (int64_t)y0 - 1 + jy, zz = (int64_t)z - 1 + kz;
+        if (yy < 0 || zz < 0 || yy >= (int64_t)ncy) continue;
+        const uint32_t* a = A.bits + ((uint64_t)zz * A.ny + yy) * A.W;
+        const uint32_t* b = a + A.W;
+        const uint32_t* cz = a + (uint64_t)A.ny * A.W;
+        const uint32_t* d = cz + A.W;
+        const int cls_yz = (yy == 0 ? 2 : 0) | (zz == 0 ? 4 : 0);
+        uint32_t carry = 0;
+        for (uint32_t c = 0; c < A.W; ++c) {
+            uint32_t x = 32 * c + lane;
+            uint32_t cs = cell_case(a, b, cz, d, c, A.W, lane);
+            uint32_t nv = 0;
+            if (x < ncx) nv = __popc((uint32_t)tb.edge_mask[cs] & tb.owned[cls_yz | (x == 0 ? 1 : 0)]);
+            uint32_t inc = warp_incl_scan(nv, lane);
+            if (x < ncx) {
+                s_case[sr * ncx + x] = (uint8_t)cs;
+                s_vpre[sr * ncx + x] = (uint16_t)(carry + inc - nv);
+            }
+            carry += __shfl_sync(FULL, inc, 31);
+        }
+        if (lane == 0) s_rowv[sr] = A.rowvert[(uint64_t)zz * ncy + yy];
+    }
+    // active-cell lists of the strip's own rows (kz = 1, jy = w + 1)
+    for (int w = warp; w < rows_here; w += WARPS) {
+        const int sr = (rb + 1) + w + 1;
+        uint32_t tcarry = 0, n = 0;
+        for (uint32_t c = 0; c * 32 < ncx; ++c) {
+            uint32_t x = 32 * c + lane;
+            uint32_t cs = x < ncx ? s_case[sr * ncx + x] : 0u;
+            uint32_t nt = tb.tri_count[cs];
+            uint32_t tinc = warp_incl_scan(nt, lane);
+            bool act = nt != 0;
+            uint32_t m = __ballot_sync(FULL, act);
+            if (act) {
+                uint32_t at = n + __popc(m & ((1u << lane) - 1u));
+                s_lx[w * ncx + at] = (uint16_t)x;
+                s_lt[w * ncx + at] = tcarry + tinc - nt;
+            }
+            n += __popc(m);
+            tcarry += __shfl_sync(FULL, tinc, 31);
+        }
+        if (lane == 0) s_nact[w] = n;
+    }
+    __syncthreads();
+
+    const bool explicit_pos = A.positions != nullptr;
+    for (int w = warp; w < rows_here; w += WARPS) {
+        const uint32_t y = y0 + w;
+        const uint32_t row = z * ncy + y;
+        const int sr_self = (rb + 1) + w + 1;
+        const uint32_t tbase = A.rowtri[row];
+        const uint32_t vbase = s_rowv[sr_self];
+        const uint32_t n = s_nact[w];
+        for (uint32_t i = lane; i < n; i += 32) {
+            const uint32_t x = s_lx[w * ncx + i];
+            const uint32_t tpre = s_lt[w * ncx + i];
+            const uint32_t cs = s_case[sr_self * ncx + x];
+            const int cls = (x == 0 ? 1 : 0) | (y == 0 ? 2 : 0) | (z == 0 ? 4 : 0);
+            const uint32_t own = tb.owned[cls];
+            const uint32_t vstart = vbase + s_vpre[sr_self * ncx + x];
+            // vertices owned by this cell, in first-use order
+            {
+                const uint64_t ord = tb.edge_order[cs];
+                const uint32_t ne = tb.edge_count[cs];
+                uint32_t r = 0;
+                for (uint32_t k = 0; k < ne; ++k) {
+                    const uint32_t e = (uint32_t)(ord >> (4 * k)) & 15u;
+                    if (!((own >> e) & 1u)) continue;
+                    const uint32_t u = iso_edge_connection[e][0], v = iso_edge_connection[e][1];
+                    const uint32_t ux = x + iso_corners[u][0], uy = y + iso_corners[u][1], uz = z + iso_corners[u][2];
+                    const uint32_t vx = x + iso_corners[v][0], vy = y + iso_corners[v][1], vz = z + iso_corners[v][2];
+                    const uint64_t iu = ((uint64_t)uz * A.ny + uy) * A.pitch + ux;
+                    const uint64_t iv = ((uint64_t)vz * A.ny + vy) * A.pitch + vx;
+                    const float fa = __ldg(A.values + iu), fb = __ldg(A.values + iv);
+                    float pax, pay, paz, pbx, pby, pbz;
+                    if (explicit_pos) {
+                        const float4 qa = __ldg(A.positions + ((uint64_t)uz * A.ny + uy) * A.nx + ux);
+                        const float4 qb = __ldg(A.positions + ((uint64_t)vz * A.ny + vy) * A.nx + vx);
+                        pax = qa.x; pay = qa.y; paz = qa.z; pbx = qb.x; pby = qb.y; pbz = qb.z;
+                    } else {
+                        pax = (float)ux * A.inv; pay = (float)uy * A.inv; paz = (float)uz * A.inv;
+                        pbx = (float)vx * A.inv; pby = (float)vy * A.inv; pbz = (float)vz * A.inv;
+                    }
+                    // Signed::find_crossing_point (distance.rs:64-69)
+                    const float delta = fb - fa;
+                    const float t = (delta == 0.0f) ? 0.5f : -fa / delta;
+                    const float omt = 1.0f - t;
+                    const uint64_t vid = (uint64_t)vstart + r;
+                    if (vid < A.cap_v) {
+                        A.out_v[3 * vid + 0] = pax * omt + pbx * t;
+                        A.out_v[3 * vid + 1] = pay * omt + pby * t;
+                        A.out_v[3 * vid + 2] = paz * omt + pbz * t;
+                        if (A.out_k) {
+                            const uint32_t lx = x + c_edge_lo[e][0], ly = y + c_edge_lo[e][1], lz = z + c_edge_lo[e][2];
+                            A.out_k[2 * vid] = (((uint64_t)lz * A.ny + ly) * A.nx + lx) * 3 + c_edge_axis[e];
+                            A.out_k[2 * vid + 1] = 0;
+                        }
+                    } else {
+                        atomicOr(A.err, DERR_CAPACITY);
+                    }
+                    ++r;
+                }
+            }
+            // triangles (march_cube, marching_cubes_impl.rs:102-117)
+            {
+                const uint64_t te = tb.tri_edges[cs];
+                const uint32_t nt = tb.tri_count[cs];
+                for (uint32_t k = 0; k < 3 * nt; ++k) {
+                    const uint32_t e = (uint32_t)(te >> (4 * k)) & 15u;
+                    uint32_t id;
+                    if ((own >> e) & 1u) {
+                        id = vstart + owned_rank(tb, cs, own, e);
+                    } else {
+                        // owner: lowest (z, y, x) cell adjacent to the lattice edge
+                        const uint32_t ax = c_edge_axis[e];
+                        const uint32_t lx = x + c_edge_lo[e][0], ly = y + c_edge_lo[e][1], lz = z + c_edge_lo[e][2];
+                        uint32_t ox = lx, oy = ly, oz = lz, d1, d2;
+                        if (ax != 0) ox = lx > 0 ? lx - 1 : 0;
+                        if (ax != 1) oy = ly > 0 ? ly - 1 : 0;
+                        if (ax != 2) oz = lz > 0 ? lz - 1 : 0;
+                        if (ax == 0) { d1 = ly - oy; d2 = lz - oz; }
+                        else if (ax == 1) { d1 = lx - ox; d2 = lz - oz; }
+                        else { d1 = lx - ox; d2 = ly - oy; }
+                        const uint32_t oe = c_local_edge[ax][d1 + 2 * d2];
+                        const int sr = (int)(oz + 1 - z) * (rb + 1) + (int)(oy + 1 - y0);
+                        const uint32_t ocs = s_case[sr * ncx + ox];
+                        const int ocls = (ox == 0 ? 1 : 0) | (oy == 0 ? 2 : 0) | (oz == 0 ? 4 : 0);
+                        id = s_rowv[sr] + s_vpre[sr * ncx + ox] + owned_rank(tb, ocs, tb.owned[ocls], oe);
+                    }
+                    const uint64_t at = 3ull * (tbase + tpre) + k;
+                    if (at < 3 * A.cap_t) A.out_i[at] = id;
+                    else atomicOr(A.err, DERR_CAPACITY);
+                }
+            }
+        }
+    }
+}
+
+__global__ void mc_cases_kernel(const uint32_t* bits, uint32_t W, uint32_t nx, uint32_t ny, uint32_t nz,
+                                uint8_t* out) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t row = (uint64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
+    const uint32_t ncx = nx - 1, ncy = ny - 1;
+    if (row >= (uint64_t)ncy * (nz - 1)) return;
+    const uint32_t y = row % ncy, z = row / ncy;
+    const uint32_t* a = bits + ((uint64_t)z * ny + y) * W;
+    const uint32_t* b = a + W;
+    const uint32_t* cz = a + (uint64_t)ny * W;
+    const uint32_t* d = cz + W;
+    for (uint32_t c = 0; c < W; ++c) {
+        uint32_t x = 32 * c + lane;
+        uint32_t cs = cell_case(a, b, cz, d, c, W, lane);
+        if (x < ncx) out[row * ncx + x] = (uint8_t)cs;
+    }
+}
+
+size_t emit_smem(uint32_t ncx, int rb) {
+    size_t nrows = 2 * (rb + 1);
+    size_t s = sizeof(Tables);
+    s += (nrows * ncx + 15) & ~(size_t)15;
+    s += 2 * ((nrows * ncx + 7) & ~(size_t)7);
+    s += 4 * ((nrows + 3) & ~(size_t)3);
+    s += 2 * ((rb * ncx + 7) & ~(size_t)7);
+    s += 4 * rb * ncx;
+    return s;
+}
+
+}  // namespace
+
+iso_status mc_cases_lattice(iso_ctx* ctx, const Lattice& L, uint8_t* d_cases) {
+    if (L.nx < 2 || L.ny < 2 || L.nz < 2) return ISO_OK;
+    uint64_t rows = (uint64_t)(L.ny - 1) * (L.nz - 1);
+    StageTimer timer(ctx, ISO_STAGE_CLASSIFY);
+    mc_cases_kernel<<<(unsigned)((rows + WARPS - 1) / WARPS), WARPS * 32, 0, ctx->stream>>>(L.bits, L.words_per_row,
+                                                                                       L.nx, L.ny, L.nz, d_cases);
+    ctx->launches++;
+    return check_launch(ctx, "mc_cases");
+}
+
+iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, iso_mesh_info* info) {
+    ctx->last = iso_mesh_info{};
+    ctx->last_flags = flags;
+    ctx->last_vertex_floats = 3;
+    if (L.nx < 2 || L.ny < 2 || L.nz < 2) {
+        if (info) *info = ctx->last;
+        return ISO_OK;
+    }
+    if (L.nx - 1 > 65535) return fail(ctx, ISO_ERR_INVALID_ARG, "rows longer than 65535 cells are not supported");
+    const uint64_t rows = (uint64_t)(L.ny - 1) * (L.nz - 1);
+    if (rows >= (1ull << 31)) return fail(ctx, ISO_ERR_TOO_LARGE, "too many cell rows");
+    const uint32_t nblocks = (uint32_t)((rows + WARPS - 1) / WARPS);
+    iso_status s;
+    if ((s = ensure(ctx, ctx->rowtri, 4 * (rows + 1))) != ISO_OK) return s;
+    if ((s = ensure(ctx, ctx->rowvert, 4 * (rows + 1))) != ISO_OK) return s;
+    if ((s = ensure(ctx, ctx->scan, 8 * (size_t)nblocks + 64)) != ISO_OK) return s;
+    uint64_t* status = (uint64_t*)ctx->scan.p;
+    uint32_t* ticket = (uint32_t*)(status + nblocks);
+    uint64_t* totals = (uint64_t*)(status + nblocks + 2);
+    cudaError_t e = cudaMemsetAsync(ctx->scan.p, 0, 8 * (size_t)nblocks + 64, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "memset scan state");
+    CountArgs ca{L.bits, L.words_per_row, L.nx, L.ny, L.nz, (uint32_t)rows, (uint32_t*)ctx->rowtri.p,
+                 (uint32_t*)ctx->rowvert.p, status, ticket, totals, ctx->d_err};
+    {
+        StageTimer timer(ctx, ISO_STAGE_CLASSIFY);
+        mc_count_scan<<<nblocks, WARPS * 32, 0, ctx->stream>>>(ca);
+    }
+    ctx->launches++;
+    if ((s = check_launch(ctx, "mc_count_scan")) != ISO_OK) return s;
+    e = cudaMemcpyAsync(ctx->h_pinned, totals, 16, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "read totals");
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "sync after count");
+    if ((s = read_device_errors(ctx)) != ISO_OK) return s;
+    const uint64_t nt = ctx->h_pinned[0], nv = ctx->h_pinned[1];
+    if (nv >= (1ull << 31) || nt >= (1ull << 31))
+        return fail(ctx, ISO_ERR_TOO_LARGE, "mesh exceeds 2^31 vertices or triangles");
+    const bool keys = (flags & ISO_FLAG_KEYS) != 0;
+    if ((s = ensure(ctx, ctx->mesh_v, 12 * std::max<uint64_t>(nv, 1))) != ISO_OK) return s;
+    if ((s = ensure(ctx, ctx->mesh_i, 12 * std::max<uint64_t>(nt, 1))) != ISO_OK) return s;
+    if (keys && (s = ensure(ctx, ctx->mesh_k, 16 * std::max<uint64_t>(nv, 1))) != ISO_OK) return s;
+    if (nt > 0) {
+        const uint32_t ncx = L.nx - 1;
+        int rb = 8;
+        while (rb > 1 && emit_smem(ncx, rb) > 200 * 1024) rb /= 2;
+        const size_t smem = emit_smem(ncx, rb);
+        if (smem > 220 * 1024) return fail(ctx, ISO_ERR_INVALID_ARG, "rows too long for the emit pass");
+        e = cudaFuncSetAttribute(mc_emit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "emit smem attribute");
+        EmitArgs ea{L.bits, L.values, L.positions, L.pitch, L.words_per_row, L.nx, L.ny, L.nz, L.inv, rb,
+                    (const uint32_t*)ctx->rowtri.p, (const uint32_t*)ctx->rowvert.p, (float*)ctx->mesh_v.p,
+                    (uint32_t*)ctx->mesh_i.p, keys ? (uint64_t*)ctx->mesh_k.p : nullptr, nv, nt, ctx->d_err};
+        dim3 grid((L.ny - 1 + rb - 1) / rb, L.nz - 1);
+        {
+            StageTimer timer(ctx, ISO_STAGE_EMIT);
+            mc_emit<<<grid, WARPS * 32, smem, ctx->stream>>>(ea);
+        }
+        ctx->launches++;
+        if ((s = check_launch(ctx, "mc_emit")) != ISO_OK) return s;
+    }
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "sync after emit");
+    if ((s = read_device_errors(ctx)) != ISO_OK) return s;
+    ctx->last.num_vertices = nv;
+    ctx->last.num_triangles = nt;
+    ctx->last.num_cells = (uint64_t)(L.nx - 1) * (L.ny - 1) * (L.nz - 1);
+    if (info) *info = ctx->last;
+    return ISO_OK;
+}
+
+}  // namespace iso

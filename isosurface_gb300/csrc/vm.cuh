@@ -1,0 +1,242 @@
+// Device evaluator of source programs (format: include/isosurface_gpu.h).
+//
+// The arithmetic restates the reference's f32 operation order exactly
+// (src/math/vector.rs len_sq = (x*x + y*y) + z*z, src/implicit/*.rs), and the
+// translation units that include this header are built with -fmad=false so
+// that no a*b+c is fused: corner values are bit-identical to the reference's,
+// which keeps cube classification bit-exact.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "internal.h"
+
+namespace iso {
+
+enum : uint32_t {
+    OP_PT_DOMAIN = 0x01, OP_PT_TRANSLATE = 0x02, OP_PT_RIGID = 0x03, OP_PT_POP = 0x04,
+    OP_SPHERE = 0x10, OP_BOX = 0x11, OP_CYLINDER = 0x12, OP_TORUS = 0x13,
+    OP_UNION = 0x20, OP_INTERSECTION = 0x21, OP_DIFFERENCE = 0x22, OP_SMOOTH_UNION = 0x23,
+    OP_SPHERE_SET = 0x30, OP_CD_BEGIN = 0x40, OP_CD_END = 0x41,
+};
+
+struct V3 {
+    float x, y, z;
+};
+
+__host__ __device__ __forceinline__ V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ V3 operator*(V3 a, float f) { return v3(a.x * f, a.y * f, a.z * f); }
+__device__ __forceinline__ float len_sq(V3 a) { return (a.x * a.x + a.y * a.y) + a.z * a.z; }
+__device__ __forceinline__ float vlen(V3 a) { return sqrtf(len_sq(a)); }
+__device__ __forceinline__ V3 vmin(V3 a, V3 b) { return v3(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z)); }
+
+// primitives: sphere.rs:35-63, rectangular_prism.rs:36-80, cylinder.rs:41-85, torus.rs:40-108
+__device__ __forceinline__ float sd_sphere(V3 q, float r) { return vlen(q) - r; }
+__device__ __forceinline__ float sd_box(V3 q, float hx, float hy, float hz) {
+    float ax = fabsf(q.x) - hx, ay = fabsf(q.y) - hy, az = fabsf(q.z) - hz;
+    float l = vlen(v3(fmaxf(ax, 0.0f), fmaxf(ay, 0.0f), fmaxf(az, 0.0f)));
+    return l + fminf(fmaxf(ax, fmaxf(ay, az)), 0.0f);
+}
+__device__ __forceinline__ float sd_cylinder(V3 q, float r, float hl) {
+    float qx = fabsf(sqrtf(q.x * q.x + q.y * q.y)) - r;
+    float qz = fabsf(q.z) - hl;
+    float dx = fmaxf(qx, 0.0f), dz = fmaxf(qz, 0.0f);
+    float l = sqrtf((dx * dx + dz * dz) + 0.0f * 0.0f);
+    return fminf(fmaxf(qx, qz), 0.0f) + l;
+}
+__device__ __forceinline__ float sd_torus(V3 q, float R, float r) {
+    float qx = fabsf(sqrtf(q.x * q.x + q.y * q.y)) - R;
+    float l = sqrtf(qx * qx + q.z * q.z);
+    return l - r;
+}
+// Polynomial smooth minimum (Quilez 2013)
+__device__ __forceinline__ float smooth_min(float a, float b, float k) {
+    float h = fmaxf(k - fabsf(a - b), 0.0f) / k;
+    return fminf(a, b) - ((h * h) * k) * 0.25f;
+}
+
+__device__ __forceinline__ V3 n_box(V3 p) {  // vector.rs:612-621
+    float ax = fabsf(p.x), ay = fabsf(p.y), az = fabsf(p.z);
+    if (ax > ay && ax > az) return v3(p.x, 0.0f, 0.0f);
+    if (ay > az) return v3(0.0f, p.y, 0.0f);
+    return v3(0.0f, 0.0f, p.z);
+}
+__device__ __forceinline__ V3 n_cylinder(V3 p, float r, float hl) {
+    float z = fabsf(p.z) / hl;
+    float rr = sqrtf(p.x * p.x + p.y * p.y) / r;
+    if (z > rr) return v3(0.0f, 0.0f, p.z);
+    return v3(p.x, p.y, 0.0f);
+}
+__device__ __forceinline__ V3 n_torus(V3 p, float R) {
+    float l = sqrtf((p.x * p.x + p.y * p.y) + 0.0f * 0.0f);
+    V3 ring;
+    if (fabsf(l) < 1.1920929e-07f) ring = v3(1.0f, 0.0f, 0.0f);
+    else ring = v3(p.x / l, p.y / l, 0.0f / l);
+    return p - ring * R;
+}
+
+__device__ __forceinline__ V3 pt_apply(uint32_t op, const float* k, V3 p) {
+    if (op == OP_PT_DOMAIN) return v3(p.x * k[0] + k[3], p.y * k[1] + k[4], p.z * k[2] + k[5]);
+    if (op == OP_PT_TRANSLATE) return v3(p.x - k[0], p.y - k[1], p.z - k[2]);
+    V3 d = v3(p.x - k[0], p.y - k[1], p.z - k[2]);
+    const float* m = k + 3;
+    return v3((m[0] * d.x + m[1] * d.y) + m[2] * d.z, (m[3] * d.x + m[4] * d.y) + m[5] * d.z,
+              (m[6] * d.x + m[7] * d.y) + m[8] * d.z);
+}
+
+// Scalar evaluation of ops[begin, end) at p (one value left on the stack).
+__device__ __noinline__ float eval_range(const ProgView& pv, uint32_t begin, uint32_t end, V3 p) {
+    float vs[VSTACK];
+    V3 ps[PSTACK];
+    int vsp = 0, psp = 0;
+    ps[0] = p;
+    for (uint32_t pc = begin; pc < end; ++pc) {
+        uint32_t w = pv.ops[pc];
+        uint32_t op = w & 0xFFu;
+        const float* k = pv.k + (w >> 8);
+        V3 q = ps[psp];
+        switch (op) {
+        case OP_PT_DOMAIN: case OP_PT_TRANSLATE: case OP_PT_RIGID:
+            ps[++psp] = pt_apply(op, k, q);
+            break;
+        case OP_PT_POP: --psp; break;
+        case OP_SPHERE: vs[vsp++] = sd_sphere(q, k[0]); break;
+        case OP_BOX: vs[vsp++] = sd_box(q, k[0], k[1], k[2]); break;
+        case OP_CYLINDER: vs[vsp++] = sd_cylinder(q, k[0], k[1]); break;
+        case OP_TORUS: vs[vsp++] = sd_torus(q, k[0], k[1]); break;
+        case OP_UNION: --vsp; vs[vsp - 1] = fminf(vs[vsp - 1], vs[vsp]); break;
+        case OP_INTERSECTION: --vsp; vs[vsp - 1] = fmaxf(vs[vsp - 1], vs[vsp]); break;
+        case OP_DIFFERENCE: --vsp; vs[vsp - 1] = fmaxf(vs[vsp], -vs[vsp - 1]); break;
+        case OP_SMOOTH_UNION: --vsp; vs[vsp - 1] = smooth_min(vs[vsp - 1], vs[vsp], k[0]); break;
+        case OP_SPHERE_SET: {
+            uint32_t n = (uint32_t)k[0];
+            bool smooth = k[1] != 0.0f;
+            float kk = k[2];
+            float v = 0.0f;
+            for (uint32_t i = 0; i < n; ++i) {
+                const float* c = k + 3 + 4 * i;
+                float d = vlen(v3(q.x - c[0], q.y - c[1], q.z - c[2])) - c[3];
+                v = (i == 0) ? d : (smooth ? smooth_min(v, d, kk) : fminf(v, d));
+            }
+            vs[vsp++] = v;
+            break;
+        }
+        default: break;  // CD_BEGIN / CD_END are markers in scalar mode
+        }
+    }
+    return vs[0];
+}
+
+__device__ __forceinline__ float eval_scalar(const ProgView& pv, V3 p) { return eval_range(pv, 0, pv.n_ops, p); }
+
+// Value and (unnormalised) normal: HermiteSource::sample_normal semantics.
+__device__ __noinline__ float eval_hermite(const ProgView& pv, V3 p, V3* normal) {
+    float vs[VSTACK];
+    V3 ns[VSTACK];
+    V3 ps[PSTACK];
+    uint32_t pop_op[PSTACK];
+    const float* pop_k[PSTACK];
+    int vsp = 0, psp = 0;
+    ps[0] = p;
+    for (uint32_t pc = 0; pc < pv.n_ops; ++pc) {
+        uint32_t w = pv.ops[pc];
+        uint32_t op = w & 0xFFu;
+        const float* k = pv.k + (w >> 8);
+        V3 q = ps[psp];
+        switch (op) {
+        case OP_PT_DOMAIN: case OP_PT_TRANSLATE: case OP_PT_RIGID:
+            ps[++psp] = pt_apply(op, k, q);
+            pop_op[psp] = op;
+            pop_k[psp] = k;
+            break;
+        case OP_PT_POP:
+            if (pop_op[psp] == OP_PT_RIGID) {
+                const float* m = pop_k[psp] + 3;
+                V3 n = ns[vsp - 1];
+                ns[vsp - 1] = v3((m[0] * n.x + m[3] * n.y) + m[6] * n.z, (m[1] * n.x + m[4] * n.y) + m[7] * n.z,
+                                 (m[2] * n.x + m[5] * n.y) + m[8] * n.z);
+            }
+            --psp;
+            break;
+        case OP_SPHERE: vs[vsp] = sd_sphere(q, k[0]); ns[vsp++] = q; break;
+        case OP_BOX: vs[vsp] = sd_box(q, k[0], k[1], k[2]); ns[vsp++] = n_box(q); break;
+        case OP_CYLINDER: vs[vsp] = sd_cylinder(q, k[0], k[1]); ns[vsp++] = n_cylinder(q, k[0], k[1]); break;
+        case OP_TORUS: vs[vsp] = sd_torus(q, k[0], k[1]); ns[vsp++] = n_torus(q, k[0]); break;
+        case OP_UNION:
+            --vsp;
+            vs[vsp - 1] = fminf(vs[vsp - 1], vs[vsp]);
+            ns[vsp - 1] = vmin(ns[vsp - 1], ns[vsp]);
+            break;
+        case OP_INTERSECTION: {
+            --vsp;
+            float a = vs[vsp - 1], b = vs[vsp];
+            vs[vsp - 1] = fmaxf(a, b);
+            if (!(a >= b)) ns[vsp - 1] = ns[vsp];
+            break;
+        }
+        case OP_DIFFERENCE: {
+            --vsp;
+            float a = vs[vsp - 1], b = vs[vsp];
+            vs[vsp - 1] = fmaxf(b, -a);
+            V3 na = ns[vsp - 1];
+            ns[vsp - 1] = (b >= -a) ? ns[vsp] : v3(-na.x, -na.y, -na.z);
+            break;
+        }
+        case OP_SMOOTH_UNION: {
+            --vsp;
+            float a = vs[vsp - 1], b = vs[vsp];
+            vs[vsp - 1] = smooth_min(a, b, k[0]);
+            if (!(a <= b)) ns[vsp - 1] = ns[vsp];
+            break;
+        }
+        case OP_SPHERE_SET: {
+            uint32_t n = (uint32_t)k[0];
+            bool smooth = k[1] != 0.0f;
+            float kk = k[2];
+            float v = 0.0f;
+            V3 nn = v3(0.0f, 0.0f, 0.0f);
+            for (uint32_t i = 0; i < n; ++i) {
+                V3 c = v3(k[3 + 4 * i], k[4 + 4 * i], k[5 + 4 * i]);
+                V3 d3 = q - c;
+                float d = vlen(d3) - k[6 + 4 * i];
+                if (i == 0) {
+                    v = d;
+                    nn = d3;
+                } else if (smooth) {
+                    if (!(v <= d)) nn = d3;
+                    v = smooth_min(v, d, kk);
+                } else {
+                    v = fminf(v, d);
+                    nn = vmin(nn, d3);
+                }
+            }
+            vs[vsp] = v;
+            ns[vsp++] = nn;
+            break;
+        }
+        case OP_CD_BEGIN: {
+            // source.rs:52-95: (f(q+e) - f(q-e)) / (2 eps) per axis
+            uint32_t end = (uint32_t)pv.jump[pc];
+            float eps = k[0];
+            float v = eval_range(pv, pc + 1, end, q);
+            float vx = eval_range(pv, pc + 1, end, v3(q.x + eps, q.y + 0.0f, q.z + 0.0f)) -
+                       eval_range(pv, pc + 1, end, v3(q.x - eps, q.y - 0.0f, q.z - 0.0f));
+            float vy = eval_range(pv, pc + 1, end, v3(q.x + 0.0f, q.y + eps, q.z + 0.0f)) -
+                       eval_range(pv, pc + 1, end, v3(q.x - 0.0f, q.y - eps, q.z - 0.0f));
+            float vz = eval_range(pv, pc + 1, end, v3(q.x + 0.0f, q.y + 0.0f, q.z + eps)) -
+                       eval_range(pv, pc + 1, end, v3(q.x - 0.0f, q.y - 0.0f, q.z - eps));
+            float e2 = 2.0f * eps;
+            vs[vsp] = v;
+            ns[vsp++] = v3(vx / e2, vy / e2, vz / e2);
+            pc = end;  // loop increment skips the CD_END
+            break;
+        }
+        default: break;
+        }
+    }
+    *normal = ns[0];
+    return vs[0];
+}
+
+}  // namespace iso

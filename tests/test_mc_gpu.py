@@ -1,0 +1,189 @@
+"""GPU parity of the source evaluator, the grid sampler and MarchingCubes
+against the oracle (CPU restatement of the reference), through the C ABI.
+
+Parity bar: bit-exact.  The library reproduces MarchingCubes::extract's
+IndexedVertices output byte for byte: same vertex order (first use in (z,y,x)
+cell order), same positions, same index buffer."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from isosurface_gb300 import IsoError, scenes
+from isosurface_gb300 import source as S
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _normalised(n):
+    n = np.asarray(n, np.float32)
+    l = np.float32(np.sqrt(np.float32(np.float32(n[0] * n[0] + n[1] * n[1]) + n[2] * n[2])))
+    return n / l
+
+
+def test_reference_kats_on_gpu(ctx):
+    """The reference's primitive known answers, evaluated by the device VM."""
+    for kat in json.load(open(os.path.join(GOLDEN, "kats.json"))):
+        src = S.from_spec(kat["source"])
+        if kat["kind"] == "scalar":
+            v = ctx.sample_points(src, [kat["point"]])
+            assert v[0] == np.float32(kat["expected"]), kat
+        else:
+            _, n = ctx.sample_points(src, [kat["point"]], normals=True)
+            assert np.array_equal(_normalised(n[0]), np.asarray(kat["expected"], np.float32)), kat
+
+
+def _sources():
+    rng = np.random.default_rng(5)
+    sph = rng.uniform(-0.8, 0.8, size=(20, 4)).astype(np.float32)
+    sph[:, 3] = np.abs(sph[:, 3]) * 0.3 + 0.05
+    return {
+        "sphere": scenes.sphere(),
+        "box": S.unit_to_cube(S.RectangularPrism((0.5, 0.3, 0.7))),
+        "cylinder": S.unit_to_cube(S.Cylinder(0.4, 0.6)),
+        "torus": scenes.bench_torus(),
+        "csg": scenes.csg(),
+        "intersection": S.unit_to_cube(S.Intersection(S.Sphere(0.8), S.RectangularPrism((0.6, 0.6, 0.6)))),
+        "smooth": S.unit_to_cube(S.SmoothUnion(S.Translate(S.Sphere(0.3), (0.2, 0, 0)),
+                                               S.Translate(S.Sphere(0.3), (-0.2, 0, 0)), 0.1)),
+        "central_difference": S.unit_to_cube(S.CentralDifference(
+            S.Union(S.Difference(S.Sphere(0.25), S.RectangularPrism((0.2, 0.2, 0.2))), S.Cylinder(0.02, 0.25)))),
+        "sphere_set": S.unit_to_cube(S.SphereSet(sph)),
+        "smooth_set": S.unit_to_cube(S.SphereSet(sph, smooth_k=0.05)),
+        "set_nodomain": S.SphereSet(sph * np.float32([0.5, 0.5, 0.5, 0.5]) + np.float32([0.5, 0.5, 0.5, 0])),
+    }
+
+
+@pytest.mark.parametrize("name", sorted(_sources()))
+def test_point_values_and_normals_bit_exact(ctx, name):
+    src = _sources()[name]
+    pts = np.random.default_rng(11).uniform(-0.1, 1.1, size=(4096, 3)).astype(np.float32)
+    o = oracle.Program(S.lower(src))
+    v, n = ctx.sample_points(src, pts, normals=True)
+    assert np.array_equal(v, o.sample_scalar(pts))
+    assert np.array_equal(n, o.sample_normal(pts))
+
+
+@pytest.mark.parametrize("name", sorted(_sources()))
+@pytest.mark.parametrize("size", [2, 5, 17, 40])
+def test_mesh_bytes_identical(ctx, name, size):
+    src = _sources()[name]
+    o = oracle.Program(S.lower(src))
+    want = o.marching_cubes(size)
+    info = ctx.mc_extract(src, size, keys=True)
+    got = ctx.download(info, keys=True)
+    assert info.num_cells == (size - 1) * (size - 1) * size
+    assert np.array_equal(got.keys, want.keys)
+    assert np.array_equal(got.indices, want.indices)
+    assert np.array_equal(got.vertices, want.vertices)
+
+
+@pytest.mark.parametrize("name", ["sphere", "csg", "sphere_set", "torus"])
+def test_cases_and_field_bit_exact(ctx, name):
+    import torch
+    src = _sources()[name]
+    o = oracle.Program(S.lower(src))
+    size = 33
+    assert np.array_equal(ctx.mc_cases(src, size), o.mc_cases(size))
+    pitch = 40
+    field = torch.full(((size + 1) * size * pitch,), float("nan"), dtype=torch.float32, device="cuda")
+    ctx.sample_grid(src, size, field.data_ptr(), pitch)
+    got = field.view(size + 1, size, pitch)[:, :, :size].cpu().numpy()
+    assert np.array_equal(got, o.sample_grid(size))
+
+
+def test_c1_sphere_64(ctx):
+    """64^3 cells over [-1,1]^3, sphere r=0.75: the reference's own CPU case."""
+    src = scenes.sphere()
+    want = oracle.Program(S.lower(src)).marching_cubes(65)
+    got = ctx.download(ctx.mc_extract(src, 65, keys=True), keys=True)
+    assert np.array_equal(got.vertices, want.vertices)
+    assert np.array_equal(got.indices, want.indices)
+
+
+def test_bench_torus_128(ctx):
+    """The reference benchmark's MarchingCubes::new(128) on Torus(0.25, 0.1)."""
+    src = scenes.bench_torus()
+    want = oracle.Program(S.lower(src)).marching_cubes(128)
+    got = ctx.download(ctx.mc_extract(src, 128))
+    assert np.array_equal(got.vertices, want.vertices)
+    assert np.array_equal(got.indices, want.indices)
+
+
+def test_sphere_union_129(ctx):
+    src = scenes.sphere_union()
+    want = oracle.Program(S.lower(src)).marching_cubes(129)
+    got = ctx.download(ctx.mc_extract(src, 129))
+    assert np.array_equal(got.vertices, want.vertices)
+    assert np.array_equal(got.indices, want.indices)
+
+
+def test_extract_from_caller_field(ctx):
+    import torch
+    src = scenes.csg()
+    o = oracle.Program(S.lower(src))
+    size = 33
+    g = torch.from_numpy(o.sample_grid(size)).cuda().contiguous()
+    info = ctx.mc_extract_field(g.data_ptr(), size, size, size + 1, size)
+    got = ctx.download(info)
+    want = o.marching_cubes(size)
+    assert np.array_equal(got.vertices, want.vertices)
+    assert np.array_equal(got.indices, want.indices)
+
+
+def test_full_size_512_slab_parity(ctx):
+    """512^3 cells, 64-sphere union: the full GPU mesh's triangles of a middle
+    slab of cell layers equal the oracle's traversal of that slab (relabelled
+    by lattice-edge key; triangle order preserved)."""
+    src = scenes.sphere_union()
+    size = 513
+    info = ctx.mc_extract(src, size, keys=True)
+    got = ctx.download(info, keys=True)
+    cases = ctx.mc_cases(src, size)
+    tri_count = np.array(json.load(open(os.path.join(GOLDEN, "mc_tables.json")))["TRIANGLE_CONNECTION"])
+    ntri = (tri_count[:, 0::3][:, :5] >= 0).sum(1)
+    per_layer = ntri[cases.reshape(size, -1)].sum(1)
+    assert per_layer.sum() == info.num_triangles
+    z0, z1 = 250, 258
+    t0, t1 = int(per_layer[:z0].sum()), int(per_layer[:z1].sum())
+    o = oracle.Program(S.lower(src))
+    want = o.marching_cubes_slab(size, z0, z1)
+    got_keys = got.keys[:, 0][got.indices[3 * t0:3 * t1]]
+    want_keys = want.keys[:, 0][want.indices]
+    assert np.array_equal(got_keys, want_keys)
+    # positions per lattice edge: bit-exact except edges whose first visitor
+    # lies below the slab (their direction differs), within 1e-5 cell there
+    gv = got.vertices[got.indices[3 * t0:3 * t1]]
+    wv = want.vertices[want.indices]
+    assert np.max(np.abs(gv - wv)) <= 1e-5 / (size - 1)
+    # whole-mesh properties: closed, oriented, every key unique
+    from test_oracle import edge_manifold_stats
+    ne, bad, dup = edge_manifold_stats(got.triangles)
+    assert dup == 0 and bad == 0
+    assert len(np.unique(got.keys[:, 0])) == len(got.keys)
+
+
+def test_degenerate_sizes_and_errors(ctx):
+    src = scenes.sphere()
+    info = ctx.mc_extract(src, 1)
+    assert info.num_vertices == 0 and info.num_triangles == 0
+    with pytest.raises(IsoError):
+        ctx.mc_extract(src, 0)
+    for empty in (S.Sphere(-1.0), S.Sphere(10.0)):
+        info = ctx.mc_extract(empty, 17)
+        assert info.num_vertices == 0 and info.num_triangles == 0
+    with pytest.raises(IsoError):
+        ctx.program(b"ISO1" + b"\0" * 12)
+
+
+def test_reference_style_api(ctx):
+    """MarchingCubes::new(n).extract(&Sampler::new(&source), &mut IndexedVertices)."""
+    from isosurface_gb300 import IndexedVertices, MarchingCubes, Sampler
+    vertices, indices = [], []
+    MarchingCubes(33, context=ctx).extract(Sampler(scenes.sphere()), IndexedVertices(vertices, indices))
+    want = oracle.Program(S.lower(scenes.sphere())).marching_cubes(33)
+    assert np.array_equal(np.asarray(vertices, np.float32), want.vertices.reshape(-1))
+    assert np.array_equal(np.asarray(indices, np.uint32), want.indices)
