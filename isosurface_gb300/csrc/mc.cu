@@ -319,6 +319,7 @@ __global__ void __launch_bounds__(WARPS * 32) mc_emit(EmitArgs A) {
         }
         if (lane == 0) s_rowv[sr] = A.rowvert[(uint64_t)zz * ncy + yy];
     }
+    __syncthreads();
     // active-cell lists of the strip's own rows (kz = 1, jy = w + 1)
     for (int w = warp; w < rows_here; w += WARPS) {
         const int sr = (rb + 1) + w + 1;
