@@ -201,6 +201,37 @@ ISO_API iso_status iso_mc_extract(iso_ctx* ctx, const iso_program* prog, uint32_
 ISO_API iso_status iso_mc_extract_field(iso_ctx* ctx, const float* field, uint32_t nx, uint32_t ny, uint32_t nz,
                                 uint64_t pitch, uint32_t flags, iso_mesh_info* info);
 
+/* Marching cubes over a caller-supplied device field that allocates nothing.
+ *
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc or cudaFree -- code whose GPU memory is owned by a host
+ * application's own allocator or fixed budget, and per-frame loops (a
+ * renderer's or game engine's remeshing step) that cannot absorb the implicit
+ * device synchronisation and unbounded latency of those calls.  It needs no
+ * iso_ctx (creating one allocates).
+ *
+ * Input and layout as iso_mc_extract_field.  The caller owns the outputs:
+ * `vertices` (3 floats per vertex, room for vertex_cap vertices) and
+ * `indices` (3 u32 per triangle, room for triangle_cap triangles), both
+ * device memory; work is queued on `stream` (a cudaStream_t, NULL for the
+ * default stream) and the call returns when it has finished.  The mesh equals
+ * iso_mc_extract_field's.  `info` always receives the mesh size; when a
+ * buffer is too small the call writes nothing and returns ISO_ERR_CAPACITY,
+ * so a caller can size its buffers and call again.
+ *
+ * Scratch lives in a 32 MiB array of device memory inside the library, which
+ * every GPU that loads the library keeps until the process exits.  A grid
+ * needs about nx*ny*nz/8 + 9*ny*nz bytes of it; the largest cubic grid that
+ * fits is 613 x 613 x 614 samples (MarchingCubes::new(613)), and grids whose
+ * scratch would not fit are rejected with ISO_ERR_TOO_LARGE.  The first call on each device looks up that
+ * array's device address; make that first call before any stream capture.
+ * All calls share the one array, so calls whose GPU work overlaps (other
+ * streams or host threads) race and must be serialised by the caller. */
+ISO_API iso_status iso_mc_extract_field_noalloc(const float* field, uint32_t nx, uint32_t ny, uint32_t nz,
+                                                uint64_t pitch, float* vertices, uint64_t vertex_cap,
+                                                uint32_t* indices, uint64_t triangle_cap, void* stream,
+                                                iso_mesh_info* info);
+
 /* Case index of every cell of MarchingCubes::new(size) (the bits of
  * classify_corners, marching_cubes_impl.rs:26-37) into host memory:
  * size x (size-1) x (size-1) bytes, traversal order (z, y, x). */

@@ -115,6 +115,9 @@ iso_status launch_sign_bits(iso_ctx* ctx, const float* field, uint32_t nx, uint3
                             uint64_t pitch, uint32_t* bits);
 iso_status launch_sample_points(iso_ctx* ctx, const iso_program* prog, const float* d_pts, uint64_t n,
                                 float* d_vals, float* d_normals);
+// context-free launch of the sign-bit kernel (used by the allocation-free entry point)
+cudaError_t launch_sign_bits_on(cudaStream_t stream, const float* field, uint32_t nx, uint32_t ny, uint32_t nz,
+                                uint64_t pitch, uint32_t* bits);
 
 // mc.cu -- marching cubes over a lattice of samples (sign bits + values)
 struct Lattice {

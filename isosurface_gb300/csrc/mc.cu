@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "internal.h"
 #define ISO_TABLE static __device__ const
@@ -548,3 +549,119 @@ iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, is
 }
 
 }  // namespace iso
+
+// ---------------------------------------------------------------------------
+// Allocation-free marching cubes (iso_mc_extract_field_noalloc).
+//
+// Everything the three passes need besides the caller's field and output
+// buffers -- sign bits, per-row offsets, look-back status words, totals and
+// the error word -- lives in one fixed device array declared below.  Every GPU
+// that loads this library reserves NOALLOC_SCRATCH_BYTES for it until the
+// process exits.  All calls share the array and it keeps the previous call's
+// contents, so each call clears the part that must start at zero; calls whose
+// work overlaps on the GPU (other streams, other host threads) race on it and
+// must be serialised by the caller.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t NOALLOC_SCRATCH_BYTES = 32ull << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+// Host handle of the array per device: the array's name is only a host-side
+// stand-in, so its device address is looked up once per device.
+std::mutex g_noalloc_mutex;
+void* g_noalloc_addr[256] = {};
+
+iso_status noalloc_scratch(int device, unsigned char** out) {
+    if (device < 0 || device >= 256) return ISO_ERR_NO_DEVICE;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr) {
+            cudaGetLastError();
+            return ISO_ERR_CUDA;
+        }
+        g_noalloc_addr[device] = p;
+    }
+    *out = (unsigned char*)g_noalloc_addr[device];
+    return ISO_OK;
+}
+
+inline size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+}  // namespace
+
+extern "C" ISO_API iso_status iso_mc_extract_field_noalloc(const float* field, uint32_t nx, uint32_t ny, uint32_t nz,
+                                                            uint64_t pitch, float* vertices, uint64_t vertex_cap,
+                                                            uint32_t* indices, uint64_t triangle_cap, void* stream,
+                                                            iso_mesh_info* info) {
+    using namespace iso;
+    if (!field || !info) return ISO_ERR_INVALID_ARG;
+    *info = iso_mesh_info{};
+    if (nx != ny || nx < 2 || nz < 2 || pitch < nx || nx > 65536 || nz > 65537) return ISO_ERR_INVALID_ARG;
+    const uint32_t W = words_per_row(nx);
+    const uint64_t rows = (uint64_t)(ny - 1) * (nz - 1);
+    const uint64_t nblocks = (rows + WARPS - 1) / WARPS;
+    // scratch layout: [err | totals, ticket | status | rowtri | rowvert | bits]
+    const size_t off_head = 0, head_bytes = 256;
+    const size_t off_status = off_head + head_bytes;
+    const size_t off_rowtri = align256(off_status + 8 * nblocks);
+    const size_t off_rowvert = align256(off_rowtri + 4 * (rows + 1));
+    const size_t off_bits = align256(off_rowvert + 4 * (rows + 1));
+    const size_t need = align256(off_bits + 4ull * W * ny * nz);
+    if (need > NOALLOC_SCRATCH_BYTES) return ISO_ERR_TOO_LARGE;
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess) {
+        cudaGetLastError();
+        return ISO_ERR_NO_DEVICE;
+    }
+    unsigned char* s = nullptr;
+    iso_status st = noalloc_scratch(device, &s);
+    if (st != ISO_OK) return st;
+    cudaStream_t cs = (cudaStream_t)stream;
+    uint32_t* err = (uint32_t*)(s + off_head);
+    uint64_t* totals = (uint64_t*)(s + off_head + 64);
+    uint32_t* ticket = (uint32_t*)(s + off_head + 128);
+    uint64_t* status = (uint64_t*)(s + off_status);
+    uint32_t* rowtri = (uint32_t*)(s + off_rowtri);
+    uint32_t* rowvert = (uint32_t*)(s + off_rowvert);
+    uint32_t* bits = (uint32_t*)(s + off_bits);
+    // error word, totals, ticket and look-back status must start at zero
+    cudaError_t e = cudaMemsetAsync(s, 0, off_status + 8 * nblocks, cs);
+    if (e == cudaSuccess) e = launch_sign_bits_on(cs, field, nx, ny, nz, pitch, bits);
+    if (e != cudaSuccess) return ISO_ERR_CUDA;
+    CountArgs ca{bits, W, nx, ny, nz, (uint32_t)rows, rowtri, rowvert, status, ticket, totals, err};
+    mc_count_scan<<<(unsigned)nblocks, WARPS * 32, 0, cs>>>(ca);
+    uint64_t h[3] = {0, 0, 0};
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, totals, 16, cudaMemcpyDeviceToHost, cs);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h + 2, err, 4, cudaMemcpyDeviceToHost, cs);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+    if (e != cudaSuccess) return ISO_ERR_CUDA;
+    if ((uint32_t)h[2] & DERR_SCAN_TIMEOUT) return ISO_ERR_TIMEOUT;
+    const uint64_t nt = h[0], nv = h[1];
+    if (nv >= (1ull << 31) || nt >= (1ull << 31) || ((uint32_t)h[2] & DERR_CAPACITY)) return ISO_ERR_TOO_LARGE;
+    info->num_vertices = nv;
+    info->num_triangles = nt;
+    info->num_cells = (uint64_t)(nx - 1) * (ny - 1) * (nz - 1);
+    if ((nv && (!vertices || vertex_cap < nv)) || (nt && (!indices || triangle_cap < nt))) return ISO_ERR_CAPACITY;
+    if (nt == 0) return ISO_OK;
+    const uint32_t ncx = nx - 1;
+    int rb = 8;
+    while (rb > 1 && emit_smem(ncx, rb) > 200 * 1024) rb /= 2;
+    const size_t smem = emit_smem(ncx, rb);
+    if (smem > 220 * 1024) return ISO_ERR_INVALID_ARG;
+    e = cudaFuncSetAttribute(mc_emit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return ISO_ERR_CUDA;
+    EmitArgs ea{bits, field, nullptr, pitch, W, nx, ny, nz, 1.0f / (float)(nx - 1), rb, rowtri, rowvert,
+                vertices, indices, nullptr, nv, nt, err};
+    dim3 grid((ny - 1 + rb - 1) / rb, nz - 1);
+    mc_emit<<<grid, WARPS * 32, smem, cs>>>(ea);
+    e = cudaGetLastError();
+    uint32_t herr = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, cs);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+    if (e != cudaSuccess) return ISO_ERR_CUDA;
+    return herr ? ISO_ERR_CAPACITY : ISO_OK;
+}

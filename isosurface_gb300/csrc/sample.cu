@@ -217,6 +217,14 @@ iso_status launch_sign_bits(iso_ctx* ctx, const float* field, uint32_t nx, uint3
     return check_launch(ctx, "sign_bits");
 }
 
+cudaError_t launch_sign_bits_on(cudaStream_t stream, const float* field, uint32_t nx, uint32_t ny, uint32_t nz,
+                                uint64_t pitch, uint32_t* bits) {
+    const uint32_t W = words_per_row(nx);
+    uint64_t warps = (uint64_t)W * ny * nz;
+    sign_bits<<<(unsigned)((warps + 7) / 8), 256, 0, stream>>>(field, nx, ny, nz, pitch, bits, W);
+    return cudaGetLastError();
+}
+
 iso_status launch_sample_points(iso_ctx* ctx, const iso_program* prog, const float* d_pts, uint64_t n, float* d_vals,
                                 float* d_normals) {
     if (n == 0) return ISO_OK;
