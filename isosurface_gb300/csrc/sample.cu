@@ -46,7 +46,8 @@ __global__ void __launch_bounds__(256) sample_generic(ProgView pv, uint32_t nx, 
 // A dropped sphere's value exceeds the kept minimum at every point of the
 // tile (the margin covers f32 rounding of both bounds and values), and min is
 // exact, so the field equals the full fold over all spheres bit for bit.
-constexpr int TZ = 8;
+constexpr int TZ = 16;
+constexpr int KEEP_REGS = 6;  // kept spheres held in registers (more: shared-memory loop)
 
 struct SetArgs {
     const float* spheres;  // n x (cx, cy, cz, r)
@@ -129,6 +130,37 @@ __global__ void __launch_bounds__(256) sample_sphere_set(SetArgs A) {
     if (y >= A.ny) return;
     const float px = world((float)x * A.inv, A.sx, A.ox, A.domain);
     const float py = world((float)y * A.inv, A.sy, A.oy, A.domain);
+    const bool valid = x < A.nx;
+    if (nk <= KEEP_REGS) {
+        // kept spheres in registers; (dx*dx + dy*dy) is shared by the whole
+        // z column and is exactly the first partial sum of len_sq
+        float dxy[KEEP_REGS], cz[KEEP_REGS], cr[KEEP_REGS];
+#pragma unroll
+        for (int i = 0; i < KEEP_REGS; ++i) {
+            const float4 c = s_keep[i < (int)nk ? i : 0];
+            const float dx = px - c.x, dy = py - c.y;
+            dxy[i] = dx * dx + dy * dy;
+            cz[i] = c.z;
+            cr[i] = c.w;
+        }
+        for (uint32_t z = z0; z <= z1; ++z) {
+            const float pz = world((float)z * A.inv, A.sz, A.oz, A.domain);
+            float dz = pz - cz[0];
+            float v = sqrtf(dxy[0] + dz * dz) - cr[0];
+#pragma unroll
+            for (int i = 1; i < KEEP_REGS; ++i) {
+                if (i < (int)nk) {
+                    dz = pz - cz[i];
+                    v = fminf(v, sqrtf(dxy[i] + dz * dz) - cr[i]);
+                }
+            }
+            const uint64_t row = (uint64_t)z * A.ny + y;
+            if (valid) A.field[row * A.pitch + x] = v;
+            const uint32_t b = __ballot_sync(FULL, valid && !(v > 0.0f));
+            if (lane == 0) A.bits[row * A.W + blockIdx.x] = b;
+        }
+        return;
+    }
     for (uint32_t z = z0; z <= z1; ++z) {
         const float pz = world((float)z * A.inv, A.sz, A.oz, A.domain);
         float v = 0.0f;
@@ -138,7 +170,6 @@ __global__ void __launch_bounds__(256) sample_sphere_set(SetArgs A) {
             v = (i == 0) ? d : fminf(v, d);
         }
         const uint64_t row = (uint64_t)z * A.ny + y;
-        const bool valid = x < A.nx;
         if (valid) A.field[row * A.pitch + x] = v;
         uint32_t b = __ballot_sync(FULL, valid && !(v > 0.0f));
         if (lane == 0) A.bits[row * A.W + blockIdx.x] = b;
