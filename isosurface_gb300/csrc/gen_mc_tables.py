@@ -74,6 +74,50 @@ def derive(t):
     return counts, packed, order, nord, masks
 
 
+def owned_mask(t, cls):
+    """Edges a cell of boundary class cls ((x==0) | (y==0)<<1 | (z==0)<<2) is the
+    first visitor of: an edge whose lower endpoint sits at offset 0 on an
+    off-axis is first visited by the neighbour below on that axis, unless the
+    cell is on the grid's low face there."""
+    corners, ec = t["CORNERS"], t["EDGE_CONNECTION"]
+    m = 0
+    for e, (u, v) in enumerate(ec):
+        lo = [min(corners[u][a], corners[v][a]) for a in range(3)]
+        axis = [a for a in range(3) if corners[u][a] != corners[v][a]][0]
+        own = all(lo[a] == 1 or (cls >> a) & 1 for a in range(3) if a != axis)
+        if own:
+            m |= 1 << e
+    return m
+
+
+def derive_ranks(t):
+    """rank[cls][case]: 4 bits per edge e, the number of edges owned by class
+    cls that precede e in the case's first-use order; slot[case]: 4 bits per
+    triangle vertex, the index of its edge in the first-use order."""
+    counts, packed, order, nord, masks = derive(t)
+    rank = []
+    for cls in range(8):
+        om = owned_mask(t, cls)
+        row = []
+        for case in range(256):
+            firsts = [(order[case] >> (4 * k)) & 15 for k in range(nord[case])]
+            w, r = 0, 0
+            for e in firsts:
+                w |= r << (4 * e)
+                r += (om >> e) & 1
+            row.append(w)
+        rank.append(row)
+    slot = []
+    for case in range(256):
+        firsts = [(order[case] >> (4 * k)) & 15 for k in range(nord[case])]
+        w = 0
+        for k in range(3 * counts[case]):
+            e = (packed[case] >> (4 * k)) & 15
+            w |= firsts.index(e) << (4 * k)
+        slot.append(w)
+    return rank, slot
+
+
 def fmt_rows(vals, per, fmt):
     lines = []
     for i in range(0, len(vals), per):
@@ -115,7 +159,21 @@ def write_device_header(t, path):
          "// Crossing-edge masks (equal to EDGE_CROSSING_MASK, marching_cubes_tables.rs:49-70).",
          "ISO_TABLE uint16_t iso_edge_mask[256] = {",
          fmt_rows(masks, 16, lambda v: "0x%03x" % v),
-         "};", ""]
+         "};"]
+    rank, slot = derive_ranks(t)
+    s += ["// Edges each boundary class (x==0) | (y==0)<<1 | (z==0)<<2 is the first visitor of.",
+          "ISO_TABLE uint16_t iso_owned_mask[8] = {" + ", ".join("0x%03x" % owned_mask(t, c) for c in range(8)) + "};",
+          "// Per class and case, 4 bits per edge: owned edges of that class before the edge in first-use order.",
+          "ISO_TABLE uint64_t iso_owned_rank[8][256] = {"]
+    for cls in range(8):
+        s.append("  {")
+        s.append(fmt_rows(rank[cls], 4, lambda v: "0x%012xull" % v))
+        s.append("  },")
+    s += ["};",
+          "// Per case, 4 bits per triangle vertex: index of its edge in the first-use order.",
+          "ISO_TABLE uint64_t iso_tri_slot[256] = {",
+          fmt_rows(slot, 4, lambda v: "0x%015xull" % v),
+          "};", ""]
     open(path, "w").write("\n".join(s))
 
 

@@ -511,465 +511,7 @@ __device__ __forceinline__ uint32_t owned_count(const Corners& q, uint32_t sel, 
     return n;
 }
 
-struct ChunkCountArgs {
-    const uint32_t* bits;
-    uint32_t W, CW, nx, ny, nz;
-    uint64_t chunks;
-    uint2* base;          // chunks + 1: (vertex base, triangle base), exclusive
-    uint64_t* status;
-    uint32_t* ticket;
-    uint64_t* totals;     // [0] triangles [1] vertices
-    uint32_t* err;
-};
-
-constexpr int CHUNK_ROUNDS = 4;  // chunks per thread; a block covers 1024 chunks
-
-// Pass 1: counts per chunk + decoupled look-back scan over blocks.
-__global__ void __launch_bounds__(256) mc_chunk_count_scan(ChunkCountArgs A) {
-    __shared__ uint8_t s_ntri[256];
-    __shared__ uint16_t s_owned[8];
-    __shared__ uint32_t s_bid;
-    __shared__ uint32_t s_wt[8], s_wv[8];
-    __shared__ uint64_t s_excl_t, s_excl_v;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    s_ntri[threadIdx.x] = iso_tri_count[threadIdx.x];
-    if (threadIdx.x < 8) s_owned[threadIdx.x] = (uint16_t)owned_mask(threadIdx.x);
-    if (threadIdx.x == 0) s_bid = atomicAdd(A.ticket, 1u);
-    __syncthreads();
-    const uint32_t bid = s_bid;
-    const uint32_t ncx = A.nx - 1, ncy = A.ny - 1;
-    uint32_t my_t[CHUNK_ROUNDS], my_v[CHUNK_ROUNDS];
-    uint32_t agg_t = 0, agg_v = 0;
-#pragma unroll
-    for (int r = 0; r < CHUNK_ROUNDS; ++r) {
-        const uint64_t ch = (uint64_t)bid * (256 * CHUNK_ROUNDS) + r * 256 + threadIdx.x;
-        uint32_t t = 0, v = 0;
-        if (ch < A.chunks) {
-            const uint32_t c = (uint32_t)(ch % A.CW);
-            const uint64_t row = ch / A.CW;
-            const uint32_t y = (uint32_t)(row % ncy), z = (uint32_t)(row / ncy);
-            const Corners q = load_corners(A.bits, A.W, A.ny, y, z, c);
-            const uint32_t valid = chunk_valid(c, ncx);
-            uint32_t act = active_cells(q, valid);
-            const int cls = (y == 0 ? 2 : 0) | (z == 0 ? 4 : 0);
-            v = owned_count(q, act, s_owned[cls], s_owned[cls | 1], c == 0 ? 1u : 0u);
-            while (act) {
-                const uint32_t i = __ffs(act) - 1;
-                act &= act - 1;
-                t += s_ntri[case_at(q, i)];
-            }
-        }
-        my_t[r] = t;
-        my_v[r] = v;
-        // block-wide exclusive scan of this round
-        uint32_t ti = warp_incl_scan(t, lane), vi = warp_incl_scan(v, lane);
-        if (lane == 31) {
-            s_wt[warp] = ti;
-            s_wv[warp] = vi;
-        }
-        __syncthreads();
-        uint32_t bt = 0, bv = 0, tt = 0, tv = 0;
-#pragma unroll
-        for (int w = 0; w < 8; ++w) {
-            if (w < warp) {
-                bt += s_wt[w];
-                bv += s_wv[w];
-            }
-            tt += s_wt[w];
-            tv += s_wv[w];
-        }
-        my_t[r] = agg_t + bt + ti - t;  // exclusive within the block
-        my_v[r] = agg_v + bv + vi - v;
-        agg_t += tt;
-        agg_v += tv;
-        __syncthreads();
-    }
-    if (warp == 0) {
-        volatile uint64_t* st = A.status;
-        if (lane == 0) {
-            __threadfence();
-            st[bid] = pack(bid == 0 ? FLAG_P : FLAG_A, agg_t, agg_v);
-        }
-        uint64_t ex_t = 0, ex_v = 0;
-        if (bid > 0) {
-            int64_t base = (int64_t)bid - 1;
-            while (true) {
-                const int64_t j = base - lane;
-                uint64_t s = FLAG_P;
-                if (j >= 0) {
-                    uint32_t it = 0;
-                    s = st[j];
-                    while ((s & FLAG_MASK) == 0 && it < SPIN_LIMIT) {
-                        __nanosleep(32);
-                        s = st[j];
-                        ++it;
-                    }
-                    if ((s & FLAG_MASK) == 0) {
-                        atomicOr(A.err, DERR_SCAN_TIMEOUT);
-                        s = FLAG_P;
-                    }
-                }
-                const uint32_t pmask = __ballot_sync(FULL, (s & FLAG_MASK) == FLAG_P);
-                const int first = pmask ? __ffs(pmask) - 1 : 32;
-                uint64_t ct = lane <= first ? unpack_t(s) : 0, cv = lane <= first ? unpack_v(s) : 0;
-                for (int o = 16; o > 0; o >>= 1) {
-                    ct += __shfl_xor_sync(FULL, ct, o);
-                    cv += __shfl_xor_sync(FULL, cv, o);
-                }
-                ex_t += ct;
-                ex_v += cv;
-                if (pmask) break;
-                base -= 32;
-            }
-            if (lane == 0) {
-                const uint64_t it_ = ex_t + agg_t, iv_ = ex_v + agg_v;
-                if (it_ > F31 || iv_ > F31) atomicOr(A.err, DERR_CAPACITY);
-                __threadfence();
-                st[bid] = pack(FLAG_P, it_ & F31, iv_ & F31);
-            }
-        }
-        if (lane == 0) {
-            s_excl_t = ex_t;
-            s_excl_v = ex_v;
-            if (bid == gridDim.x - 1) {
-                A.totals[0] = ex_t + agg_t;
-                A.totals[1] = ex_v + agg_v;
-                A.base[A.chunks] = make_uint2((uint32_t)(ex_v + agg_v), (uint32_t)(ex_t + agg_t));
-            }
-        }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < CHUNK_ROUNDS; ++r) {
-        const uint64_t ch = (uint64_t)bid * (256 * CHUNK_ROUNDS) + r * 256 + threadIdx.x;
-        if (ch < A.chunks) A.base[ch] = make_uint2((uint32_t)(s_excl_v + my_v[r]), (uint32_t)(s_excl_t + my_t[r]));
-    }
-}
-
-struct ChunkEmitArgs {
-    const uint32_t* bits;
-    const float* values;
-    const float4* positions;  // null: regular grid
-    uint64_t pitch;
-    uint32_t W, CW, nx, ny, nz;
-    uint64_t chunks;
-    float inv;
-    const uint2* base;
-    float* out_v;
-    uint32_t* out_i;
-    uint64_t* out_k;
-    uint64_t cap_v, cap_t;
-    uint32_t* err;
-};
-
-// Vertex id of the edge `e` owned (in its first-use rank) by cell (ox, oy, oz).
-__device__ __forceinline__ uint32_t owner_vertex_id(const ChunkEmitArgs& A, const Tables& tb, uint32_t ox, uint32_t oy,
-                                                    uint32_t oz, uint32_t oe) {
-    const uint32_t c = ox >> 5, i = ox & 31;
-    const Corners q = load_corners(A.bits, A.W, A.ny, oy, oz, c);
-    const int cls = (oy == 0 ? 2 : 0) | (oz == 0 ? 4 : 0);
-    const uint32_t before = (1u << i) - 1u;  // cells without a crossing edge own nothing
-    const uint32_t own = tb.owned[cls], own0 = tb.owned[cls | 1];
-    const uint32_t cell0 = c == 0 ? 1u : 0u;
-    const uint32_t prior = owned_count(q, before, own, own0, cell0);
-    const uint32_t ocs = case_at(q, i);
-    const uint32_t oown = (ox == 0) ? own0 : own;
-    const uint64_t ch = ((uint64_t)oz * (A.ny - 1) + oy) * A.CW + c;
-    return __ldg(&A.base[ch].x) + prior + owned_rank(tb, ocs, oown, oe);
-}
-
-// Pass 2: one thread per chunk; writes the chunk's owned vertices and its triangles.
-__global__ void __launch_bounds__(256) mc_chunk_emit(ChunkEmitArgs A) {
-    __shared__ Tables tb;
-    load_tables(&tb, true);
-    __syncthreads();
-    const uint64_t ch = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (ch >= A.chunks) return;
-    const uint2 b0 = __ldg(&A.base[ch]);
-    const uint32_t t_end = __ldg(&A.base[ch + 1].y);
-    if (b0.y == t_end) return;  // no triangle in this chunk
-    const uint32_t ncx = A.nx - 1, ncy = A.ny - 1;
-    const uint32_t c = (uint32_t)(ch % A.CW);
-    const uint64_t row = ch / A.CW;
-    const uint32_t y = (uint32_t)(row % ncy), z = (uint32_t)(row / ncy);
-    const Corners q = load_corners(A.bits, A.W, A.ny, y, z, c);
-    uint32_t act = active_cells(q, chunk_valid(c, ncx));
-    const int cls_yz = (y == 0 ? 2 : 0) | (z == 0 ? 4 : 0);
-    const bool explicit_pos = A.positions != nullptr;
-    uint32_t vcur = b0.x, tcur = b0.y;
-    while (act) {
-        const uint32_t i = __ffs(act) - 1;
-        act &= act - 1;
-        const uint32_t x = 32 * c + i;
-        const uint32_t cs = case_at(q, i);
-        const uint32_t own = tb.owned[cls_yz | (x == 0 ? 1 : 0)];
-        // owned vertices in first-use order
-        const uint64_t ord = tb.edge_order[cs];
-        const uint32_t ne = tb.edge_count[cs];
-        uint32_t r = 0;
-        for (uint32_t k = 0; k < ne; ++k) {
-            const uint32_t e = (uint32_t)(ord >> (4 * k)) & 15u;
-            if (!((own >> e) & 1u)) continue;
-            const uint32_t u = iso_edge_connection[e][0], v = iso_edge_connection[e][1];
-            const uint32_t ux = x + iso_corners[u][0], uy = y + iso_corners[u][1], uz = z + iso_corners[u][2];
-            const uint32_t vx = x + iso_corners[v][0], vy = y + iso_corners[v][1], vz = z + iso_corners[v][2];
-            const float fa = __ldg(A.values + ((uint64_t)uz * A.ny + uy) * A.pitch + ux);
-            const float fb = __ldg(A.values + ((uint64_t)vz * A.ny + vy) * A.pitch + vx);
-            float pax, pay, paz, pbx, pby, pbz;
-            if (explicit_pos) {
-                const float4 qa = __ldg(A.positions + ((uint64_t)uz * A.ny + uy) * A.nx + ux);
-                const float4 qb = __ldg(A.positions + ((uint64_t)vz * A.ny + vy) * A.nx + vx);
-                pax = qa.x; pay = qa.y; paz = qa.z; pbx = qb.x; pby = qb.y; pbz = qb.z;
-            } else {
-                pax = (float)ux * A.inv; pay = (float)uy * A.inv; paz = (float)uz * A.inv;
-                pbx = (float)vx * A.inv; pby = (float)vy * A.inv; pbz = (float)vz * A.inv;
-            }
-            // Signed::find_crossing_point (distance.rs:64-69)
-            const float delta = fb - fa;
-            const float t = (delta == 0.0f) ? 0.5f : -fa / delta;
-            const float omt = 1.0f - t;
-            const uint64_t vid = (uint64_t)vcur + r;
-            if (vid < A.cap_v) {
-                A.out_v[3 * vid + 0] = pax * omt + pbx * t;
-                A.out_v[3 * vid + 1] = pay * omt + pby * t;
-                A.out_v[3 * vid + 2] = paz * omt + pbz * t;
-                if (A.out_k) {
-                    const uint32_t lx = x + c_edge_lo[e][0], ly = y + c_edge_lo[e][1], lz = z + c_edge_lo[e][2];
-                    A.out_k[2 * vid] = (((uint64_t)lz * A.ny + ly) * A.nx + lx) * 3 + c_edge_axis[e];
-                    A.out_k[2 * vid + 1] = 0;
-                }
-            } else {
-                atomicOr(A.err, DERR_CAPACITY);
-            }
-            ++r;
-        }
-        // triangles (march_cube, marching_cubes_impl.rs:102-117)
-        const uint64_t te = tb.tri_edges[cs];
-        const uint32_t nt = tb.tri_count[cs];
-        for (uint32_t k = 0; k < 3 * nt; ++k) {
-            const uint32_t e = (uint32_t)(te >> (4 * k)) & 15u;
-            uint32_t id;
-            if ((own >> e) & 1u) {
-                id = vcur + owned_rank(tb, cs, own, e);
-            } else {
-                const uint32_t ax = c_edge_axis[e];
-                const uint32_t lx = x + c_edge_lo[e][0], ly = y + c_edge_lo[e][1], lz = z + c_edge_lo[e][2];
-                uint32_t ox = lx, oy = ly, oz = lz, d1, d2;
-                if (ax != 0) ox = lx > 0 ? lx - 1 : 0;
-                if (ax != 1) oy = ly > 0 ? ly - 1 : 0;
-                if (ax != 2) oz = lz > 0 ? lz - 1 : 0;
-                if (ax == 0) { d1 = ly - oy; d2 = lz - oz; }
-                else if (ax == 1) { d1 = lx - ox; d2 = lz - oz; }
-                else { d1 = lx - ox; d2 = ly - oy; }
-                id = owner_vertex_id(A, tb, ox, oy, oz, c_local_edge[ax][d1 + 2 * d2]);
-            }
-            const uint64_t at = 3ull * tcur + k;
-            if (at < 3 * A.cap_t) A.out_i[at] = id;
-            else atomicOr(A.err, DERR_CAPACITY);
-        }
-        vcur += r;
-        tcur += nt;
-    }
-}
-
-// Pass 2 (block form).  Block b owns chunks [c0, c0+256).  Every non-owned
-// edge of a cell in those chunks is owned by a cell in chunk ch-1, ch-CW or
-// ch-CW-1 (same layer) or ch-S, ch-S-1, ch-S-CW, ch-S-CW-1 (layer below,
-// S = CW*(ny-1)), so the block caches the corner vectors and vertex bases of
-// the bands R1 = [c0-CW-1, c0+256) and R2 = R1 - S in shared memory.  Active
-// cells are compacted in chunk order and processed one per thread in rounds of
-// 256, with block scans giving each cell's output offsets.
-constexpr int EMIT_LIST_CAP = 256 * 32;
-
-size_t block_emit_smem(uint32_t CW) {
-    const size_t span = 256 + CW + 1;
-    return sizeof(Tables) + 2 * span * 8 * 4 + 2 * span * 4 + EMIT_LIST_CAP * 2;
-}
-
-__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_w, uint32_t* total) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t inc = warp_incl_scan(v, lane);
-    if (lane == 31) s_w[warp] = inc;
-    __syncthreads();
-    uint32_t before = 0, all = 0;
-#pragma unroll
-    for (int w = 0; w < 8; ++w) {
-        const uint32_t t = s_w[w];
-        if (w < warp) before += t;
-        all += t;
-    }
-    __syncthreads();
-    *total = all;
-    return before + inc - v;
-}
-
-__global__ void __launch_bounds__(256) mc_block_emit(ChunkEmitArgs A) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ uint32_t s_w[8], s_w2[8];
-    Tables& tb = *reinterpret_cast<Tables*>(smem);
-    const uint32_t CW = A.CW, ncx = A.nx - 1, ncy = A.ny - 1;
-    const int64_t span = 256 + CW + 1;
-    uint32_t* q1 = reinterpret_cast<uint32_t*>(smem + sizeof(Tables));
-    uint32_t* q2 = q1 + span * 8;
-    uint32_t* vb1 = q2 + span * 8;
-    uint32_t* vb2 = vb1 + span;
-    uint16_t* list = reinterpret_cast<uint16_t*>(vb2 + span);
-    const int64_t c0 = (int64_t)blockIdx.x * 256;
-    const int64_t S = (int64_t)CW * ncy;
-    const int64_t r1 = c0 - CW - 1, r2 = r1 - S;
-    const uint2 bb = __ldg(&A.base[c0]);
-    const uint64_t c_end = min((uint64_t)c0 + 256, A.chunks);
-    if (__ldg(&A.base[c_end].y) == bb.y) return;  // no triangle in the block
-    load_tables(&tb, true);
-    for (int64_t i = threadIdx.x; i < 2 * span; i += 256) {
-        const int64_t ch = (i < span) ? r1 + i : r2 + (i - span);
-        if (ch < 0 || ch >= (int64_t)A.chunks) continue;
-        const uint32_t c = (uint32_t)(ch % CW);
-        const uint64_t row = (uint64_t)ch / CW;
-        const Corners q = load_corners(A.bits, A.W, A.ny, (uint32_t)(row % ncy), (uint32_t)(row / ncy), c);
-        uint32_t* dst = (i < span) ? q1 + i * 8 : q2 + (i - span) * 8;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) dst[k] = q.k[k];
-        ((i < span) ? vb1 : vb2)[(i < span) ? i : i - span] = __ldg(&A.base[ch].x);
-    }
-    __syncthreads();
-
-    // compact the block's active cells, in chunk order
-    const uint64_t mych = (uint64_t)c0 + threadIdx.x;
-    uint32_t act = 0;
-    if (mych < A.chunks) {
-        Corners q;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) q.k[k] = q1[(CW + 1 + threadIdx.x) * 8 + k];
-        act = active_cells(q, chunk_valid((uint32_t)(mych % CW), ncx));
-    }
-    uint32_t nlist;
-    uint32_t pos = block_excl_scan(__popc(act), s_w, &nlist);
-    while (act) {
-        const uint32_t i = __ffs(act) - 1;
-        act &= act - 1;
-        list[pos++] = (uint16_t)((threadIdx.x << 5) | i);
-    }
-    __syncthreads();
-
-    const bool explicit_pos = A.positions != nullptr;
-    uint32_t vcarry = bb.x, tcarry = bb.y;
-    for (uint32_t r0 = 0; r0 < nlist; r0 += 256) {
-        const uint32_t j = r0 + threadIdx.x;
-        const bool have = j < nlist;
-        uint32_t x = 0, y = 0, z = 0, cs = 0, own = 0, nown = 0, nt = 0;
-        if (have) {
-            const uint32_t ent = list[j];
-            const uint32_t t = ent >> 5, i = ent & 31;
-            const uint64_t ch = (uint64_t)c0 + t;
-            const uint64_t row = ch / CW;
-            y = (uint32_t)(row % ncy);
-            z = (uint32_t)(row / ncy);
-            x = 32 * (uint32_t)(ch % CW) + i;
-            uint32_t cs_ = 0;
-#pragma unroll
-            for (int k = 0; k < 8; ++k) cs_ |= ((q1[(CW + 1 + t) * 8 + k] >> i) & 1u) << k;
-            cs = cs_;
-            own = tb.owned[(x == 0 ? 1 : 0) | (y == 0 ? 2 : 0) | (z == 0 ? 4 : 0)];
-            nown = __popc((uint32_t)tb.edge_mask[cs] & own);
-            nt = tb.tri_count[cs];
-        }
-        uint32_t vtot, ttot;
-        const uint32_t vpre = block_excl_scan(nown, s_w, &vtot);
-        const uint32_t tpre = block_excl_scan(nt, s_w2, &ttot);
-        if (have) {
-            const uint32_t vstart = vcarry + vpre;
-            // owned vertices in first-use order; the field loads are issued first
-            const uint64_t ord = tb.edge_order[cs];
-            const uint32_t ne = tb.edge_count[cs];
-            uint32_t r = 0;
-            for (uint32_t k = 0; k < ne; ++k) {
-                const uint32_t e = (uint32_t)(ord >> (4 * k)) & 15u;
-                if (!((own >> e) & 1u)) continue;
-                const uint32_t u = iso_edge_connection[e][0], v = iso_edge_connection[e][1];
-                const uint32_t ux = x + iso_corners[u][0], uy = y + iso_corners[u][1], uz = z + iso_corners[u][2];
-                const uint32_t vx = x + iso_corners[v][0], vy = y + iso_corners[v][1], vz = z + iso_corners[v][2];
-                const float fa = __ldg(A.values + ((uint64_t)uz * A.ny + uy) * A.pitch + ux);
-                const float fb = __ldg(A.values + ((uint64_t)vz * A.ny + vy) * A.pitch + vx);
-                float pax, pay, paz, pbx, pby, pbz;
-                if (explicit_pos) {
-                    const float4 qa = __ldg(A.positions + ((uint64_t)uz * A.ny + uy) * A.nx + ux);
-                    const float4 qb = __ldg(A.positions + ((uint64_t)vz * A.ny + vy) * A.nx + vx);
-                    pax = qa.x; pay = qa.y; paz = qa.z; pbx = qb.x; pby = qb.y; pbz = qb.z;
-                } else {
-                    pax = (float)ux * A.inv; pay = (float)uy * A.inv; paz = (float)uz * A.inv;
-                    pbx = (float)vx * A.inv; pby = (float)vy * A.inv; pbz = (float)vz * A.inv;
-                }
-                // Signed::find_crossing_point (distance.rs:64-69)
-                const float delta = fb - fa;
-                const float tt = (delta == 0.0f) ? 0.5f : -fa / delta;
-                const float omt = 1.0f - tt;
-                const uint64_t vid = (uint64_t)vstart + r;
-                if (vid < A.cap_v) {
-                    A.out_v[3 * vid + 0] = pax * omt + pbx * tt;
-                    A.out_v[3 * vid + 1] = pay * omt + pby * tt;
-                    A.out_v[3 * vid + 2] = paz * omt + pbz * tt;
-                    if (A.out_k) {
-                        const uint32_t lx = x + c_edge_lo[e][0], ly = y + c_edge_lo[e][1], lz = z + c_edge_lo[e][2];
-                        A.out_k[2 * vid] = (((uint64_t)lz * A.ny + ly) * A.nx + lx) * 3 + c_edge_axis[e];
-                        A.out_k[2 * vid + 1] = 0;
-                    }
-                } else {
-                    atomicOr(A.err, DERR_CAPACITY);
-                }
-                ++r;
-            }
-            // triangles (march_cube, marching_cubes_impl.rs:102-117)
-            const uint64_t te = tb.tri_edges[cs];
-            const uint64_t tstart = (uint64_t)tcarry + tpre;
-            for (uint32_t k = 0; k < 3 * nt; ++k) {
-                const uint32_t e = (uint32_t)(te >> (4 * k)) & 15u;
-                uint32_t id;
-                if ((own >> e) & 1u) {
-                    id = vstart + owned_rank(tb, cs, own, e);
-                } else {
-                    const uint32_t ax = c_edge_axis[e];
-                    const uint32_t lx = x + c_edge_lo[e][0], ly = y + c_edge_lo[e][1], lz = z + c_edge_lo[e][2];
-                    uint32_t ox = lx, oy = ly, oz = lz, d1, d2;
-                    if (ax != 0) ox = lx > 0 ? lx - 1 : 0;
-                    if (ax != 1) oy = ly > 0 ? ly - 1 : 0;
-                    if (ax != 2) oz = lz > 0 ? lz - 1 : 0;
-                    if (ax == 0) { d1 = ly - oy; d2 = lz - oz; }
-                    else if (ax == 1) { d1 = lx - ox; d2 = lz - oz; }
-                    else { d1 = lx - ox; d2 = ly - oy; }
-                    const uint32_t oe = c_local_edge[ax][d1 + 2 * d2];
-                    const uint32_t oc = ox >> 5, oi = ox & 31;
-                    const int64_t och = ((int64_t)oz * ncy + oy) * CW + oc;
-                    const uint32_t* oq;
-                    uint32_t obase;
-                    if (och >= r1 && och < r1 + span) {
-                        oq = q1 + (och - r1) * 8;
-                        obase = vb1[och - r1];
-                    } else if (och >= r2 && och < r2 + span) {
-                        oq = q2 + (och - r2) * 8;
-                        obase = vb2[och - r2];
-                    } else {
-                        atomicOr(A.err, DERR_CAPACITY);
-                        oq = q1;
-                        obase = 0;
-                    }
-                    Corners q;
-#pragma unroll
-                    for (int kk = 0; kk < 8; ++kk) q.k[kk] = oq[kk];
-                    const int ocls = (oy == 0 ? 2 : 0) | (oz == 0 ? 4 : 0);
-                    const uint32_t oown = tb.owned[ocls], oown0 = tb.owned[ocls | 1];
-                    const uint32_t prior = owned_count(q, (1u << oi) - 1u, oown, oown0, oc == 0 ? 1u : 0u);
-                    id = obase + prior + owned_rank(tb, case_at(q, oi), ox == 0 ? oown0 : oown, oe);
-                }
-                const uint64_t at = 3 * tstart + k;
-                if (at < 3 * A.cap_t) A.out_i[at] = id;
-                else atomicOr(A.err, DERR_CAPACITY);
-            }
-        }
-        vcarry += vtot;
-        tcarry += ttot;
-    }
-}
+#include "mc_chunk.cuh"
 
 __global__ void mc_cases_kernel(const uint32_t* bits, uint32_t W, uint32_t nx, uint32_t ny, uint32_t nz,
                                 uint8_t* out) {
@@ -1023,26 +565,26 @@ iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, is
     const uint32_t ncx = L.nx - 1;
     const uint32_t CW = (ncx + 31) / 32;
     const uint64_t chunks = (uint64_t)CW * (L.ny - 1) * (L.nz - 1);
-    const uint64_t per_block = 256 * CHUNK_ROUNDS;
-    const uint64_t nblocks = (chunks + per_block - 1) / per_block;
-    if (nblocks >= (1ull << 31)) return fail(ctx, ISO_ERR_TOO_LARGE, "grid too large");
+    if (chunks >= 0xFFFFFFF0ull) return fail(ctx, ISO_ERR_TOO_LARGE, "grid too large");
+    const uint32_t nranges = (uint32_t)((chunks + RANGE - 1) / RANGE);
+    const FastDiv div_cw = make_fastdiv(CW), div_ncy = make_fastdiv(L.ny - 1);
     iso_status s;
     if ((s = ensure(ctx, ctx->rowtri, 8 * (chunks + 1))) != ISO_OK) return s;
-    if ((s = ensure(ctx, ctx->scan, 8 * (size_t)nblocks + 64)) != ISO_OK) return s;
-    uint64_t* status = (uint64_t*)ctx->scan.p;
-    uint32_t* ticket = (uint32_t*)(status + nblocks);
-    uint64_t* totals = (uint64_t*)(status + nblocks + 2);
-    uint2* base = (uint2*)ctx->rowtri.p;
-    cudaError_t e = cudaMemsetAsync(ctx->scan.p, 0, 8 * (size_t)nblocks + 64, ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "memset scan state");
-    ChunkCountArgs ca{L.bits, L.words_per_row, CW, L.nx, L.ny, L.nz, chunks, base, status, ticket, totals, ctx->d_err};
+    if ((s = ensure(ctx, ctx->scan, 16 * (size_t)nranges + 64)) != ISO_OK) return s;
+    uint2* local = (uint2*)ctx->rowtri.p;
+    uint2* rangeagg = (uint2*)ctx->scan.p;
+    uint2* rangepre = rangeagg + nranges;
+    uint64_t* totals = (uint64_t*)(rangepre + nranges + 2);
+    ChunkCountArgs ca{L.bits, L.words_per_row, CW, L.nx, L.ny, L.nz, (uint32_t)chunks, div_cw, div_ncy, local, rangeagg};
     {
         StageTimer timer(ctx, ISO_STAGE_CLASSIFY);
-        mc_chunk_count_scan<<<(unsigned)nblocks, 256, 0, ctx->stream>>>(ca);
+        mc_chunk_count<<<(nranges + 7) / 8, 256, 0, ctx->stream>>>(ca);
+        mc_range_scan<<<1, 1024, 0, ctx->stream>>>(rangeagg, nranges, rangepre, totals, local, (uint32_t)chunks,
+                                                   ctx->d_err);
     }
-    ctx->launches++;
-    if ((s = check_launch(ctx, "mc_chunk_count_scan")) != ISO_OK) return s;
-    e = cudaMemcpyAsync(ctx->h_pinned, totals, 16, cudaMemcpyDeviceToHost, ctx->stream);
+    ctx->launches += 2;
+    if ((s = check_launch(ctx, "mc_chunk_count")) != ISO_OK) return s;
+    cudaError_t e = cudaMemcpyAsync(ctx->h_pinned, totals, 16, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_pinned + 2, ctx->d_err, 4, cudaMemcpyDeviceToHost, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "read totals");
     e = cudaStreamSynchronize(ctx->stream);
@@ -1056,8 +598,9 @@ iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, is
     if ((s = ensure(ctx, ctx->mesh_i, 12 * std::max<uint64_t>(nt, 1))) != ISO_OK) return s;
     if (keys && (s = ensure(ctx, ctx->mesh_k, 16 * std::max<uint64_t>(nv, 1))) != ISO_OK) return s;
     if (nt > 0) {
-        ChunkEmitArgs ea{L.bits, L.values, L.positions, L.pitch, L.words_per_row, CW, L.nx, L.ny, L.nz, chunks, L.inv,
-                         base, (float*)ctx->mesh_v.p, (uint32_t*)ctx->mesh_i.p,
+        ChunkEmitArgs ea{L.bits, L.values, L.positions, L.pitch, L.words_per_row, CW, L.nx, L.ny, L.nz,
+                         (uint32_t)chunks, div_cw, div_ncy, L.inv, local, rangepre, (float*)ctx->mesh_v.p,
+                         (uint32_t*)ctx->mesh_i.p,
                          keys ? (uint64_t*)ctx->mesh_k.p : nullptr, nv, nt, ctx->d_err};
         const size_t smem = block_emit_smem(CW);
         if (smem > 220 * 1024) return fail(ctx, ISO_ERR_INVALID_ARG, "rows too long for the emit pass");

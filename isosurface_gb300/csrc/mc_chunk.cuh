@@ -1,0 +1,388 @@
+// Chunked marching-cubes passes (included by mc.cu inside iso::{anonymous}).
+//
+// A chunk is 32 consecutive cells of a row (x = 32c .. 32c+31); chunk id =
+// row * CW + c with CW = ceil((nx-1)/32), which is the reference's (z, y, x)
+// visit order.  A chunk's eight corner bit-vectors (bit i: corner k of cell
+// 32c+i is inside) come from four sign-bit rows with funnel shifts, so
+// activity and owned-vertex counts cost a few dozen bit operations per 32
+// cells.  Offsets: pass 1 gives every chunk its exclusive prefix inside a
+// range of RANGE chunks (one warp's work) plus each range's total; a one-block
+// scan turns range totals into range offsets; chunk base = range offset +
+// in-range prefix.  Corners, load_corners, case_at, chunk_valid, active_cells
+// and owned_count are defined in mc.cu above the include.
+
+constexpr uint32_t RANGE = 256;  // chunks per counting warp / per emit block
+constexpr int RANGE_ROUNDS = RANGE / 32;
+constexpr uint32_t OWN_INTERIOR = 0x460;  // edges 5, 6, 10: the far-corner edges
+
+// q = n / d for n < 2^32, d < 2^31, with m = floor(2^64 / d) + 1 (d > 1)
+struct FastDiv {
+    uint32_t d;
+    uint64_t m;
+};
+inline FastDiv make_fastdiv(uint32_t d) { return FastDiv{d, d > 1 ? (~0ull / d + 1) : 0ull}; }
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
+    return f.d == 1 ? n : (uint32_t)__umul64hi((uint64_t)n, f.m);
+}
+
+struct ChunkCountArgs {
+    const uint32_t* bits;
+    uint32_t W, CW, nx, ny, nz;
+    uint32_t chunks;
+    FastDiv div_cw, div_ncy;
+    uint2* local;      // chunks + 1: (vertex, triangle) exclusive prefix inside the range
+    uint2* rangeagg;   // per range: (vertices, triangles)
+};
+
+// Pass 1: per-chunk counts, in-range prefixes (one warp per range, no barriers).
+__global__ void __launch_bounds__(256) mc_chunk_count(ChunkCountArgs A) {
+    __shared__ uint8_t s_ntri[256];
+    __shared__ uint16_t s_owned[8];
+    const int lane = threadIdx.x & 31;
+    s_ntri[threadIdx.x] = iso_tri_count[threadIdx.x];
+    if (threadIdx.x < 8) s_owned[threadIdx.x] = iso_owned_mask[threadIdx.x];
+    __syncthreads();
+    const uint32_t range = blockIdx.x * 8 + (threadIdx.x >> 5);
+    const uint32_t ncx = A.nx - 1;
+    uint32_t agg_t = 0, agg_v = 0;
+    for (int r = 0; r < RANGE_ROUNDS; ++r) {
+        const uint32_t ch = range * RANGE + r * 32 + lane;
+        uint32_t t = 0, v = 0;
+        if (ch < A.chunks) {
+            const uint32_t row = fdiv(ch, A.div_cw);
+            const uint32_t c = ch - row * A.CW;
+            const uint32_t z = fdiv(row, A.div_ncy);
+            const uint32_t y = row - z * (A.ny - 1);
+            const Corners q = load_corners(A.bits, A.W, A.ny, y, z, c);
+            uint32_t act = active_cells(q, chunk_valid(c, ncx));
+            if (act) {
+                const int cls = (y == 0 ? 2 : 0) | (z == 0 ? 4 : 0);
+                v = owned_count(q, act, s_owned[cls], s_owned[cls | 1], c == 0 ? 1u : 0u);
+                while (act) {
+                    const uint32_t i = __ffs(act) - 1;
+                    act &= act - 1;
+                    t += s_ntri[case_at(q, i)];
+                }
+            }
+        }
+        const uint32_t ti = warp_incl_scan(t, lane), vi = warp_incl_scan(v, lane);
+        if (ch <= A.chunks) A.local[ch] = make_uint2(agg_v + vi - v, agg_t + ti - t);
+        agg_t += __shfl_sync(FULL, ti, 31);
+        agg_v += __shfl_sync(FULL, vi, 31);
+    }
+    if (lane == 0 && range * RANGE < A.chunks + 1) A.rangeagg[range] = make_uint2(agg_v, agg_t);
+}
+
+// Exclusive scan of the range totals (one block).  rangepre[nr] and totals
+// receive the grand totals; local[chunks] is cleared when `chunks` starts a
+// range that no warp counted.
+__global__ void __launch_bounds__(1024) mc_range_scan(const uint2* rangeagg, uint32_t nr, uint2* rangepre,
+                                                      uint64_t* totals, uint2* local, uint32_t chunks, uint32_t* err) {
+    __shared__ uint64_t s_wt[32], s_wv[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint64_t carry_t = 0, carry_v = 0;
+    for (uint32_t base = 0; base < nr; base += 1024) {
+        const uint32_t i = base + threadIdx.x;
+        const uint2 a = i < nr ? rangeagg[i] : make_uint2(0, 0);
+        uint64_t vi = a.x, ti = a.y;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t tv = __shfl_up_sync(FULL, vi, o), tt = __shfl_up_sync(FULL, ti, o);
+            if (lane >= o) {
+                vi += tv;
+                ti += tt;
+            }
+        }
+        if (lane == 31) {
+            s_wv[warp] = vi;
+            s_wt[warp] = ti;
+        }
+        __syncthreads();
+        uint64_t bv = 0, bt = 0, av = 0, at = 0;
+        for (int w = 0; w < 32; ++w) {
+            if (w < warp) {
+                bv += s_wv[w];
+                bt += s_wt[w];
+            }
+            av += s_wv[w];
+            at += s_wt[w];
+        }
+        const uint64_t ev = carry_v + bv + vi - a.x, et = carry_t + bt + ti - a.y;
+        if (i < nr) {
+            if (ev > 0xFFFFFFFFull || et > 0xFFFFFFFFull) atomicOr(err, DERR_CAPACITY);
+            rangepre[i] = make_uint2((uint32_t)ev, (uint32_t)et);
+        }
+        carry_v += av;
+        carry_t += at;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        totals[0] = carry_t;
+        totals[1] = carry_v;
+        rangepre[nr] = make_uint2((uint32_t)carry_v, (uint32_t)carry_t);
+        if (chunks % RANGE == 0) local[chunks] = make_uint2(0, 0);
+    }
+}
+
+struct ChunkEmitArgs {
+    const uint32_t* bits;
+    const float* values;
+    const float4* positions;  // null: regular grid
+    uint64_t pitch;
+    uint32_t W, CW, nx, ny, nz;
+    uint32_t chunks;
+    FastDiv div_cw, div_ncy;
+    float inv;
+    const uint2* local;
+    const uint2* rangepre;
+    float* out_v;
+    uint32_t* out_i;
+    uint64_t* out_k;
+    uint64_t cap_v, cap_t;
+    uint32_t* err;
+};
+
+__device__ __forceinline__ uint2 chunk_base(const ChunkEmitArgs& A, uint32_t ch) {
+    const uint2 l = __ldg(&A.local[ch]);
+    const uint2 b = __ldg(&A.rangepre[ch / RANGE]);
+    return make_uint2(l.x + b.x, l.y + b.y);
+}
+
+// Pass 2.  Block b emits chunks [c0, c0+256) (one counting range).  Every
+// non-owned edge of a cell in those chunks is owned by a cell in chunk ch-1,
+// ch-CW or ch-CW-1 (same layer) or ch-S, ch-S-1, ch-S-CW, ch-S-CW-1 (layer
+// below, S = CW*(ny-1)), so the block caches the corner vectors and vertex
+// bases of the bands R1 = [c0-CW-1, c0+256) and R2 = R1 - S in shared memory.
+// Active cells are compacted in chunk order and processed one per thread in
+// rounds of 256, with block scans giving each cell's output offsets; each
+// distinct edge of a cell is resolved to its vertex id once.
+constexpr int EMIT_LIST_CAP = 256 * 32;
+
+struct EmitTables {
+    uint8_t tri_count[256];
+    uint8_t edge_count[256];
+    uint16_t edge_mask[256];
+    uint64_t tri_edges[256];
+    uint64_t edge_order[256];
+    uint64_t tri_slot[256];
+    uint64_t rank[2][256];  // classes 0 (interior) and 1 (x == 0)
+    uint16_t owned[8];
+};
+
+size_t block_emit_smem(uint32_t CW) {
+    const size_t span = RANGE + CW + 1;
+    return ((sizeof(EmitTables) + 15) & ~(size_t)15) + 2 * span * 8 * 4 + 2 * span * 4 + EMIT_LIST_CAP * 2;
+}
+
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_w, uint32_t* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t inc = warp_incl_scan(v, lane);
+    if (lane == 31) s_w[warp] = inc;
+    __syncthreads();
+    uint32_t before = 0, all = 0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) {
+        const uint32_t t = s_w[w];
+        if (w < warp) before += t;
+        all += t;
+    }
+    __syncthreads();
+    *total = all;
+    return before + inc - v;
+}
+
+__device__ __forceinline__ uint32_t rank_of(const EmitTables& tb, int cls, uint32_t cs, uint32_t e) {
+    const uint64_t w = cls < 2 ? tb.rank[cls][cs] : iso_owned_rank[cls][cs];
+    return (uint32_t)(w >> (4 * e)) & 15u;
+}
+
+__global__ void __launch_bounds__(256) mc_block_emit(ChunkEmitArgs A) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ uint32_t s_w[8], s_w2[8];
+    EmitTables& tb = *reinterpret_cast<EmitTables*>(smem);
+    const uint32_t CW = A.CW, ncx = A.nx - 1, ncy = A.ny - 1;
+    const int span = RANGE + (int)CW + 1;
+    uint32_t* q1 = reinterpret_cast<uint32_t*>(smem + ((sizeof(EmitTables) + 15) & ~(size_t)15));
+    uint32_t* q2 = q1 + span * 8;
+    uint32_t* vb1 = q2 + span * 8;
+    uint32_t* vb2 = vb1 + span;
+    uint16_t* list = reinterpret_cast<uint16_t*>(vb2 + span);
+    const uint32_t c0 = blockIdx.x * RANGE;
+    const int64_t S = (int64_t)CW * ncy;
+    const int64_t r1 = (int64_t)c0 - CW - 1, r2 = r1 - S;
+    const uint2 bb = chunk_base(A, c0);
+    const uint32_t c_end = min(c0 + RANGE, A.chunks);
+    if (chunk_base(A, c_end).y == bb.y) return;  // no triangle in the block
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+        tb.tri_count[i] = iso_tri_count[i];
+        tb.edge_count[i] = iso_edge_count[i];
+        tb.edge_mask[i] = iso_edge_mask[i];
+        tb.tri_edges[i] = iso_tri_edges[i];
+        tb.edge_order[i] = iso_edge_order[i];
+        tb.tri_slot[i] = iso_tri_slot[i];
+        tb.rank[0][i] = iso_owned_rank[0][i];
+        tb.rank[1][i] = iso_owned_rank[1][i];
+    }
+    if (threadIdx.x < 8) tb.owned[threadIdx.x] = iso_owned_mask[threadIdx.x];
+    for (int i = threadIdx.x; i < 2 * span; i += 256) {
+        const bool first = i < span;
+        const int64_t ch = first ? r1 + i : r2 + (i - span);
+        if (ch < 0 || ch >= (int64_t)A.chunks) continue;
+        const uint32_t chu = (uint32_t)ch;
+        const uint32_t row = fdiv(chu, A.div_cw);
+        const uint32_t c = chu - row * CW;
+        const uint32_t z = fdiv(row, A.div_ncy);
+        const Corners q = load_corners(A.bits, A.W, A.ny, row - z * ncy, z, c);
+        uint32_t* dst = first ? q1 + i * 8 : q2 + (i - span) * 8;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) dst[k] = q.k[k];
+        (first ? vb1 : vb2)[first ? i : i - span] = chunk_base(A, chu).x;
+    }
+    __syncthreads();
+
+    // compact the block's active cells, in chunk order
+    const uint32_t mych = c0 + threadIdx.x;
+    uint32_t act = 0;
+    if (mych < A.chunks) {
+        Corners q;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) q.k[k] = q1[(CW + 1 + threadIdx.x) * 8 + k];
+        act = active_cells(q, chunk_valid(mych - fdiv(mych, A.div_cw) * CW, ncx));
+    }
+    uint32_t nlist;
+    uint32_t pos = block_excl_scan(__popc(act), s_w, &nlist);
+    while (act) {
+        const uint32_t i = __ffs(act) - 1;
+        act &= act - 1;
+        list[pos++] = (uint16_t)((threadIdx.x << 5) | i);
+    }
+    __syncthreads();
+
+    const bool explicit_pos = A.positions != nullptr;
+    uint32_t vcarry = bb.x, tcarry = bb.y;
+    for (uint32_t r0 = 0; r0 < nlist; r0 += 256) {
+        const uint32_t j = r0 + threadIdx.x;
+        const bool have = j < nlist;
+        uint32_t x = 0, y = 0, z = 0, cs = 0, nown = 0, nt = 0;
+        int cls = 0;
+        if (have) {
+            const uint32_t ent = list[j];
+            const uint32_t t = ent >> 5, i = ent & 31;
+            const uint32_t ch = c0 + t;
+            const uint32_t row = fdiv(ch, A.div_cw);
+            z = fdiv(row, A.div_ncy);
+            y = row - z * ncy;
+            x = 32 * (ch - row * CW) + i;
+            uint32_t cs_ = 0;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) cs_ |= ((q1[(CW + 1 + t) * 8 + k] >> i) & 1u) << k;
+            cs = cs_;
+            cls = (x == 0 ? 1 : 0) | (y == 0 ? 2 : 0) | (z == 0 ? 4 : 0);
+            nown = __popc((uint32_t)tb.edge_mask[cs] & tb.owned[cls]);
+            nt = tb.tri_count[cs];
+        }
+        uint32_t vtot, ttot;
+        const uint32_t vpre = block_excl_scan(nown, s_w, &vtot);
+        const uint32_t tpre = block_excl_scan(nt, s_w2, &ttot);
+        if (have) {
+            const uint32_t own = tb.owned[cls];
+            const uint32_t vstart = vcarry + vpre;
+            const uint64_t ord = tb.edge_order[cs];
+            const uint32_t ne = tb.edge_count[cs];
+            uint32_t ids[12];
+            uint32_t r = 0;
+            for (uint32_t k = 0; k < ne; ++k) {
+                const uint32_t e = (uint32_t)(ord >> (4 * k)) & 15u;
+                if ((own >> e) & 1u) {
+                    // owned: this cell writes the vertex (first use in visit order)
+                    const uint32_t u = iso_edge_connection[e][0], v = iso_edge_connection[e][1];
+                    const uint32_t ux = x + iso_corners[u][0], uy = y + iso_corners[u][1], uz = z + iso_corners[u][2];
+                    const uint32_t vx = x + iso_corners[v][0], vy = y + iso_corners[v][1], vz = z + iso_corners[v][2];
+                    const float fa = __ldg(A.values + ((size_t)uz * A.ny + uy) * A.pitch + ux);
+                    const float fb = __ldg(A.values + ((size_t)vz * A.ny + vy) * A.pitch + vx);
+                    float pax, pay, paz, pbx, pby, pbz;
+                    if (explicit_pos) {
+                        const float4 qa = __ldg(A.positions + ((size_t)uz * A.ny + uy) * A.nx + ux);
+                        const float4 qb = __ldg(A.positions + ((size_t)vz * A.ny + vy) * A.nx + vx);
+                        pax = qa.x; pay = qa.y; paz = qa.z; pbx = qb.x; pby = qb.y; pbz = qb.z;
+                    } else {
+                        pax = (float)ux * A.inv; pay = (float)uy * A.inv; paz = (float)uz * A.inv;
+                        pbx = (float)vx * A.inv; pby = (float)vy * A.inv; pbz = (float)vz * A.inv;
+                    }
+                    // Signed::find_crossing_point (distance.rs:64-69)
+                    const float delta = fb - fa;
+                    const float tt = (delta == 0.0f) ? 0.5f : -fa / delta;
+                    const float omt = 1.0f - tt;
+                    const uint32_t vid = vstart + r;
+                    if (vid < A.cap_v) {
+                        A.out_v[3 * (size_t)vid + 0] = pax * omt + pbx * tt;
+                        A.out_v[3 * (size_t)vid + 1] = pay * omt + pby * tt;
+                        A.out_v[3 * (size_t)vid + 2] = paz * omt + pbz * tt;
+                        if (A.out_k) {
+                            const uint32_t lx = x + c_edge_lo[e][0], ly = y + c_edge_lo[e][1], lz = z + c_edge_lo[e][2];
+                            A.out_k[2 * (size_t)vid] = (((uint64_t)lz * A.ny + ly) * A.nx + lx) * 3 + c_edge_axis[e];
+                            A.out_k[2 * (size_t)vid + 1] = 0;
+                        }
+                    } else {
+                        atomicOr(A.err, DERR_CAPACITY);
+                    }
+                    ids[k] = vid;
+                    ++r;
+                    continue;
+                }
+                // not owned: the lowest (z, y, x) cell adjacent to the lattice edge owns it
+                const uint32_t ax = c_edge_axis[e];
+                const uint32_t lx = x + c_edge_lo[e][0], ly = y + c_edge_lo[e][1], lz = z + c_edge_lo[e][2];
+                uint32_t ox = lx, oy = ly, oz = lz, d1, d2;
+                if (ax != 0) ox = lx > 0 ? lx - 1 : 0;
+                if (ax != 1) oy = ly > 0 ? ly - 1 : 0;
+                if (ax != 2) oz = lz > 0 ? lz - 1 : 0;
+                if (ax == 0) { d1 = ly - oy; d2 = lz - oz; }
+                else if (ax == 1) { d1 = lx - ox; d2 = lz - oz; }
+                else { d1 = lx - ox; d2 = ly - oy; }
+                const uint32_t oe = c_local_edge[ax][d1 + 2 * d2];
+                const uint32_t oc = ox >> 5, oi = ox & 31;
+                const int64_t och = ((int64_t)oz * ncy + oy) * CW + oc;
+                const uint32_t* oq;
+                uint32_t obase;
+                if (och >= r1 && och < r1 + span) {
+                    oq = q1 + (och - r1) * 8;
+                    obase = vb1[och - r1];
+                } else if (och >= r2 && och < r2 + span) {
+                    oq = q2 + (och - r2) * 8;
+                    obase = vb2[och - r2];
+                } else {
+                    atomicOr(A.err, DERR_CAPACITY);
+                    oq = q1;
+                    obase = 0;
+                }
+                Corners q;
+#pragma unroll
+                for (int kk = 0; kk < 8; ++kk) q.k[kk] = oq[kk];
+                const uint32_t sel = (1u << oi) - 1u;
+                const int ocls = (ox == 0 ? 1 : 0) | (oy == 0 ? 2 : 0) | (oz == 0 ? 4 : 0);
+                uint32_t prior;
+                if (oy > 0 && oz > 0) {
+                    // interior row: cells own edges 5 (k5^k6), 6 (k6^k7), 10 (k2^k6);
+                    // the row's x == 0 cell also owns 7 (k7^k4) and 11 (k3^k7)
+                    prior = __popc((q.k[5] ^ q.k[6]) & sel) + __popc((q.k[6] ^ q.k[7]) & sel) +
+                            __popc((q.k[2] ^ q.k[6]) & sel);
+                    if (oc == 0 && oi > 0) prior += ((q.k[7] ^ q.k[4]) & 1u) + ((q.k[3] ^ q.k[7]) & 1u);
+                } else {
+                    const int rcls = (oy == 0 ? 2 : 0) | (oz == 0 ? 4 : 0);
+                    prior = owned_count(q, sel, tb.owned[rcls], tb.owned[rcls | 1], oc == 0 ? 1u : 0u);
+                }
+                ids[k] = obase + prior + rank_of(tb, ocls, case_at(q, oi), oe);
+            }
+            // triangles (march_cube, marching_cubes_impl.rs:102-117)
+            const uint64_t slot = tb.tri_slot[cs];
+            const size_t tstart = (size_t)tcarry + tpre;
+            if (tstart + nt <= A.cap_t) {
+                for (uint32_t k = 0; k < 3 * nt; ++k) A.out_i[3 * tstart + k] = ids[(slot >> (4 * k)) & 15u];
+            } else {
+                atomicOr(A.err, DERR_CAPACITY);
+            }
+        }
+        vcarry += vtot;
+        tcarry += ttot;
+    }
+}

@@ -64,6 +64,37 @@ struct SetArgs {
 
 __device__ __forceinline__ float world(float g, float s, float o, bool dom) { return dom ? g * s + o : g; }
 
+// One thread's z column with the N kept spheres in registers.  (dx*dx + dy*dy)
+// is shared by the whole column and is exactly len_sq's first partial sum.
+template <int N>
+__device__ __forceinline__ void sphere_column(const SetArgs& A, const float4* keep, float px, float py, uint32_t x,
+                                              uint32_t y, uint32_t z0, uint32_t z1, bool valid, int lane) {
+    float dxy[N], cz[N], cr[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        const float4 c = keep[i];
+        const float dx = px - c.x, dy = py - c.y;
+        dxy[i] = dx * dx + dy * dy;
+        cz[i] = c.z;
+        cr[i] = c.w;
+    }
+#pragma unroll 2
+    for (uint32_t z = z0; z <= z1; ++z) {
+        const float pz = world((float)z * A.inv, A.sz, A.oz, A.domain);
+        float dz = pz - cz[0];
+        float v = sqrtf(dxy[0] + dz * dz) - cr[0];
+#pragma unroll
+        for (int i = 1; i < N; ++i) {
+            dz = pz - cz[i];
+            v = fminf(v, sqrtf(dxy[i] + dz * dz) - cr[i]);
+        }
+        const size_t row = (size_t)z * A.ny + y;
+        if (valid) A.field[row * A.pitch + x] = v;
+        const uint32_t b = __ballot_sync(0xFFFFFFFFu, valid && !(v > 0.0f));
+        if (lane == 0) A.bits[row * A.W + blockIdx.x] = b;
+    }
+}
+
 __global__ void __launch_bounds__(256) sample_sphere_set(SetArgs A) {
     extern __shared__ float4 s_keep[];
     __shared__ float s_red[8];
@@ -131,35 +162,14 @@ __global__ void __launch_bounds__(256) sample_sphere_set(SetArgs A) {
     const float px = world((float)x * A.inv, A.sx, A.ox, A.domain);
     const float py = world((float)y * A.inv, A.sy, A.oy, A.domain);
     const bool valid = x < A.nx;
-    if (nk <= KEEP_REGS) {
-        // kept spheres in registers; (dx*dx + dy*dy) is shared by the whole
-        // z column and is exactly the first partial sum of len_sq
-        float dxy[KEEP_REGS], cz[KEEP_REGS], cr[KEEP_REGS];
-#pragma unroll
-        for (int i = 0; i < KEEP_REGS; ++i) {
-            const float4 c = s_keep[i < (int)nk ? i : 0];
-            const float dx = px - c.x, dy = py - c.y;
-            dxy[i] = dx * dx + dy * dy;
-            cz[i] = c.z;
-            cr[i] = c.w;
-        }
-        for (uint32_t z = z0; z <= z1; ++z) {
-            const float pz = world((float)z * A.inv, A.sz, A.oz, A.domain);
-            float dz = pz - cz[0];
-            float v = sqrtf(dxy[0] + dz * dz) - cr[0];
-#pragma unroll
-            for (int i = 1; i < KEEP_REGS; ++i) {
-                if (i < (int)nk) {
-                    dz = pz - cz[i];
-                    v = fminf(v, sqrtf(dxy[i] + dz * dz) - cr[i]);
-                }
-            }
-            const uint64_t row = (uint64_t)z * A.ny + y;
-            if (valid) A.field[row * A.pitch + x] = v;
-            const uint32_t b = __ballot_sync(FULL, valid && !(v > 0.0f));
-            if (lane == 0) A.bits[row * A.W + blockIdx.x] = b;
-        }
-        return;
+    switch (nk) {
+    case 1: sphere_column<1>(A, s_keep, px, py, x, y, z0, z1, valid, lane); return;
+    case 2: sphere_column<2>(A, s_keep, px, py, x, y, z0, z1, valid, lane); return;
+    case 3: sphere_column<3>(A, s_keep, px, py, x, y, z0, z1, valid, lane); return;
+    case 4: sphere_column<4>(A, s_keep, px, py, x, y, z0, z1, valid, lane); return;
+    case 5: sphere_column<5>(A, s_keep, px, py, x, y, z0, z1, valid, lane); return;
+    case 6: sphere_column<6>(A, s_keep, px, py, x, y, z0, z1, valid, lane); return;
+    default: break;
     }
     for (uint32_t z = z0; z <= z1; ++z) {
         const float pz = world((float)z * A.inv, A.sz, A.oz, A.domain);
