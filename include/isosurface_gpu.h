@@ -238,6 +238,19 @@ ISO_API iso_status iso_mc_extract_field_noalloc(const float* field, uint32_t nx,
 ISO_API iso_status iso_mc_cases(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint8_t* cases_host);
 
 /* ------------------------------------------------------------------------ */
+/* DualContouring (src/dual_contouring.rs:42-105)                             */
+/* ------------------------------------------------------------------------ */
+#define ISO_PLACER_MINIMISE_QEF 0u    /* MinimiseQEF, feature/qef.rs:23-68 */
+#define ISO_PLACER_PARTICLES 1u       /* ParticleBasedMinimisation, feature/particle_minimisation.rs:25-72 */
+/* DualContouring::new(size, placer).extract(&sampler, &mut e): one vertex per
+ * primal cell (placed by `placer` in active cells, the cell centre elsewhere),
+ * then marching cubes over the dual cubes (DualGrid, traversal/dual_grid.rs).
+ * Needs a source with normals (HermiteSource); keys (ISO_FLAG_KEYS) are dual
+ * lattice edge ids over the (size-1) x (size-1) x size dual vertices. */
+ISO_API iso_status iso_dc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t placer,
+                                  uint32_t flags, iso_mesh_info* info);
+
+/* ------------------------------------------------------------------------ */
 /* PointCloud (src/point_cloud.rs:50-63)                                      */
 /* ------------------------------------------------------------------------ */
 ISO_API iso_status iso_point_cloud_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size,

@@ -64,6 +64,7 @@ SIGNATURES = {
     "iso_mc_extract_field_noalloc": (i32, [vp, u32, u32, u32, u64, vp, u64, vp, u64, vp, ctypes.POINTER(MeshInfo)]),
     "iso_mc_cases": (i32, [vp, vp, u32, u8p]),
     "iso_point_cloud_extract": (i32, [vp, vp, u32, ctypes.POINTER(MeshInfo)]),
+    "iso_dc_extract": (i32, [vp, vp, u32, u32, u32, ctypes.POINTER(MeshInfo)]),
     "iso_sample_points": (i32, [vp, vp, f32p, u64, f32p, f32p]),
 }
 

@@ -130,6 +130,12 @@ class Context:
                                  out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))), self.h)
         return out
 
+    def dc_extract(self, source, size, placer=0, keys=False):
+        info = MeshInfo()
+        flags = ISO_FLAG_KEYS if keys else 0
+        check(lib().iso_dc_extract(self.h, self.program(source).h, size, placer, flags, ctypes.byref(info)), self.h)
+        return info
+
     def point_cloud_extract(self, source, size):
         info = MeshInfo()
         check(lib().iso_point_cloud_extract(self.h, self.program(source).h, size, ctypes.byref(info)), self.h)
@@ -254,6 +260,34 @@ class MarchingCubes:
         if getattr(extractor, "with_normals", False):
             raise IsoError(9, "per-vertex normals are not available for MarchingCubes yet")
         info = ctx.mc_extract(source, self.size)
+        _replay(extractor, ctx.download(info))
+
+
+class MinimiseQEF:
+    """Feature placement by QEF minimisation (src/feature/qef.rs:23-68)."""
+    code = 0
+
+
+class ParticleBasedMinimisation:
+    """Feature placement by particle descent (src/feature/particle_minimisation.rs:25-72)."""
+    code = 1
+
+
+class DualContouring:
+    """DualContouring::new(size, placer) (src/dual_contouring.rs:51-56)."""
+
+    def __init__(self, size, place_feature=None, context=None):
+        if size < 1:
+            raise ValueError("size must be at least 1")
+        self.size = size
+        self.placer = (place_feature or MinimiseQEF()).code
+        self.context = context
+
+    def extract(self, sampler, extractor):
+        ctx = self.context or default_context()
+        if getattr(extractor, "with_normals", False):
+            raise IsoError(9, "per-vertex normals are not available for DualContouring yet")
+        info = ctx.dc_extract(_source_of(sampler), self.size, self.placer)
         _replay(extractor, ctx.download(info))
 
 

@@ -25,8 +25,9 @@ UNITS = {
     "ctx.cu": ["-fmad=false"],
     "sample.cu": ["-fmad=false"],
     "mc.cu": ["-fmad=false"],
+    "dc.cu": ["-fmad=false"],
 }
-HEADERS = ["internal.h", "vm.cuh", "mc_tables.h"]
+HEADERS = ["internal.h", "vm.cuh", "mc_tables.h", "mc_chunk.cuh", "qef.cuh"]
 
 
 def _deps():

@@ -1,0 +1,190 @@
+// DualContouring::new(size, placer).extract (src/dual_contouring.rs:65-105)
+// over DualGrid::traverse (src/traversal/dual_grid.rs:52-95).
+//
+// The dual lattice has one vertex per primal cell: (size-1) x (size-1) x size
+// vertices.  Its value is lerp(v0, v6, 0.5) of the primal corners
+// (dual_grid.rs:80-81); its position is the cell centre lerp(c0, c6, 0.5)
+// unless the cell is active (case not 0 or 255), where the feature placer
+// puts it (dual_contouring.rs:78-87).  The dual cubes are then meshed exactly
+// like MarchingCubes over the dual lattice with explicit vertex positions
+// (dual_contouring.rs:88-101 is the same cell kernel with GridKey dedup), so
+// the last two passes are mc_extract_lattice.
+//
+// Passes: (1) grid sampler (field + sign bits), (2) dc_dual: value and centre
+// of every dual vertex, active primal cells appended to a list, (3) dc_place:
+// one thread per active cell -- eight normals from the program
+// (sample_normals_at_corners, marching_cubes_impl.rs:58-69), tangent planes,
+// QEF or particle placement, (4) sign bits of the dual values, (5)+(6) the
+// lattice marching-cubes passes.
+#include <cuda_runtime.h>
+
+#include "internal.h"
+#include "qef.cuh"
+#include "vm.cuh"
+
+namespace iso {
+namespace {
+
+struct DualArgs {
+    const float* field;
+    uint64_t pitch;       // primal row pitch
+    uint32_t n;           // primal size: n x n x (n+1) samples
+    float inv;
+    float* dval;          // dual values, rows of dpitch
+    uint64_t dpitch;
+    float4* dpos;         // dual positions, dense (n-1) x (n-1) x n
+    uint32_t* list;       // active primal cells (linear dual index)
+    uint32_t* count;
+    uint32_t cap;
+    uint32_t* err;
+};
+
+__global__ void __launch_bounds__(256) dc_dual(DualArgs A) {
+    const uint32_t m = A.n - 1;
+    const uint64_t total = (uint64_t)m * m * A.n;
+    const uint64_t id = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool active = false;
+    if (id < total) {
+        const uint32_t x = (uint32_t)(id % m);
+        const uint64_t r = id / m;
+        const uint32_t y = (uint32_t)(r % m), z = (uint32_t)(r / m);
+        // corners in CORNERS order (marching_cubes_tables.rs:16-25)
+        const float* f0 = A.field + ((size_t)z * A.n + y) * A.pitch + x;
+        const float* f1 = f0 + (size_t)A.n * A.pitch;
+        const float v0 = __ldg(f0), v1 = __ldg(f0 + 1), v2 = __ldg(f0 + A.pitch + 1), v3 = __ldg(f0 + A.pitch);
+        const float v4 = __ldg(f1), v5 = __ldg(f1 + 1), v6 = __ldg(f1 + A.pitch + 1), v7 = __ldg(f1 + A.pitch);
+        uint32_t cs = 0;
+        cs |= !(v0 > 0.0f) ? 1u : 0u;
+        cs |= !(v1 > 0.0f) ? 2u : 0u;
+        cs |= !(v2 > 0.0f) ? 4u : 0u;
+        cs |= !(v3 > 0.0f) ? 8u : 0u;
+        cs |= !(v4 > 0.0f) ? 16u : 0u;
+        cs |= !(v5 > 0.0f) ? 32u : 0u;
+        cs |= !(v6 > 0.0f) ? 64u : 0u;
+        cs |= !(v7 > 0.0f) ? 128u : 0u;
+        // Vec3::lerp / Signed::lerp with f = 0.5: (1 - f) * a + f * b
+        const float c0x = (float)x * A.inv, c0y = (float)y * A.inv, c0z = (float)z * A.inv;
+        const float c6x = (float)(x + 1) * A.inv, c6y = (float)(y + 1) * A.inv, c6z = (float)(z + 1) * A.inv;
+        const float of = 1.0f - 0.5f;
+        A.dpos[id] = make_float4(of * c0x + 0.5f * c6x, of * c0y + 0.5f * c6y, of * c0z + 0.5f * c6z, 0.0f);
+        A.dval[((size_t)z * m + y) * A.dpitch + x] = of * v0 + 0.5f * v6;
+        active = cs != 0 && cs != 255;
+    }
+    // warp-aggregated append of the active cells (their order does not matter)
+    const uint32_t mask = __ballot_sync(0xFFFFFFFFu, active);
+    if (mask) {
+        const int lane = threadIdx.x & 31;
+        uint32_t base = 0;
+        if (lane == __ffs(mask) - 1) base = atomicAdd(A.count, (uint32_t)__popc(mask));
+        base = __shfl_sync(0xFFFFFFFFu, base, __ffs(mask) - 1);
+        if (active) {
+            const uint32_t at = base + __popc(mask & ((1u << lane) - 1u));
+            if (at < A.cap) A.list[at] = (uint32_t)id;
+            else atomicOr(A.err, DERR_CAPACITY);
+        }
+    }
+}
+
+struct PlaceArgs {
+    ProgView pv;
+    uint32_t n;
+    float inv;
+    const uint32_t* list;
+    const uint32_t* count;
+    float4* dpos;
+    int placer;  // 0 MinimiseQEF, 1 ParticleBasedMinimisation
+    uint32_t* err;
+};
+
+__device__ void place_one(const PlaceArgs& A, uint32_t i) {
+    const uint32_t m = A.n - 1;
+    const uint32_t id = A.list[i];
+    const uint32_t x = id % m, r = id / m;
+    const uint32_t y = r % m, z = r / m;
+    const uint8_t cornr[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+    qef::F3 corners[8], normals[8];
+    for (int k = 0; k < 8; ++k) {
+        const float px = (float)(x + cornr[k][0]) * A.inv, py = (float)(y + cornr[k][1]) * A.inv,
+                    pz = (float)(z + cornr[k][2]) * A.inv;
+        corners[k] = qef::f3(px, py, pz);
+        V3 nn;
+        eval_hermite(A.pv, v3(px, py, pz), &nn);
+        normals[k] = qef::normalised_or_zero(qef::f3(nn.x, nn.y, nn.z));
+    }
+    qef::F3 p;
+    if (A.placer == 0) {
+        qef::Planes t;
+        qef::tangent_planes(corners, normals, &t);
+        bool ok;
+        p = qef::minimise_qef(t, &ok);
+        if (!ok) atomicOr(A.err, DERR_SVD_ITER);
+    } else {
+        p = qef::particle_placement(corners, normals);
+    }
+    A.dpos[id] = make_float4(p.x, p.y, p.z, 0.0f);
+}
+
+// one thread per active cell, grid-stride over the list built by dc_dual
+__global__ void __launch_bounds__(128) dc_place(PlaceArgs A) {
+    const uint32_t count = *A.count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+        place_one(A, i);
+}
+
+}  // namespace
+}  // namespace iso
+
+using namespace iso;
+
+extern "C" iso_status iso_dc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t placer,
+                                     uint32_t flags, iso_mesh_info* info) {
+    if (!ctx || !prog) return ISO_ERR_INVALID_ARG;
+    if (prog->ctx != ctx) return fail(ctx, ISO_ERR_INVALID_ARG, "program belongs to another context");
+    if (size == 0 || size > 16384) return fail(ctx, ISO_ERR_INVALID_ARG, "size out of range");
+    if (placer > 1) return fail(ctx, ISO_ERR_INVALID_ARG, "placer must be 0 (MinimiseQEF) or 1 (particles)");
+    if (flags & ~(uint32_t)ISO_FLAG_KEYS) return fail(ctx, ISO_ERR_INVALID_ARG, "unsupported flags");
+    iso_status s = set_device(ctx);
+    if (s != ISO_OK) return s;
+    ctx->last = iso_mesh_info{};
+    ctx->last_flags = flags;
+    ctx->last_vertex_floats = 3;
+    if (size < 3) {  // the dual lattice has no cube
+        if (info) *info = ctx->last;
+        return ISO_OK;
+    }
+    const uint32_t n = size, m = size - 1;
+    const uint64_t pitch = default_pitch(n), W = words_per_row(n);
+    const uint64_t ndual = (uint64_t)m * m * n;
+    if (ndual >= 0xFFFFFFFFull) return fail(ctx, ISO_ERR_TOO_LARGE, "grid too large");
+    const uint64_t dpitch = default_pitch(m), dW = words_per_row(m);
+    // primal field + bits | dual values | dual positions | dual bits | active list
+    if ((s = ensure(ctx, ctx->field, 4ull * pitch * n * (n + 1))) != ISO_OK) return s;
+    if ((s = ensure(ctx, ctx->bits, 4ull * W * n * (n + 1))) != ISO_OK) return s;
+    if ((s = ensure(ctx, ctx->aux, 4ull * dpitch * m * n)) != ISO_OK) return s;
+    if ((s = ensure(ctx, ctx->aux2, 16ull * ndual)) != ISO_OK) return s;
+    if ((s = ensure(ctx, ctx->aux3, 4ull * dW * m * n + 4ull * ndual + 256)) != ISO_OK) return s;
+    float* field = (float*)ctx->field.p;
+    uint32_t* bits = (uint32_t*)ctx->bits.p;
+    float* dval = (float*)ctx->aux.p;
+    float4* dpos = (float4*)ctx->aux2.p;
+    uint32_t* dbits = (uint32_t*)ctx->aux3.p;
+    uint32_t* count = dbits + dW * m * n;
+    uint32_t* list = count + 64;
+    const float inv = 1.0f / (float)(n - 1);
+    if ((s = launch_sample_grid(ctx, prog, n, n, n + 1, inv, field, pitch, bits)) != ISO_OK) return s;
+    cudaError_t e = cudaMemsetAsync(count, 0, 4, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "memset");
+    {
+        StageTimer timer(ctx, ISO_STAGE_PLACE);
+        DualArgs da{field, pitch, n, inv, dval, dpitch, dpos, list, count, (uint32_t)ndual, ctx->d_err};
+        dc_dual<<<(unsigned)((ndual + 255) / 256), 256, 0, ctx->stream>>>(da);
+        PlaceArgs pa{prog->view(), n, inv, list, count, dpos, (int)placer, ctx->d_err};
+        const uint64_t place_blocks = std::min<uint64_t>((ndual + 127) / 128, 152 * 64);
+        dc_place<<<(unsigned)place_blocks, 128, 0, ctx->stream>>>(pa);
+    }
+    ctx->launches += 2;
+    if ((s = check_launch(ctx, "dc passes")) != ISO_OK) return s;
+    if ((s = launch_sign_bits(ctx, dval, m, m, n, dpitch, dbits)) != ISO_OK) return s;
+    Lattice L{m, m, n, dpitch, dval, dbits, (uint32_t)dW, 0.0f, dpos};
+    return mc_extract_lattice(ctx, L, flags, info);
+}

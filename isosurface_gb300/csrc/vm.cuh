@@ -86,7 +86,7 @@ __device__ __forceinline__ V3 pt_apply(uint32_t op, const float* k, V3 p) {
 }
 
 // Scalar evaluation of ops[begin, end) at p (one value left on the stack).
-__device__ __noinline__ float eval_range(const ProgView& pv, uint32_t begin, uint32_t end, V3 p) {
+static __device__ __noinline__ float eval_range(const ProgView& pv, uint32_t begin, uint32_t end, V3 p) {
     float vs[VSTACK];
     V3 ps[PSTACK];
     int vsp = 0, psp = 0;
@@ -131,7 +131,7 @@ __device__ __noinline__ float eval_range(const ProgView& pv, uint32_t begin, uin
 __device__ __forceinline__ float eval_scalar(const ProgView& pv, V3 p) { return eval_range(pv, 0, pv.n_ops, p); }
 
 // Value and (unnormalised) normal: HermiteSource::sample_normal semantics.
-__device__ __noinline__ float eval_hermite(const ProgView& pv, V3 p, V3* normal) {
+static __device__ __noinline__ float eval_hermite(const ProgView& pv, V3 p, V3* normal) {
     float vs[VSTACK];
     V3 ns[VSTACK];
     V3 ps[PSTACK];
