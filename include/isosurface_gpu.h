@@ -251,6 +251,24 @@ ISO_API iso_status iso_dc_extract(iso_ctx* ctx, const iso_program* prog, uint32_
                                   uint32_t flags, iso_mesh_info* info);
 
 /* ------------------------------------------------------------------------ */
+/* LinearHashedMarchingCubes (src/linear_hashed_marching_cubes.rs:40-84)      */
+/* ------------------------------------------------------------------------ */
+/* LinearHashedMarchingCubes::new(max_depth).extract(&sampler, &mut e):
+ * Morton-keyed octree (linear_hashed_octree.rs), refined where |f| is below
+ * the node's half-diagonal, then marching cubes on the dual cubes of its
+ * leaves (traversal/implicit_octree.rs) with MortonKey dedup.  max_depth <= 10.
+ * The reference emits the mesh in HashMap order, so only the triangle set is
+ * defined; keys (ISO_FLAG_KEYS) are the MortonKey pair of each vertex. */
+ISO_API iso_status iso_lhmc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t max_depth, uint32_t flags,
+                                    iso_mesh_info* info);
+
+/* Dual-cube corners of the last iso_lhmc_extract call on `ctx` whose parent
+ * walk found no node.  The reference keeps the previous primal vertex's
+ * corner data there (traversal/implicit_octree.rs:84-95), which depends on its
+ * HashMap order; 0 means the extraction involved no such corner. */
+ISO_API uint64_t iso_lhmc_stale_corners(const iso_ctx* ctx);
+
+/* ------------------------------------------------------------------------ */
 /* PointCloud (src/point_cloud.rs:50-63)                                      */
 /* ------------------------------------------------------------------------ */
 ISO_API iso_status iso_point_cloud_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size,

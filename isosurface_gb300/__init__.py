@@ -6,13 +6,13 @@ declared in include/isosurface_gpu.h.
 from .source import (CentralDifference, Cylinder, Difference, DomainMap, Intersection, RectangularPrism, Rigid,
                      Sampler, SmoothUnion, Source, Sphere, SphereSet, Torus, Translate, Union, lower, unit_to_cube)
 from ._capi import IsoError
-from .api import (Context, DualContouring, IndexedInterleavedNormals, IndexedVertices, MarchingCubes, Mesh,
-                  MinimiseQEF, OnlyInterleavedNormals, OnlyVertices, ParticleBasedMinimisation, PointCloud, Program,
-                  default_context)
+from .api import (Context, DualContouring, IndexedInterleavedNormals, IndexedVertices, LinearHashedMarchingCubes,
+                  MarchingCubes, Mesh, MinimiseQEF, OnlyInterleavedNormals, OnlyVertices, ParticleBasedMinimisation,
+                  PointCloud, Program, default_context)
 
 __all__ = [
     "CentralDifference", "Cylinder", "Difference", "DomainMap", "Intersection", "RectangularPrism", "Rigid", "Sampler",
     "SmoothUnion", "Source", "Sphere", "SphereSet", "Torus", "Translate", "Union", "lower", "unit_to_cube",
-    "IsoError", "Context", "DualContouring", "MinimiseQEF", "ParticleBasedMinimisation", "IndexedInterleavedNormals", "IndexedVertices", "MarchingCubes", "Mesh",
+    "IsoError", "Context", "DualContouring", "LinearHashedMarchingCubes", "MinimiseQEF", "ParticleBasedMinimisation", "IndexedInterleavedNormals", "IndexedVertices", "MarchingCubes", "Mesh",
     "OnlyInterleavedNormals", "OnlyVertices", "PointCloud", "Program", "default_context",
 ]

@@ -65,6 +65,8 @@ SIGNATURES = {
     "iso_mc_cases": (i32, [vp, vp, u32, u8p]),
     "iso_point_cloud_extract": (i32, [vp, vp, u32, ctypes.POINTER(MeshInfo)]),
     "iso_dc_extract": (i32, [vp, vp, u32, u32, u32, ctypes.POINTER(MeshInfo)]),
+    "iso_lhmc_extract": (i32, [vp, vp, u32, u32, ctypes.POINTER(MeshInfo)]),
+    "iso_lhmc_stale_corners": (u64, [vp]),
     "iso_sample_points": (i32, [vp, vp, f32p, u64, f32p, f32p]),
 }
 

@@ -136,6 +136,16 @@ class Context:
         check(lib().iso_dc_extract(self.h, self.program(source).h, size, placer, flags, ctypes.byref(info)), self.h)
         return info
 
+    def lhmc_extract(self, source, max_depth, keys=False):
+        info = MeshInfo()
+        flags = ISO_FLAG_KEYS if keys else 0
+        check(lib().iso_lhmc_extract(self.h, self.program(source).h, max_depth, flags, ctypes.byref(info)), self.h)
+        return info
+
+    @property
+    def lhmc_stale_corners(self):
+        return lib().iso_lhmc_stale_corners(self.h)
+
     def point_cloud_extract(self, source, size):
         info = MeshInfo()
         check(lib().iso_point_cloud_extract(self.h, self.program(source).h, size, ctypes.byref(info)), self.h)
@@ -288,6 +298,21 @@ class DualContouring:
         if getattr(extractor, "with_normals", False):
             raise IsoError(9, "per-vertex normals are not available for DualContouring yet")
         info = ctx.dc_extract(_source_of(sampler), self.size, self.placer)
+        _replay(extractor, ctx.download(info))
+
+
+class LinearHashedMarchingCubes:
+    """LinearHashedMarchingCubes::new(max_depth) (src/linear_hashed_marching_cubes.rs:51-53)."""
+
+    def __init__(self, max_depth, context=None):
+        self.max_depth = max_depth
+        self.context = context
+
+    def extract(self, sampler, extractor):
+        ctx = self.context or default_context()
+        if getattr(extractor, "with_normals", False):
+            raise IsoError(9, "per-vertex normals are not available for LinearHashedMarchingCubes yet")
+        info = ctx.lhmc_extract(_source_of(sampler), self.max_depth)
         _replay(extractor, ctx.download(info))
 
 

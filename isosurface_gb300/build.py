@@ -26,6 +26,7 @@ UNITS = {
     "sample.cu": ["-fmad=false"],
     "mc.cu": ["-fmad=false"],
     "dc.cu": ["-fmad=false"],
+    "lhmc.cu": ["-fmad=false"],
 }
 HEADERS = ["internal.h", "vm.cuh", "mc_tables.h", "mc_chunk.cuh", "qef.cuh"]
 

@@ -57,6 +57,7 @@ struct iso_ctx {
     uint64_t* h_pinned = nullptr;
     uint32_t* d_err = nullptr;
     uint64_t launches = 0;
+    uint64_t lhmc_stale = 0;  // dual-cube corners with no ancestor node in the last LHMC call
     std::string last_error;
     // per-stage event timing (iso_ctx_enable_stage_timing)
     bool timing = false;

@@ -1,0 +1,711 @@
+// LinearHashedMarchingCubes::new(max_depth).extract
+// (src/linear_hashed_marching_cubes.rs:62-84) over ImplicitOctree::traverse
+// (src/traversal/implicit_octree.rs:39-99) and LinearHashedOctree
+// (src/linear_hashed_octree.rs:30-51), with Morton keys (src/morton.rs).
+//
+// GPU form:
+// 1. Octree build, one generation at a time: evaluate the source at every
+//    frontier node's centre, apply should_refine (level < 2 || (level <
+//    max_depth && |d| < size * sqrt 3)), and write the children of refined
+//    nodes, in order, as the next frontier.  Generation g holds keys with
+//    3g+1 bits in ascending order, so the concatenated node array is sorted
+//    and a binary search replaces the HashMap<Morton, Node>.
+// 2. Primal vertices: every leaf emits primal_vertex(level, i) for i < 8; a
+//    GPU hash table keeps, per vertex, the deepest level (the reference's
+//    max-level map) and, among leaves of that level, the smallest key.  That
+//    leaf owns the vertex, which gives a deterministic order (leaf order, then
+//    i) for the walk the reference does in HashMap order.
+// 3. Dual cubes: for each primal vertex and corner i, dual_vertex(level,
+//    REMAP_CUBE[i]) walks parent() until a node exists; the corner is that
+//    node's centre and value.  A corner with no ancestor keeps the previous
+//    corner's data in the reference (an order-dependent case); it is counted
+//    and reported through iso_lhmc_stale_corners.
+// 4. Marching cubes on the dual cubes with MortonKey dedup: each vertex is
+//    owned by the first (cube, first-use rank) that references its key, found
+//    with a 64-bit atomicMin in a second hash table.
+//
+// The reference's output order is that of a RandomState HashMap, so only the
+// triangle set (keyed by MortonKey pairs) is defined; this order is
+// deterministic.  Keys must fit 31 bits: max_depth <= 10.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "internal.h"
+#include "vm.cuh"
+#define ISO_TABLE static __device__ const
+#include "mc_tables.h"
+
+namespace iso {
+namespace {
+
+constexpr uint32_t FULL = 0xFFFFFFFFu;
+
+// ---------------------------------------------------------------- Morton ---
+namespace morton {
+constexpr uint64_t DILATE_MASK_2 = 0x7FC0000FF80001FFull;
+constexpr uint64_t DILATE_MASK_1 = 0x01C0E070381C0E07ull;
+constexpr uint64_t DILATE_MASK_0 = 0x9249249249249249ull;
+constexpr uint64_t DILATE_TZ = 0x4924924924924924ull;
+constexpr uint64_t DILATE_TY = 0x2492492492492492ull;
+constexpr uint64_t DILATE_TX = 0x9249249249249249ull;
+constexpr uint64_t DILATE_T1 = 0xB6DB6DB6DB6DB6DBull;
+constexpr uint64_t DILATE_T2 = 0xDB6DB6DB6DB6DB6Dull;
+constexpr uint64_t DILATE_T3 = 0x6DB6DB6DB6DB6DB6ull;
+constexpr int MAX_LEVEL = 21;
+
+// morton.rs:54-59 computes floor(ln(k) * 0.48089834696); the constant sits
+// just below 1/(3 ln 2), so the result is floor(log2(k) / 3) except at exact
+// powers of 8 above 1, where it is one less (checked against the formula for
+// every key below 2^31 by the tests).
+__host__ __device__ inline int level(uint64_t k) {
+    if (k == 0) return 0;
+#ifdef __CUDA_ARCH__
+    const int msb = 63 - __clzll((long long)k);
+#else
+    const int msb = 63 - __builtin_clzll(k);
+#endif
+    int lv = msb / 3;
+    if (lv > 0 && k == (1ull << (3 * lv))) lv -= 1;
+    return lv;
+}
+__device__ inline uint64_t parent(uint64_t k) { return max(k >> 3, (uint64_t)1); }
+__device__ inline float size(uint64_t k) { return 1.0f / (float)((uint64_t)2 << level(k)); }
+__device__ inline uint64_t add(uint64_t a, uint64_t b) {  // morton.rs:147-157
+    return (((a | DILATE_T1) + (b & DILATE_TZ)) & DILATE_TZ) | (((a | DILATE_T2) + (b & DILATE_TY)) & DILATE_TY) |
+           (((a | DILATE_T3) + (b & DILATE_TX)) & DILATE_TX);
+}
+__device__ inline uint64_t sub(uint64_t a, uint64_t b) {  // morton.rs:159-169
+    return (((a & DILATE_TZ) - (b & DILATE_TZ)) & DILATE_TZ) | (((a & DILATE_TY) - (b & DILATE_TY)) & DILATE_TY) |
+           (((a & DILATE_TX) - (b & DILATE_TX)) & DILATE_TX);
+}
+__device__ inline V3 center(uint64_t k) {  // morton.rs:78-116
+    uint64_t bz = (k >> 2) & DILATE_MASK_0, by = (k >> 1) & DILATE_MASK_0, bx = k & DILATE_MASK_0;
+    const int lv = level(k);
+    if (lv > 1) {
+        bz = (bz | (bz >> 2) | (bz >> 4)) & DILATE_MASK_1;
+        by = (by | (by >> 2) | (by >> 4)) & DILATE_MASK_1;
+        bx = (bx | (bx >> 2) | (bx >> 4)) & DILATE_MASK_1;
+        if (lv > 3) {
+            bz = (bz | (bz >> 6) | (bz >> 12)) & DILATE_MASK_2;
+            by = (by | (by >> 6) | (by >> 12)) & DILATE_MASK_2;
+            bx = (bx | (bx >> 6) | (bx >> 12)) & DILATE_MASK_2;
+            if (lv > 9) {
+                bz = bz | (bz >> 18) | (bz >> 36);
+                by = by | (by >> 18) | (by >> 36);
+                bx = bx | (bx >> 18) | (bx >> 36);
+            }
+        }
+    }
+    const uint64_t length_mask = (1ull << lv) - 1;
+    bz &= length_mask;
+    by &= length_mask;
+    bx &= length_mask;
+    const float s = 1.0f / (float)((uint64_t)2 << lv);
+    const float s2 = s * 2.0f;
+    return v3((float)bx * s2 + s, (float)by * s2 + s, (float)bz * s2 + s);
+}
+__device__ inline uint64_t primal_vertex(uint64_t self, int lv, uint64_t which) {  // morton.rs:120-136
+    const uint64_t k = 1ull << (3 * lv);
+    const uint64_t k1 = k << 1;
+    const uint64_t vk = add(self, which);
+    const uint64_t dk = sub(vk, k);
+    if (vk >= k1 || (dk & DILATE_TX) == 0 || (dk & DILATE_TY) == 0 || (dk & DILATE_TZ) == 0) return 0;
+    return vk << (3 * (MAX_LEVEL - lv));
+}
+__device__ inline uint64_t dual_vertex(uint64_t self, int lv, uint64_t which) {  // morton.rs:140-144
+    return sub(self >> (3 * (MAX_LEVEL - lv)), which);
+}
+}  // namespace morton
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// open-addressing table: key 0 = empty; returns the slot or UINT32_MAX when full
+__device__ __forceinline__ uint32_t ht_insert(unsigned long long* keys, uint32_t mask, uint64_t key) {
+    uint32_t slot = (uint32_t)mix64(key) & mask;
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        const unsigned long long prev = atomicCAS(keys + slot, 0ull, (unsigned long long)key);
+        if (prev == 0ull || prev == key) return slot;
+        slot = (slot + 1) & mask;
+    }
+    return 0xFFFFFFFFu;
+}
+__device__ __forceinline__ uint32_t ht_find(const unsigned long long* keys, uint32_t mask, uint64_t key) {
+    uint32_t slot = (uint32_t)mix64(key) & mask;
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        const unsigned long long k = keys[slot];
+        if (k == key) return slot;
+        if (k == 0ull) return 0xFFFFFFFFu;
+        slot = (slot + 1) & mask;
+    }
+    return 0xFFFFFFFFu;
+}
+
+// ----------------------------------------------------------- exclusive scan ---
+__global__ void __launch_bounds__(1024) scan_blocks(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* sums) {
+    __shared__ uint32_t s_w[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t i = blockIdx.x * 1024 + threadIdx.x;
+    const uint32_t v = i < n ? in[i] : 0u;
+    uint32_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(FULL, x, o);
+        if (lane >= o) x += t;
+    }
+    if (lane == 31) s_w[warp] = x;
+    __syncthreads();
+    uint32_t before = 0, all = 0;
+    for (int w = 0; w < 32; ++w) {
+        if (w < warp) before += s_w[w];
+        all += s_w[w];
+    }
+    if (i < n) out[i] = before + x - v;
+    if (threadIdx.x == 0) sums[blockIdx.x] = all;
+}
+
+__global__ void __launch_bounds__(1024) scan_sums(uint32_t* sums, uint32_t nb, uint32_t* total) {
+    __shared__ uint32_t s_w[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < nb; base += 1024) {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t v = i < nb ? sums[i] : 0u;
+        uint32_t x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(FULL, x, o);
+            if (lane >= o) x += t;
+        }
+        if (lane == 31) s_w[warp] = x;
+        __syncthreads();
+        uint32_t before = 0, all = 0;
+        for (int w = 0; w < 32; ++w) {
+            if (w < warp) before += s_w[w];
+            all += s_w[w];
+        }
+        if (i < nb) sums[i] = carry + before + x - v;
+        carry += all;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void scan_add(uint32_t* out, uint32_t n, const uint32_t* sums) {
+    const uint32_t i = blockIdx.x * 1024 + threadIdx.x;
+    if (i < n) out[i] += sums[blockIdx.x];
+}
+
+// ------------------------------------------------------------ octree build ---
+struct GenArgs {
+    ProgView pv;
+    unsigned long long* keys;  // all nodes, BFS (= ascending) order
+    float* vals;
+    uint32_t* refine;         // 1 = refined
+    uint32_t off, cnt;        // this generation
+    uint32_t max_depth;
+};
+
+__global__ void oct_eval(GenArgs A) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.cnt) return;
+    const uint64_t key = A.keys[A.off + i];
+    const float d = eval_scalar(A.pv, morton::center(key));  // construct_node, implicit_octree.rs:56-59
+    const int lv = morton::level(key);
+    const float sz = 1.0f / (float)((uint64_t)2 << lv);
+    // should_refine (implicit_octree.rs:47-55) with Signed::within_extent (distance.rs:60-62)
+    const bool r = lv < 2 || (lv < (int)A.max_depth && fabsf(d) < sz * 1.73205080757f);
+    A.vals[A.off + i] = d;
+    A.refine[A.off + i] = r ? 1u : 0u;
+}
+
+__global__ void oct_expand(unsigned long long* keys, const uint32_t* refine, const uint32_t* rank, uint32_t off,
+                           uint32_t cnt, uint32_t next_off) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cnt || !refine[off + i]) return;
+    const uint64_t key = keys[off + i];
+    const uint32_t at = next_off + 8 * rank[i];
+    for (uint32_t c = 0; c < 8; ++c) keys[at + c] = (key << 3) | c;  // Morton::child
+}
+
+// ----------------------------------------------------------- primal vertices ---
+constexpr uint64_t MASK58 = (1ull << 58) - 1;
+
+__device__ __forceinline__ uint64_t owner_code(int lv, uint64_t key) { return ((uint64_t)lv << 58) | (MASK58 - key); }
+
+struct LeafArgs {
+    const unsigned long long* keys;
+    const uint32_t* refine;
+    uint32_t nodes;
+    unsigned long long* hkeys;
+    unsigned long long* hvals;
+    uint32_t hmask;
+    uint32_t* counts;   // per node: owned primal vertices
+    uint32_t* err;
+};
+
+__global__ void leaf_insert(LeafArgs A) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t node = t >> 3, i = t & 7;
+    if (node >= A.nodes || A.refine[node]) return;
+    const uint64_t key = A.keys[node];
+    const int lv = morton::level(key);
+    const uint64_t v = morton::primal_vertex(key, lv, i);
+    if (v == 0) return;
+    const uint32_t slot = ht_insert(A.hkeys, A.hmask, v);
+    if (slot == 0xFFFFFFFFu) {
+        atomicOr(A.err, DERR_CAPACITY);
+        return;
+    }
+    atomicMax(A.hvals + slot, (unsigned long long)owner_code(lv, key));
+}
+
+__global__ void leaf_count(LeafArgs A) {
+    const uint32_t node = blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= A.nodes) return;
+    uint32_t n = 0;
+    if (!A.refine[node]) {
+        const uint64_t key = A.keys[node];
+        const int lv = morton::level(key);
+        for (uint32_t i = 0; i < 8; ++i) {
+            const uint64_t v = morton::primal_vertex(key, lv, i);
+            if (v == 0) continue;
+            const uint32_t slot = ht_find(A.hkeys, A.hmask, v);
+            if (slot != 0xFFFFFFFFu && A.hvals[slot] == owner_code(lv, key)) ++n;
+        }
+    }
+    A.counts[node] = n;
+}
+
+__global__ void leaf_write(LeafArgs A, const uint32_t* offsets, unsigned long long* pv_key, uint8_t* pv_level) {
+    const uint32_t node = blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= A.nodes || A.refine[node]) return;
+    const uint64_t key = A.keys[node];
+    const int lv = morton::level(key);
+    uint32_t at = offsets[node];
+    for (uint32_t i = 0; i < 8; ++i) {
+        const uint64_t v = morton::primal_vertex(key, lv, i);
+        if (v == 0) continue;
+        const uint32_t slot = ht_find(A.hkeys, A.hmask, v);
+        if (slot != 0xFFFFFFFFu && A.hvals[slot] == owner_code(lv, key)) {
+            pv_key[at] = v;
+            pv_level[at] = (uint8_t)lv;
+            ++at;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- dual cubes ---
+struct CubeArgs {
+    const unsigned long long* nkeys;  // sorted node keys
+    const float* nvals;
+    uint32_t nodes;
+    const unsigned long long* pv_key;
+    const uint8_t* pv_level;
+    uint32_t ncubes;
+    uint32_t* corner;      // 8 node indices per cube (UINT32_MAX: no ancestor)
+    uint8_t* cases;
+    uint32_t* tri_counts;
+    unsigned long long* stale;
+};
+
+__device__ __forceinline__ uint32_t find_node(const unsigned long long* keys, uint32_t n, uint64_t key) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (keys[mid] < key) lo = mid + 1;
+        else hi = mid;
+    }
+    return (lo < n && keys[lo] == key) ? lo : 0xFFFFFFFFu;
+}
+
+__global__ void cube_gather(CubeArgs A) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= A.ncubes) return;
+    const uint64_t v = A.pv_key[j];
+    const int lv = A.pv_level[j];
+    uint32_t cs = 0;
+    uint32_t prev = 0xFFFFFFFFu;
+    for (int i = 0; i < 8; ++i) {
+        uint64_t m = morton::dual_vertex(v, lv, iso_remap_cube[i]);
+        uint32_t found = 0xFFFFFFFFu;
+        while (m > 1) {
+            found = find_node(A.nkeys, A.nodes, m);
+            if (found != 0xFFFFFFFFu) break;
+            m = morton::parent(m);
+        }
+        if (found == 0xFFFFFFFFu) {
+            // the reference keeps the previous corner's data here (implicit_octree.rs:84-95)
+            atomicAdd(A.stale, 1ull);
+            found = prev;
+        }
+        A.corner[8 * (size_t)j + i] = found;
+        const float d = found != 0xFFFFFFFFu ? A.nvals[found] : 0.0f;
+        if (!(d > 0.0f)) cs |= 1u << i;
+        prev = found;
+    }
+    A.cases[j] = (uint8_t)cs;
+    A.tri_counts[j] = iso_tri_count[cs];
+}
+
+__device__ __forceinline__ uint64_t edge_key(const unsigned long long* nkeys, const uint32_t* corner, uint32_t e) {
+    const uint32_t u = corner[iso_edge_connection[e][0]], w = corner[iso_edge_connection[e][1]];
+    const uint64_t a = u != 0xFFFFFFFFu ? nkeys[u] : 1ull, b = w != 0xFFFFFFFFu ? nkeys[w] : 1ull;
+    return a > b ? ((b << 32) | a) : ((a << 32) | b);  // MortonKey::new, index_cache.rs:63-73
+}
+
+struct EdgeArgs {
+    const unsigned long long* nkeys;
+    const uint32_t* corner;
+    const uint8_t* cases;
+    uint32_t ncubes;
+    unsigned long long* hkeys;
+    unsigned long long* hvals;  // first visitor: cube << 4 | first-use rank
+    uint32_t hmask;
+    uint32_t* vcounts;
+    uint16_t* owned;            // per cube: owned first-use ranks
+    uint32_t* err;
+};
+
+__global__ void edge_visit(EdgeArgs A) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= A.ncubes) return;
+    const uint32_t cs = A.cases[j];
+    const uint64_t ord = iso_edge_order[cs];
+    const uint32_t ne = iso_edge_count[cs];
+    for (uint32_t r = 0; r < ne; ++r) {
+        const uint32_t e = (uint32_t)(ord >> (4 * r)) & 15u;
+        const uint64_t k = edge_key(A.nkeys, A.corner + 8 * (size_t)j, e);
+        const uint32_t slot = ht_insert(A.hkeys, A.hmask, k);
+        if (slot == 0xFFFFFFFFu) {
+            atomicOr(A.err, DERR_CAPACITY);
+            continue;
+        }
+        atomicMin(A.hvals + slot, (unsigned long long)(((uint64_t)j << 4) | r));
+    }
+}
+
+__global__ void edge_own(EdgeArgs A) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= A.ncubes) return;
+    const uint32_t cs = A.cases[j];
+    const uint64_t ord = iso_edge_order[cs];
+    const uint32_t ne = iso_edge_count[cs];
+    uint32_t mask = 0;
+    for (uint32_t r = 0; r < ne; ++r) {
+        const uint32_t e = (uint32_t)(ord >> (4 * r)) & 15u;
+        const uint32_t slot = ht_find(A.hkeys, A.hmask, edge_key(A.nkeys, A.corner + 8 * (size_t)j, e));
+        if (slot != 0xFFFFFFFFu && A.hvals[slot] == (((uint64_t)j << 4) | r)) mask |= 1u << r;
+    }
+    A.owned[j] = (uint16_t)mask;
+    A.vcounts[j] = __popc(mask);
+}
+
+struct EmitArgs {
+    const unsigned long long* nkeys;
+    const float* nvals;
+    const uint32_t* corner;
+    const uint8_t* cases;
+    const uint16_t* owned;
+    const uint32_t* vbase;
+    const uint32_t* tbase;
+    uint32_t ncubes;
+    const unsigned long long* hkeys;
+    const unsigned long long* hvals;
+    uint32_t hmask;
+    float* out_v;
+    uint32_t* out_i;
+    uint64_t* out_k;
+    uint32_t* err;
+};
+
+__global__ void cube_emit(EmitArgs A) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= A.ncubes) return;
+    const uint32_t cs = A.cases[j];
+    const uint32_t nt = iso_tri_count[cs];
+    if (nt == 0) return;
+    const uint32_t* corner = A.corner + 8 * (size_t)j;
+    const uint64_t ord = iso_edge_order[cs];
+    const uint32_t ne = iso_edge_count[cs];
+    const uint32_t own = A.owned[j];
+    const uint32_t vb = A.vbase[j];
+    uint32_t ids[12];
+    for (uint32_t r = 0; r < ne; ++r) {
+        const uint32_t e = (uint32_t)(ord >> (4 * r)) & 15u;
+        const uint64_t k = edge_key(A.nkeys, corner, e);
+        if ((own >> r) & 1u) {
+            // find_crossing_point over the two corner nodes (distance.rs:64-69)
+            const uint32_t u = corner[iso_edge_connection[e][0]], w = corner[iso_edge_connection[e][1]];
+            const uint64_t ku = u != 0xFFFFFFFFu ? A.nkeys[u] : 1ull, kw = w != 0xFFFFFFFFu ? A.nkeys[w] : 1ull;
+            const float fa = u != 0xFFFFFFFFu ? A.nvals[u] : 0.0f, fb = w != 0xFFFFFFFFu ? A.nvals[w] : 0.0f;
+            const V3 pa = morton::center(ku), pb = morton::center(kw);
+            const float delta = fb - fa;
+            const float t = (delta == 0.0f) ? 0.5f : -fa / delta;
+            const float omt = 1.0f - t;
+            const uint32_t vid = vb + __popc(own & ((1u << r) - 1u));
+            A.out_v[3 * (size_t)vid + 0] = pa.x * omt + pb.x * t;
+            A.out_v[3 * (size_t)vid + 1] = pa.y * omt + pb.y * t;
+            A.out_v[3 * (size_t)vid + 2] = pa.z * omt + pb.z * t;
+            if (A.out_k) {
+                A.out_k[2 * (size_t)vid] = k >> 32;
+                A.out_k[2 * (size_t)vid + 1] = k & 0xFFFFFFFFull;
+            }
+            ids[r] = vid;
+        } else {
+            const uint32_t slot = ht_find(A.hkeys, A.hmask, k);
+            if (slot == 0xFFFFFFFFu) {
+                atomicOr(A.err, DERR_CAPACITY);
+                ids[r] = 0;
+                continue;
+            }
+            const uint64_t code = A.hvals[slot];
+            const uint32_t oj = (uint32_t)(code >> 4), orank = (uint32_t)(code & 15u);
+            ids[r] = A.vbase[oj] + __popc((uint32_t)A.owned[oj] & ((1u << orank) - 1u));
+        }
+    }
+    const uint64_t slotw = iso_tri_slot[cs];
+    const size_t t0 = A.tbase[j];
+    for (uint32_t k = 0; k < 3 * nt; ++k) A.out_i[3 * t0 + k] = ids[(slotw >> (4 * k)) & 15u];
+}
+
+}  // namespace
+}  // namespace iso
+
+using namespace iso;
+
+namespace {
+
+struct Arena {
+    char* base;
+    size_t used, cap;
+    template <class T>
+    T* take(size_t n) {
+        size_t at = (used + 255) & ~(size_t)255;
+        used = at + n * sizeof(T);
+        return used <= cap ? reinterpret_cast<T*>(base + at) : nullptr;
+    }
+};
+
+iso_status scan_u32(iso_ctx* ctx, const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* sums, uint32_t* total) {
+    const uint32_t nb = (n + 1023) / 1024;
+    if (n == 0) {
+        cudaMemsetAsync(total, 0, 4, ctx->stream);
+        return ISO_OK;
+    }
+    scan_blocks<<<nb, 1024, 0, ctx->stream>>>(in, out, n, sums);
+    scan_sums<<<1, 1024, 0, ctx->stream>>>(sums, nb, total);
+    scan_add<<<nb, 1024, 0, ctx->stream>>>(out, n, sums);
+    ctx->launches += 3;
+    return check_launch(ctx, "scan");
+}
+
+uint32_t pow2_at_least(uint64_t v) {
+    uint64_t p = 1024;
+    while (p < v) p <<= 1;
+    return (uint32_t)std::min<uint64_t>(p, 1ull << 31);
+}
+
+iso_status read_u32(iso_ctx* ctx, const uint32_t* d, uint32_t* h) {
+    cudaError_t e = cudaMemcpyAsync(ctx->h_pinned, d, 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "read count");
+    *h = *(uint32_t*)ctx->h_pinned;
+    return ISO_OK;
+}
+
+inline size_t scan_sums_for(uint64_t n) { return (size_t)((n + 1023) / 1024) + 64; }
+
+}  // namespace
+
+extern "C" iso_status iso_lhmc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t max_depth, uint32_t flags,
+                                       iso_mesh_info* info) {
+    if (!ctx || !prog) return ISO_ERR_INVALID_ARG;
+    if (prog->ctx != ctx) return fail(ctx, ISO_ERR_INVALID_ARG, "program belongs to another context");
+    if (max_depth > 10) return fail(ctx, ISO_ERR_INVALID_ARG, "max_depth above 10 (Morton keys must fit 31 bits)");
+    if (flags & ~(uint32_t)ISO_FLAG_KEYS) return fail(ctx, ISO_ERR_INVALID_ARG, "unsupported flags");
+    iso_status s = set_device(ctx);
+    if (s != ISO_OK) return s;
+    ctx->last = iso_mesh_info{};
+    ctx->last_flags = flags;
+    ctx->last_vertex_floats = 3;
+    StageTimer timer(ctx, ISO_STAGE_OCTREE);
+    // ---- 1. octree, generation by generation (root, then 8 per refined node)
+    uint64_t max_nodes = 1;
+    {
+        uint64_t gen = 1;
+        for (uint32_t g = 0; g < max_depth + 2; ++g) {
+            gen *= 8;
+            max_nodes += gen;
+            if (max_nodes > (1ull << 28)) break;
+        }
+    }
+    // node arrays grow as generations are built
+    size_t node_cap = (size_t)std::min<uint64_t>(max_nodes, 1ull << 20);
+    auto node_bytes = [](size_t cap) { return cap * (8 + 4 + 4 + 4) + 4 * scan_sums_for(cap) + 4 * 1024 + 4096; };
+    if ((s = ensure(ctx, ctx->aux, node_bytes(node_cap))) != ISO_OK) return s;
+    auto carve = [&](size_t cap, unsigned long long** keys, float** vals, uint32_t** refine, uint32_t** rank,
+                     uint32_t** sums, uint32_t** total) {
+        Arena a{(char*)ctx->aux.p, 0, ctx->aux.bytes};
+        *keys = a.take<unsigned long long>(cap);
+        *vals = a.take<float>(cap);
+        *refine = a.take<uint32_t>(cap);
+        *rank = a.take<uint32_t>(cap);
+        *sums = a.take<uint32_t>(scan_sums_for(cap));
+        *total = a.take<uint32_t>(64);
+    };
+    unsigned long long* nkeys;
+    float* nvals;
+    uint32_t *refine, *rank, *sums, *total;
+    carve(node_cap, &nkeys, &nvals, &refine, &rank, &sums, &total);
+    unsigned long long root = 1;
+    cudaError_t e = cudaMemcpyAsync(nkeys, &root, 8, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "root");
+    uint32_t off = 0, cnt = 1;
+    while (cnt > 0) {
+        GenArgs ga{prog->view(), nkeys, nvals, refine, off, cnt, max_depth};
+        oct_eval<<<(cnt + 127) / 128, 128, 0, ctx->stream>>>(ga);
+        ctx->launches++;
+        if ((s = scan_u32(ctx, refine + off, rank, cnt, sums, total)) != ISO_OK) return s;
+        uint32_t nref = 0;
+        if ((s = read_u32(ctx, total, &nref)) != ISO_OK) return s;
+        const uint64_t next = 8ull * nref;
+        const uint64_t need = (uint64_t)off + cnt + next;
+        if (need >= 0xFFFFFFF0ull) return fail(ctx, ISO_ERR_TOO_LARGE, "octree too large");
+        if (need > node_cap) {
+            // grow: copy the built prefix into a larger arena
+            const size_t new_cap = (size_t)std::max<uint64_t>(need, 2 * node_cap);
+            void* fresh = nullptr;
+            e = cudaMalloc(&fresh, node_bytes(new_cap));
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "grow octree");
+            Arena a{(char*)fresh, 0, node_bytes(new_cap)};
+            unsigned long long* k2 = a.take<unsigned long long>(new_cap);
+            float* v2 = a.take<float>(new_cap);
+            uint32_t* r2 = a.take<uint32_t>(new_cap);
+            uint32_t* q2 = a.take<uint32_t>(new_cap);
+            cudaMemcpyAsync(k2, nkeys, 8ull * (off + cnt), cudaMemcpyDeviceToDevice, ctx->stream);
+            cudaMemcpyAsync(v2, nvals, 4ull * (off + cnt), cudaMemcpyDeviceToDevice, ctx->stream);
+            cudaMemcpyAsync(r2, refine, 4ull * (off + cnt), cudaMemcpyDeviceToDevice, ctx->stream);
+            cudaMemcpyAsync(q2, rank, 4ull * cnt, cudaMemcpyDeviceToDevice, ctx->stream);
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(ctx->aux.p);
+            ctx->aux.p = fresh;
+            ctx->aux.bytes = node_bytes(new_cap);
+            node_cap = new_cap;
+            nkeys = k2;
+            nvals = v2;
+            refine = r2;
+            rank = q2;
+            Arena rest{(char*)fresh, 0, ctx->aux.bytes};
+            rest.take<unsigned long long>(new_cap);
+            rest.take<float>(new_cap);
+            rest.take<uint32_t>(new_cap);
+            rest.take<uint32_t>(new_cap);
+            sums = rest.take<uint32_t>(scan_sums_for(new_cap));
+            total = rest.take<uint32_t>(64);
+        }
+        if (nref) {
+            oct_expand<<<(cnt + 127) / 128, 128, 0, ctx->stream>>>(nkeys, refine, rank, off, cnt, off + cnt);
+            ctx->launches++;
+        }
+        off += cnt;
+        cnt = (uint32_t)next;
+    }
+    const uint32_t nodes = off;
+    if ((s = check_launch(ctx, "octree")) != ISO_OK) return s;
+
+    // ---- 2. primal vertices (hash: vertex -> deepest level, smallest key)
+    const uint32_t hcap1 = pow2_at_least(16ull * nodes);
+    const size_t pv_cap = 8ull * nodes;
+    {
+        const size_t bytes = 16ull * hcap1 + 4ull * nodes * 2 + 9ull * pv_cap + 4 * scan_sums_for(nodes) + 4096;
+        if ((s = ensure(ctx, ctx->aux2, bytes)) != ISO_OK) return s;
+    }
+    Arena a2{(char*)ctx->aux2.p, 0, ctx->aux2.bytes};
+    unsigned long long* hk1 = a2.take<unsigned long long>(hcap1);
+    unsigned long long* hv1 = a2.take<unsigned long long>(hcap1);
+    uint32_t* counts = a2.take<uint32_t>(nodes);
+    uint32_t* offsets = a2.take<uint32_t>(nodes);
+    unsigned long long* pv_key = a2.take<unsigned long long>(pv_cap);
+    uint8_t* pv_level = a2.take<uint8_t>(pv_cap);
+    uint32_t* sums2 = a2.take<uint32_t>(scan_sums_for(nodes));
+    uint32_t* total2 = a2.take<uint32_t>(64);
+    e = cudaMemsetAsync(hk1, 0, 16ull * hcap1, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "memset table");
+    LeafArgs la{nkeys, refine, nodes, hk1, hv1, hcap1 - 1, counts, ctx->d_err};
+    leaf_insert<<<(unsigned)((8ull * nodes + 255) / 256), 256, 0, ctx->stream>>>(la);
+    leaf_count<<<(nodes + 255) / 256, 256, 0, ctx->stream>>>(la);
+    ctx->launches += 2;
+    if ((s = scan_u32(ctx, counts, offsets, nodes, sums2, total2)) != ISO_OK) return s;
+    leaf_write<<<(nodes + 255) / 256, 256, 0, ctx->stream>>>(la, offsets, pv_key, pv_level);
+    ctx->launches++;
+    uint32_t ncubes = 0;
+    if ((s = read_u32(ctx, total2, &ncubes)) != ISO_OK) return s;
+
+    // ---- 3./4. dual cubes and their marching cubes
+    const uint32_t hcap2 = pow2_at_least(8ull * ncubes + 1024);
+    {
+        const size_t bytes = 32ull * ncubes + ncubes + 4ull * ncubes * 4 + 2ull * ncubes + 16ull * hcap2 +
+                             8 * scan_sums_for(ncubes) + 8192;
+        if ((s = ensure(ctx, ctx->aux3, bytes)) != ISO_OK) return s;
+    }
+    Arena a3{(char*)ctx->aux3.p, 0, ctx->aux3.bytes};
+    uint32_t* corner = a3.take<uint32_t>(8ull * ncubes);
+    uint8_t* cases = a3.take<uint8_t>(ncubes);
+    uint32_t* tcount = a3.take<uint32_t>(ncubes);
+    uint32_t* tbase = a3.take<uint32_t>(ncubes);
+    uint32_t* vcount = a3.take<uint32_t>(ncubes);
+    uint32_t* vbase = a3.take<uint32_t>(ncubes);
+    uint16_t* owned = a3.take<uint16_t>(ncubes);
+    unsigned long long* hk2 = a3.take<unsigned long long>(hcap2);
+    unsigned long long* hv2 = a3.take<unsigned long long>(hcap2);
+    uint32_t* sums3 = a3.take<uint32_t>(2 * scan_sums_for(ncubes));
+    uint32_t* tot3 = a3.take<uint32_t>(16);
+    unsigned long long* stale = (unsigned long long*)(tot3 + 8);
+    e = cudaMemsetAsync(hk2, 0, 8ull * hcap2, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(hv2, 0xFF, 8ull * hcap2, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(stale, 0, 8, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "memset");
+    if (ncubes) {
+        CubeArgs ca{nkeys, nvals, nodes, pv_key, pv_level, ncubes, corner, cases, tcount, stale};
+        cube_gather<<<(ncubes + 127) / 128, 128, 0, ctx->stream>>>(ca);
+        EdgeArgs ea{nkeys, corner, cases, ncubes, hk2, hv2, hcap2 - 1, vcount, owned, ctx->d_err};
+        edge_visit<<<(ncubes + 127) / 128, 128, 0, ctx->stream>>>(ea);
+        edge_own<<<(ncubes + 127) / 128, 128, 0, ctx->stream>>>(ea);
+        ctx->launches += 3;
+    }
+    if ((s = scan_u32(ctx, tcount, tbase, ncubes, sums3, tot3)) != ISO_OK) return s;
+    if ((s = scan_u32(ctx, vcount, vbase, ncubes, sums3 + scan_sums_for(ncubes), tot3 + 1)) != ISO_OK) return s;
+    e = cudaMemcpyAsync(ctx->h_pinned, tot3, 16, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_pinned + 2, stale, 8, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "read totals");
+    if ((s = read_device_errors(ctx)) != ISO_OK) return s;
+    const uint32_t nt = ((uint32_t*)ctx->h_pinned)[0], nv = ((uint32_t*)ctx->h_pinned)[1];
+    ctx->lhmc_stale = ctx->h_pinned[2];
+    const bool keys = (flags & ISO_FLAG_KEYS) != 0;
+    if ((s = ensure(ctx, ctx->mesh_v, 12ull * std::max<uint32_t>(nv, 1))) != ISO_OK) return s;
+    if ((s = ensure(ctx, ctx->mesh_i, 12ull * std::max<uint32_t>(nt, 1))) != ISO_OK) return s;
+    if (keys && (s = ensure(ctx, ctx->mesh_k, 16ull * std::max<uint32_t>(nv, 1))) != ISO_OK) return s;
+    if (nt) {
+        EmitArgs ma{nkeys, nvals, corner, cases, owned, vbase, tbase, ncubes, hk2, hv2, hcap2 - 1,
+                    (float*)ctx->mesh_v.p, (uint32_t*)ctx->mesh_i.p, keys ? (uint64_t*)ctx->mesh_k.p : nullptr,
+                    ctx->d_err};
+        cube_emit<<<(ncubes + 127) / 128, 128, 0, ctx->stream>>>(ma);
+        ctx->launches++;
+        if ((s = check_launch(ctx, "cube_emit")) != ISO_OK) return s;
+    }
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "sync");
+    if ((s = read_device_errors(ctx)) != ISO_OK) return s;
+    ctx->last.num_vertices = nv;
+    ctx->last.num_triangles = nt;
+    ctx->last.num_cells = ncubes;
+    if (info) *info = ctx->last;
+    return ISO_OK;
+}
+
+extern "C" uint64_t iso_lhmc_stale_corners(const iso_ctx* ctx) { return ctx ? ctx->lhmc_stale : 0; }

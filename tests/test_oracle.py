@@ -151,6 +151,21 @@ def test_morton_level_rule():
     assert [oracle.lib().oracle_morton_level(k) for k in (1, 7, 8, 9, 63, 64, 65, 512)] == [0, 0, 0, 1, 1, 1, 2, 2]
 
 
+def test_morton_level_rule_up_to_depth_10():
+    """Both level functions are monotone step functions that can only differ
+    near powers of 8, so checking a window around each power up to 8^10 (keys
+    of depth <= 10 are below 2^31) extends the exhaustive check above."""
+    L = oracle.lib()
+    for lv in range(9, 11):
+        p = 1 << (3 * lv)
+        for k in list(range(p - 4096, p + 4096)) + [2 * p - 1, 2 * p, 2 * p + 1]:
+            msb = k.bit_length() - 1
+            rule = msb // 3
+            if rule > 0 and k == 1 << (3 * rule):
+                rule -= 1
+            assert L.oracle_morton_level(k) == rule, k
+
+
 def test_morton_primal_dual_roundtrip():
     L = oracle.lib()
     key = (1 << 9) | 0b101_011_110  # a level-3 node
