@@ -269,6 +269,40 @@ ISO_API iso_status iso_lhmc_extract(iso_ctx* ctx, const iso_program* prog, uint3
 ISO_API uint64_t iso_lhmc_stale_corners(const iso_ctx* ctx);
 
 /* ------------------------------------------------------------------------ */
+/* Batches of independent MarchingCubes chunks                               */
+/* ------------------------------------------------------------------------ */
+/* No single reference call: a batch stands for a loop of
+ * MarchingCubes::new(size_i).extract(&source_i, &mut e_i) over many chunks
+ * (marching_cubes.rs:59-82), each chunk its own IndexedVertices mesh.
+ * The context's mesh holds all chunks' vertices and triangles back to back,
+ * indices local to each chunk; iso_batch_extents gives, per chunk, (first
+ * vertex, vertex count, first triangle, triangle count). */
+typedef struct iso_chunk_desc {
+    uint32_t program;   /* index into the programs array */
+    uint32_t size;      /* MarchingCubes::new(size), 2..1025 */
+} iso_chunk_desc;
+typedef struct iso_batch iso_batch;
+#define ISO_BATCH_GRAPH 1u   /* replay the batch as one CUDA graph (sized by the previous run) */
+
+ISO_API iso_status iso_batch_create(iso_ctx* ctx, const iso_program* const* programs, uint32_t nprograms,
+                                    const iso_chunk_desc* chunks, uint32_t nchunks, iso_batch** out);
+ISO_API iso_status iso_batch_destroy(iso_batch* batch);
+/* Run every chunk: work-queue sampler + chunked classify/scan/emit over all
+ * chunks at once.  The first run (and any run after a capacity overflow) is
+ * eager; with ISO_BATCH_GRAPH later runs replay one captured CUDA graph. */
+ISO_API iso_status iso_batch_run(iso_batch* batch, uint32_t flags, iso_mesh_info* info);
+/* The same chunks one extraction at a time (the per-chunk-launch baseline). */
+ISO_API iso_status iso_batch_run_per_chunk(iso_batch* batch, iso_mesh_info* info);
+ISO_API iso_status iso_batch_extents(iso_batch* batch, uint32_t* extents /* 4 per chunk */);
+/* Sampler slab depth (z layers per work-queue tile) for chunks of `size`
+ * (0: all sizes); depth 0 = whole chunk. */
+ISO_API iso_status iso_batch_set_slab(iso_batch* batch, uint32_t size, uint32_t depth);
+/* Times the sampler at each candidate slab depth for every chunk-size class
+ * of the batch and keeps the fastest; results are cached per GPU model in
+ * `cache_path` (nullable).  `chosen` (nullable) receives (size, depth) pairs. */
+ISO_API iso_status iso_batch_autotune(iso_batch* batch, const char* cache_path, uint32_t* chosen);
+
+/* ------------------------------------------------------------------------ */
 /* PointCloud (src/point_cloud.rs:50-63)                                      */
 /* ------------------------------------------------------------------------ */
 ISO_API iso_status iso_point_cloud_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size,

@@ -31,6 +31,12 @@ class MeshInfo(ctypes.Structure):
                 ("num_cells", ctypes.c_uint64)]
 
 
+class ChunkDesc(ctypes.Structure):
+    _fields_ = [("program", ctypes.c_uint32), ("size", ctypes.c_uint32)]
+
+
+ISO_BATCH_GRAPH = 1
+
 _lib = None
 
 vp = ctypes.c_void_p
@@ -67,6 +73,13 @@ SIGNATURES = {
     "iso_dc_extract": (i32, [vp, vp, u32, u32, u32, ctypes.POINTER(MeshInfo)]),
     "iso_lhmc_extract": (i32, [vp, vp, u32, u32, ctypes.POINTER(MeshInfo)]),
     "iso_lhmc_stale_corners": (u64, [vp]),
+    "iso_batch_create": (i32, [vp, ctypes.POINTER(vp), u32, ctypes.POINTER(ChunkDesc), u32, ctypes.POINTER(vp)]),
+    "iso_batch_destroy": (i32, [vp]),
+    "iso_batch_run": (i32, [vp, u32, ctypes.POINTER(MeshInfo)]),
+    "iso_batch_run_per_chunk": (i32, [vp, ctypes.POINTER(MeshInfo)]),
+    "iso_batch_extents": (i32, [vp, u32p]),
+    "iso_batch_set_slab": (i32, [vp, u32, u32]),
+    "iso_batch_autotune": (i32, [vp, ctypes.c_char_p, u32p]),
     "iso_sample_points": (i32, [vp, vp, f32p, u64, f32p, f32p]),
 }
 

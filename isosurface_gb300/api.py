@@ -187,6 +187,80 @@ class Context:
         return v.value, i.value, k.value, info
 
 
+class Batch:
+    """Many independent MarchingCubes chunks extracted together.
+
+    chunks: list of (size, source); each chunk is MarchingCubes::new(size)
+    over its source.  run() meshes all of them (graph=True replays one CUDA
+    graph after the first, eager run); meshes() splits the result per chunk."""
+
+    def __init__(self, ctx, chunks):
+        from ._capi import ChunkDesc
+        self.ctx = ctx
+        progs, index, descs = [], {}, []
+        for size, src in chunks:
+            data = bytes(src if isinstance(src, (bytes, bytearray)) else lower(src))
+            if data not in index:
+                index[data] = len(progs)
+                progs.append(ctx.program(data))
+            descs.append(ChunkDesc(index[data], size))
+        self.n = len(descs)
+        self.sizes = [d.size for d in descs]
+        arr = (ctypes.c_void_p * len(progs))(*[p.h.value for p in progs])
+        darr = (ChunkDesc * len(descs))(*descs)
+        h = ctypes.c_void_p()
+        check(lib().iso_batch_create(ctx.h, arr, len(progs), darr, len(descs), ctypes.byref(h)), ctx.h)
+        self.h = h
+        self._programs = progs
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().iso_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, graph=True):
+        from ._capi import ISO_BATCH_GRAPH
+        info = MeshInfo()
+        check(lib().iso_batch_run(self.h, ISO_BATCH_GRAPH if graph else 0, ctypes.byref(info)), self.ctx.h)
+        return info
+
+    def run_per_chunk(self):
+        info = MeshInfo()
+        check(lib().iso_batch_run_per_chunk(self.h, ctypes.byref(info)), self.ctx.h)
+        return info
+
+    def set_slab(self, size, depth):
+        check(lib().iso_batch_set_slab(self.h, size, depth), self.ctx.h)
+
+    def autotune(self, cache_path=None):
+        out = (ctypes.c_uint32 * 64)()
+        check(lib().iso_batch_autotune(self.h, cache_path.encode() if cache_path else None, out), self.ctx.h)
+        chosen = {}
+        for k in range(32):
+            if out[2 * k]:
+                chosen[int(out[2 * k])] = int(out[2 * k + 1])
+        return chosen
+
+    def extents(self):
+        ext = np.empty((self.n, 4), np.uint32)
+        check(lib().iso_batch_extents(self.h, ext.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))), self.ctx.h)
+        return ext
+
+    def meshes(self, info):
+        whole = self.ctx.download(info)
+        ext = self.extents()
+        out = []
+        for v0, nv, t0, nt in ext:
+            out.append(Mesh(whole.vertices[v0:v0 + nv], whole.indices[3 * t0:3 * (t0 + nt)]))
+        return out
+
+
 _default = {}
 
 

@@ -27,6 +27,7 @@ UNITS = {
     "mc.cu": ["-fmad=false"],
     "dc.cu": ["-fmad=false"],
     "lhmc.cu": ["-fmad=false"],
+    "batch.cu": ["-fmad=false"],
 }
 HEADERS = ["internal.h", "vm.cuh", "mc_tables.h", "mc_chunk.cuh", "qef.cuh"]
 

@@ -1,0 +1,538 @@
+// Batched MarchingCubes: thousands of independent chunks, each a
+// MarchingCubes::new(size_i).extract over its own source, in one pass.
+//
+// * Sampling: one persistent kernel drains a work queue of (chunk, z-slab)
+//   tiles (largest cost first); each block evaluates its tile's points with
+//   the chunk's program and writes the chunk's field and sign bits.  The slab
+//   depth per chunk-size class comes from iso_batch_autotune.
+// * Classification, scan and emission: the chunked marching-cubes passes of
+//   mc.cu over a table of grids whose 32-cell chunks are laid out
+//   range-aligned in one global index space (mc_chunk.cuh).
+// * iso_batch_run with ISO_BATCH_GRAPH captures all of it in one CUDA graph
+//   and replays it; output capacities come from the previous run (the first
+//   run is eager and sizes them), and an overflow is detected on the device
+//   and answered with an eager re-run.
+// * iso_batch_run_per_chunk runs the same chunks one extraction at a time
+//   (sample, count, scan, emit, with the host syncs of iso_mc_extract) and
+//   concatenates the meshes: the comparison point for the batch.
+//
+// Output: the context's mesh holds all chunks' vertices and triangles
+// back to back; indices are local to each chunk (each chunk is its own
+// IndexedVertices mesh); iso_batch_extents gives each chunk's
+// (first vertex, vertices, first triangle, triangles).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+#include "vm.cuh"
+
+namespace iso {
+// defined in mc.cu
+iso_status mc_extract_grids(iso_ctx* ctx, const void* d_grids, uint32_t ngrids, const uint32_t* d_range_grid,
+                            uint32_t chunks, uint32_t max_cw, void* scratch, uint64_t cap_v, uint64_t cap_t,
+                            float* out_v, uint32_t* out_i, uint32_t* extents, uint64_t* totals, bool sync_sizes);
+size_t mc_grid_bytes();
+void mc_fill_grid(void* dst, const Lattice& L, uint32_t chunk0, uint32_t* nchunks, uint32_t* cw);
+size_t mc_grids_scratch_bytes(uint32_t chunks, uint32_t ngrids);
+}  // namespace iso
+
+using namespace iso;
+
+namespace {
+
+struct SampleGrid {
+    ProgView pv;
+    uint32_t n;  // MarchingCubes::new(n): n x n x (n+1) samples
+    float inv;
+    float* field;
+    uint64_t pitch;
+    uint32_t* bits;
+    uint32_t W;
+};
+
+struct Tile {
+    uint32_t grid, z0, z1;
+};
+
+__global__ void __launch_bounds__(256) batch_sample(const Tile* tiles, uint32_t ntiles, const SampleGrid* grids,
+                                                    uint32_t* next) {
+    __shared__ uint32_t s_tile;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    while (true) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_tile = atomicAdd(next, 1u);
+        __syncthreads();
+        const uint32_t t = s_tile;
+        if (t >= ntiles) return;
+        const Tile tl = tiles[t];
+        const SampleGrid g = grids[tl.grid];
+        const uint32_t tasks = (tl.z1 - tl.z0) * g.n * g.W;
+        for (uint32_t task = warp; task < tasks; task += 8) {
+            const uint32_t w = task % g.W, r = task / g.W;
+            const uint32_t y = r % g.n, z = tl.z0 + r / g.n;
+            const uint32_t x = 32 * w + lane;
+            bool inside = false;
+            const size_t row = (size_t)z * g.n + y;
+            if (x < g.n) {
+                const float v = eval_scalar(g.pv, v3((float)x * g.inv, (float)y * g.inv, (float)z * g.inv));
+                g.field[row * g.pitch + x] = v;
+                inside = !(v > 0.0f);
+            }
+            const uint32_t b = __ballot_sync(0xFFFFFFFFu, inside);
+            if (lane == 0) g.bits[row * g.W + w] = b;
+        }
+    }
+}
+
+struct Chunk {
+    uint32_t prog, size;
+};
+
+}  // namespace
+
+struct iso_batch {
+    iso_ctx* ctx = nullptr;
+    std::vector<const iso_program*> programs;
+    std::vector<Chunk> chunks;
+    std::vector<uint32_t> slab;      // slab depth per chunk (0 = whole grid)
+    // device layout
+    void* arena = nullptr;
+    size_t arena_bytes = 0;
+    SampleGrid* d_sgrids = nullptr;
+    void* d_grids = nullptr;
+    uint32_t* d_range_grid = nullptr;
+    Tile* d_tiles = nullptr;
+    uint32_t ntiles = 0;
+    uint32_t* d_next = nullptr;
+    uint32_t* d_extents = nullptr;   // 4 per chunk
+    uint64_t* d_totals = nullptr;    // [0] triangles [1] vertices
+    void* d_scratch = nullptr;       // chunk-pass scratch
+    uint32_t total_chunks = 0, max_cw = 0;
+    std::vector<SampleGrid> sgrids;
+    std::vector<uint32_t> grid_chunk0;
+    // outputs and graph
+    uint64_t cap_v = 0, cap_t = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool sized = false;
+};
+
+namespace {
+
+uint32_t size_class(uint32_t size) {
+    uint32_t c = 0;
+    while ((1u << (c + 1)) < size) ++c;
+    return c;  // 17 -> 4, 33 -> 5, 65 -> 6
+}
+
+iso_status build_tiles(iso_batch* b) {
+    std::vector<std::pair<double, Tile>> t;
+    for (uint32_t i = 0; i < b->chunks.size(); ++i) {
+        const uint32_t n = b->chunks[i].size, nz = n + 1;
+        const uint32_t depth = b->slab[i] ? b->slab[i] : nz;
+        const double cost_per_layer = (double)n * ((n + 31) / 32 * 32) * (double)b->programs[b->chunks[i].prog]->ops.size();
+        for (uint32_t z0 = 0; z0 < nz; z0 += depth) {
+            const uint32_t z1 = std::min(nz, z0 + depth);
+            t.push_back({cost_per_layer * (z1 - z0), Tile{i, z0, z1}});
+        }
+    }
+    std::stable_sort(t.begin(), t.end(), [](const auto& a, const auto& c) { return a.first > c.first; });
+    std::vector<Tile> tiles(t.size());
+    for (size_t i = 0; i < t.size(); ++i) tiles[i] = t[i].second;
+    if (b->d_tiles) cudaFree(b->d_tiles);
+    b->d_tiles = nullptr;
+    b->ntiles = (uint32_t)tiles.size();
+    cudaError_t e = cudaMalloc(&b->d_tiles, sizeof(Tile) * std::max<size_t>(tiles.size(), 1));
+    if (e == cudaSuccess && !tiles.empty())
+        e = cudaMemcpy(b->d_tiles, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice);
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    if (b->graph) {
+        cudaGraphDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    return e == cudaSuccess ? ISO_OK : cuda_fail(b->ctx, e, "tiles");
+}
+
+int sample_blocks() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return std::max(1, sms) * 8;
+}
+
+// enqueue the whole batch on the context's stream (no host sync)
+iso_status enqueue(iso_batch* b, bool sync_sizes) {
+    iso_ctx* ctx = b->ctx;
+    cudaError_t e = cudaMemsetAsync(b->d_next, 0, 4, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "memset queue");
+    {
+        StageTimer timer(ctx, ISO_STAGE_SAMPLE);
+        batch_sample<<<sample_blocks(), 256, 0, ctx->stream>>>(b->d_tiles, b->ntiles, b->d_sgrids, b->d_next);
+    }
+    ctx->launches++;
+    iso_status s = check_launch(ctx, "batch_sample");
+    if (s != ISO_OK) return s;
+    return mc_extract_grids(ctx, b->d_grids, (uint32_t)b->chunks.size(), b->d_range_grid, b->total_chunks, b->max_cw,
+                            b->d_scratch, b->cap_v, b->cap_t, (float*)ctx->mesh_v.p, (uint32_t*)ctx->mesh_i.p,
+                            b->d_extents, b->d_totals, sync_sizes);
+}
+
+iso_status finish(iso_batch* b, iso_mesh_info* info) {
+    iso_ctx* ctx = b->ctx;
+    cudaError_t e = cudaMemcpyAsync(ctx->h_pinned, b->d_totals, 16, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_pinned + 2, ctx->d_err, 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "batch totals");
+    const uint64_t nt = ctx->h_pinned[0], nv = ctx->h_pinned[1];
+    uint64_t cells = 0;
+    for (auto& c : b->chunks) cells += (uint64_t)(c.size - 1) * (c.size - 1) * c.size;
+    ctx->last.num_vertices = nv;
+    ctx->last.num_triangles = nt;
+    ctx->last.num_cells = cells;
+    ctx->last_flags = 0;
+    ctx->last_vertex_floats = 3;
+    if (info) *info = ctx->last;
+    if ((uint32_t)ctx->h_pinned[2]) return read_device_errors(ctx);
+    return ISO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+iso_status iso_batch_create(iso_ctx* ctx, const iso_program* const* programs, uint32_t nprograms,
+                            const iso_chunk_desc* chunks, uint32_t nchunks, iso_batch** out) {
+    if (!ctx || !out || (!programs && nprograms) || (!chunks && nchunks) || nchunks == 0) return ISO_ERR_INVALID_ARG;
+    *out = nullptr;
+    iso_status s = set_device(ctx);
+    if (s != ISO_OK) return s;
+    iso_batch* b = new iso_batch();
+    b->ctx = ctx;
+    b->programs.assign(programs, programs + nprograms);
+    for (uint32_t i = 0; i < nprograms; ++i)
+        if (!programs[i] || programs[i]->ctx != ctx) {
+            delete b;
+            return fail(ctx, ISO_ERR_INVALID_ARG, "null program or program of another context");
+        }
+    for (uint32_t i = 0; i < nchunks; ++i) {
+        if (chunks[i].program >= nprograms || chunks[i].size < 2 || chunks[i].size > 1025) {
+            delete b;
+            return fail(ctx, ISO_ERR_INVALID_ARG, "chunk program index out of range or size not in [2, 1025]");
+        }
+        b->chunks.push_back(Chunk{chunks[i].program, chunks[i].size});
+    }
+    b->slab.assign(nchunks, 4);
+    // layout: per chunk field + bits; grid tables; chunk-pass scratch
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        off = (off + 255) & ~(size_t)255;
+        const size_t at = off;
+        off += bytes;
+        return at;
+    };
+    std::vector<size_t> field_off(nchunks), bits_off(nchunks);
+    uint32_t chunk0 = 0;
+    b->grid_chunk0.resize(nchunks);
+    for (uint32_t i = 0; i < nchunks; ++i) {
+        const uint32_t n = b->chunks[i].size;
+        field_off[i] = take(4ull * default_pitch(n) * n * (n + 1));
+        bits_off[i] = take(4ull * words_per_row(n) * n * (n + 1));
+        const uint32_t cw = (n - 1 + 31) / 32;
+        const uint32_t nch = cw * (n - 1) * n;
+        b->grid_chunk0[i] = chunk0;
+        chunk0 += (nch + 255) / 256 * 256;
+        b->max_cw = std::max(b->max_cw, cw);
+    }
+    b->total_chunks = chunk0;
+    const uint32_t nranges = chunk0 / 256;
+    const size_t sg_off = take(sizeof(SampleGrid) * nchunks);
+    const size_t g_off = take(mc_grid_bytes() * nchunks);
+    const size_t rg_off = take(4ull * nranges);
+    const size_t next_off = take(256);
+    const size_t ext_off = take(16ull * nchunks);
+    const size_t tot_off = take(64);
+    const size_t scr_off = take(mc_grids_scratch_bytes(b->total_chunks, nchunks));
+    b->arena_bytes = off;
+    cudaError_t e = cudaMalloc(&b->arena, b->arena_bytes);
+    if (e != cudaSuccess) {
+        delete b;
+        return cuda_fail(ctx, e, "batch arena");
+    }
+    char* base = (char*)b->arena;
+    b->d_sgrids = (SampleGrid*)(base + sg_off);
+    b->d_grids = base + g_off;
+    b->d_range_grid = (uint32_t*)(base + rg_off);
+    b->d_next = (uint32_t*)(base + next_off);
+    b->d_extents = (uint32_t*)(base + ext_off);
+    b->d_totals = (uint64_t*)(base + tot_off);
+    b->d_scratch = base + scr_off;
+    std::vector<char> grids(mc_grid_bytes() * nchunks);
+    std::vector<uint32_t> range_grid(nranges);
+    b->sgrids.resize(nchunks);
+    for (uint32_t i = 0; i < nchunks; ++i) {
+        const uint32_t n = b->chunks[i].size;
+        const iso_program* p = b->programs[b->chunks[i].prog];
+        SampleGrid sg{p->view(), n, 1.0f / (float)(n - 1), (float*)(base + field_off[i]), default_pitch(n),
+                      (uint32_t*)(base + bits_off[i]), words_per_row(n)};
+        b->sgrids[i] = sg;
+        Lattice L{n, n, n + 1, default_pitch(n), sg.field, sg.bits, sg.W, sg.inv, nullptr};
+        uint32_t nch = 0, cw = 0;
+        mc_fill_grid(grids.data() + mc_grid_bytes() * i, L, b->grid_chunk0[i], &nch, &cw);
+        for (uint32_t r = b->grid_chunk0[i] / 256; r < (b->grid_chunk0[i] + nch + 255) / 256; ++r) range_grid[r] = i;
+    }
+    e = cudaMemcpy(b->d_sgrids, b->sgrids.data(), sizeof(SampleGrid) * nchunks, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_grids, grids.data(), grids.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && nranges)
+        e = cudaMemcpy(b->d_range_grid, range_grid.data(), 4ull * nranges, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        iso_batch_destroy(b);
+        return cuda_fail(ctx, e, "batch tables");
+    }
+    if ((s = build_tiles(b)) != ISO_OK) {
+        iso_batch_destroy(b);
+        return s;
+    }
+    *out = b;
+    return ISO_OK;
+}
+
+iso_status iso_batch_destroy(iso_batch* b) {
+    if (!b) return ISO_ERR_INVALID_ARG;
+    cudaSetDevice(b->ctx->device);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->d_tiles) cudaFree(b->d_tiles);
+    if (b->arena) cudaFree(b->arena);
+    delete b;
+    return ISO_OK;
+}
+
+iso_status iso_batch_set_slab(iso_batch* b, uint32_t size, uint32_t depth) {
+    if (!b) return ISO_ERR_INVALID_ARG;
+    for (size_t i = 0; i < b->chunks.size(); ++i)
+        if (size == 0 || b->chunks[i].size == size) b->slab[i] = depth;
+    return build_tiles(b);
+}
+
+iso_status iso_batch_run(iso_batch* b, uint32_t flags, iso_mesh_info* info) {
+    if (!b) return ISO_ERR_INVALID_ARG;
+    iso_ctx* ctx = b->ctx;
+    iso_status s = set_device(ctx);
+    if (s != ISO_OK) return s;
+    const bool graph = (flags & ISO_BATCH_GRAPH) != 0;
+    if (!graph || !b->sized) {
+        // eager: sizes are read back between the count and the emit passes
+        s = enqueue(b, true);
+        if (s != ISO_OK) return s;
+        if ((s = finish(b, info)) != ISO_OK) return s;
+        if (!b->sized || ctx->last.num_vertices > b->cap_v || ctx->last.num_triangles > b->cap_t) {
+            b->cap_v = ctx->last.num_vertices + ctx->last.num_vertices / 4 + 1024;
+            b->cap_t = ctx->last.num_triangles + ctx->last.num_triangles / 4 + 1024;
+            b->sized = true;
+            if (b->exec) {
+                cudaGraphExecDestroy(b->exec);
+                b->exec = nullptr;
+            }
+            if (b->graph) {
+                cudaGraphDestroy(b->graph);
+                b->graph = nullptr;
+            }
+        }
+        return ISO_OK;
+    }
+    if ((s = ensure(ctx, ctx->mesh_v, 12 * b->cap_v)) != ISO_OK) return s;
+    if ((s = ensure(ctx, ctx->mesh_i, 12 * b->cap_t)) != ISO_OK) return s;
+    if (!b->exec) {
+        cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "begin capture");
+        const bool timing = ctx->timing;
+        ctx->timing = false;  // no events inside the graph
+        s = enqueue(b, false);
+        ctx->timing = timing;
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(ctx->stream, &g);
+        if (s != ISO_OK) {
+            if (g) cudaGraphDestroy(g);
+            return s;
+        }
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "end capture");
+        b->graph = g;
+        e = cudaGraphInstantiate(&b->exec, g, 0);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "instantiate graph");
+    }
+    {
+        StageTimer timer(ctx, ISO_STAGE_OTHER);
+        cudaError_t e = cudaGraphLaunch(b->exec, ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "graph launch");
+    }
+    ctx->launches += 6;
+    s = finish(b, info);
+    if (s == ISO_ERR_CAPACITY || ctx->last.num_vertices > b->cap_v || ctx->last.num_triangles > b->cap_t) {
+        b->sized = false;  // grow and run eagerly
+        return iso_batch_run(b, 0, info);
+    }
+    return s;
+}
+
+iso_status iso_batch_run_per_chunk(iso_batch* b, iso_mesh_info* info) {
+    if (!b) return ISO_ERR_INVALID_ARG;
+    iso_ctx* ctx = b->ctx;
+    iso_status s = set_device(ctx);
+    if (s != ISO_OK) return s;
+    // each chunk through the single-grid path, then appended to the batch output
+    std::vector<uint32_t> ext(4 * b->chunks.size());
+    uint64_t nv = 0, nt = 0;
+    std::vector<float> hv;
+    std::vector<uint32_t> hi;
+    if ((s = ensure(ctx, ctx->aux3, 12 * std::max<uint64_t>(b->cap_v, 1 << 20) + 12 * std::max<uint64_t>(b->cap_t, 1 << 20))) != ISO_OK)
+        return s;
+    uint64_t cap_v = ctx->aux3.bytes / 24, cap_t = ctx->aux3.bytes / 24;
+    float* out_v = (float*)ctx->aux3.p;
+    uint32_t* out_i = (uint32_t*)((char*)ctx->aux3.p + 12 * cap_v);
+    for (size_t i = 0; i < b->chunks.size(); ++i) {
+        const SampleGrid& g = b->sgrids[i];
+        const uint32_t n = g.n;
+        if ((s = launch_sample_grid(ctx, b->programs[b->chunks[i].prog], n, n, n + 1, g.inv, g.field, g.pitch,
+                                    g.bits)) != ISO_OK)
+            return s;
+        Lattice L{n, n, n + 1, g.pitch, g.field, g.bits, g.W, g.inv, nullptr};
+        iso_mesh_info mi;
+        if ((s = mc_extract_lattice(ctx, L, 0, &mi)) != ISO_OK) return s;
+        if (nv + mi.num_vertices > cap_v || nt + mi.num_triangles > cap_t)
+            return fail(ctx, ISO_ERR_CAPACITY, "per-chunk output arena too small");
+        cudaMemcpyAsync(out_v + 3 * nv, ctx->mesh_v.p, 12 * mi.num_vertices, cudaMemcpyDeviceToDevice, ctx->stream);
+        cudaMemcpyAsync(out_i + 3 * nt, ctx->mesh_i.p, 12 * mi.num_triangles, cudaMemcpyDeviceToDevice, ctx->stream);
+        ext[4 * i + 0] = (uint32_t)nv;
+        ext[4 * i + 1] = (uint32_t)mi.num_vertices;
+        ext[4 * i + 2] = (uint32_t)nt;
+        ext[4 * i + 3] = (uint32_t)mi.num_triangles;
+        nv += mi.num_vertices;
+        nt += mi.num_triangles;
+    }
+    // hand the concatenated mesh over as the context's mesh
+    if ((s = ensure(ctx, ctx->mesh_v, 12 * std::max<uint64_t>(nv, 1))) != ISO_OK) return s;
+    if ((s = ensure(ctx, ctx->mesh_i, 12 * std::max<uint64_t>(nt, 1))) != ISO_OK) return s;
+    cudaMemcpyAsync(ctx->mesh_v.p, out_v, 12 * nv, cudaMemcpyDeviceToDevice, ctx->stream);
+    cudaMemcpyAsync(ctx->mesh_i.p, out_i, 12 * nt, cudaMemcpyDeviceToDevice, ctx->stream);
+    cudaMemcpyAsync(b->d_extents, ext.data(), 4 * ext.size(), cudaMemcpyHostToDevice, ctx->stream);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "per-chunk run");
+    uint64_t cells = 0;
+    for (auto& c : b->chunks) cells += (uint64_t)(c.size - 1) * (c.size - 1) * c.size;
+    ctx->last = iso_mesh_info{nv, nt, cells};
+    ctx->last_flags = 0;
+    ctx->last_vertex_floats = 3;
+    if (info) *info = ctx->last;
+    return ISO_OK;
+}
+
+iso_status iso_batch_extents(iso_batch* b, uint32_t* extents) {
+    if (!b || !extents) return ISO_ERR_INVALID_ARG;
+    iso_ctx* ctx = b->ctx;
+    cudaError_t e = cudaMemcpyAsync(extents, b->d_extents, 16ull * b->chunks.size(), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return e == cudaSuccess ? ISO_OK : cuda_fail(ctx, e, "extents");
+}
+
+iso_status iso_batch_autotune(iso_batch* b, const char* cache_path, uint32_t* chosen) {
+    if (!b) return ISO_ERR_INVALID_ARG;
+    iso_ctx* ctx = b->ctx;
+    iso_status s = set_device(ctx);
+    if (s != ISO_OK) return s;
+    cudaDeviceProp prop;
+    cudaGetDeviceProperties(&prop, ctx->device);
+    const std::string gpu = prop.name;
+    std::map<uint32_t, uint32_t> classes;  // size -> chunk count
+    for (auto& c : b->chunks) classes[c.size]++;
+    std::map<uint32_t, uint32_t> best;
+    // cache lines: "<gpu>|<size>|<depth>"
+    if (cache_path) {
+        if (FILE* f = std::fopen(cache_path, "r")) {
+            char line[512];
+            while (std::fgets(line, sizeof(line), f)) {
+                std::string l(line);
+                size_t a = l.find('|'), c = l.rfind('|');
+                if (a == std::string::npos || c == a) continue;
+                if (l.substr(0, a) != gpu) continue;
+                best[(uint32_t)std::stoul(l.substr(a + 1, c - a - 1))] = (uint32_t)std::stoul(l.substr(c + 1));
+            }
+            std::fclose(f);
+        }
+    }
+    const uint32_t candidates[] = {1, 2, 4, 8, 16, 0};
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    std::vector<uint32_t> saved = b->slab;
+    bool wrote = false;
+    for (auto& cl : classes) {
+        if (best.count(cl.first)) continue;
+        float best_ms = 1e30f;
+        uint32_t best_depth = 4;
+        for (uint32_t d : candidates) {
+            // time the sampler on this class's chunks only, slab depth d
+            std::vector<std::pair<double, Tile>> t;
+            for (uint32_t i = 0; i < b->chunks.size(); ++i) {
+                if (b->chunks[i].size != cl.first) continue;
+                const uint32_t nz = cl.first + 1, depth = d ? d : nz;
+                for (uint32_t z0 = 0; z0 < nz; z0 += depth) t.push_back({0.0, Tile{i, z0, std::min(nz, z0 + depth)}});
+            }
+            std::vector<Tile> tiles(t.size());
+            for (size_t i = 0; i < t.size(); ++i) tiles[i] = t[i].second;
+            Tile* d_t = nullptr;
+            if (cudaMalloc(&d_t, sizeof(Tile) * tiles.size()) != cudaSuccess) return ISO_ERR_OUT_OF_MEMORY;
+            cudaMemcpy(d_t, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice);
+            float ms = 1e30f;
+            for (int rep = 0; rep < 4; ++rep) {
+                cudaMemsetAsync(b->d_next, 0, 4, ctx->stream);
+                cudaEventRecord(e0, ctx->stream);
+                batch_sample<<<sample_blocks(), 256, 0, ctx->stream>>>(d_t, (uint32_t)tiles.size(), b->d_sgrids,
+                                                                       b->d_next);
+                cudaEventRecord(e1, ctx->stream);
+                cudaEventSynchronize(e1);
+                float t_ms = 0.0f;
+                cudaEventElapsedTime(&t_ms, e0, e1);
+                if (rep > 0) ms = std::min(ms, t_ms);
+            }
+            cudaFree(d_t);
+            if (ms < best_ms) {
+                best_ms = ms;
+                best_depth = d;
+            }
+        }
+        best[cl.first] = best_depth;
+        wrote = true;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "autotune");
+    if (cache_path && wrote) {
+        if (FILE* f = std::fopen(cache_path, "a")) {
+            for (auto& kv : best) std::fprintf(f, "%s|%u|%u\n", gpu.c_str(), kv.first, kv.second);
+            std::fclose(f);
+        }
+    }
+    for (size_t i = 0; i < b->chunks.size(); ++i) b->slab[i] = best[b->chunks[i].size];
+    if (chosen) {
+        size_t k = 0;
+        for (auto& kv : best) {
+            chosen[2 * k] = kv.first;
+            chosen[2 * k + 1] = kv.second;
+            ++k;
+        }
+    }
+    (void)saved;
+    return build_tiles(b);
+}
+
+}  // extern "C"

@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 #include <mutex>
 
 #include "internal.h"
@@ -567,15 +568,18 @@ iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, is
     const uint64_t chunks = (uint64_t)CW * (L.ny - 1) * (L.nz - 1);
     if (chunks >= 0xFFFFFFF0ull) return fail(ctx, ISO_ERR_TOO_LARGE, "grid too large");
     const uint32_t nranges = (uint32_t)((chunks + RANGE - 1) / RANGE);
-    const FastDiv div_cw = make_fastdiv(CW), div_ncy = make_fastdiv(L.ny - 1);
     iso_status s;
     if ((s = ensure(ctx, ctx->rowtri, 8 * (chunks + 1))) != ISO_OK) return s;
-    if ((s = ensure(ctx, ctx->scan, 16 * (size_t)nranges + 64)) != ISO_OK) return s;
+    if ((s = ensure(ctx, ctx->scan, 16 * (size_t)nranges + 64 + sizeof(Grid) + 256)) != ISO_OK) return s;
     uint2* local = (uint2*)ctx->rowtri.p;
     uint2* rangeagg = (uint2*)ctx->scan.p;
     uint2* rangepre = rangeagg + nranges;
     uint64_t* totals = (uint64_t*)(rangepre + nranges + 2);
-    ChunkCountArgs ca{L.bits, L.words_per_row, CW, L.nx, L.ny, L.nz, (uint32_t)chunks, div_cw, div_ncy, local, rangeagg};
+    Grid* d_grid = (Grid*)(((uintptr_t)(totals + 4) + 255) & ~(uintptr_t)255);
+    const Grid grid = make_grid(L, 0);
+    cudaError_t e0 = cudaMemcpyAsync(d_grid, &grid, sizeof(Grid), cudaMemcpyHostToDevice, ctx->stream);
+    if (e0 != cudaSuccess) return cuda_fail(ctx, e0, "upload grid");
+    ChunkCountArgs ca{d_grid, nullptr, (uint32_t)chunks, local, rangeagg};
     {
         StageTimer timer(ctx, ISO_STAGE_CLASSIFY);
         mc_chunk_count<<<(nranges + 7) / 8, 256, 0, ctx->stream>>>(ca);
@@ -598,17 +602,15 @@ iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, is
     if ((s = ensure(ctx, ctx->mesh_i, 12 * std::max<uint64_t>(nt, 1))) != ISO_OK) return s;
     if (keys && (s = ensure(ctx, ctx->mesh_k, 16 * std::max<uint64_t>(nv, 1))) != ISO_OK) return s;
     if (nt > 0) {
-        ChunkEmitArgs ea{L.bits, L.values, L.positions, L.pitch, L.words_per_row, CW, L.nx, L.ny, L.nz,
-                         (uint32_t)chunks, div_cw, div_ncy, L.inv, local, rangepre, (float*)ctx->mesh_v.p,
-                         (uint32_t*)ctx->mesh_i.p,
-                         keys ? (uint64_t*)ctx->mesh_k.p : nullptr, nv, nt, ctx->d_err};
+        ChunkEmitArgs ea{d_grid, nullptr, (uint32_t)chunks, local, rangepre, (float*)ctx->mesh_v.p,
+                         (uint32_t*)ctx->mesh_i.p, keys ? (uint64_t*)ctx->mesh_k.p : nullptr, nv, nt, ctx->d_err};
         const size_t smem = block_emit_smem(CW);
         if (smem > 220 * 1024) return fail(ctx, ISO_ERR_INVALID_ARG, "rows too long for the emit pass");
         e = cudaFuncSetAttribute(mc_block_emit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "emit smem attribute");
         {
             StageTimer timer(ctx, ISO_STAGE_EMIT);
-            mc_block_emit<<<(unsigned)((chunks + 255) / 256), 256, smem, ctx->stream>>>(ea);
+            mc_block_emit<<<(unsigned)((chunks + 255) / 256), 256, smem, ctx->stream>>>(ea, CW);
         }
         ctx->launches++;
         if ((s = check_launch(ctx, "mc_block_emit")) != ISO_OK) return s;
@@ -623,6 +625,69 @@ iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, is
     ctx->last.num_cells = (uint64_t)(L.nx - 1) * (L.ny - 1) * (L.nz - 1);
     if (info) *info = ctx->last;
     return ISO_OK;
+}
+
+// ---- many grids in one launch (batch.cu) ----------------------------------
+size_t mc_grid_bytes() { return sizeof(Grid); }
+
+void mc_fill_grid(void* dst, const Lattice& L, uint32_t chunk0, uint32_t* nchunks, uint32_t* cw) {
+    const Grid g = make_grid(L, chunk0);
+    std::memcpy(dst, &g, sizeof(Grid));
+    *nchunks = g.nchunks;
+    *cw = g.CW;
+}
+
+size_t mc_grids_scratch_bytes(uint32_t chunks, uint32_t ngrids) {
+    const size_t nranges = (chunks + RANGE - 1) / RANGE;
+    (void)ngrids;
+    return 8 * ((size_t)chunks + 1) + 16 * nranges + 512;
+}
+
+// Count, scan and emit over a table of grids (chunks = padded global chunk
+// count).  sync_sizes: read the totals back and size the context's mesh
+// buffers before the emit (eager); otherwise write into the context's mesh
+// buffers with the given capacities (graph capture: no host synchronisation).
+iso_status mc_extract_grids(iso_ctx* ctx, const void* d_grids, uint32_t ngrids, const uint32_t* d_range_grid,
+                            uint32_t chunks, uint32_t max_cw, void* scratch, uint64_t cap_v, uint64_t cap_t,
+                            float* out_v, uint32_t* out_i, uint32_t* extents, uint64_t* totals, bool sync_sizes) {
+    const uint32_t nranges = (chunks + RANGE - 1) / RANGE;
+    uint2* local = (uint2*)scratch;
+    uint2* rangeagg = local + ((chunks + 1 + 31) & ~31u);
+    uint2* rangepre = rangeagg + nranges;
+    const Grid* grids = (const Grid*)d_grids;
+    ChunkCountArgs ca{grids, d_range_grid, chunks, local, rangeagg};
+    {
+        StageTimer timer(ctx, ISO_STAGE_CLASSIFY);
+        mc_chunk_count<<<(nranges + 1 + 7) / 8, 256, 0, ctx->stream>>>(ca);
+        mc_range_scan<<<1, 1024, 0, ctx->stream>>>(rangeagg, nranges, rangepre, totals, local, chunks, ctx->d_err);
+    }
+    ctx->launches += 2;
+    iso_status s = check_launch(ctx, "batch count");
+    if (s != ISO_OK) return s;
+    if (sync_sizes) {
+        cudaError_t e = cudaMemcpyAsync(ctx->h_pinned, totals, 16, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "batch totals");
+        cap_t = ctx->h_pinned[0];
+        cap_v = ctx->h_pinned[1];
+        if (cap_v >= (1ull << 31) || cap_t >= (1ull << 31)) return fail(ctx, ISO_ERR_TOO_LARGE, "batch mesh too large");
+        if ((s = ensure(ctx, ctx->mesh_v, 12 * std::max<uint64_t>(cap_v, 1))) != ISO_OK) return s;
+        if ((s = ensure(ctx, ctx->mesh_i, 12 * std::max<uint64_t>(cap_t, 1))) != ISO_OK) return s;
+        out_v = (float*)ctx->mesh_v.p;
+        out_i = (uint32_t*)ctx->mesh_i.p;
+    }
+    const size_t smem = block_emit_smem(max_cw);
+    cudaError_t e = cudaFuncSetAttribute(mc_block_emit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "emit smem attribute");
+    ChunkEmitArgs ea{grids, d_range_grid, chunks, local, rangepre, out_v, out_i, nullptr, cap_v, cap_t, ctx->d_err};
+    {
+        StageTimer timer(ctx, ISO_STAGE_EMIT);
+        mc_block_emit<<<nranges, 256, smem, ctx->stream>>>(ea, max_cw);
+        mc_grid_extents<<<(ngrids + 127) / 128, 128, 0, ctx->stream>>>(grids, ngrids, local, rangepre,
+                                                                       (uint4*)extents);
+    }
+    ctx->launches += 2;
+    return check_launch(ctx, "batch emit");
 }
 
 }  // namespace iso

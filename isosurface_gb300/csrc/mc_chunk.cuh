@@ -1,19 +1,24 @@
 // Chunked marching-cubes passes (included by mc.cu inside iso::{anonymous}).
 //
-// A chunk is 32 consecutive cells of a row (x = 32c .. 32c+31); chunk id =
-// row * CW + c with CW = ceil((nx-1)/32), which is the reference's (z, y, x)
-// visit order.  A chunk's eight corner bit-vectors (bit i: corner k of cell
-// 32c+i is inside) come from four sign-bit rows with funnel shifts, so
-// activity and owned-vertex counts cost a few dozen bit operations per 32
-// cells.  Offsets: pass 1 gives every chunk its exclusive prefix inside a
-// range of RANGE chunks (one warp's work) plus each range's total; a one-block
-// scan turns range totals into range offsets; chunk base = range offset +
-// in-range prefix.  Corners, load_corners, case_at, chunk_valid, active_cells
-// and owned_count are defined in mc.cu above the include.
+// A chunk is 32 consecutive cells of a row (x = 32c .. 32c+31); inside a
+// grid, chunk id = row * CW + c with CW = ceil((nx-1)/32), which is the
+// reference's (z, y, x) visit order.  A chunk's eight corner bit-vectors (bit
+// i: corner k of cell 32c+i is inside) come from four sign-bit rows with
+// funnel shifts, so activity and owned-vertex counts cost a few dozen bit
+// operations per 32 cells.
+//
+// Several grids can be processed by one launch: each grid's chunks occupy a
+// run of whole RANGEs (256 chunks) of a global chunk index space, and
+// range_grid maps a range to its grid (a null map means one grid).  Offsets:
+// pass 1 gives every chunk its exclusive prefix inside its range plus each
+// range's total; a one-block scan turns range totals into range offsets;
+// chunk base = range offset + in-range prefix.  Vertex indices are written
+// relative to the grid's first vertex, so each grid gets its own mesh.
+// Corners, load_corners, case_at, chunk_valid, active_cells and owned_count
+// are defined in mc.cu above the include.
 
 constexpr uint32_t RANGE = 256;  // chunks per counting warp / per emit block
 constexpr int RANGE_ROUNDS = RANGE / 32;
-constexpr uint32_t OWN_INTERIOR = 0x460;  // edges 5, 6, 10: the far-corner edges
 
 // q = n / d for n < 2^32, d < 2^31, with m = floor(2^64 / d) + 1 (d > 1)
 struct FastDiv {
@@ -25,11 +30,47 @@ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
     return f.d == 1 ? n : (uint32_t)__umul64hi((uint64_t)n, f.m);
 }
 
-struct ChunkCountArgs {
+// One lattice: nx x ny x nz samples (sign bits + values, optional explicit
+// positions) and where its chunks sit in the global chunk index space.
+struct Grid {
     const uint32_t* bits;
+    const float* values;
+    const float4* positions;  // null: regular grid, point = (x, y, z) * inv
+    uint64_t pitch;
     uint32_t W, CW, nx, ny, nz;
-    uint32_t chunks;
     FastDiv div_cw, div_ncy;
+    float inv;
+    uint32_t chunk0;   // first global chunk id (a multiple of RANGE)
+    uint32_t nchunks;  // CW * (ny-1) * (nz-1)
+};
+
+inline Grid make_grid(const Lattice& L, uint32_t chunk0) {
+    Grid g;
+    g.bits = L.bits;
+    g.values = L.values;
+    g.positions = L.positions;
+    g.pitch = L.pitch;
+    g.W = L.words_per_row;
+    g.nx = L.nx;
+    g.ny = L.ny;
+    g.nz = L.nz;
+    g.CW = (L.nx - 1 + 31) / 32;
+    g.div_cw = make_fastdiv(g.CW);
+    g.div_ncy = make_fastdiv(L.ny - 1);
+    g.inv = L.inv;
+    g.chunk0 = chunk0;
+    g.nchunks = g.CW * (L.ny - 1) * (L.nz - 1);
+    return g;
+}
+
+__device__ __forceinline__ uint32_t grid_of_range(const uint32_t* range_grid, uint32_t range) {
+    return range_grid ? __ldg(range_grid + range) : 0u;
+}
+
+struct ChunkCountArgs {
+    const Grid* grids;
+    const uint32_t* range_grid;
+    uint32_t chunks;   // global (padded) chunk count
     uint2* local;      // chunks + 1: (vertex, triangle) exclusive prefix inside the range
     uint2* rangeagg;   // per range: (vertices, triangles)
 };
@@ -43,17 +84,20 @@ __global__ void __launch_bounds__(256) mc_chunk_count(ChunkCountArgs A) {
     if (threadIdx.x < 8) s_owned[threadIdx.x] = iso_owned_mask[threadIdx.x];
     __syncthreads();
     const uint32_t range = blockIdx.x * 8 + (threadIdx.x >> 5);
-    const uint32_t ncx = A.nx - 1;
+    if (range * RANGE > A.chunks) return;  // warp-uniform
+    const Grid g = A.grids[grid_of_range(A.range_grid, min(range, A.chunks / RANGE - (A.chunks % RANGE == 0)))];
+    const uint32_t ncx = g.nx - 1;
     uint32_t agg_t = 0, agg_v = 0;
     for (int r = 0; r < RANGE_ROUNDS; ++r) {
         const uint32_t ch = range * RANGE + r * 32 + lane;
+        const uint32_t lc = ch - g.chunk0;
         uint32_t t = 0, v = 0;
-        if (ch < A.chunks) {
-            const uint32_t row = fdiv(ch, A.div_cw);
-            const uint32_t c = ch - row * A.CW;
-            const uint32_t z = fdiv(row, A.div_ncy);
-            const uint32_t y = row - z * (A.ny - 1);
-            const Corners q = load_corners(A.bits, A.W, A.ny, y, z, c);
+        if (ch < A.chunks && lc < g.nchunks) {
+            const uint32_t row = fdiv(lc, g.div_cw);
+            const uint32_t c = lc - row * g.CW;
+            const uint32_t z = fdiv(row, g.div_ncy);
+            const uint32_t y = row - z * (g.ny - 1);
+            const Corners q = load_corners(g.bits, g.W, g.ny, y, z, c);
             uint32_t act = active_cells(q, chunk_valid(c, ncx));
             if (act) {
                 const int cls = (y == 0 ? 2 : 0) | (z == 0 ? 4 : 0);
@@ -70,7 +114,7 @@ __global__ void __launch_bounds__(256) mc_chunk_count(ChunkCountArgs A) {
         agg_t += __shfl_sync(FULL, ti, 31);
         agg_v += __shfl_sync(FULL, vi, 31);
     }
-    if (lane == 0 && range * RANGE < A.chunks + 1) A.rangeagg[range] = make_uint2(agg_v, agg_t);
+    if (lane == 0 && range * RANGE < A.chunks) A.rangeagg[range] = make_uint2(agg_v, agg_t);
 }
 
 // Exclusive scan of the range totals (one block).  rangepre[nr] and totals
@@ -124,14 +168,9 @@ __global__ void __launch_bounds__(1024) mc_range_scan(const uint2* rangeagg, uin
 }
 
 struct ChunkEmitArgs {
-    const uint32_t* bits;
-    const float* values;
-    const float4* positions;  // null: regular grid
-    uint64_t pitch;
-    uint32_t W, CW, nx, ny, nz;
+    const Grid* grids;
+    const uint32_t* range_grid;
     uint32_t chunks;
-    FastDiv div_cw, div_ncy;
-    float inv;
     const uint2* local;
     const uint2* rangepre;
     float* out_v;
@@ -147,14 +186,14 @@ __device__ __forceinline__ uint2 chunk_base(const ChunkEmitArgs& A, uint32_t ch)
     return make_uint2(l.x + b.x, l.y + b.y);
 }
 
-// Pass 2.  Block b emits chunks [c0, c0+256) (one counting range).  Every
-// non-owned edge of a cell in those chunks is owned by a cell in chunk ch-1,
-// ch-CW or ch-CW-1 (same layer) or ch-S, ch-S-1, ch-S-CW, ch-S-CW-1 (layer
-// below, S = CW*(ny-1)), so the block caches the corner vectors and vertex
-// bases of the bands R1 = [c0-CW-1, c0+256) and R2 = R1 - S in shared memory.
-// Active cells are compacted in chunk order and processed one per thread in
-// rounds of 256, with block scans giving each cell's output offsets; each
-// distinct edge of a cell is resolved to its vertex id once.
+// Pass 2.  Block b emits the chunks of range b (one grid).  Every non-owned
+// edge of a cell in those chunks is owned by a cell in chunk ch-1, ch-CW or
+// ch-CW-1 (same layer) or ch-S, ch-S-1, ch-S-CW, ch-S-CW-1 (layer below,
+// S = CW*(ny-1)), so the block caches the corner vectors and vertex bases of
+// the bands R1 = [c0-CW-1, c0+256) and R2 = R1 - S (grid-local chunk ids) in
+// shared memory.  Active cells are compacted in chunk order and processed one
+// per thread in rounds of 256, with block scans giving each cell's output
+// offsets; each distinct edge of a cell is resolved to its vertex id once.
 constexpr int EMIT_LIST_CAP = 256 * 32;
 
 struct EmitTables {
@@ -195,23 +234,28 @@ __device__ __forceinline__ uint32_t rank_of(const EmitTables& tb, int cls, uint3
     return (uint32_t)(w >> (4 * e)) & 15u;
 }
 
-__global__ void __launch_bounds__(256) mc_block_emit(ChunkEmitArgs A) {
+__global__ void __launch_bounds__(256) mc_block_emit(ChunkEmitArgs A, uint32_t max_cw) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ uint32_t s_w[8], s_w2[8];
     EmitTables& tb = *reinterpret_cast<EmitTables*>(smem);
-    const uint32_t CW = A.CW, ncx = A.nx - 1, ncy = A.ny - 1;
+    const Grid g = A.grids[grid_of_range(A.range_grid, blockIdx.x)];
+    const uint32_t CW = g.CW, ncx = g.nx - 1, ncy = g.ny - 1;
     const int span = RANGE + (int)CW + 1;
+    const int span_max = RANGE + (int)max_cw + 1;
     uint32_t* q1 = reinterpret_cast<uint32_t*>(smem + ((sizeof(EmitTables) + 15) & ~(size_t)15));
-    uint32_t* q2 = q1 + span * 8;
-    uint32_t* vb1 = q2 + span * 8;
-    uint32_t* vb2 = vb1 + span;
-    uint16_t* list = reinterpret_cast<uint16_t*>(vb2 + span);
-    const uint32_t c0 = blockIdx.x * RANGE;
+    uint32_t* q2 = q1 + span_max * 8;
+    uint32_t* vb1 = q2 + span_max * 8;
+    uint32_t* vb2 = vb1 + span_max;
+    uint16_t* list = reinterpret_cast<uint16_t*>(vb2 + span_max);
+    const uint32_t gc0 = blockIdx.x * RANGE;           // global chunk id of the block's first chunk
+    const uint32_t c0 = gc0 - g.chunk0;                 // grid-local
+    if (c0 >= g.nchunks) return;                        // padding range
     const int64_t S = (int64_t)CW * ncy;
     const int64_t r1 = (int64_t)c0 - CW - 1, r2 = r1 - S;
-    const uint2 bb = chunk_base(A, c0);
-    const uint32_t c_end = min(c0 + RANGE, A.chunks);
-    if (chunk_base(A, c_end).y == bb.y) return;  // no triangle in the block
+    const uint2 bb = chunk_base(A, gc0);
+    const uint32_t c_end = min(c0 + RANGE, g.nchunks);
+    if (chunk_base(A, g.chunk0 + c_end).y == bb.y) return;  // no triangle in the block
+    const uint32_t grid_v0 = chunk_base(A, g.chunk0).x;     // first vertex of this grid's mesh
     for (int i = threadIdx.x; i < 256; i += blockDim.x) {
         tb.tri_count[i] = iso_tri_count[i];
         tb.edge_count[i] = iso_edge_count[i];
@@ -226,27 +270,27 @@ __global__ void __launch_bounds__(256) mc_block_emit(ChunkEmitArgs A) {
     for (int i = threadIdx.x; i < 2 * span; i += 256) {
         const bool first = i < span;
         const int64_t ch = first ? r1 + i : r2 + (i - span);
-        if (ch < 0 || ch >= (int64_t)A.chunks) continue;
+        if (ch < 0 || ch >= (int64_t)g.nchunks) continue;
         const uint32_t chu = (uint32_t)ch;
-        const uint32_t row = fdiv(chu, A.div_cw);
+        const uint32_t row = fdiv(chu, g.div_cw);
         const uint32_t c = chu - row * CW;
-        const uint32_t z = fdiv(row, A.div_ncy);
-        const Corners q = load_corners(A.bits, A.W, A.ny, row - z * ncy, z, c);
+        const uint32_t z = fdiv(row, g.div_ncy);
+        const Corners q = load_corners(g.bits, g.W, g.ny, row - z * ncy, z, c);
         uint32_t* dst = first ? q1 + i * 8 : q2 + (i - span) * 8;
 #pragma unroll
         for (int k = 0; k < 8; ++k) dst[k] = q.k[k];
-        (first ? vb1 : vb2)[first ? i : i - span] = chunk_base(A, chu).x;
+        (first ? vb1 : vb2)[first ? i : i - span] = chunk_base(A, g.chunk0 + chu).x - grid_v0;
     }
     __syncthreads();
 
     // compact the block's active cells, in chunk order
     const uint32_t mych = c0 + threadIdx.x;
     uint32_t act = 0;
-    if (mych < A.chunks) {
+    if (mych < g.nchunks) {
         Corners q;
 #pragma unroll
         for (int k = 0; k < 8; ++k) q.k[k] = q1[(CW + 1 + threadIdx.x) * 8 + k];
-        act = active_cells(q, chunk_valid(mych - fdiv(mych, A.div_cw) * CW, ncx));
+        act = active_cells(q, chunk_valid(mych - fdiv(mych, g.div_cw) * CW, ncx));
     }
     uint32_t nlist;
     uint32_t pos = block_excl_scan(__popc(act), s_w, &nlist);
@@ -257,8 +301,8 @@ __global__ void __launch_bounds__(256) mc_block_emit(ChunkEmitArgs A) {
     }
     __syncthreads();
 
-    const bool explicit_pos = A.positions != nullptr;
-    uint32_t vcarry = bb.x, tcarry = bb.y;
+    const bool explicit_pos = g.positions != nullptr;
+    uint32_t vcarry = bb.x, tcarry = bb.y;  // global offsets
     for (uint32_t r0 = 0; r0 < nlist; r0 += 256) {
         const uint32_t j = r0 + threadIdx.x;
         const bool have = j < nlist;
@@ -268,8 +312,8 @@ __global__ void __launch_bounds__(256) mc_block_emit(ChunkEmitArgs A) {
             const uint32_t ent = list[j];
             const uint32_t t = ent >> 5, i = ent & 31;
             const uint32_t ch = c0 + t;
-            const uint32_t row = fdiv(ch, A.div_cw);
-            z = fdiv(row, A.div_ncy);
+            const uint32_t row = fdiv(ch, g.div_cw);
+            z = fdiv(row, g.div_ncy);
             y = row - z * ncy;
             x = 32 * (ch - row * CW) + i;
             uint32_t cs_ = 0;
@@ -285,10 +329,10 @@ __global__ void __launch_bounds__(256) mc_block_emit(ChunkEmitArgs A) {
         const uint32_t tpre = block_excl_scan(nt, s_w2, &ttot);
         if (have) {
             const uint32_t own = tb.owned[cls];
-            const uint32_t vstart = vcarry + vpre;
+            const uint32_t vstart = vcarry + vpre;  // global vertex slot
             const uint64_t ord = tb.edge_order[cs];
             const uint32_t ne = tb.edge_count[cs];
-            uint32_t ids[12];
+            uint32_t ids[12];  // grid-local vertex ids by first-use rank
             uint32_t r = 0;
             for (uint32_t k = 0; k < ne; ++k) {
                 const uint32_t e = (uint32_t)(ord >> (4 * k)) & 15u;
@@ -297,16 +341,16 @@ __global__ void __launch_bounds__(256) mc_block_emit(ChunkEmitArgs A) {
                     const uint32_t u = iso_edge_connection[e][0], v = iso_edge_connection[e][1];
                     const uint32_t ux = x + iso_corners[u][0], uy = y + iso_corners[u][1], uz = z + iso_corners[u][2];
                     const uint32_t vx = x + iso_corners[v][0], vy = y + iso_corners[v][1], vz = z + iso_corners[v][2];
-                    const float fa = __ldg(A.values + ((size_t)uz * A.ny + uy) * A.pitch + ux);
-                    const float fb = __ldg(A.values + ((size_t)vz * A.ny + vy) * A.pitch + vx);
+                    const float fa = __ldg(g.values + ((size_t)uz * g.ny + uy) * g.pitch + ux);
+                    const float fb = __ldg(g.values + ((size_t)vz * g.ny + vy) * g.pitch + vx);
                     float pax, pay, paz, pbx, pby, pbz;
                     if (explicit_pos) {
-                        const float4 qa = __ldg(A.positions + ((size_t)uz * A.ny + uy) * A.nx + ux);
-                        const float4 qb = __ldg(A.positions + ((size_t)vz * A.ny + vy) * A.nx + vx);
+                        const float4 qa = __ldg(g.positions + ((size_t)uz * g.ny + uy) * g.nx + ux);
+                        const float4 qb = __ldg(g.positions + ((size_t)vz * g.ny + vy) * g.nx + vx);
                         pax = qa.x; pay = qa.y; paz = qa.z; pbx = qb.x; pby = qb.y; pbz = qb.z;
                     } else {
-                        pax = (float)ux * A.inv; pay = (float)uy * A.inv; paz = (float)uz * A.inv;
-                        pbx = (float)vx * A.inv; pby = (float)vy * A.inv; pbz = (float)vz * A.inv;
+                        pax = (float)ux * g.inv; pay = (float)uy * g.inv; paz = (float)uz * g.inv;
+                        pbx = (float)vx * g.inv; pby = (float)vy * g.inv; pbz = (float)vz * g.inv;
                     }
                     // Signed::find_crossing_point (distance.rs:64-69)
                     const float delta = fb - fa;
@@ -319,13 +363,13 @@ __global__ void __launch_bounds__(256) mc_block_emit(ChunkEmitArgs A) {
                         A.out_v[3 * (size_t)vid + 2] = paz * omt + pbz * tt;
                         if (A.out_k) {
                             const uint32_t lx = x + c_edge_lo[e][0], ly = y + c_edge_lo[e][1], lz = z + c_edge_lo[e][2];
-                            A.out_k[2 * (size_t)vid] = (((uint64_t)lz * A.ny + ly) * A.nx + lx) * 3 + c_edge_axis[e];
+                            A.out_k[2 * (size_t)vid] = (((uint64_t)lz * g.ny + ly) * g.nx + lx) * 3 + c_edge_axis[e];
                             A.out_k[2 * (size_t)vid + 1] = 0;
                         }
                     } else {
                         atomicOr(A.err, DERR_CAPACITY);
                     }
-                    ids[k] = vid;
+                    ids[k] = vid - grid_v0;
                     ++r;
                     continue;
                 }
@@ -385,4 +429,16 @@ __global__ void __launch_bounds__(256) mc_block_emit(ChunkEmitArgs A) {
         vcarry += vtot;
         tcarry += ttot;
     }
+}
+
+// Per-grid mesh extents: (first vertex, vertex count, first triangle, triangle count).
+__global__ void mc_grid_extents(const Grid* grids, uint32_t ngrids, const uint2* local, const uint2* rangepre,
+                                uint4* out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ngrids) return;
+    const Grid g = grids[i];
+    const uint32_t a = g.chunk0, b = g.chunk0 + g.nchunks;
+    const uint2 la = local[a], ra = rangepre[a / RANGE], lb = local[b], rb = rangepre[b / RANGE];
+    const uint32_t v0 = la.x + ra.x, t0 = la.y + ra.y, v1 = lb.x + rb.x, t1 = lb.y + rb.y;
+    out[i] = make_uint4(v0, v1 - v0, t0, t1 - t0);
 }
