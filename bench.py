@@ -114,6 +114,51 @@ def cpu_baseline_port(src_bytes, budget_s=12.0, threads=1):
                       % (z0, z0 + layers, cells, secs)}
 
 
+def secondary_workloads(ctx, torch, steps):
+    """The other workloads, timed with CUDA events on the library's stream:
+    the 4096-chunk batch (one CUDA graph vs one extraction per chunk),
+    DualContouring at 256^3 and LinearHashedMarchingCubes at depth 8."""
+    from isosurface_gb300 import scenes
+    from isosurface_gb300.api import Batch
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def timed(fn, reps):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        for a, b in ev:
+            a.record(stream)
+            fn()
+            b.record(stream)
+        torch.cuda.synchronize()
+        return min(a.elapsed_time(b) for a, b in ev)
+
+    out = {}
+    chunks = scenes.chunks(seed=7, count=4096)
+    batch = Batch(ctx, chunks)
+    cache = os.path.join(ROOT, "isosurface_gb300", "_build", "autotune.txt")
+    chosen = batch.autotune(cache)
+    batch.run(graph=False)
+    batch.run(graph=True)
+    graph_ms = timed(lambda: batch.run(graph=True), max(steps, 3))
+    info = batch.run(graph=True)
+    per_ms = timed(batch.run_per_chunk, 2)
+    cells = info.num_cells
+    out["batch_4096_chunks"] = {"cells": int(cells), "graph_ms": graph_ms, "per_chunk_ms": per_ms,
+                                "speedup": per_ms / graph_ms, "cells_per_s": cells / (graph_ms / 1e3),
+                                "triangles": int(info.num_triangles), "slab_depth_by_size": chosen}
+    batch.close()
+    src = scenes.csg()
+    for _ in range(2):
+        info = ctx.dc_extract(src, 257)
+    ms = timed(lambda: ctx.dc_extract(src, 257), max(steps, 3))
+    out["dc_256"] = {"cells": int(info.num_cells), "ms": ms, "cells_per_s": 256 * 256 * 257 / (ms / 1e3),
+                     "triangles": int(info.num_triangles), "placer": "MinimiseQEF"}
+    for _ in range(2):
+        info = ctx.lhmc_extract(src, 8)
+    ms = timed(lambda: ctx.lhmc_extract(src, 8), max(steps, 3))
+    out["lhmc_depth8"] = {"dual_cubes": int(info.num_cells), "ms": ms, "triangles": int(info.num_triangles)}
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -155,6 +200,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the batch / DC / LHMC timings")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -287,6 +333,10 @@ def main():
     e2e = {"value": world * CELLS / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": len(src_bytes),
            "d2h_bytes_per_step": 12 * mi.num_vertices + 12 * mi.num_triangles, "ms_per_step": 1e3 * e2e_s}
 
+    secondary = None
+    if not args.no_secondary:
+        secondary = secondary_workloads(ctx, torch, args.steps)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline_port(src_bytes)
@@ -298,7 +348,7 @@ def main():
                "config": dict(WORKLOAD, parallelism="replicas" if world > 1 else "single", vertices=nv,
                               triangles=nt),
                "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "stages": per_stage,
-               "cpu_baseline": cpu, "clocks": clk}
+               "cpu_baseline": cpu, "clocks": clk, "secondary": secondary}
         print(json.dumps(out))
     ctx.close()
     if dist:
