@@ -303,6 +303,80 @@ ISO_API iso_status iso_batch_set_slab(iso_batch* batch, uint32_t size, uint32_t 
 ISO_API iso_status iso_batch_autotune(iso_batch* batch, const char* cache_path, uint32_t* chosen);
 
 /* ------------------------------------------------------------------------ */
+/* Learned SDF surrogate (no reference counterpart)                          */
+/* ------------------------------------------------------------------------ */
+/* A Fourier-feature MLP (3 -> 96 features -> 6 x 256 softplus (beta 100) -> 1) that
+ * stands in for an expensive many-primitive source.  It is trained on the GPU
+ * by the library's own forward, backward and Adam kernels on samples labelled
+ * by the exact program.  Points are in the source's own coordinates (for a
+ * DomainMap(source) program, the mapped coordinates). */
+typedef struct iso_mlp iso_mlp;
+ISO_API iso_status iso_mlp_create(iso_ctx* ctx, uint64_t seed, iso_mlp** out);
+ISO_API iso_status iso_mlp_destroy(iso_mlp* net);
+ISO_API uint64_t iso_mlp_num_params(void);
+/* fp32 parameters: W0[256][96], b0[256], W1..W5[256][256], b1..b5[256], w_out[256], b_out */
+ISO_API iso_status iso_mlp_get_params(iso_mlp* net, float* host);
+ISO_API iso_status iso_mlp_set_params(iso_mlp* net, const float* host);
+/* fp32 forward of n host points (x,y,z) into n host values */
+ISO_API iso_status iso_mlp_forward(iso_mlp* net, const float* points, uint32_t n, float* values);
+/* the same forward on the tensor cores: bf16 weights and activations, fp32
+ * accumulation (tcgen05); the bf16 copy is refreshed after every update */
+ISO_API iso_status iso_mlp_forward_bf16(iso_mlp* net, const float* points, uint32_t n, float* values);
+/* training loss and its gradient (NPARAMS floats, nullable): mean |e| with
+ * e = y - t where |t| < d, min(y - d, 0) where t >= d, max(y + d, 0) where t <= -d */
+ISO_API iso_status iso_mlp_loss_grad(iso_mlp* net, const float* points, const float* targets, uint32_t n,
+                                     float clamp_d, float* loss, float* grad);
+/* n training samples in [lo, hi]^3: all candidates with |f| < 0.05 and a
+ * quarter of the rest, labelled by `exact` */
+ISO_API iso_status iso_mlp_make_dataset(iso_mlp* net, const iso_program* exact, uint32_t n, float lo, float hi,
+                                        uint64_t seed);
+/* `steps` Adam steps on random batches of the dataset (cosine-decayed lr);
+ * the loss of each step into history (nullable) */
+ISO_API iso_status iso_mlp_train(iso_mlp* net, uint32_t steps, uint32_t batch, float lr, float clamp_d,
+                                 uint64_t seed, float* history);
+
+/* Learned-surrogate marching cubes.  The field of MarchingCubes::new(size)
+ * for `exact` is built as: the network (bf16 tensor cores) on every
+ * coarse_step-th lattice point; its trilinear interpolation at every fine
+ * point; fine points whose interpolated value is within band_cells fine cells
+ * of zero re-sampled with `exact` (bit-identical to iso_sample_grid there).
+ * The network sees the exact program's frame: a program that starts with a
+ * domain map p -> p * scale + offset gives the network q = p * scale + offset,
+ * and a cell is 1/(size-1) times the smallest scale. */
+typedef struct iso_surrogate_stats {
+    uint64_t coarse_points; /* network evaluations                         */
+    uint64_t band_points;   /* fine points re-sampled with the exact source */
+    uint64_t total_points;  /* fine points: size * size * (size + 1)        */
+} iso_surrogate_stats;
+/* the field into device memory laid out as iso_sample_grid writes it */
+ISO_API iso_status iso_surrogate_field(iso_ctx* ctx, iso_mlp* net, const iso_program* exact, uint32_t size,
+                                       uint32_t coarse_step, float band_cells, float* field, uint64_t pitch,
+                                       iso_surrogate_stats* stats);
+/* the field, then marching cubes on it; the mesh stays in the context as
+ * after iso_mc_extract (stats nullable) */
+ISO_API iso_status iso_surrogate_extract(iso_ctx* ctx, iso_mlp* net, const iso_program* exact, uint32_t size,
+                                         uint32_t coarse_step, float band_cells, uint32_t flags,
+                                         iso_surrogate_stats* stats, iso_mesh_info* info);
+
+/* Nearest-vertex distances between vertex sets a and b (host, xyz f32):
+ * mean and max over a of the distance to the nearest b, and the reverse.
+ * Chamfer = (mean_ab + mean_ba) / 2, Hausdorff = max(max_ab, max_ba).  The
+ * search uses buckets of edge `bucket` and gives up after max_rings rings
+ * (such points count in `capped` and report the best distance seen, or the
+ * searched radius). */
+typedef struct iso_mesh_distance_result {
+    double mean_ab, mean_ba, max_ab, max_ba;
+    uint64_t capped;
+} iso_mesh_distance_result;
+ISO_API iso_status iso_mesh_distance(iso_ctx* ctx, const float* a, uint64_t na, const float* b, uint64_t nb,
+                                     float bucket, uint32_t max_rings, iso_mesh_distance_result* out);
+/* Cells of an nx x ny x nz lattice (x < nx-1, y < ny-1, z < nz-1) whose
+ * corner signs (!(v > 0)) differ between two device fields of row pitch
+ * `pitch` floats. */
+ISO_API iso_status iso_field_case_disagreement(iso_ctx* ctx, const float* fa, const float* fb, uint32_t nx,
+                                               uint32_t ny, uint32_t nz, uint64_t pitch, uint64_t* cells);
+
+/* ------------------------------------------------------------------------ */
 /* PointCloud (src/point_cloud.rs:50-63)                                      */
 /* ------------------------------------------------------------------------ */
 ISO_API iso_status iso_point_cloud_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size,

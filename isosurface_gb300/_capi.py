@@ -31,6 +31,16 @@ class MeshInfo(ctypes.Structure):
                 ("num_cells", ctypes.c_uint64)]
 
 
+class SurrogateStats(ctypes.Structure):
+    _fields_ = [("coarse_points", ctypes.c_uint64), ("band_points", ctypes.c_uint64),
+                ("total_points", ctypes.c_uint64)]
+
+
+class MeshDistance(ctypes.Structure):
+    _fields_ = [("mean_ab", ctypes.c_double), ("mean_ba", ctypes.c_double), ("max_ab", ctypes.c_double),
+                ("max_ba", ctypes.c_double), ("capped", ctypes.c_uint64)]
+
+
 class ChunkDesc(ctypes.Structure):
     _fields_ = [("program", ctypes.c_uint32), ("size", ctypes.c_uint32)]
 
@@ -80,6 +90,21 @@ SIGNATURES = {
     "iso_batch_extents": (i32, [vp, u32p]),
     "iso_batch_set_slab": (i32, [vp, u32, u32]),
     "iso_batch_autotune": (i32, [vp, ctypes.c_char_p, u32p]),
+    "iso_mlp_create": (i32, [vp, u64, ctypes.POINTER(vp)]),
+    "iso_mlp_destroy": (i32, [vp]),
+    "iso_mlp_num_params": (u64, []),
+    "iso_mlp_get_params": (i32, [vp, f32p]),
+    "iso_mlp_set_params": (i32, [vp, f32p]),
+    "iso_mlp_forward": (i32, [vp, f32p, u32, f32p]),
+    "iso_mlp_forward_bf16": (i32, [vp, f32p, u32, f32p]),
+    "iso_mlp_loss_grad": (i32, [vp, f32p, f32p, u32, ctypes.c_float, f32p, f32p]),
+    "iso_mlp_make_dataset": (i32, [vp, vp, u32, ctypes.c_float, ctypes.c_float, u64]),
+    "iso_mlp_train": (i32, [vp, u32, u32, ctypes.c_float, ctypes.c_float, u64, f32p]),
+    "iso_surrogate_field": (i32, [vp, vp, vp, u32, u32, ctypes.c_float, vp, u64, ctypes.POINTER(SurrogateStats)]),
+    "iso_surrogate_extract": (i32, [vp, vp, vp, u32, u32, ctypes.c_float, u32, ctypes.POINTER(SurrogateStats),
+                                    ctypes.POINTER(MeshInfo)]),
+    "iso_mesh_distance": (i32, [vp, f32p, u64, f32p, u64, ctypes.c_float, u32, ctypes.POINTER(MeshDistance)]),
+    "iso_field_case_disagreement": (i32, [vp, vp, vp, u32, u32, u32, u64, u64p]),
     "iso_sample_points": (i32, [vp, vp, f32p, u64, f32p, f32p]),
 }
 

@@ -28,8 +28,11 @@ UNITS = {
     "dc.cu": ["-fmad=false"],
     "lhmc.cu": ["-fmad=false"],
     "batch.cu": ["-fmad=false"],
+    "mlp.cu": [],
+    "mlp_infer.cu": [],
+    "surrogate.cu": ["-fmad=false"],
 }
-HEADERS = ["internal.h", "vm.cuh", "mc_tables.h", "mc_chunk.cuh", "qef.cuh"]
+HEADERS = ["internal.h", "vm.cuh", "mc_tables.h", "mc_chunk.cuh", "qef.cuh", "mlp.h"]
 
 
 def _deps():

@@ -133,6 +133,10 @@ struct Lattice {
 iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, iso_mesh_info* info);
 iso_status mc_cases_lattice(iso_ctx* ctx, const Lattice& L, uint8_t* d_cases);
 
+// exclusive scan of n u32 into out (3 launches on ctx's stream); total
+// receives the sum; sums is scratch of (n + 1023) / 1024 entries
+iso_status scan_u32(iso_ctx* ctx, const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* sums, uint32_t* total);
+
 inline uint32_t words_per_row(uint32_t nx) { return (nx + 31) / 32; }
 inline uint64_t default_pitch(uint32_t nx) { return ((uint64_t)nx + 7) & ~7ull; }
 

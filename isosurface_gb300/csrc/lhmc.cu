@@ -473,6 +473,21 @@ __global__ void cube_emit(EmitArgs A) {
 }
 
 }  // namespace
+
+// exclusive scan of n u32 into out; sums needs (n + 1023) / 1024 entries
+iso_status scan_u32(iso_ctx* ctx, const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* sums, uint32_t* total) {
+    const uint32_t nb = (n + 1023) / 1024;
+    if (n == 0) {
+        cudaMemsetAsync(total, 0, 4, ctx->stream);
+        return ISO_OK;
+    }
+    scan_blocks<<<nb, 1024, 0, ctx->stream>>>(in, out, n, sums);
+    scan_sums<<<1, 1024, 0, ctx->stream>>>(sums, nb, total);
+    scan_add<<<nb, 1024, 0, ctx->stream>>>(out, n, sums);
+    ctx->launches += 3;
+    return check_launch(ctx, "scan");
+}
+
 }  // namespace iso
 
 using namespace iso;
@@ -489,19 +504,6 @@ struct Arena {
         return used <= cap ? reinterpret_cast<T*>(base + at) : nullptr;
     }
 };
-
-iso_status scan_u32(iso_ctx* ctx, const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* sums, uint32_t* total) {
-    const uint32_t nb = (n + 1023) / 1024;
-    if (n == 0) {
-        cudaMemsetAsync(total, 0, 4, ctx->stream);
-        return ISO_OK;
-    }
-    scan_blocks<<<nb, 1024, 0, ctx->stream>>>(in, out, n, sums);
-    scan_sums<<<1, 1024, 0, ctx->stream>>>(sums, nb, total);
-    scan_add<<<nb, 1024, 0, ctx->stream>>>(out, n, sums);
-    ctx->launches += 3;
-    return check_launch(ctx, "scan");
-}
 
 uint32_t pow2_at_least(uint64_t v) {
     uint64_t p = 1024;

@@ -52,7 +52,11 @@ __device__ __forceinline__ float sd_torus(V3 q, float R, float r) {
 }
 // Polynomial smooth minimum (Quilez 2013)
 __device__ __forceinline__ float smooth_min(float a, float b, float k) {
-    float h = fmaxf(k - fabsf(a - b), 0.0f) / k;
+    const float gap = k - fabsf(a - b);
+    // with k > 0 and no overlap, h is +0 and the formula gives min(a, b) - 0
+    // exactly (also for -0 and NaN operands): skip the division
+    if (k > 0.0f && !(gap > 0.0f)) return fminf(a, b);
+    float h = fmaxf(gap, 0.0f) / k;
     return fminf(a, b) - ((h * h) * k) * 0.25f;
 }
 

@@ -220,6 +220,23 @@ def test_lhmc_runs_without_stale_corners():
     assert np.max(np.abs(vals)) < 2.0 / 32
 
 
+def test_mlp_oracle_gradient_by_finite_differences():
+    """The numpy MLP oracle's analytic gradient agrees with central differences."""
+    from oracle import mlp_ref
+    rng = np.random.default_rng(0)
+    n = mlp_ref.FF * 256 + 256 + 5 * (256 * 256 + 256) + 257
+    p = rng.normal(0, 0.05, n)
+    x = rng.uniform(-1, 1, (8, 3))
+    t = rng.normal(0, 0.02, 8)
+    loss, g = mlp_ref.loss_grad(p, x, t, 10.0)
+    for idx in list(rng.choice(n, 12, replace=False)) + [n - 1, n - 2]:
+        e = np.zeros(n)
+        e[idx] = 1e-6
+        lp, _ = mlp_ref.loss_grad(p + e, x, t, 10.0)
+        lm, _ = mlp_ref.loss_grad(p - e, x, t, 10.0)
+        assert abs((lp - lm) / 2e-6 - g[idx]) <= 1e-6 + 1e-4 * abs(g[idx])
+
+
 def test_program_validation_rejects_garbage():
     good = S.lower(scenes.csg())
     oracle.Program(good)
