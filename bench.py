@@ -159,6 +159,88 @@ def secondary_workloads(ctx, torch, steps):
     return out
 
 
+MLP_FLOPS_PER_POINT = 2 * (96 * 256 + 5 * 256 * 256 + 256)
+
+
+def surrogate_workload(ctx, torch, train_steps):
+    """The learned surrogate on the 4096-sphere smooth union (k = 0.05) at
+    512^3: train the network (16M samples, Adam), then time the exact path
+    (the brute O(4096)-per-point sampler, then marching cubes) against the
+    surrogate path (network on every 4th lattice point, exact re-sampling of
+    points within `band` cells of its surface, marching cubes), both with CUDA
+    events on the library's stream, and score each surrogate mesh against the
+    exact mesh (nearest-vertex Chamfer / Hausdorff in cells, fraction of cells
+    whose corner signs differ)."""
+    import ctypes
+    from isosurface_gb300 import scenes
+    from isosurface_gb300._capi import lib
+    from isosurface_gb300.surrogate import Surrogate, case_disagreement, mesh_distance
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def timed(fn, reps):
+        best = None
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            r = fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            best = a.elapsed_time(b) if best is None else min(best, a.elapsed_time(b))
+        return best, r
+
+    src = scenes.smooth_spheres()
+    net = Surrogate(ctx, seed=5)
+    t0 = time.time()
+    net.make_dataset(src.source, 1 << 24, -1.0, 1.0, seed=9)
+    hist = net.train(train_steps, batch=65536, lr=2e-3)
+    train_s = time.time() - t0
+    size, pitch = SIZE, SIZE
+    nz = size + 1
+    field = torch.empty((nz * size * pitch,), dtype=torch.float32, device="cuda")
+    sfield = torch.empty_like(field)
+    torch.cuda.synchronize()
+
+    def exact_path():
+        ctx.sample_grid(src, size, field.data_ptr(), pitch)
+        return ctx.mc_extract_field(field.data_ptr(), size, size, nz, pitch)
+
+    exact_ms, info = timed(exact_path, 2)
+    exact = ctx.download(info)
+    cell = 1.0 / (size - 1)
+    out = {"workload": "MarchingCubes::new(513) of a smooth-min (k=0.05) union of 4096 spheres (seed 99), "
+                       "exact sampler O(4096) per point",
+           "train": {"samples": 1 << 24, "steps": train_steps, "batch": 65536, "seconds": train_s,
+                     "loss_first": float(hist[0]), "loss_last": float(np.mean(hist[-20:]))},
+           "exact_ms": exact_ms, "exact_triangles": int(info.num_triangles), "bands": {}}
+    ms_buf = (ctypes.c_double * 8)()
+    ln_buf = (ctypes.c_uint64 * 8)()
+    for band in (1.0, 2.0):
+        def surrogate_path():
+            st = net.field(src, size, sfield.data_ptr(), pitch, coarse_step=4, band_cells=band)
+            return st, ctx.mc_extract_field(sfield.data_ptr(), size, size, nz, pitch)
+
+        surrogate_path()
+        ms, (st, sinfo) = timed(surrogate_path, 3)
+        lib().iso_ctx_stage_times(ctx.h, ms_buf, ln_buf)
+        lib().iso_ctx_enable_stage_timing(ctx.h, 1)
+        surrogate_path()
+        lib().iso_ctx_stage_times(ctx.h, ms_buf, ln_buf)
+        lib().iso_ctx_enable_stage_timing(ctx.h, 0)
+        mlp_ms, band_ms = ms_buf[6], ms_buf[0]
+        m = ctx.download(sinfo)
+        d = mesh_distance(ctx, m.vertices, exact.vertices, 2 * cell, max_rings=64)
+        dis = case_disagreement(ctx, field.data_ptr(), sfield.data_ptr(), size, size, nz, pitch)
+        out["bands"]["%g" % band] = {
+            "ms": ms, "speedup_vs_exact": exact_ms / ms, "band_fraction": st["band_points"] / st["total_points"],
+            "network_points": st["coarse_points"], "network_ms": mlp_ms, "exact_resample_ms": band_ms,
+            "network_tflops": MLP_FLOPS_PER_POINT * st["coarse_points"] / (mlp_ms / 1e3) / 1e12,
+            "chamfer_cells": d["chamfer"] / cell, "hausdorff_cells": d["hausdorff"] / cell,
+            "distance_search_capped": d["capped"],
+            "case_disagreement": dis / float((size - 1) * (size - 1) * size), "triangles": int(sinfo.num_triangles)}
+    net.close()
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -201,6 +283,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true", help="skip the batch / DC / LHMC timings")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-surrogate workload")
+    ap.add_argument("--surrogate-train-steps", type=int, default=4000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -336,6 +420,8 @@ def main():
     secondary = None
     if not args.no_secondary:
         secondary = secondary_workloads(ctx, torch, args.steps)
+        if not args.no_surrogate:
+            secondary["surrogate_512"] = surrogate_workload(ctx, torch, args.surrogate_train_steps)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

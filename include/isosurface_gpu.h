@@ -379,8 +379,11 @@ ISO_API iso_status iso_field_case_disagreement(iso_ctx* ctx, const float* fa, co
 /* ------------------------------------------------------------------------ */
 /* PointCloud (src/point_cloud.rs:50-63)                                      */
 /* ------------------------------------------------------------------------ */
-ISO_API iso_status iso_point_cloud_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size,
-                                   iso_mesh_info* info);
+/* PointCloud::<Signed>::new(size).extract: the centre of every cell whose
+ * case is neither 0 nor 255, in traversal order, as vertices (no indices);
+ * flags: ISO_FLAG_NORMALS for the *InterleavedNormals sinks. */
+ISO_API iso_status iso_point_cloud_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t flags,
+                                           iso_mesh_info* info);
 
 /* ------------------------------------------------------------------------ */
 /* Host-side sampling helpers                                                */

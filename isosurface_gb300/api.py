@@ -72,6 +72,7 @@ class Context:
         self.h = h
         self.device = device
         self._programs = {}
+        self._vertex_floats = 3  # 6 after an extraction with per-vertex normals
 
     def close(self):
         if getattr(self, "h", None):
@@ -111,15 +112,19 @@ class Context:
         return p
 
     # -- extraction ---------------------------------------------------------
-    def mc_extract(self, source, size, keys=False):
+    def _flags(self, keys, normals):
+        self._vertex_floats = 6 if normals else 3
+        return (ISO_FLAG_KEYS if keys else 0) | (ISO_FLAG_NORMALS if normals else 0)
+
+    def mc_extract(self, source, size, keys=False, normals=False):
         info = MeshInfo()
-        flags = ISO_FLAG_KEYS if keys else 0
+        flags = self._flags(keys, normals)
         check(lib().iso_mc_extract(self.h, self.program(source).h, size, flags, ctypes.byref(info)), self.h)
         return info
 
     def mc_extract_field(self, field_ptr, nx, ny, nz, pitch, keys=False):
         info = MeshInfo()
-        flags = ISO_FLAG_KEYS if keys else 0
+        flags = self._flags(keys, False)
         check(lib().iso_mc_extract_field(self.h, ctypes.c_void_p(field_ptr), nx, ny, nz, pitch, flags,
                                          ctypes.byref(info)), self.h)
         return info
@@ -130,15 +135,15 @@ class Context:
                                  out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))), self.h)
         return out
 
-    def dc_extract(self, source, size, placer=0, keys=False):
+    def dc_extract(self, source, size, placer=0, keys=False, normals=False):
         info = MeshInfo()
-        flags = ISO_FLAG_KEYS if keys else 0
+        flags = self._flags(keys, normals)
         check(lib().iso_dc_extract(self.h, self.program(source).h, size, placer, flags, ctypes.byref(info)), self.h)
         return info
 
-    def lhmc_extract(self, source, max_depth, keys=False):
+    def lhmc_extract(self, source, max_depth, keys=False, normals=False):
         info = MeshInfo()
-        flags = ISO_FLAG_KEYS if keys else 0
+        flags = self._flags(keys, normals)
         check(lib().iso_lhmc_extract(self.h, self.program(source).h, max_depth, flags, ctypes.byref(info)), self.h)
         return info
 
@@ -146,9 +151,10 @@ class Context:
     def lhmc_stale_corners(self):
         return lib().iso_lhmc_stale_corners(self.h)
 
-    def point_cloud_extract(self, source, size):
+    def point_cloud_extract(self, source, size, normals=False):
         info = MeshInfo()
-        check(lib().iso_point_cloud_extract(self.h, self.program(source).h, size, ctypes.byref(info)), self.h)
+        flags = self._flags(False, normals)
+        check(lib().iso_point_cloud_extract(self.h, self.program(source).h, size, flags, ctypes.byref(info)), self.h)
         return info
 
     def sample_grid(self, source, size, field_ptr, pitch):
@@ -164,8 +170,11 @@ class Context:
                                       nrm.ctypes.data_as(f32p) if normals else None), self.h)
         return (vals, nrm) if normals else vals
 
-    def download(self, info, keys=False, vertex_floats=3, out=None):
-        """Copy the last mesh to host numpy arrays (or into `out` = (vertices, indices))."""
+    def download(self, info, keys=False, vertex_floats=None, out=None):
+        """Copy the last mesh to host numpy arrays (or into `out` = (vertices, indices)).
+        Vertices are (n, 3), or (n, 6) = x y z nx ny nz after an extraction with normals."""
+        if vertex_floats is None:
+            vertex_floats = self._vertex_floats
         nv, nt = info.num_vertices, info.num_triangles
         if out is not None:
             v, i = out
@@ -227,11 +236,13 @@ class Batch:
     def run(self, graph=True):
         from ._capi import ISO_BATCH_GRAPH
         info = MeshInfo()
+        self.ctx._vertex_floats = 3
         check(lib().iso_batch_run(self.h, ISO_BATCH_GRAPH if graph else 0, ctypes.byref(info)), self.ctx.h)
         return info
 
     def run_per_chunk(self):
         info = MeshInfo()
+        self.ctx._vertex_floats = 3
         check(lib().iso_batch_run_per_chunk(self.h, ctypes.byref(info)), self.ctx.h)
         return info
 
@@ -306,13 +317,24 @@ class IndexedVertices(_Extractor):
 
 
 class OnlyInterleavedNormals(OnlyVertices):
-    """x y z nx ny nz per vertex, faces discarded (extractor.rs:46-69)."""
+    """x y z nx ny nz per vertex, faces discarded (extractor.rs:46-69): the
+    normal is source.sample_normal(vertex), computed on the device from the
+    source being extracted (`source` is accepted for the reference's
+    signature)."""
     with_normals = True
+
+    def __init__(self, vertices, source=None):
+        super().__init__(vertices)
+        self.source = source
 
 
 class IndexedInterleavedNormals(IndexedVertices):
     """x y z nx ny nz per vertex plus indices (extractor.rs:97-127)."""
     with_normals = True
+
+    def __init__(self, vertices, indices, source=None):
+        super().__init__(vertices, indices)
+        self.source = source
 
 
 def _replay(extractor, mesh):
@@ -341,9 +363,7 @@ class MarchingCubes:
     def extract(self, sampler, extractor):
         ctx = self.context or default_context()
         source = _source_of(sampler)
-        if getattr(extractor, "with_normals", False):
-            raise IsoError(9, "per-vertex normals are not available for MarchingCubes yet")
-        info = ctx.mc_extract(source, self.size)
+        info = ctx.mc_extract(source, self.size, normals=getattr(extractor, "with_normals", False))
         _replay(extractor, ctx.download(info))
 
 
@@ -369,9 +389,8 @@ class DualContouring:
 
     def extract(self, sampler, extractor):
         ctx = self.context or default_context()
-        if getattr(extractor, "with_normals", False):
-            raise IsoError(9, "per-vertex normals are not available for DualContouring yet")
-        info = ctx.dc_extract(_source_of(sampler), self.size, self.placer)
+        info = ctx.dc_extract(_source_of(sampler), self.size, self.placer,
+                              normals=getattr(extractor, "with_normals", False))
         _replay(extractor, ctx.download(info))
 
 
@@ -384,9 +403,8 @@ class LinearHashedMarchingCubes:
 
     def extract(self, sampler, extractor):
         ctx = self.context or default_context()
-        if getattr(extractor, "with_normals", False):
-            raise IsoError(9, "per-vertex normals are not available for LinearHashedMarchingCubes yet")
-        info = ctx.lhmc_extract(_source_of(sampler), self.max_depth)
+        info = ctx.lhmc_extract(_source_of(sampler), self.max_depth,
+                                normals=getattr(extractor, "with_normals", False))
         _replay(extractor, ctx.download(info))
 
 
@@ -399,5 +417,6 @@ class PointCloud:
 
     def extract(self, sampler, extractor):
         ctx = self.context or default_context()
-        info = ctx.point_cloud_extract(_source_of(sampler), self.size)
+        info = ctx.point_cloud_extract(_source_of(sampler), self.size,
+                                       normals=getattr(extractor, "with_normals", False))
         _replay(extractor, ctx.download(info))

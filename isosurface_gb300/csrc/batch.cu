@@ -120,6 +120,10 @@ struct iso_batch {
     uint64_t cap_v = 0, cap_t = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    // the context's mesh buffers the graph was captured with: another
+    // extraction on the context may regrow (free and reallocate) them
+    void* graph_v = nullptr;
+    void* graph_i = nullptr;
     bool sized = false;
 };
 
@@ -351,6 +355,12 @@ iso_status iso_batch_run(iso_batch* b, uint32_t flags, iso_mesh_info* info) {
     }
     if ((s = ensure(ctx, ctx->mesh_v, 12 * b->cap_v)) != ISO_OK) return s;
     if ((s = ensure(ctx, ctx->mesh_i, 12 * b->cap_t)) != ISO_OK) return s;
+    if (b->exec && (b->graph_v != ctx->mesh_v.p || b->graph_i != ctx->mesh_i.p)) {
+        cudaGraphExecDestroy(b->exec);
+        cudaGraphDestroy(b->graph);
+        b->exec = nullptr;
+        b->graph = nullptr;
+    }
     if (!b->exec) {
         cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "begin capture");
@@ -368,6 +378,8 @@ iso_status iso_batch_run(iso_batch* b, uint32_t flags, iso_mesh_info* info) {
         b->graph = g;
         e = cudaGraphInstantiate(&b->exec, g, 0);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "instantiate graph");
+        b->graph_v = ctx->mesh_v.p;
+        b->graph_i = ctx->mesh_i.p;
     }
     {
         StageTimer timer(ctx, ISO_STAGE_OTHER);

@@ -1,6 +1,8 @@
 // Contexts, programs, buffers and the C ABI entry points (include/isosurface_gpu.h).
 #include <cuda_runtime.h>
 
+#include <utility>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -449,17 +451,19 @@ iso_status iso_mc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, 
     iso_status s = check_size(ctx, prog, size);
     if (s != ISO_OK) return s;
     if (flags & ~(uint32_t)(ISO_FLAG_KEYS | ISO_FLAG_NORMALS)) return fail(ctx, ISO_ERR_INVALID_ARG, "unknown flags");
-    if (flags & ISO_FLAG_NORMALS) return fail(ctx, ISO_ERR_UNSUPPORTED, "normals flag not available for MC yet");
     if (size == 1) {
         ctx->last = iso_mesh_info{};
         ctx->last_flags = flags;
+        ctx->last_vertex_floats = (flags & ISO_FLAG_NORMALS) ? 6 : 3;
         if (info) *info = ctx->last;
         return ISO_OK;
     }
     Lattice L;
     if ((s = sample_into_ctx(ctx, prog, size, &L)) != ISO_OK) return s;
-    return mc_extract_lattice(ctx, L, flags, info);
+    if ((s = mc_extract_lattice(ctx, L, flags & ~(uint32_t)ISO_FLAG_NORMALS, info)) != ISO_OK) return s;
+    return (flags & ISO_FLAG_NORMALS) ? attach_normals(ctx, prog) : ISO_OK;
 }
+
 
 iso_status iso_mc_extract_field(iso_ctx* ctx, const float* field, uint32_t nx, uint32_t ny, uint32_t nz, uint64_t pitch,
                                 uint32_t flags, iso_mesh_info* info) {
@@ -510,11 +514,23 @@ iso_status iso_sample_points(iso_ctx* ctx, const iso_program* prog, const float*
     return e == cudaSuccess ? ISO_OK : cuda_fail(ctx, e, "sample points");
 }
 
-iso_status iso_point_cloud_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, iso_mesh_info* info) {
-    (void)prog;
-    (void)size;
-    (void)info;
-    return fail(ctx, ISO_ERR_UNSUPPORTED, "point cloud not built yet");
+iso_status iso_point_cloud_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t flags,
+                                   iso_mesh_info* info) {
+    iso_status s = check_size(ctx, prog, size);
+    if (s != ISO_OK) return s;
+    if (flags & ~(uint32_t)ISO_FLAG_NORMALS) return fail(ctx, ISO_ERR_INVALID_ARG, "unsupported flags");
+    if (size == 1) {  // no cell
+        ctx->last = iso_mesh_info{};
+        ctx->last_flags = 0;
+        ctx->last_vertex_floats = 3;
+    } else {
+        Lattice L;
+        if ((s = sample_into_ctx(ctx, prog, size, &L)) != ISO_OK) return s;
+        if ((s = point_cloud_lattice(ctx, L, nullptr)) != ISO_OK) return s;
+    }
+    if ((flags & ISO_FLAG_NORMALS) && (s = attach_normals(ctx, prog)) != ISO_OK) return s;
+    if (info) *info = ctx->last;
+    return ISO_OK;
 }
 
 }  // extern "C"

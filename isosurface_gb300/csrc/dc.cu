@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(128) dc_place(PlaceArgs A) {
 
 using namespace iso;
 
-extern "C" iso_status iso_dc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t placer,
+static iso_status dc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t placer,
                                      uint32_t flags, iso_mesh_info* info) {
     if (!ctx || !prog) return ISO_ERR_INVALID_ARG;
     if (prog->ctx != ctx) return fail(ctx, ISO_ERR_INVALID_ARG, "program belongs to another context");
@@ -187,4 +187,13 @@ extern "C" iso_status iso_dc_extract(iso_ctx* ctx, const iso_program* prog, uint
     if ((s = launch_sign_bits(ctx, dval, m, m, n, dpitch, dbits)) != ISO_OK) return s;
     Lattice L{m, m, n, dpitch, dval, dbits, (uint32_t)dW, 0.0f, dpos};
     return mc_extract_lattice(ctx, L, flags, info);
+}
+
+// ISO_FLAG_NORMALS: the *InterleavedNormals sinks, sample_normal at every vertex
+extern "C" iso_status iso_dc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t placer, uint32_t flags, iso_mesh_info* info) {
+    if (!ctx || !prog) return ISO_ERR_INVALID_ARG;
+    if (flags & ~(uint32_t)(ISO_FLAG_KEYS | ISO_FLAG_NORMALS)) return fail(ctx, ISO_ERR_INVALID_ARG, "unsupported flags");
+    iso_status s = dc_extract_impl(ctx, prog, size, placer, flags & ~(uint32_t)ISO_FLAG_NORMALS, info);
+    if (s != ISO_OK || !(flags & ISO_FLAG_NORMALS)) return s;
+    return attach_normals(ctx, prog);
 }

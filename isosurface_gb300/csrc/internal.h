@@ -132,6 +132,14 @@ struct Lattice {
 };
 iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, iso_mesh_info* info);
 iso_status mc_cases_lattice(iso_ctx* ctx, const Lattice& L, uint8_t* d_cases);
+// PointCloud::extract over a sampled lattice: active-cell centres into the context's mesh
+iso_status point_cloud_lattice(iso_ctx* ctx, const Lattice& L, iso_mesh_info* info);
+
+// x y z -> x y z nx ny nz for n device vertices (out must not alias v)
+iso_status launch_vertex_normals(iso_ctx* ctx, const iso_program* prog, const float* v, uint64_t n, float* out);
+// replace the context's last mesh vertices by interleaved vertex + normal
+// (the *InterleavedNormals sinks) and mark the mesh as 6 floats per vertex
+iso_status attach_normals(iso_ctx* ctx, const iso_program* prog);
 
 // exclusive scan of n u32 into out (3 launches on ctx's stream); total
 // receives the sum; sums is scratch of (n + 1023) / 1024 entries

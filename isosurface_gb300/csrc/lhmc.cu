@@ -523,7 +523,7 @@ inline size_t scan_sums_for(uint64_t n) { return (size_t)((n + 1023) / 1024) + 6
 
 }  // namespace
 
-extern "C" iso_status iso_lhmc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t max_depth, uint32_t flags,
+static iso_status lhmc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint32_t max_depth, uint32_t flags,
                                        iso_mesh_info* info) {
     if (!ctx || !prog) return ISO_ERR_INVALID_ARG;
     if (prog->ctx != ctx) return fail(ctx, ISO_ERR_INVALID_ARG, "program belongs to another context");
@@ -711,3 +711,12 @@ extern "C" iso_status iso_lhmc_extract(iso_ctx* ctx, const iso_program* prog, ui
 }
 
 extern "C" uint64_t iso_lhmc_stale_corners(const iso_ctx* ctx) { return ctx ? ctx->lhmc_stale : 0; }
+
+// ISO_FLAG_NORMALS: the *InterleavedNormals sinks, sample_normal at every vertex
+extern "C" iso_status iso_lhmc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t max_depth, uint32_t flags, iso_mesh_info* info) {
+    if (!ctx || !prog) return ISO_ERR_INVALID_ARG;
+    if (flags & ~(uint32_t)(ISO_FLAG_KEYS | ISO_FLAG_NORMALS)) return fail(ctx, ISO_ERR_INVALID_ARG, "unsupported flags");
+    iso_status s = lhmc_extract_impl(ctx, prog, max_depth, flags & ~(uint32_t)ISO_FLAG_NORMALS, info);
+    if (s != ISO_OK || !(flags & ISO_FLAG_NORMALS)) return s;
+    return attach_normals(ctx, prog);
+}

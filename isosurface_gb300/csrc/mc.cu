@@ -690,6 +690,118 @@ iso_status mc_extract_grids(iso_ctx* ctx, const void* d_grids, uint32_t ngrids, 
     return check_launch(ctx, "batch emit");
 }
 
+// ---- PointCloud::extract (src/point_cloud.rs:50-63) -------------------------
+// Every cell whose case is neither 0 nor 255 emits corners[0].lerp(corners[6],
+// 0.5) in traversal order.  A cell is active iff its eight sign bits are not
+// all equal: with the four sign rows around a cell row, the cells whose x and
+// x+1 corners are all set or all clear come out of word-wide AND / OR.
+namespace {
+
+struct PcArgs {
+    const uint32_t* bits;
+    uint32_t W;         // sign words per sample row
+    uint32_t nx, ny;    // samples per row, rows per layer
+    uint32_t cy, cz;    // cell rows per layer, cell layers
+    float inv;
+    uint32_t* counts;   // per (cell row, word)
+    const uint32_t* offsets;
+    float* out;
+};
+
+__device__ __forceinline__ uint32_t pc_active(const PcArgs& A, uint32_t w, uint32_t y, uint32_t z) {
+    const uint32_t* r00 = A.bits + ((size_t)z * A.ny + y) * A.W;
+    const uint32_t* r10 = r00 + A.W;
+    const uint32_t* r01 = r00 + (size_t)A.ny * A.W;
+    const uint32_t* r11 = r01 + A.W;
+    const uint32_t a = r00[w] & r10[w] & r01[w] & r11[w], o = r00[w] | r10[w] | r01[w] | r11[w];
+    uint32_t an = 0, on = 0;
+    if (w + 1 < A.W) {
+        an = r00[w + 1] & r10[w + 1] & r01[w + 1] & r11[w + 1];
+        on = r00[w + 1] | r10[w + 1] | r01[w + 1] | r11[w + 1];
+    }
+    const uint32_t all_in = a & ((a >> 1) | (an << 31));   // corners x and x+1 all inside
+    const uint32_t any_in = o | (o >> 1) | (on << 31);
+    uint32_t act = any_in & ~all_in;
+    const uint32_t first = 32 * w, ncx = A.nx - 1;       // cells along x
+    if (first + 32 > ncx) act &= first >= ncx ? 0u : ((1u << (ncx - first)) - 1u);
+    return act;
+}
+
+__global__ void pc_count(PcArgs A) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (uint64_t)A.W * A.cy * A.cz) return;
+    const uint32_t w = (uint32_t)(t % A.W);
+    const uint64_t r = t / A.W;
+    A.counts[t] = __popc(pc_active(A, w, (uint32_t)(r % A.cy), (uint32_t)(r / A.cy)));
+}
+
+__global__ void pc_emit(PcArgs A) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (uint64_t)A.W * A.cy * A.cz) return;
+    const uint32_t w = (uint32_t)(t % A.W);
+    const uint64_t r = t / A.W;
+    const uint32_t y = (uint32_t)(r % A.cy), z = (uint32_t)(r / A.cy);
+    uint32_t act = pc_active(A, w, y, z);
+    uint32_t at = A.offsets[t];
+    // Vec3::lerp(other, f) = (1 - f) * self + f * other (vector.rs:325-333)
+    const float f = 0.5f, of = 1.0f - f;
+    const float y0 = (float)y * A.inv, y1 = (float)(y + 1) * A.inv;
+    const float z0 = (float)z * A.inv, z1 = (float)(z + 1) * A.inv;
+    const float py = of * y0 + f * y1, pz = of * z0 + f * z1;
+    while (act) {
+        const uint32_t b = __ffs(act) - 1;
+        act &= act - 1;
+        const uint32_t x = 32 * w + b;
+        const float x0 = (float)x * A.inv, x1 = (float)(x + 1) * A.inv;
+        float* o = A.out + 3 * (size_t)at++;
+        o[0] = of * x0 + f * x1;
+        o[1] = py;
+        o[2] = pz;
+    }
+}
+
+}  // namespace
+
+iso_status point_cloud_lattice(iso_ctx* ctx, const Lattice& L, iso_mesh_info* info) {
+    const uint32_t cy = L.ny - 1, cz = L.nz - 1;
+    const uint64_t nwords = (uint64_t)L.words_per_row * cy * cz;
+    if (nwords >= 0xFFFFFFFFull) return fail(ctx, ISO_ERR_TOO_LARGE, "grid too large");
+    const uint64_t sums = (nwords + 1023) / 1024 + 64;
+    iso_status s;
+    if ((s = ensure(ctx, ctx->scan, 4 * (2 * nwords + sums + 64))) != ISO_OK) return s;
+    uint32_t* counts = (uint32_t*)ctx->scan.p;
+    uint32_t* offsets = counts + nwords;
+    uint32_t* scratch = offsets + nwords;
+    uint32_t* total = scratch + sums;
+    PcArgs a{L.bits, L.words_per_row, L.nx, L.ny, cy, cz, L.inv, counts, offsets, nullptr};
+    const unsigned blocks = (unsigned)((nwords + 255) / 256);
+    {
+        StageTimer timer(ctx, ISO_STAGE_CLASSIFY);
+        pc_count<<<blocks, 256, 0, ctx->stream>>>(a);
+        ctx->launches++;
+        if ((s = scan_u32(ctx, counts, offsets, (uint32_t)nwords, scratch, total)) != ISO_OK) return s;
+    }
+    cudaError_t e = cudaMemcpyAsync(ctx->h_pinned, total, 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "point count");
+    const uint64_t np = *(uint32_t*)ctx->h_pinned;
+    if ((s = ensure(ctx, ctx->mesh_v, 12 * std::max<uint64_t>(np, 1))) != ISO_OK) return s;
+    a.out = (float*)ctx->mesh_v.p;
+    {
+        StageTimer timer(ctx, ISO_STAGE_EMIT);
+        pc_emit<<<blocks, 256, 0, ctx->stream>>>(a);
+    }
+    ctx->launches++;
+    if ((s = check_launch(ctx, "point cloud")) != ISO_OK) return s;
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "point cloud");
+    ctx->last = iso_mesh_info{np, 0, (uint64_t)(L.nx - 1) * cy * cz};
+    ctx->last_flags = 0;
+    ctx->last_vertex_floats = 3;
+    if (info) *info = ctx->last;
+    return ISO_OK;
+}
+
 }  // namespace iso
 
 // ---------------------------------------------------------------------------

@@ -9,6 +9,8 @@
 // the reference's f32 evaluation.
 #include <cuda_runtime.h>
 
+#include <utility>
+
 #include "internal.h"
 #include "vm.cuh"
 
@@ -216,7 +218,51 @@ __global__ void sample_points(ProgView pv, const float* pts, uint64_t n, float* 
     }
 }
 
+// IndexedInterleavedNormals / OnlyInterleavedNormals (extractor.rs:46-69,
+// 97-127): each emitted vertex followed by source.sample_normal(vertex),
+// unnormalised, x y z nx ny nz per vertex.
+__global__ void vertex_normals(ProgView pv, const float* v, uint64_t n, float* out) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const V3 p = v3(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+    V3 nn;
+    eval_hermite(pv, p, &nn);
+    float* o = out + 6 * i;
+    o[0] = p.x;
+    o[1] = p.y;
+    o[2] = p.z;
+    o[3] = nn.x;
+    o[4] = nn.y;
+    o[5] = nn.z;
+}
+
 }  // namespace
+
+iso_status launch_vertex_normals(iso_ctx* ctx, const iso_program* prog, const float* v, uint64_t n, float* out) {
+    if (n == 0) return ISO_OK;
+    {
+        StageTimer timer(ctx, ISO_STAGE_OTHER);
+        vertex_normals<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(prog->view(), v, n, out);
+    }
+    ctx->launches++;
+    return check_launch(ctx, "vertex normals");
+}
+
+iso_status attach_normals(iso_ctx* ctx, const iso_program* prog) {
+    const uint64_t nv = ctx->last.num_vertices;
+    iso_status s;
+    if (nv) {
+        if ((s = ensure(ctx, ctx->aux3, 24 * nv)) != ISO_OK) return s;
+        if ((s = launch_vertex_normals(ctx, prog, (const float*)ctx->mesh_v.p, nv, (float*)ctx->aux3.p)) != ISO_OK)
+            return s;
+        std::swap(ctx->mesh_v, ctx->aux3);
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "vertex normals");
+    }
+    ctx->last_flags |= ISO_FLAG_NORMALS;
+    ctx->last_vertex_floats = 6;
+    return ISO_OK;
+}
 
 iso_status launch_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t nx, uint32_t ny, uint32_t nz, float inv,
                               float* field, uint64_t pitch, uint32_t* bits) {

@@ -86,6 +86,7 @@ class Surrogate:
         """Marching cubes over the surrogate field; the mesh stays in the
         context (Context.download).  Returns (MeshInfo, band statistics)."""
         st, info = SurrogateStats(), MeshInfo()
+        self.ctx._vertex_floats = 3
         check(lib().iso_surrogate_extract(self.ctx.h, self.h, self.ctx.program(exact_source).h, size, coarse_step,
                                           band_cells, ISO_FLAG_KEYS if keys else 0, ctypes.byref(st),
                                           ctypes.byref(info)), self.ctx.h)

@@ -68,3 +68,17 @@ def test_batch_same_program_many_sizes(ctx):
         w = oracle.Program(S.lower(src)).marching_cubes(size)
         assert np.array_equal(got.vertices, w.vertices) and np.array_equal(got.indices, w.indices)
     b.close()
+
+
+def test_batch_graph_survives_mesh_buffer_regrowth(ctx, chunk_set, want):
+    """The captured graph writes into the context's mesh buffers; a larger
+    extraction in between regrows (reallocates) them, and the next replay must
+    notice and capture again instead of writing to the freed buffers."""
+    b = Batch(ctx, chunk_set)
+    b.run(graph=False)
+    b.run(graph=True)
+    big = ctx.mc_extract(scenes.sphere_union(), 385)  # many more vertices than the batch
+    assert big.num_vertices > 0
+    info = b.run(graph=True)
+    _check(b.meshes(info), want)
+    b.close()

@@ -70,3 +70,16 @@ def test_dc_small_sizes(ctx):
     for size in (1, 2):
         info = ctx.dc_extract(scenes.sphere(), size)
         assert info.num_triangles == 0
+
+
+@pytest.mark.parametrize("placer", [0, 1])
+def test_dc_interleaved_normals(ctx, placer):
+    """DualContouring into IndexedInterleavedNormals: the DC mesh plus
+    sample_normal at each placed vertex, bit for bit."""
+    src = scenes.csg()
+    o = oracle.Program(S.lower(src))
+    want = o.dual_contouring(33, placer)
+    got = ctx.download(ctx.dc_extract(src, 33, placer, normals=True))
+    assert np.array_equal(got.vertices[:, :3], want.vertices)
+    assert np.array_equal(got.vertices[:, 3:], o.sample_normal(want.vertices))
+    assert np.array_equal(got.indices, want.indices)

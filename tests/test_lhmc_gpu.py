@@ -86,3 +86,13 @@ def test_lhmc_reference_style_api(ctx):
     LinearHashedMarchingCubes(5, context=ctx).extract(Sampler(scenes.sphere()), IndexedVertices(v, i))
     want = oracle.Program(S.lower(scenes.sphere())).lhmc(5)
     assert len(i) == len(want.indices) and len(v) == 3 * len(want.vertices)
+
+
+def test_lhmc_interleaved_normals(ctx):
+    src = scenes.csg()
+    plain = ctx.download(ctx.lhmc_extract(src, 6))
+    got = ctx.download(ctx.lhmc_extract(src, 6, normals=True))
+    assert np.array_equal(got.vertices[:, :3], plain.vertices)
+    assert np.array_equal(got.indices, plain.indices)
+    o = oracle.Program(S.lower(src))
+    assert np.array_equal(got.vertices[:, 3:], o.sample_normal(plain.vertices))

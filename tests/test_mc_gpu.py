@@ -187,3 +187,67 @@ def test_reference_style_api(ctx):
     want = oracle.Program(S.lower(scenes.sphere())).marching_cubes(33)
     assert np.array_equal(np.asarray(vertices, np.float32), want.vertices.reshape(-1))
     assert np.array_equal(np.asarray(indices, np.uint32), want.indices)
+
+
+@pytest.mark.parametrize("name", ["sphere", "csg", "torus", "smooth", "central_difference", "sphere_set"])
+def test_mc_interleaved_normals(ctx, name):
+    """IndexedInterleavedNormals (extractor.rs:97-127): each vertex followed
+    by source.sample_normal(vertex), bit for bit as the oracle."""
+    src = _sources()[name]
+    want = oracle.Program(S.lower(src)).marching_cubes(33, normals=True)
+    got = ctx.download(ctx.mc_extract(src, 33, normals=True))
+    assert got.vertices.shape == (len(want.vertices), 6)
+    assert np.array_equal(got.vertices[:, :3], want.vertices)
+    assert np.array_equal(got.vertices[:, 3:], want.normals)
+    assert np.array_equal(got.indices, want.indices)
+    # the next plain extraction is 3 floats per vertex again
+    plain = ctx.download(ctx.mc_extract(src, 33))
+    assert plain.vertices.shape == (len(want.vertices), 3)
+
+
+def test_reference_style_normals_sink(ctx):
+    from isosurface_gb300 import IndexedInterleavedNormals, MarchingCubes, OnlyInterleavedNormals, Sampler
+    src = scenes.csg()
+    want = oracle.Program(S.lower(src)).marching_cubes(21, normals=True)
+    v, i = [], []
+    MarchingCubes(21, context=ctx).extract(Sampler(src), IndexedInterleavedNormals(v, i, src))
+    inter = np.concatenate([want.vertices, want.normals], 1).reshape(-1)
+    assert np.array_equal(np.asarray(v, np.float32), inter)
+    assert np.array_equal(np.asarray(i, np.uint32), want.indices)
+    v2 = []
+    MarchingCubes(21, context=ctx).extract(Sampler(src), OnlyInterleavedNormals(v2, src))
+    assert np.array_equal(np.asarray(v2, np.float32), inter)
+
+
+@pytest.mark.parametrize("name", sorted(_sources()))
+@pytest.mark.parametrize("size", [1, 2, 5, 17, 40])
+def test_point_cloud_bytes_identical(ctx, name, size):
+    """PointCloud::extract (point_cloud.rs:50-63): active-cell centres in
+    traversal order."""
+    src = _sources()[name]
+    want = oracle.Program(S.lower(src)).point_cloud(size)
+    info = ctx.point_cloud_extract(src, size)
+    got = ctx.download(info)
+    assert info.num_triangles == 0 and info.num_cells == want.cells
+    assert np.array_equal(got.vertices, want.vertices)
+
+
+def test_point_cloud_full_size_and_normals(ctx):
+    src = scenes.sphere_union()
+    o = oracle.Program(S.lower(src))
+    want = o.point_cloud(129)
+    got = ctx.download(ctx.point_cloud_extract(src, 129, normals=True))
+    assert np.array_equal(got.vertices[:, :3], want.vertices)
+    assert np.array_equal(got.vertices[:, 3:], o.sample_normal(want.vertices))
+    # 512^3: count and a slab of centres against the oracle's cases
+    info = ctx.point_cloud_extract(src, 513)
+    cases = ctx.mc_cases(src, 513)
+    assert info.num_vertices == int(np.count_nonzero((cases != 0) & (cases != 255)))
+
+
+def test_point_cloud_reference_style_api(ctx):
+    from isosurface_gb300 import OnlyVertices, PointCloud, Sampler
+    v = []
+    PointCloud(33, context=ctx).extract(Sampler(scenes.bench_torus()), OnlyVertices(v))
+    want = oracle.Program(S.lower(scenes.bench_torus())).point_cloud(33)
+    assert np.array_equal(np.asarray(v, np.float32), want.vertices.reshape(-1))
