@@ -258,7 +258,7 @@ iso_status iso_ctx_destroy(iso_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     DevBuf* bufs[] = {&ctx->field, &ctx->bits, &ctx->rowtri, &ctx->rowvert, &ctx->scan, &ctx->aux,
-                      &ctx->aux2, &ctx->aux3, &ctx->mesh_v, &ctx->mesh_i, &ctx->mesh_k};
+                      &ctx->aux2, &ctx->aux3, &ctx->tiles, &ctx->mesh_v, &ctx->mesh_i, &ctx->mesh_k};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     if (ctx->d_err) cudaFree(ctx->d_err);
@@ -420,7 +420,10 @@ static iso_status sample_into_ctx(iso_ctx* ctx, const iso_program* prog, uint32_
     if ((s = ensure(ctx, ctx->field, 4ull * pitch * ny * nz)) != ISO_OK) return s;
     if ((s = ensure(ctx, ctx->bits, 4ull * W * ny * nz)) != ISO_OK) return s;
     const float inv = 1.0f / (float)(size - 1);
-    if ((s = launch_sample_grid(ctx, prog, nx, ny, nz, inv, (float*)ctx->field.p, pitch, (uint32_t*)ctx->bits.p)) != ISO_OK)
+    // marching cubes reads values only at the ends of crossing edges: the
+    // sampler may skip the values far from the surface
+    if ((s = launch_sample_grid(ctx, prog, nx, ny, nz, inv, (float*)ctx->field.p, pitch, (uint32_t*)ctx->bits.p,
+                                true)) != ISO_OK)
         return s;
     *L = Lattice{nx, ny, nz, pitch, (const float*)ctx->field.p, (const uint32_t*)ctx->bits.p, W, inv, nullptr};
     return ISO_OK;

@@ -47,7 +47,7 @@ struct iso_ctx {
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     // work buffers (grow-only, reused across calls)
-    iso::DevBuf field, bits, rowtri, rowvert, scan, aux, aux2, aux3;
+    iso::DevBuf field, bits, rowtri, rowvert, scan, aux, aux2, aux3, tiles;
     // last mesh
     iso::DevBuf mesh_v, mesh_i, mesh_k;
     iso_mesh_info last{};
@@ -111,7 +111,7 @@ iso_status set_device(iso_ctx* ctx);
 
 // sample.cu
 iso_status launch_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t nx, uint32_t ny, uint32_t nz,
-                              float inv, float* field, uint64_t pitch, uint32_t* bits);
+                              float inv, float* field, uint64_t pitch, uint32_t* bits, bool near_only = false);
 iso_status launch_sign_bits(iso_ctx* ctx, const float* field, uint32_t nx, uint32_t ny, uint32_t nz,
                             uint64_t pitch, uint32_t* bits);
 iso_status launch_sample_points(iso_ctx* ctx, const iso_program* prog, const float* d_pts, uint64_t n,

@@ -122,12 +122,15 @@ __global__ void __launch_bounds__(256) mc_chunk_count(ChunkCountArgs A) {
 // range that no warp counted.
 __global__ void __launch_bounds__(1024) mc_range_scan(const uint2* rangeagg, uint32_t nr, uint2* rangepre,
                                                       uint64_t* totals, uint2* local, uint32_t chunks, uint32_t* err) {
-    __shared__ uint64_t s_wt[32], s_wv[32];
+    __shared__ uint64_t s_wv[32], s_wt[32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint64_t carry_t = 0, carry_v = 0;
+    uint2 next = threadIdx.x < nr ? rangeagg[threadIdx.x] : make_uint2(0, 0);
     for (uint32_t base = 0; base < nr; base += 1024) {
         const uint32_t i = base + threadIdx.x;
-        const uint2 a = i < nr ? rangeagg[i] : make_uint2(0, 0);
+        const uint2 a = next;
+        // the next round's load overlaps this round's scan
+        next = i + 1024 < nr ? rangeagg[i + 1024] : make_uint2(0, 0);
         uint64_t vi = a.x, ti = a.y;
         for (int o = 1; o < 32; o <<= 1) {
             const uint64_t tv = __shfl_up_sync(FULL, vi, o), tt = __shfl_up_sync(FULL, ti, o);
@@ -141,22 +144,27 @@ __global__ void __launch_bounds__(1024) mc_range_scan(const uint2* rangeagg, uin
             s_wt[warp] = ti;
         }
         __syncthreads();
-        uint64_t bv = 0, bt = 0, av = 0, at = 0;
-        for (int w = 0; w < 32; ++w) {
-            if (w < warp) {
-                bv += s_wv[w];
-                bt += s_wt[w];
+        if (warp == 0) {  // inclusive scan of the 32 warp totals
+            uint64_t wv = s_wv[lane], wt = s_wt[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint64_t tv = __shfl_up_sync(FULL, wv, o), tt = __shfl_up_sync(FULL, wt, o);
+                if (lane >= o) {
+                    wv += tv;
+                    wt += tt;
+                }
             }
-            av += s_wv[w];
-            at += s_wt[w];
+            s_wv[lane] = wv;
+            s_wt[lane] = wt;
         }
+        __syncthreads();
+        const uint64_t bv = warp ? s_wv[warp - 1] : 0, bt = warp ? s_wt[warp - 1] : 0;
         const uint64_t ev = carry_v + bv + vi - a.x, et = carry_t + bt + ti - a.y;
         if (i < nr) {
             if (ev > 0xFFFFFFFFull || et > 0xFFFFFFFFull) atomicOr(err, DERR_CAPACITY);
             rangepre[i] = make_uint2((uint32_t)ev, (uint32_t)et);
         }
-        carry_v += av;
-        carry_t += at;
+        carry_v += s_wv[31];
+        carry_t += s_wt[31];
         __syncthreads();
     }
     if (threadIdx.x == 0) {

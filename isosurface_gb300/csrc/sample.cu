@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(256) sample_generic(ProgView pv, uint32_t nx, 
 // tile (the margin covers f32 rounding of both bounds and values), and min is
 // exact, so the field equals the full fold over all spheres bit for bit.
 constexpr int TZ = 16;
-constexpr int KEEP_REGS = 6;  // kept spheres held in registers (more: shared-memory loop)
+constexpr int KEEP_REGS = 4;  // kept spheres held in registers (more: shared-memory loop)
 
 struct SetArgs {
     const float* spheres;  // n x (cx, cy, cz, r)
@@ -62,16 +62,64 @@ struct SetArgs {
     uint64_t pitch;
     uint32_t* bits;
     uint32_t W;
+    // near-only mode: values are written only where |v| <= reach (a world
+    // distance at least one lattice step plus rounding slack); signs everywhere
+    bool near_only;
+    float reach;
 };
 
 __device__ __forceinline__ float world(float g, float s, float o, bool dom) { return dom ? g * s + o : g; }
 
+// Thresholds that decide a sample from its squared distance s to a sphere
+// (s = (dx*dx + dy*dy) + dz*dz in f32, as vector.rs's length computes it):
+//   T: the largest f32 s with sqrt_rn(s) <= r, so sqrt(s) - r <= 0, i.e. the
+//      sample is inside this sphere, exactly when s <= T (f32 subtraction of
+//      finite values keeps the sign of the exact difference);
+//   U: sqrt(s) - r <= reach implies s <= U (a rounded-up bound);
+//   L: s < L implies sqrt(s) - r < -reach (a rounded-down bound, -1 if none).
+// A sample whose value lies within reach of zero has some s <= U and no
+// s < L; only those samples need their exact value (see sphere_column).
+__device__ __forceinline__ float4 sphere_thresholds(float r, float reach) {
+    float T = -1.0f;
+    if (r >= 0.0f) {
+        T = r * r;
+        while (T > 0.0f && sqrtf(T) > r) T = nextafterf(T, 0.0f);
+        for (int i = 0; i < 16; ++i) {  // fl(r*r) is within a few ulps of the bound
+            const float up = nextafterf(T, 3.0e38f);
+            if (sqrtf(up) > r) break;
+            T = up;
+        }
+    }
+    const float hi = fmaxf(r + reach, 0.0f);
+    const float U = hi * hi * 1.0001f + 1e-30f;
+    const float lo = r - reach;
+    const float L = lo > 0.0f ? lo * lo * 0.9999f : -1.0f;
+    return make_float4(T, U, L, 0.0f);
+}
+
+// Exact values of `count` queued samples of row y (entry = N squared
+// distances + (z << 5 | x - x0)): the same fold as the inline path.
+template <int N>
+__device__ __forceinline__ void near_flush(const SetArgs& A, const float* queue, const float* cr, uint32_t y,
+                                           uint32_t x0, int lane, uint32_t count) {
+    if ((uint32_t)lane >= count) return;
+    const uint32_t e = reinterpret_cast<const uint32_t*>(queue + 32 * N)[lane];
+    float v = sqrtf(queue[lane]) - cr[0];
+#pragma unroll
+    for (int i = 1; i < N; ++i) v = fminf(v, sqrtf(queue[32 * i + lane]) - cr[i]);
+    A.field[((size_t)(e >> 5) * A.ny + y) * A.pitch + x0 + (e & 31u)] = v;
+}
+
 // One thread's z column with the N kept spheres in registers.  (dx*dx + dy*dy)
 // is shared by the whole column and is exactly len_sq's first partial sum.
+// Full mode: the exact value of every sample.  Near-only mode: the sign of
+// every sample from the thresholds, and the exact value (the same fold) only
+// where some sphere puts the sample within reach of the surface.
 template <int N>
-__device__ __forceinline__ void sphere_column(const SetArgs& A, const float4* keep, float px, float py, uint32_t x,
-                                              uint32_t y, uint32_t z0, uint32_t z1, bool valid, int lane) {
-    float dxy[N], cz[N], cr[N];
+__device__ __forceinline__ void sphere_column(const SetArgs& A, const float4* keep, const float4* thr, float px,
+                                              float py, uint32_t x, uint32_t y, uint32_t z0, uint32_t z1, bool valid,
+                                              int lane, uint32_t wx, float* queue) {
+    float dxy[N], cz[N], cr[N], T[N], U[N], L[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) {
         const float4 c = keep[i];
@@ -79,21 +127,111 @@ __device__ __forceinline__ void sphere_column(const SetArgs& A, const float4* ke
         dxy[i] = dx * dx + dy * dy;
         cz[i] = c.z;
         cr[i] = c.w;
+        if (A.near_only) {
+            const float4 t = thr[i];
+            T[i] = t.x;
+            U[i] = t.y;
+            L[i] = t.z;
+        }
     }
+    uint32_t qn = 0;  // queued near samples (warp-uniform)
 #pragma unroll 2
     for (uint32_t z = z0; z <= z1; ++z) {
         const float pz = world((float)z * A.inv, A.sz, A.oz, A.domain);
-        float dz = pz - cz[0];
-        float v = sqrtf(dxy[0] + dz * dz) - cr[0];
-#pragma unroll
-        for (int i = 1; i < N; ++i) {
-            dz = pz - cz[i];
-            v = fminf(v, sqrtf(dxy[i] + dz * dz) - cr[i]);
-        }
         const size_t row = (size_t)z * A.ny + y;
-        if (valid) A.field[row * A.pitch + x] = v;
-        const uint32_t b = __ballot_sync(0xFFFFFFFFu, valid && !(v > 0.0f));
-        if (lane == 0) A.bits[row * A.W + blockIdx.x] = b;
+        bool inside;
+        if (A.near_only) {
+            float sq[N];
+            bool in = false, hi = false, deep = false;
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+                const float dz = pz - cz[i];
+                sq[i] = dxy[i] + dz * dz;
+                in |= sq[i] <= T[i];
+                hi |= sq[i] <= U[i];
+                deep |= sq[i] < L[i];
+            }
+            inside = in;
+            const bool near = valid && hi && !deep;
+            if (!queue) {
+                if (near) {
+                    float v = sqrtf(sq[0]) - cr[0];
+#pragma unroll
+                    for (int i = 1; i < N; ++i) v = fminf(v, sqrtf(sq[i]) - cr[i]);
+                    A.field[row * A.pitch + x] = v;
+                }
+            } else {
+                // near samples queue up (squared distances + position); a full
+                // queue is evaluated by the whole warp, one entry per lane
+                const uint32_t m = __ballot_sync(FULL, near);
+                if (m) {
+                    const uint32_t cnt = __popc(m), pos = qn + __popc(m & ((1u << lane) - 1u));
+                    uint32_t* qpos = reinterpret_cast<uint32_t*>(queue + 32 * N);
+                    if (near && pos < 32) {
+#pragma unroll
+                        for (int i = 0; i < N; ++i) queue[32 * i + pos] = sq[i];
+                        qpos[pos] = (z << 5) | (uint32_t)lane;
+                    }
+                    if (qn + cnt >= 32) {
+                        __syncwarp();
+                        near_flush<N>(A, queue, cr, y, x - lane, lane, 32);
+                        __syncwarp();
+                        if (near && pos >= 32) {
+#pragma unroll
+                            for (int i = 0; i < N; ++i) queue[32 * i + pos - 32] = sq[i];
+                            qpos[pos - 32] = (z << 5) | (uint32_t)lane;
+                        }
+                        qn = qn + cnt - 32;
+                    } else {
+                        qn += cnt;
+                    }
+                }
+            }
+        } else {
+            float dz = pz - cz[0];
+            float v = sqrtf(dxy[0] + dz * dz) - cr[0];
+#pragma unroll
+            for (int i = 1; i < N; ++i) {
+                dz = pz - cz[i];
+                v = fminf(v, sqrtf(dxy[i] + dz * dz) - cr[i]);
+            }
+            if (valid) A.field[row * A.pitch + x] = v;
+            inside = !(v > 0.0f);
+        }
+        const uint32_t b = __ballot_sync(0xFFFFFFFFu, valid && inside);
+        if (lane == 0) A.bits[row * A.W + wx] = b;
+    }
+    if (queue && qn) {
+        __syncwarp();
+        near_flush<N>(A, queue, cr, y, x - lane, lane, qn);
+        __syncwarp();
+    }
+}
+
+// The samples of column (x, y), layers z0..z1, from the nk kept spheres;
+// sign words go to word wx of each row.
+__device__ __forceinline__ void sample_column(const SetArgs& A, const float4* keep, const float4* thr, uint32_t nk,
+                                              float px, float py, uint32_t x, uint32_t y, uint32_t z0, uint32_t z1,
+                                              bool valid, int lane, uint32_t wx, float* queue = nullptr) {
+    switch (nk) {
+    case 1: sphere_column<1>(A, keep, thr, px, py, x, y, z0, z1, valid, lane, wx, queue); return;
+    case 2: sphere_column<2>(A, keep, thr, px, py, x, y, z0, z1, valid, lane, wx, queue); return;
+    case 3: sphere_column<3>(A, keep, thr, px, py, x, y, z0, z1, valid, lane, wx, queue); return;
+    case 4: sphere_column<4>(A, keep, thr, px, py, x, y, z0, z1, valid, lane, wx, queue); return;
+    default: break;
+    }
+    for (uint32_t z = z0; z <= z1; ++z) {
+        const float pz = world((float)z * A.inv, A.sz, A.oz, A.domain);
+        float v = 0.0f;
+        for (uint32_t i = 0; i < nk; ++i) {
+            float4 c = keep[i];
+            float d = vlen(v3(px - c.x, py - c.y, pz - c.z)) - c.w;
+            v = (i == 0) ? d : fminf(v, d);
+        }
+        const uint64_t row = (uint64_t)z * A.ny + y;
+        if (valid) A.field[row * A.pitch + x] = v;  // near-only mode writes all values here: a superset
+        uint32_t b = __ballot_sync(FULL, valid && !(v > 0.0f));
+        if (lane == 0) A.bits[row * A.W + wx] = b;
     }
 }
 
@@ -130,6 +268,7 @@ __global__ void __launch_bounds__(256) sample_sphere_set(SetArgs A) {
     for (int i = 1; i < 8; ++i) U = fminf(U, s_red[i]);
     // stable compaction of the kept spheres
     uint32_t base = 0;
+    float lbl = 3.0e38f;  // lower bound of the field over the tile
     for (uint32_t r0 = 0; r0 < A.n; r0 += blockDim.x) {
         uint32_t i = r0 + threadIdx.x;
         bool keep = false;
@@ -142,6 +281,7 @@ __global__ void __launch_bounds__(256) sample_sphere_set(SetArgs A) {
             float near = sqrtf(dx * dx + dy * dy + dz * dz);
             float margin = 1e-4f + 1e-5f * (near + fabsf(c.w) + 4.0f);
             keep = near - c.w - margin <= U;
+            lbl = fminf(lbl, near - c.w - margin);
         }
         uint32_t m = __ballot_sync(FULL, keep);
         if (lane == 0) s_cnt[warp] = __popc(m);
@@ -151,41 +291,39 @@ __global__ void __launch_bounds__(256) sample_sphere_set(SetArgs A) {
             if (wv < warp) before += s_cnt[wv];
             total += s_cnt[wv];
         }
-        if (keep) s_keep[base + before + __popc(m & ((1u << lane) - 1u))] = c;
+        if (keep) {
+            const uint32_t at = base + before + __popc(m & ((1u << lane) - 1u));
+            s_keep[at] = c;
+            if (A.near_only) s_keep[A.n + at] = sphere_thresholds(c.w, A.reach);
+        }
         base += total;
         __syncthreads();
     }
     if (threadIdx.x == 0) s_nkeep = base;
+    for (int o = 16; o > 0; o >>= 1) lbl = fminf(lbl, __shfl_xor_sync(FULL, lbl, o));
+    if (lane == 0) s_red[warp] = lbl;  // s_red's first use ended at the loop's barriers
     __syncthreads();
     const uint32_t nk = s_nkeep;
+    if (A.near_only) {
+        // every sample v of the tile satisfies LB <= v <= U: a tile wholly
+        // beyond reach on one side needs sign words only
+        float LB = s_red[0];
+        for (int i = 1; i < 8; ++i) LB = fminf(LB, s_red[i]);
+        const bool far_out = LB > A.reach, deep_in = U < -A.reach;
+        if (far_out || deep_in) {
+            const uint32_t y = y0 + warp;
+            const uint32_t word = __ballot_sync(FULL, deep_in && x0 + lane < A.nx);
+            if (y < A.ny && lane <= z1 - z0) A.bits[((size_t)(z0 + lane) * A.ny + y) * A.W + blockIdx.x] = word;
+            return;
+        }
+    }
 
     const uint32_t x = x0 + lane, y = y0 + warp;
     if (y >= A.ny) return;
     const float px = world((float)x * A.inv, A.sx, A.ox, A.domain);
     const float py = world((float)y * A.inv, A.sy, A.oy, A.domain);
     const bool valid = x < A.nx;
-    switch (nk) {
-    case 1: sphere_column<1>(A, s_keep, px, py, x, y, z0, z1, valid, lane); return;
-    case 2: sphere_column<2>(A, s_keep, px, py, x, y, z0, z1, valid, lane); return;
-    case 3: sphere_column<3>(A, s_keep, px, py, x, y, z0, z1, valid, lane); return;
-    case 4: sphere_column<4>(A, s_keep, px, py, x, y, z0, z1, valid, lane); return;
-    case 5: sphere_column<5>(A, s_keep, px, py, x, y, z0, z1, valid, lane); return;
-    case 6: sphere_column<6>(A, s_keep, px, py, x, y, z0, z1, valid, lane); return;
-    default: break;
-    }
-    for (uint32_t z = z0; z <= z1; ++z) {
-        const float pz = world((float)z * A.inv, A.sz, A.oz, A.domain);
-        float v = 0.0f;
-        for (uint32_t i = 0; i < nk; ++i) {
-            float4 c = s_keep[i];
-            float d = vlen(v3(px - c.x, py - c.y, pz - c.z)) - c.w;
-            v = (i == 0) ? d : fminf(v, d);
-        }
-        const uint64_t row = (uint64_t)z * A.ny + y;
-        if (valid) A.field[row * A.pitch + x] = v;
-        uint32_t b = __ballot_sync(FULL, valid && !(v > 0.0f));
-        if (lane == 0) A.bits[row * A.W + blockIdx.x] = b;
-    }
+    sample_column(A, s_keep, s_keep + A.n, nk, px, py, x, y, z0, z1, valid, lane, blockIdx.x);
 }
 
 // Sign bits of a caller-supplied field (one warp per 32-point chunk of a row).
@@ -215,6 +353,178 @@ __global__ void sample_points(ProgView pv, const float* pts, uint64_t n, float* 
         normals[3 * i + 2] = nn.z;
     } else {
         vals[i] = eval_scalar(pv, p);
+    }
+}
+
+// Unions of at most WARP_SET_MAX spheres take two barrier-free kernels over
+// the same 32 x 8 x TZ tiles:
+//   set_tiles: one warp per tile computes the culling bounds with shuffles and
+//     writes a TileRec: the tile's class (mixed, or wholly beyond reach
+//     outside / inside, near-only mode) and the indices of the kept spheres
+//     (more than KEEP_MAX: all spheres);
+//   set_rows:  one warp per tile row (8 per block) reads its record; a
+//     uniform row writes its sign words, a mixed row stages its kept spheres
+//     (and thresholds) in shared memory and samples its 32 x TZ points.
+constexpr uint32_t WARP_SET_MAX = 256;
+constexpr uint32_t KEEP_MAX = 30;
+constexpr int TILE_WARPS = 4;
+
+struct TileRec {
+    uint16_t cls;  // 0 mixed, 1 far outside, 2 deep inside
+    uint16_t nk;   // kept spheres; > KEEP_MAX: use all
+    uint16_t idx[KEEP_MAX];
+};
+static_assert(sizeof(TileRec) == 64, "TileRec is one 64-byte record");
+
+struct TileBox {
+    uint32_t x0, y0, z0, x1, y1, z1;
+};
+
+__device__ __forceinline__ TileBox tile_box(const SetArgs& A, uint32_t wx, uint32_t ty, uint32_t tz) {
+    TileBox b;
+    b.x0 = wx * 32;
+    b.y0 = ty * 8;
+    b.z0 = tz * TZ;
+    b.x1 = min(b.x0 + 31, A.nx - 1);
+    b.y1 = min(b.y0 + 7, A.ny - 1);
+    b.z1 = min(b.z0 + TZ - 1, A.nz - 1);
+    return b;
+}
+
+__global__ void __launch_bounds__(32 * TILE_WARPS) set_tiles(SetArgs A, uint32_t tiles_y, uint32_t tiles_z,
+                                                            TileRec* recs, uint32_t* mixed, uint32_t* nmixed) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t t = (uint64_t)blockIdx.x * TILE_WARPS + (threadIdx.x >> 5);
+    if (t >= (uint64_t)A.W * tiles_y * tiles_z) return;
+    const uint32_t wx = (uint32_t)(t % A.W), rt = (uint32_t)(t / A.W);
+    const TileBox tb = tile_box(A, wx, rt % tiles_y, rt / tiles_y);
+    float ax = world((float)tb.x0 * A.inv, A.sx, A.ox, A.domain), bx = world((float)tb.x1 * A.inv, A.sx, A.ox, A.domain);
+    float ay = world((float)tb.y0 * A.inv, A.sy, A.oy, A.domain), by = world((float)tb.y1 * A.inv, A.sy, A.oy, A.domain);
+    float az = world((float)tb.z0 * A.inv, A.sz, A.oz, A.domain), bz = world((float)tb.z1 * A.inv, A.sz, A.oz, A.domain);
+    const float lox = fminf(ax, bx), hix = fmaxf(ax, bx), loy = fminf(ay, by), hiy = fmaxf(ay, by);
+    const float loz = fminf(az, bz), hiz = fmaxf(az, bz);
+    const float4* sp = reinterpret_cast<const float4*>(A.spheres);
+    // bounds of each sphere's value over the tile box (margins as in sample_sphere_set)
+    float U = 3.0e38f, LB = 3.0e38f, low[WARP_SET_MAX / 32];
+#pragma unroll
+    for (int k = 0; k < (int)(WARP_SET_MAX / 32); ++k) {
+        const uint32_t i = 32 * k + lane;
+        low[k] = 3.0e38f;
+        if (i < A.n) {
+            const float4 c = __ldg(sp + i);
+            const float fx = fmaxf(fabsf(c.x - lox), fabsf(c.x - hix));
+            const float fy = fmaxf(fabsf(c.y - loy), fabsf(c.y - hiy));
+            const float fz = fmaxf(fabsf(c.z - loz), fabsf(c.z - hiz));
+            const float far = sqrtf(fx * fx + fy * fy + fz * fz);
+            U = fminf(U, far - c.w + (1e-4f + 1e-5f * (far + fabsf(c.w))));
+            const float dx = fmaxf(fmaxf(lox - c.x, c.x - hix), 0.0f);
+            const float dy = fmaxf(fmaxf(loy - c.y, c.y - hiy), 0.0f);
+            const float dz = fmaxf(fmaxf(loz - c.z, c.z - hiz), 0.0f);
+            const float near = sqrtf(dx * dx + dy * dy + dz * dz);
+            low[k] = near - c.w - (1e-4f + 1e-5f * (near + fabsf(c.w) + 4.0f));
+            LB = fminf(LB, low[k]);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        U = fminf(U, __shfl_xor_sync(FULL, U, o));
+        LB = fminf(LB, __shfl_xor_sync(FULL, LB, o));
+    }
+    if (A.near_only && (LB > A.reach || U < -A.reach)) {
+        // wholly beyond reach on one side: the tile's sign words, and done
+        const uint32_t word = __ballot_sync(FULL, U < -A.reach && tb.x0 + lane < A.nx);
+        const uint32_t ny_t = tb.y1 - tb.y0 + 1, rows = ny_t * (tb.z1 - tb.z0 + 1);
+        for (uint32_t j = lane; j < rows; j += 32)
+            A.bits[((size_t)(tb.z0 + j / ny_t) * A.ny + tb.y0 + j % ny_t) * A.W + wx] = word;
+        return;
+    }
+    TileRec* rec = recs + t;
+    uint32_t nk = 0;
+#pragma unroll
+    for (int k = 0; k < (int)(WARP_SET_MAX / 32); ++k) {
+        if (32u * k >= A.n) break;
+        const bool keep = low[k] <= U;
+        const uint32_t m = __ballot_sync(FULL, keep);
+        const uint32_t at = nk + __popc(m & ((1u << lane) - 1u));
+        if (keep && at < KEEP_MAX) rec->idx[at] = (uint16_t)(32 * k + lane);
+        nk += __popc(m);
+    }
+    if (lane == 0) {
+        rec->cls = 0;
+        rec->nk = (uint16_t)min(nk, 0xFFFFu);
+        mixed[atomicAdd(nmixed, 1u)] = (uint32_t)t;
+    }
+}
+
+// thresholds of every sphere (they depend on r and the reach only)
+__global__ void set_thresholds(SetArgs A, float4* thr) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < A.n) thr[i] = sphere_thresholds(A.spheres[4 * i + 3], A.reach);
+}
+
+// persistent: warps stride over (mixed tile, row) items.  A row is first
+// bounded against the tile's kept spheres alone (they decide the minimum
+// everywhere in the tile): a row wholly beyond reach writes its sign words.
+__global__ void __launch_bounds__(256, 3) set_rows(SetArgs A, uint32_t tiles_y, const TileRec* recs,
+                                                   const uint32_t* mixed, const uint32_t* nmixed, const float4* thr_all) {
+    __shared__ float4 s_keep[8][KEEP_MAX];
+    __shared__ float4 s_thr[8][KEEP_MAX];
+    __shared__ float s_queue[8][32 * (KEEP_REGS + 1)];  // near-sample queue per warp
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const float4* sp = reinterpret_cast<const float4*>(A.spheres);
+    const uint32_t items = 8 * *nmixed;
+    for (uint32_t it = blockIdx.x * 8 + warp; it < items; it += gridDim.x * 8) {
+        const uint32_t t = mixed[it >> 3];
+        const uint32_t wx = t % A.W, rt = t / A.W;
+        const TileBox tb = tile_box(A, wx, rt % tiles_y, rt / tiles_y);
+        const uint32_t y = tb.y0 + (it & 7);
+        if (y > tb.y1) continue;
+        const TileRec* rec = recs + t;
+        const uint32_t nk = rec->nk;
+        const uint32_t x = tb.x0 + lane;
+        const bool valid = x < A.nx;
+        const float px = world((float)x * A.inv, A.sx, A.ox, A.domain);
+        const float py = world((float)y * A.inv, A.sy, A.oy, A.domain);
+        if (nk > KEEP_MAX) {  // the fold over every sphere: the same minimum
+            sample_column(A, sp, nullptr, A.n, px, py, x, y, tb.z0, tb.z1, valid, lane, wx);
+            continue;
+        }
+        __syncwarp();  // the previous item's reads of the staging slots are done
+        float up = 3.0e38f, lo = 3.0e38f;
+        if (lane < (int)nk) {
+            const uint32_t i = rec->idx[lane];
+            const float4 c = __ldg(sp + i);
+            s_keep[warp][lane] = c;
+            if (A.near_only) {
+                s_thr[warp][lane] = __ldg(thr_all + i);
+                // bounds of this sphere's value over the row box
+                const float ax = world((float)tb.x0 * A.inv, A.sx, A.ox, A.domain);
+                const float bx = world((float)tb.x1 * A.inv, A.sx, A.ox, A.domain);
+                const float az = world((float)tb.z0 * A.inv, A.sz, A.oz, A.domain);
+                const float bz = world((float)tb.z1 * A.inv, A.sz, A.oz, A.domain);
+                const float lox = fminf(ax, bx), hix = fmaxf(ax, bx), loz = fminf(az, bz), hiz = fmaxf(az, bz);
+                const float fx = fmaxf(fabsf(c.x - lox), fabsf(c.x - hix)), fy = fabsf(c.y - py);
+                const float fz = fmaxf(fabsf(c.z - loz), fabsf(c.z - hiz));
+                const float far = sqrtf(fx * fx + fy * fy + fz * fz);
+                up = far - c.w + (1e-4f + 1e-5f * (far + fabsf(c.w)));
+                const float dx = fmaxf(fmaxf(lox - c.x, c.x - hix), 0.0f);
+                const float dz = fmaxf(fmaxf(loz - c.z, c.z - hiz), 0.0f);
+                const float near = sqrtf(dx * dx + fy * fy + dz * dz);
+                lo = near - c.w - (1e-4f + 1e-5f * (near + fabsf(c.w) + 4.0f));
+            }
+        }
+        if (A.near_only) {
+            for (int o = 16; o > 0; o >>= 1) {
+                up = fminf(up, __shfl_xor_sync(FULL, up, o));
+                lo = fminf(lo, __shfl_xor_sync(FULL, lo, o));
+            }
+            if (lo > A.reach || up < -A.reach) {
+                const uint32_t word = __ballot_sync(FULL, up < -A.reach && valid);
+                if (lane <= (int)(tb.z1 - tb.z0)) A.bits[((size_t)(tb.z0 + lane) * A.ny + y) * A.W + wx] = word;
+                continue;
+            }
+        }
+        __syncwarp();
+        sample_column(A, s_keep[warp], s_thr[warp], nk, px, py, x, y, tb.z0, tb.z1, valid, lane, wx, s_queue[warp]);
     }
 }
 
@@ -265,9 +575,10 @@ iso_status attach_normals(iso_ctx* ctx, const iso_program* prog) {
 }
 
 iso_status launch_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t nx, uint32_t ny, uint32_t nz, float inv,
-                              float* field, uint64_t pitch, uint32_t* bits) {
+                              float* field, uint64_t pitch, uint32_t* bits, bool near_only) {
     const uint32_t W = words_per_row(nx);
     if (prog->kind == PK_SPHERE_SET_HARD && prog->set_n <= 8192) {
+        near_only = near_only && prog->set_n <= 4096 && nx > 1;
         SetArgs a;
         a.spheres = prog->d_set;
         a.n = prog->set_n;
@@ -276,14 +587,47 @@ iso_status launch_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t nx
         a.ox = prog->domain[3]; a.oy = prog->domain[4]; a.oz = prog->domain[5];
         a.nx = nx; a.ny = ny; a.nz = nz; a.inv = inv;
         a.field = field; a.pitch = pitch; a.bits = bits; a.W = W;
-        size_t smem = 16 * (size_t)prog->set_n;
+        a.near_only = near_only;
+        // a crossing edge joins samples one lattice step apart, and the field
+        // is 1-Lipschitz in world units: both ends lie within one step (the
+        // largest axis step after the domain map) of zero, plus rounding slack
+        const float step = inv * (prog->has_domain ? fmaxf(fabsf(a.sx), fmaxf(fabsf(a.sy), fabsf(a.sz))) : 1.0f);
+        a.reach = step * 1.001f + 1e-4f;
+        size_t smem = (near_only ? 32 : 16) * (size_t)prog->set_n;
         if (smem > 48 * 1024) {
             cudaError_t e = cudaFuncSetAttribute(sample_sphere_set, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return cuda_fail(ctx, e, "sphere-set smem attribute");
         }
-        dim3 grid(W, (ny + 7) / 8, (nz + TZ - 1) / TZ);
-        StageTimer timer(ctx, ISO_STAGE_SAMPLE);
-        sample_sphere_set<<<grid, 256, smem, ctx->stream>>>(a);
+        const uint32_t ty = (ny + 7) / 8, tz = (nz + TZ - 1) / TZ;
+        const uint64_t tiles = (uint64_t)W * ty * tz;
+        if (prog->set_n <= WARP_SET_MAX && tiles < (1ull << 31)) {
+            // records | mixed-tile list | its length | sphere thresholds
+            const size_t rec_bytes = sizeof(TileRec) * tiles, list_bytes = (4 * tiles + 255) & ~(size_t)255;
+            iso_status s = ensure(ctx, ctx->tiles, rec_bytes + list_bytes + 256 + 16 * (size_t)prog->set_n);
+            if (s != ISO_OK) return s;
+            TileRec* recs = (TileRec*)ctx->tiles.p;
+            uint32_t* mixed = (uint32_t*)((char*)ctx->tiles.p + rec_bytes);
+            uint32_t* nmixed = (uint32_t*)((char*)mixed + list_bytes);
+            float4* thr = (float4*)((char*)nmixed + 256);
+            cudaError_t e = cudaMemsetAsync(nmixed, 0, 4, ctx->stream);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "mixed-tile count");
+            int dev = 0, sms = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            StageTimer timer(ctx, ISO_STAGE_SAMPLE);
+            if (near_only) {
+                set_thresholds<<<(prog->set_n + 127) / 128, 128, 0, ctx->stream>>>(a, thr);
+                ctx->launches++;
+            }
+            set_tiles<<<(unsigned)((tiles + TILE_WARPS - 1) / TILE_WARPS), 32 * TILE_WARPS, 0, ctx->stream>>>(
+                a, ty, tz, recs, mixed, nmixed);
+            set_rows<<<(unsigned)sms * 3, 256, 0, ctx->stream>>>(a, ty, recs, mixed, nmixed, thr);
+            ctx->launches++;
+        } else {
+            dim3 grid(W, (ny + 7) / 8, (nz + TZ - 1) / TZ);
+            StageTimer timer(ctx, ISO_STAGE_SAMPLE);
+            sample_sphere_set<<<grid, 256, smem, ctx->stream>>>(a);
+        }
     } else {
         uint64_t warps = (uint64_t)W * ny * nz;
         StageTimer timer(ctx, ISO_STAGE_SAMPLE);

@@ -251,3 +251,18 @@ def test_point_cloud_reference_style_api(ctx):
     PointCloud(33, context=ctx).extract(Sampler(scenes.bench_torus()), OnlyVertices(v))
     want = oracle.Program(S.lower(scenes.bench_torus())).point_cloud(33)
     assert np.array_equal(np.asarray(v, np.float32), want.vertices.reshape(-1))
+
+
+@pytest.mark.parametrize("size", [33, 129])
+def test_sphere_union_near_only_values(ctx, size):
+    """MarchingCubes on a sphere union samples signs everywhere but exact
+    values only within one lattice step of the surface; fill the context's
+    field with another source's values first so a missing value cannot pass
+    by coincidence."""
+    for src in (scenes.sphere_union(), S.unit_to_cube(S.SphereSet(
+            np.array([[0.1, -0.2, 0.05, 0.5], [-0.3, 0.3, -0.1, 0.35], [0.35, 0.25, 0.3, 0.2]], np.float32)))):
+        ctx.mc_extract(scenes.bench_torus(), size)  # generic sampler: writes every value
+        got = ctx.download(ctx.mc_extract(src, size))
+        want = oracle.Program(S.lower(src)).marching_cubes(size)
+        assert np.array_equal(got.vertices, want.vertices)
+        assert np.array_equal(got.indices, want.indices)
