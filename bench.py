@@ -114,12 +114,12 @@ def cpu_baseline_port(src_bytes, budget_s=12.0, threads=1):
                       % (z0, z0 + layers, cells, secs)}
 
 
-def secondary_workloads(ctx, torch, steps):
+def secondary_workloads(ctx, torch, steps, only=None):
     """The other workloads, timed with CUDA events on the library's stream:
     the 4096-chunk batch (one CUDA graph vs one extraction per chunk),
-    DualContouring at 256^3 and LinearHashedMarchingCubes at depth 8."""
+    DualContouring at 256^3 and LinearHashedMarchingCubes at depth 8
+    (`only`: a set of names among batch, dc, lhmc to run just those)."""
     from isosurface_gb300 import scenes
-    from isosurface_gb300.api import Batch
     stream = torch.cuda.ExternalStream(ctx.stream)
 
     def timed(fn, reps):
@@ -131,6 +131,28 @@ def secondary_workloads(ctx, torch, steps):
         torch.cuda.synchronize()
         return min(a.elapsed_time(b) for a, b in ev)
 
+    out = {}
+    want = (lambda name: only is None or name in only)
+    if want("batch"):
+        out.update(_batch_workload(ctx, timed, steps))
+    src = scenes.csg()
+    if want("dc"):
+        for _ in range(2):
+            info = ctx.dc_extract(src, 257)
+        ms = timed(lambda: ctx.dc_extract(src, 257), max(steps, 3))
+        out["dc_256"] = {"cells": int(info.num_cells), "ms": ms, "cells_per_s": 256 * 256 * 257 / (ms / 1e3),
+                         "triangles": int(info.num_triangles), "placer": "MinimiseQEF"}
+    if want("lhmc"):
+        for _ in range(2):
+            info = ctx.lhmc_extract(src, 8)
+        ms = timed(lambda: ctx.lhmc_extract(src, 8), max(steps, 3))
+        out["lhmc_depth8"] = {"dual_cubes": int(info.num_cells), "ms": ms, "triangles": int(info.num_triangles)}
+    return out
+
+
+def _batch_workload(ctx, timed, steps):
+    from isosurface_gb300 import scenes
+    from isosurface_gb300.api import Batch
     out = {}
     chunks = scenes.chunks(seed=7, count=4096)
     batch = Batch(ctx, chunks)
@@ -146,16 +168,6 @@ def secondary_workloads(ctx, torch, steps):
                                 "speedup": per_ms / graph_ms, "cells_per_s": cells / (graph_ms / 1e3),
                                 "triangles": int(info.num_triangles), "slab_depth_by_size": chosen}
     batch.close()
-    src = scenes.csg()
-    for _ in range(2):
-        info = ctx.dc_extract(src, 257)
-    ms = timed(lambda: ctx.dc_extract(src, 257), max(steps, 3))
-    out["dc_256"] = {"cells": int(info.num_cells), "ms": ms, "cells_per_s": 256 * 256 * 257 / (ms / 1e3),
-                     "triangles": int(info.num_triangles), "placer": "MinimiseQEF"}
-    for _ in range(2):
-        info = ctx.lhmc_extract(src, 8)
-    ms = timed(lambda: ctx.lhmc_extract(src, 8), max(steps, 3))
-    out["lhmc_depth8"] = {"dual_cubes": int(info.num_cells), "ms": ms, "triangles": int(info.num_triangles)}
     return out
 
 
@@ -284,6 +296,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true", help="skip the batch / DC / LHMC timings")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-surrogate workload")
+    ap.add_argument("--secondary-only", default=None,
+                    help="comma list among batch,dc,lhmc,surrogate: run only these secondary workloads")
     ap.add_argument("--surrogate-train-steps", type=int, default=4000)
     args = ap.parse_args()
     if args.warmup < 3:
@@ -419,8 +433,9 @@ def main():
 
     secondary = None
     if not args.no_secondary:
-        secondary = secondary_workloads(ctx, torch, args.steps)
-        if not args.no_surrogate:
+        only = set(args.secondary_only.split(",")) if args.secondary_only else None
+        secondary = secondary_workloads(ctx, torch, args.steps, only)
+        if not args.no_surrogate and (only is None or "surrogate" in only):
             secondary["surrogate_512"] = surrogate_workload(ctx, torch, args.surrogate_train_steps)
 
     cpu = None

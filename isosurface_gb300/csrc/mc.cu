@@ -27,6 +27,8 @@
 //   are bit-identical.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include <algorithm>
 #include <cstring>
 #include <mutex>
@@ -555,6 +557,31 @@ iso_status mc_cases_lattice(iso_ctx* ctx, const Lattice& L, uint8_t* d_cases) {
     return check_launch(ctx, "mc_cases");
 }
 
+namespace {
+__global__ void write_grid(Grid* dst, Grid g) { *dst = g; }
+
+// cudaFuncSetAttribute only when the size grows (per device; it costs a host round trip)
+cudaError_t emit_smem_attribute(size_t smem) {
+    static std::atomic<size_t> set_to[64];  // largest value set so far, per device
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const bool cached = dev >= 0 && dev < 64;
+    if (cached && smem <= set_to[dev].load(std::memory_order_relaxed)) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(mc_block_emit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess && cached) {
+        size_t cur = set_to[dev].load(std::memory_order_relaxed);
+        while (cur < smem && !set_to[dev].compare_exchange_weak(cur, smem)) {
+        }
+    }
+    return e;
+}
+}  // namespace
+
+// One synchronisation per extraction: count, scan and emit are queued back to
+// back, the emit writing into the context's mesh buffers as sized by earlier
+// extractions (its writes are capacity-checked); the totals come back with
+// the final synchronisation, and an emit that ran out of room is repeated
+// into buffers of the exact size.
 iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, iso_mesh_info* info) {
     ctx->last = iso_mesh_info{};
     ctx->last_flags = flags;
@@ -568,17 +595,24 @@ iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, is
     const uint64_t chunks = (uint64_t)CW * (L.ny - 1) * (L.nz - 1);
     if (chunks >= 0xFFFFFFF0ull) return fail(ctx, ISO_ERR_TOO_LARGE, "grid too large");
     const uint32_t nranges = (uint32_t)((chunks + RANGE - 1) / RANGE);
+    const size_t smem = block_emit_smem(CW);
+    if (smem > 220 * 1024) return fail(ctx, ISO_ERR_INVALID_ARG, "rows too long for the emit pass");
     iso_status s;
     if ((s = ensure(ctx, ctx->rowtri, 8 * (chunks + 1))) != ISO_OK) return s;
     if ((s = ensure(ctx, ctx->scan, 16 * (size_t)nranges + 64 + sizeof(Grid) + 256)) != ISO_OK) return s;
+    const bool keys = (flags & ISO_FLAG_KEYS) != 0;
+    // a first extraction starts from a modest guess; later ones reuse what grew
+    if ((s = ensure(ctx, ctx->mesh_v, 12 * (size_t)65536)) != ISO_OK) return s;
+    if ((s = ensure(ctx, ctx->mesh_i, 12 * (size_t)131072)) != ISO_OK) return s;
+    if (keys && (s = ensure(ctx, ctx->mesh_k, 16 * (size_t)65536)) != ISO_OK) return s;
     uint2* local = (uint2*)ctx->rowtri.p;
     uint2* rangeagg = (uint2*)ctx->scan.p;
     uint2* rangepre = rangeagg + nranges;
     uint64_t* totals = (uint64_t*)(rangepre + nranges + 2);
     Grid* d_grid = (Grid*)(((uintptr_t)(totals + 4) + 255) & ~(uintptr_t)255);
-    const Grid grid = make_grid(L, 0);
-    cudaError_t e0 = cudaMemcpyAsync(d_grid, &grid, sizeof(Grid), cudaMemcpyHostToDevice, ctx->stream);
-    if (e0 != cudaSuccess) return cuda_fail(ctx, e0, "upload grid");
+    cudaError_t e = emit_smem_attribute(smem);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "emit smem attribute");
+    write_grid<<<1, 1, 0, ctx->stream>>>(d_grid, make_grid(L, 0));
     ChunkCountArgs ca{d_grid, nullptr, (uint32_t)chunks, local, rangeagg};
     {
         StageTimer timer(ctx, ISO_STAGE_CLASSIFY);
@@ -586,40 +620,46 @@ iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, is
         mc_range_scan<<<1, 1024, 0, ctx->stream>>>(rangeagg, nranges, rangepre, totals, local, (uint32_t)chunks,
                                                    ctx->d_err);
     }
-    ctx->launches += 2;
+    ctx->launches += 3;
     if ((s = check_launch(ctx, "mc_chunk_count")) != ISO_OK) return s;
-    cudaError_t e = cudaMemcpyAsync(ctx->h_pinned, totals, 16, cudaMemcpyDeviceToHost, ctx->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_pinned + 2, ctx->d_err, 4, cudaMemcpyDeviceToHost, ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "read totals");
-    e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "sync after count");
-    if ((uint32_t)ctx->h_pinned[2] && (s = read_device_errors(ctx)) != ISO_OK) return s;
-    const uint64_t nt = ctx->h_pinned[0], nv = ctx->h_pinned[1];
-    if (nv >= (1ull << 31) || nt >= (1ull << 31))
-        return fail(ctx, ISO_ERR_TOO_LARGE, "mesh exceeds 2^31 vertices or triangles");
-    const bool keys = (flags & ISO_FLAG_KEYS) != 0;
-    if ((s = ensure(ctx, ctx->mesh_v, 12 * std::max<uint64_t>(nv, 1))) != ISO_OK) return s;
-    if ((s = ensure(ctx, ctx->mesh_i, 12 * std::max<uint64_t>(nt, 1))) != ISO_OK) return s;
-    if (keys && (s = ensure(ctx, ctx->mesh_k, 16 * std::max<uint64_t>(nv, 1))) != ISO_OK) return s;
-    if (nt > 0) {
+    auto emit = [&]() -> iso_status {
+        uint64_t cap_v = ctx->mesh_v.bytes / 12, cap_t = ctx->mesh_i.bytes / 12;
+        if (keys) cap_v = std::min<uint64_t>(cap_v, ctx->mesh_k.bytes / 16);
         ChunkEmitArgs ea{d_grid, nullptr, (uint32_t)chunks, local, rangepre, (float*)ctx->mesh_v.p,
-                         (uint32_t*)ctx->mesh_i.p, keys ? (uint64_t*)ctx->mesh_k.p : nullptr, nv, nt, ctx->d_err};
-        const size_t smem = block_emit_smem(CW);
-        if (smem > 220 * 1024) return fail(ctx, ISO_ERR_INVALID_ARG, "rows too long for the emit pass");
-        e = cudaFuncSetAttribute(mc_block_emit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return cuda_fail(ctx, e, "emit smem attribute");
+                         (uint32_t*)ctx->mesh_i.p, keys ? (uint64_t*)ctx->mesh_k.p : nullptr, cap_v, cap_t,
+                         ctx->d_err};
         {
             StageTimer timer(ctx, ISO_STAGE_EMIT);
             mc_block_emit<<<(unsigned)((chunks + 255) / 256), 256, smem, ctx->stream>>>(ea, CW);
         }
         ctx->launches++;
-        if ((s = check_launch(ctx, "mc_block_emit")) != ISO_OK) return s;
-        e = cudaMemcpyAsync(ctx->h_pinned + 2, ctx->d_err, 4, cudaMemcpyDeviceToHost, ctx->stream);
-        if (e != cudaSuccess) return cuda_fail(ctx, e, "read error flags");
+        iso_status st = check_launch(ctx, "mc_block_emit");
+        if (st != ISO_OK) return st;
+        cudaError_t ce = cudaMemcpyAsync(ctx->h_pinned, totals, 16, cudaMemcpyDeviceToHost, ctx->stream);
+        if (ce == cudaSuccess) ce = cudaMemcpyAsync(ctx->h_pinned + 2, ctx->d_err, 4, cudaMemcpyDeviceToHost, ctx->stream);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+        return ce == cudaSuccess ? ISO_OK : cuda_fail(ctx, ce, "sync after emit");
+    };
+    if ((s = emit()) != ISO_OK) return s;
+    uint64_t nt = ctx->h_pinned[0], nv = ctx->h_pinned[1];
+    uint32_t err = (uint32_t)ctx->h_pinned[2];
+    if (nv >= (1ull << 31) || nt >= (1ull << 31)) {
+        cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream);
+        return fail(ctx, ISO_ERR_TOO_LARGE, "mesh exceeds 2^31 vertices or triangles");
     }
-    e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "sync after emit");
-    if ((uint32_t)ctx->h_pinned[2] && (s = read_device_errors(ctx)) != ISO_OK) return s;
+    if (err & ~(uint32_t)DERR_CAPACITY) return read_device_errors(ctx);
+    const bool grow = nv > ctx->mesh_v.bytes / 12 || nt > ctx->mesh_i.bytes / 12 ||
+                      (keys && nv > ctx->mesh_k.bytes / 16);
+    if (err || grow) {
+        // out of room (the counts are exact): again into buffers of that size
+        e = cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "clear error flags");
+        if ((s = ensure(ctx, ctx->mesh_v, 12 * std::max<uint64_t>(nv, 1))) != ISO_OK) return s;
+        if ((s = ensure(ctx, ctx->mesh_i, 12 * std::max<uint64_t>(nt, 1))) != ISO_OK) return s;
+        if (keys && (s = ensure(ctx, ctx->mesh_k, 16 * std::max<uint64_t>(nv, 1))) != ISO_OK) return s;
+        if ((s = emit()) != ISO_OK) return s;
+        if ((uint32_t)ctx->h_pinned[2] && (s = read_device_errors(ctx)) != ISO_OK) return s;
+    }
     ctx->last.num_vertices = nv;
     ctx->last.num_triangles = nt;
     ctx->last.num_cells = (uint64_t)(L.nx - 1) * (L.ny - 1) * (L.nz - 1);
@@ -677,7 +717,7 @@ iso_status mc_extract_grids(iso_ctx* ctx, const void* d_grids, uint32_t ngrids, 
         out_i = (uint32_t*)ctx->mesh_i.p;
     }
     const size_t smem = block_emit_smem(max_cw);
-    cudaError_t e = cudaFuncSetAttribute(mc_block_emit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = emit_smem_attribute(smem);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "emit smem attribute");
     ChunkEmitArgs ea{grids, d_range_grid, chunks, local, rangepre, out_v, out_i, nullptr, cap_v, cap_t, ctx->d_err};
     {
