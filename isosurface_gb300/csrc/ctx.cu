@@ -258,7 +258,7 @@ iso_status iso_ctx_destroy(iso_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     DevBuf* bufs[] = {&ctx->field, &ctx->bits, &ctx->rowtri, &ctx->rowvert, &ctx->scan, &ctx->aux,
-                      &ctx->aux2, &ctx->aux3, &ctx->tiles, &ctx->mesh_v, &ctx->mesh_i, &ctx->mesh_k};
+                      &ctx->aux2, &ctx->aux3, &ctx->tiles, &ctx->edges, &ctx->mesh_v, &ctx->mesh_i, &ctx->mesh_k};
     for (DevBuf* b : bufs)
         if (b->p) cudaFree(b->p);
     if (ctx->d_err) cudaFree(ctx->d_err);

@@ -47,7 +47,7 @@ struct iso_ctx {
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     // work buffers (grow-only, reused across calls)
-    iso::DevBuf field, bits, rowtri, rowvert, scan, aux, aux2, aux3, tiles;
+    iso::DevBuf field, bits, rowtri, rowvert, scan, aux, aux2, aux3, tiles, edges;
     // last mesh
     iso::DevBuf mesh_v, mesh_i, mesh_k;
     iso_mesh_info last{};

@@ -56,6 +56,11 @@ __device__ __constant__ uint8_t c_edge_axis[12] = {0, 1, 0, 1, 0, 1, 0, 1, 2, 2,
 // Local edge by axis and the lower endpoint's two off-axis offsets (d1 + 2*d2):
 // x: (dy, dz), y: (dx, dz), z: (dx, dy).
 __device__ __constant__ uint8_t c_local_edge[3][4] = {{0, 2, 4, 6}, {3, 1, 7, 5}, {8, 9, 11, 10}};
+// the same two tables in global memory, for lanes that index them divergently
+// (constant memory serialises distinct addresses within a warp)
+static __device__ const uint8_t g_edge_lo[12][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 0}, {0, 0, 1}, {1, 0, 1},
+                                                    {0, 1, 1}, {0, 0, 1}, {0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}};
+static __device__ const uint8_t g_edge_axis[12] = {0, 1, 0, 1, 0, 1, 0, 1, 2, 2, 2, 2};
 
 // Owned-edge masks by boundary class (x==0) | (y==0)<<1 | (z==0)<<2.  An edge
 // whose lower endpoint sits at offset d on an off-axis is owned by the cell
@@ -560,6 +565,12 @@ iso_status mc_cases_lattice(iso_ctx* ctx, const Lattice& L, uint8_t* d_cases) {
 namespace {
 __global__ void write_grid(Grid* dst, Grid g) { *dst = g; }
 
+// persistent grid for mc_cell_emit: a few blocks of 8 warps per SM, each warp
+// taking whole ranges
+unsigned emit_blocks(uint32_t nranges) {
+    return (unsigned)std::max<uint64_t>(1, nranges);  // 8 warps = one range of 256 chunks per block
+}
+
 // cudaFuncSetAttribute only when the size grows (per device; it costs a host round trip)
 cudaError_t emit_smem_attribute(size_t smem) {
     static std::atomic<size_t> set_to[64];  // largest value set so far, per device
@@ -616,24 +627,36 @@ iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, is
     ChunkCountArgs ca{d_grid, nullptr, (uint32_t)chunks, local, rangeagg};
     {
         StageTimer timer(ctx, ISO_STAGE_CLASSIFY);
-        mc_chunk_count<<<(nranges + 7) / 8, 256, 0, ctx->stream>>>(ca);
+        mc_chunk_count<<<nranges, 256, 0, ctx->stream>>>(ca);
         mc_range_scan<<<1, 1024, 0, ctx->stream>>>(rangeagg, nranges, rangepre, totals, local, (uint32_t)chunks,
                                                    ctx->d_err);
     }
     ctx->launches += 3;
     if ((s = check_launch(ctx, "mc_chunk_count")) != ISO_OK) return s;
+    // the dense edge -> vertex map (4 B per lattice edge) when the edge
+    // indices fit 32 bits; otherwise the block emit resolves owners itself
+    const uint64_t nedges = 3ull * L.nx * L.ny * L.nz;
+    const bool edge_map = nedges < (1ull << 32) && L.positions == nullptr;
+    if (edge_map && (s = ensure(ctx, ctx->edges, 4 * nedges)) != ISO_OK) return s;
     auto emit = [&]() -> iso_status {
         uint64_t cap_v = ctx->mesh_v.bytes / 12, cap_t = ctx->mesh_i.bytes / 12;
         if (keys) cap_v = std::min<uint64_t>(cap_v, ctx->mesh_k.bytes / 16);
         ChunkEmitArgs ea{d_grid, nullptr, (uint32_t)chunks, local, rangepre, (float*)ctx->mesh_v.p,
                          (uint32_t*)ctx->mesh_i.p, keys ? (uint64_t*)ctx->mesh_k.p : nullptr, cap_v, cap_t,
-                         ctx->d_err};
+                         ctx->d_err, (uint32_t*)ctx->edges.p};
         {
             StageTimer timer(ctx, ISO_STAGE_EMIT);
-            mc_block_emit<<<(unsigned)((chunks + 255) / 256), 256, smem, ctx->stream>>>(ea, CW);
+            if (edge_map) {
+                mc_cell_emit<<<emit_blocks(nranges), 256, 0, ctx->stream>>>(ea, nranges);
+                mc_resolve_ids<<<std::min<unsigned>(emit_blocks(nranges), 4096), 256, 0, ctx->stream>>>(
+                    (uint32_t*)ctx->mesh_i.p, totals, cap_t, (const uint32_t*)ctx->edges.p, (uint32_t)nedges);
+                ctx->launches++;
+            } else {
+                mc_block_emit<<<(unsigned)((chunks + 255) / 256), 256, smem, ctx->stream>>>(ea, CW);
+            }
         }
         ctx->launches++;
-        iso_status st = check_launch(ctx, "mc_block_emit");
+        iso_status st = check_launch(ctx, "mc emit");
         if (st != ISO_OK) return st;
         cudaError_t ce = cudaMemcpyAsync(ctx->h_pinned, totals, 16, cudaMemcpyDeviceToHost, ctx->stream);
         if (ce == cudaSuccess) ce = cudaMemcpyAsync(ctx->h_pinned + 2, ctx->d_err, 4, cudaMemcpyDeviceToHost, ctx->stream);
@@ -698,7 +721,7 @@ iso_status mc_extract_grids(iso_ctx* ctx, const void* d_grids, uint32_t ngrids, 
     ChunkCountArgs ca{grids, d_range_grid, chunks, local, rangeagg};
     {
         StageTimer timer(ctx, ISO_STAGE_CLASSIFY);
-        mc_chunk_count<<<(nranges + 1 + 7) / 8, 256, 0, ctx->stream>>>(ca);
+        mc_chunk_count<<<nranges + 1, 256, 0, ctx->stream>>>(ca);
         mc_range_scan<<<1, 1024, 0, ctx->stream>>>(rangeagg, nranges, rangepre, totals, local, chunks, ctx->d_err);
     }
     ctx->launches += 2;
@@ -719,7 +742,8 @@ iso_status mc_extract_grids(iso_ctx* ctx, const void* d_grids, uint32_t ngrids, 
     const size_t smem = block_emit_smem(max_cw);
     cudaError_t e = emit_smem_attribute(smem);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "emit smem attribute");
-    ChunkEmitArgs ea{grids, d_range_grid, chunks, local, rangepre, out_v, out_i, nullptr, cap_v, cap_t, ctx->d_err};
+    ChunkEmitArgs ea{grids, d_range_grid, chunks, local, rangepre, out_v, out_i, nullptr, cap_v, cap_t, ctx->d_err,
+                     nullptr};
     {
         StageTimer timer(ctx, ISO_STAGE_EMIT);
         mc_block_emit<<<nranges, 256, smem, ctx->stream>>>(ea, max_cw);

@@ -75,46 +75,59 @@ struct ChunkCountArgs {
     uint2* rangeagg;   // per range: (vertices, triangles)
 };
 
-// Pass 1: per-chunk counts, in-range prefixes (one warp per range, no barriers).
+// Pass 1: per-chunk counts and in-range prefixes.  One block per range of
+// 256 chunks, one warp per 32 of them (a single round each); the block scans
+// its eight warps' totals.
 __global__ void __launch_bounds__(256) mc_chunk_count(ChunkCountArgs A) {
     __shared__ uint8_t s_ntri[256];
     __shared__ uint16_t s_owned[8];
-    const int lane = threadIdx.x & 31;
+    __shared__ uint32_t s_segt[8], s_segv[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     s_ntri[threadIdx.x] = iso_tri_count[threadIdx.x];
     if (threadIdx.x < 8) s_owned[threadIdx.x] = iso_owned_mask[threadIdx.x];
+    const uint32_t range = blockIdx.x;
+    if (range * RANGE > A.chunks) return;  // block-uniform
     __syncthreads();
-    const uint32_t range = blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (range * RANGE > A.chunks) return;  // warp-uniform
     const Grid g = A.grids[grid_of_range(A.range_grid, min(range, A.chunks / RANGE - (A.chunks % RANGE == 0)))];
     const uint32_t ncx = g.nx - 1;
-    uint32_t agg_t = 0, agg_v = 0;
-    for (int r = 0; r < RANGE_ROUNDS; ++r) {
-        const uint32_t ch = range * RANGE + r * 32 + lane;
-        const uint32_t lc = ch - g.chunk0;
-        uint32_t t = 0, v = 0;
-        if (ch < A.chunks && lc < g.nchunks) {
-            const uint32_t row = fdiv(lc, g.div_cw);
-            const uint32_t c = lc - row * g.CW;
-            const uint32_t z = fdiv(row, g.div_ncy);
-            const uint32_t y = row - z * (g.ny - 1);
-            const Corners q = load_corners(g.bits, g.W, g.ny, y, z, c);
-            uint32_t act = active_cells(q, chunk_valid(c, ncx));
-            if (act) {
-                const int cls = (y == 0 ? 2 : 0) | (z == 0 ? 4 : 0);
-                v = owned_count(q, act, s_owned[cls], s_owned[cls | 1], c == 0 ? 1u : 0u);
-                while (act) {
-                    const uint32_t i = __ffs(act) - 1;
-                    act &= act - 1;
-                    t += s_ntri[case_at(q, i)];
-                }
+    const uint32_t ch = range * RANGE + warp * 32 + lane;
+    const uint32_t lc = ch - g.chunk0;
+    uint32_t t = 0, v = 0;
+    if (ch < A.chunks && lc < g.nchunks) {
+        const uint32_t row = fdiv(lc, g.div_cw);
+        const uint32_t c = lc - row * g.CW;
+        const uint32_t z = fdiv(row, g.div_ncy);
+        const uint32_t y = row - z * (g.ny - 1);
+        const Corners q = load_corners(g.bits, g.W, g.ny, y, z, c);
+        uint32_t act = active_cells(q, chunk_valid(c, ncx));
+        if (act) {
+            const int cls = (y == 0 ? 2 : 0) | (z == 0 ? 4 : 0);
+            v = owned_count(q, act, s_owned[cls], s_owned[cls | 1], c == 0 ? 1u : 0u);
+            while (act) {
+                const uint32_t i = __ffs(act) - 1;
+                act &= act - 1;
+                t += s_ntri[case_at(q, i)];
             }
         }
-        const uint32_t ti = warp_incl_scan(t, lane), vi = warp_incl_scan(v, lane);
-        if (ch <= A.chunks) A.local[ch] = make_uint2(agg_v + vi - v, agg_t + ti - t);
-        agg_t += __shfl_sync(FULL, ti, 31);
-        agg_v += __shfl_sync(FULL, vi, 31);
     }
-    if (lane == 0 && range * RANGE < A.chunks) A.rangeagg[range] = make_uint2(agg_v, agg_t);
+    const uint32_t ti = warp_incl_scan(t, lane), vi = warp_incl_scan(v, lane);
+    if (lane == 31) {
+        s_segt[warp] = ti;
+        s_segv[warp] = vi;
+    }
+    __syncthreads();
+    uint32_t pt = 0, pv = 0, at = 0, av = 0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) {
+        if (w < warp) {
+            pt += s_segt[w];
+            pv += s_segv[w];
+        }
+        at += s_segt[w];
+        av += s_segv[w];
+    }
+    if (ch <= A.chunks) A.local[ch] = make_uint2(pv + vi - v, pt + ti - t);
+    if (threadIdx.x == 0 && range * RANGE < A.chunks) A.rangeagg[range] = make_uint2(av, at);
 }
 
 // Exclusive scan of the range totals (one block).  rangepre[nr] and totals
@@ -186,6 +199,7 @@ struct ChunkEmitArgs {
     uint64_t* out_k;
     uint64_t cap_v, cap_t;
     uint32_t* err;
+    uint32_t* edge_id;  // mc_cell_emit: vertex id per lattice edge, (lattice point * 3 + axis)
 };
 
 __device__ __forceinline__ uint2 chunk_base(const ChunkEmitArgs& A, uint32_t ch) {
@@ -436,6 +450,158 @@ __global__ void __launch_bounds__(256) mc_block_emit(ChunkEmitArgs A, uint32_t m
         }
         vcarry += vtot;
         tcarry += ttot;
+    }
+}
+
+// Pass 2, cell-parallel.  Persistent blocks of 8 warps copy the tables to
+// shared memory once; each warp then takes whole ranges of 256 chunks, 32
+// chunks per round (lane = chunk).  The round's active cells are handed out
+// 32 at a time in chunk order (lane = cell: the owning chunk by a shuffle
+// search over the chunks' exclusive counts, the bit by __fns), so lanes stay
+// busy however the active cells are spread.  A cell's own output offsets are
+// the range's base plus a running warp scan of owned-vertex and triangle
+// counts in cell order (the reference's emission order).  Every owned vertex
+// also records its id in a dense per-lattice-edge map, and triangles are
+// written as lattice edge indices; mc_resolve_ids then replaces each index by
+// the id its owner recorded (no owner lookup in this pass; the map needs no
+// initialisation: every crossing edge has an owner, and only crossing edges
+// are referenced).
+__global__ void __launch_bounds__(256) mc_cell_emit(ChunkEmitArgs A, uint32_t nranges) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t seg = blockIdx.x * 8 + (threadIdx.x >> 5);  // 32 chunks per warp
+    const uint32_t range = seg / (RANGE / 32);
+    if (range >= nranges) return;
+    const Grid g = A.grids[grid_of_range(A.range_grid, range)];
+    const uint32_t gs0 = seg * 32;
+    if (gs0 - g.chunk0 >= g.nchunks) return;  // padding
+    const uint32_t rc = gs0 - g.chunk0, c_end = min(rc + 32, g.nchunks);
+    const uint2 bb = chunk_base(A, gs0);
+    if (chunk_base(A, g.chunk0 + c_end).y == bb.y) return;  // no triangle in these chunks
+    const uint32_t CW = g.CW, ncx = g.nx - 1, ncy = g.ny - 1;
+    const uint32_t grid_v0 = chunk_base(A, g.chunk0).x;
+    const bool explicit_pos = g.positions != nullptr;
+    uint32_t vcarry = bb.x, tcarry = bb.y;  // global offsets of the next cell's outputs
+    {
+        {
+            // lane = chunk: corner bit-vectors and active cells
+            const uint32_t ch = rc + lane;
+            Corners q;
+            uint32_t act = 0;
+            if (ch < c_end) {
+                const uint32_t row = fdiv(ch, g.div_cw);
+                const uint32_t c = ch - row * CW;
+                const uint32_t z = fdiv(row, g.div_ncy);
+                q = load_corners(g.bits, g.W, g.ny, row - z * ncy, z, c);
+                act = active_cells(q, chunk_valid(c, ncx));
+            } else {
+#pragma unroll
+                for (int k = 0; k < 8; ++k) q.k[k] = 0;
+            }
+            const uint32_t n = __popc(act);
+            const uint32_t incl = warp_incl_scan(n, lane), excl = incl - n;
+            const uint32_t total = __shfl_sync(FULL, incl, 31);
+            for (uint32_t b0 = 0; b0 < total; b0 += 32) {
+                // lane = cell number b0 + lane of these chunks, in chunk order
+                const uint32_t kk = b0 + lane;
+                const bool have = kk < total;
+                uint32_t src = 0;
+#pragma unroll
+                for (uint32_t step = 16; step > 0; step >>= 1) {
+                    const uint32_t cand = src + step;
+                    const uint32_t e = __shfl_sync(FULL, excl, cand & 31);
+                    if (cand < 32 && e <= kk) src = cand;
+                }
+                const uint32_t sact = __shfl_sync(FULL, act, src);
+                const uint32_t sexcl = __shfl_sync(FULL, excl, src);
+                Corners cq;
+#pragma unroll
+                for (int k = 0; k < 8; ++k) cq.k[k] = __shfl_sync(FULL, q.k[k], src);
+                uint32_t x = 0, y = 0, z = 0, cs = 0, nown = 0, nt = 0;
+                int cls = 0;
+                if (have) {
+                    const uint32_t i = __fns(sact, 0, (int)(kk - sexcl) + 1);
+                    const uint32_t cch = rc + src;
+                    const uint32_t row = fdiv(cch, g.div_cw);
+                    z = fdiv(row, g.div_ncy);
+                    y = row - z * ncy;
+                    x = 32 * (cch - row * CW) + i;
+                    cs = case_at(cq, i);
+                    cls = (x == 0 ? 1 : 0) | (y == 0 ? 2 : 0) | (z == 0 ? 4 : 0);
+                    nown = __popc((uint32_t)__ldg(&iso_edge_mask[cs]) & __ldg(&iso_owned_mask[cls]));
+                    nt = __ldg(&iso_tri_count[cs]);
+                }
+                const uint32_t vi = warp_incl_scan(nown, lane), ti = warp_incl_scan(nt, lane);
+                const uint32_t vstart = vcarry + vi - nown, tstart = tcarry + ti - nt;
+                vcarry += __shfl_sync(FULL, vi, 31);
+                tcarry += __shfl_sync(FULL, ti, 31);
+                if (!have) continue;
+                const uint32_t own = __ldg(&iso_owned_mask[cls]);
+                const uint64_t ord = __ldg(&iso_edge_order[cs]);
+                const uint32_t ne = __ldg(&iso_edge_count[cs]);
+                uint32_t ids[12];  // lattice edge index by first-use rank
+                uint32_t r = 0;
+                for (uint32_t k = 0; k < ne; ++k) {
+                    const uint32_t e = (uint32_t)(ord >> (4 * k)) & 15u;
+                    const uint32_t lx = x + __ldg(&g_edge_lo[e][0]), ly = y + __ldg(&g_edge_lo[e][1]), lz = z + __ldg(&g_edge_lo[e][2]);
+                    const uint32_t idx = ((lz * g.ny + ly) * g.nx + lx) * 3 + __ldg(&g_edge_axis[e]);
+                    ids[k] = idx;
+                    if (!((own >> e) & 1u)) continue;  // its owner (an earlier cell) records the id
+                    // owned: this cell writes the vertex (first use in visit order)
+                    const uint32_t u = __ldg(&iso_edge_connection[e][0]), v = __ldg(&iso_edge_connection[e][1]);
+                    const uint32_t ux = x + __ldg(&iso_corners[u][0]), uy = y + __ldg(&iso_corners[u][1]), uz = z + __ldg(&iso_corners[u][2]);
+                    const uint32_t vx = x + __ldg(&iso_corners[v][0]), vy = y + __ldg(&iso_corners[v][1]), vz = z + __ldg(&iso_corners[v][2]);
+                    const float fa = __ldg(g.values + ((size_t)uz * g.ny + uy) * g.pitch + ux);
+                    const float fb = __ldg(g.values + ((size_t)vz * g.ny + vy) * g.pitch + vx);
+                    float pax, pay, paz, pbx, pby, pbz;
+                    if (explicit_pos) {
+                        const float4 qa = __ldg(g.positions + ((size_t)uz * g.ny + uy) * g.nx + ux);
+                        const float4 qb = __ldg(g.positions + ((size_t)vz * g.ny + vy) * g.nx + vx);
+                        pax = qa.x; pay = qa.y; paz = qa.z; pbx = qb.x; pby = qb.y; pbz = qb.z;
+                    } else {
+                        pax = (float)ux * g.inv; pay = (float)uy * g.inv; paz = (float)uz * g.inv;
+                        pbx = (float)vx * g.inv; pby = (float)vy * g.inv; pbz = (float)vz * g.inv;
+                    }
+                    // Signed::find_crossing_point (distance.rs:64-69)
+                    const float delta = fb - fa;
+                    const float tt = (delta == 0.0f) ? 0.5f : -fa / delta;
+                    const float omt = 1.0f - tt;
+                    const uint32_t vid = vstart + r;
+                    ++r;
+                    if (vid < A.cap_v) {
+                        A.out_v[3 * (size_t)vid + 0] = pax * omt + pbx * tt;
+                        A.out_v[3 * (size_t)vid + 1] = pay * omt + pby * tt;
+                        A.out_v[3 * (size_t)vid + 2] = paz * omt + pbz * tt;
+                        if (A.out_k) {
+                            A.out_k[2 * (size_t)vid] = (((uint64_t)lz * g.ny + ly) * g.nx + lx) * 3 + __ldg(&g_edge_axis[e]);
+                            A.out_k[2 * (size_t)vid + 1] = 0;
+                        }
+                    } else {
+                        atomicOr(A.err, DERR_CAPACITY);
+                    }
+                    A.edge_id[idx] = vid - grid_v0;
+                }
+                // triangles (march_cube, marching_cubes_impl.rs:102-117)
+                const uint64_t slot = __ldg(&iso_tri_slot[cs]);
+                if ((uint64_t)tstart + nt <= A.cap_t) {
+                    for (uint32_t k = 0; k < 3 * nt; ++k) A.out_i[3 * (size_t)tstart + k] = ids[(slot >> (4 * k)) & 15u];
+                } else {
+                    atomicOr(A.err, DERR_CAPACITY);
+                }
+            }
+        }
+    }
+}
+
+// Triangle corners: lattice edge index -> vertex id recorded by the owner,
+// for the 3 * min(triangles, capacity) corners written (the count is read on
+// the device, so no host round trip is needed).  Indices outside the map
+// (corners of triangles an emit without room skipped) are left alone.
+__global__ void mc_resolve_ids(uint32_t* idx, const uint64_t* totals, uint64_t cap_t, const uint32_t* edge_id,
+                               uint32_t nedges) {
+    const uint64_t n = 3 * min(totals[0], cap_t);
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = idx[i];
+        if (v < nedges) idx[i] = __ldg(edge_id + v);
     }
 }
 
