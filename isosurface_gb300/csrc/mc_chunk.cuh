@@ -466,7 +466,7 @@ __global__ void __launch_bounds__(256) mc_block_emit(ChunkEmitArgs A, uint32_t m
 // the id its owner recorded (no owner lookup in this pass; the map needs no
 // initialisation: every crossing edge has an owner, and only crossing edges
 // are referenced).
-__global__ void __launch_bounds__(256) mc_cell_emit(ChunkEmitArgs A, uint32_t nranges) {
+__global__ void __launch_bounds__(256, 5) mc_cell_emit(ChunkEmitArgs A, uint32_t nranges) {
     const int lane = threadIdx.x & 31;
     const uint32_t seg = blockIdx.x * 8 + (threadIdx.x >> 5);  // 32 chunks per warp
     const uint32_t range = seg / (RANGE / 32);
@@ -538,14 +538,13 @@ __global__ void __launch_bounds__(256) mc_cell_emit(ChunkEmitArgs A, uint32_t nr
                 const uint32_t own = __ldg(&iso_owned_mask[cls]);
                 const uint64_t ord = __ldg(&iso_edge_order[cs]);
                 const uint32_t ne = __ldg(&iso_edge_count[cs]);
-                uint32_t ids[12];  // lattice edge index by first-use rank
+                const uint32_t cell = (z * g.ny + y) * g.nx + x;  // lattice point of corner 0
                 uint32_t r = 0;
                 for (uint32_t k = 0; k < ne; ++k) {
                     const uint32_t e = (uint32_t)(ord >> (4 * k)) & 15u;
+                    if (!((own >> e) & 1u)) continue;  // its owner (an earlier cell) records the id
                     const uint32_t lx = x + __ldg(&g_edge_lo[e][0]), ly = y + __ldg(&g_edge_lo[e][1]), lz = z + __ldg(&g_edge_lo[e][2]);
                     const uint32_t idx = ((lz * g.ny + ly) * g.nx + lx) * 3 + __ldg(&g_edge_axis[e]);
-                    ids[k] = idx;
-                    if (!((own >> e) & 1u)) continue;  // its owner (an earlier cell) records the id
                     // owned: this cell writes the vertex (first use in visit order)
                     const uint32_t u = __ldg(&iso_edge_connection[e][0]), v = __ldg(&iso_edge_connection[e][1]);
                     const uint32_t ux = x + __ldg(&iso_corners[u][0]), uy = y + __ldg(&iso_corners[u][1]), uz = z + __ldg(&iso_corners[u][2]);
@@ -580,10 +579,16 @@ __global__ void __launch_bounds__(256) mc_cell_emit(ChunkEmitArgs A, uint32_t nr
                     }
                     A.edge_id[idx] = vid - grid_v0;
                 }
-                // triangles (march_cube, marching_cubes_impl.rs:102-117)
-                const uint64_t slot = __ldg(&iso_tri_slot[cs]);
+                // triangles (march_cube, marching_cubes_impl.rs:102-117) as lattice
+                // edge indices: corner 0's lattice point plus the edge's lower end
+                const uint64_t tedges = __ldg(&iso_tri_edges[cs]);
                 if ((uint64_t)tstart + nt <= A.cap_t) {
-                    for (uint32_t k = 0; k < 3 * nt; ++k) A.out_i[3 * (size_t)tstart + k] = ids[(slot >> (4 * k)) & 15u];
+                    for (uint32_t k = 0; k < 3 * nt; ++k) {
+                        const uint32_t e = (uint32_t)(tedges >> (4 * k)) & 15u;
+                        const uint32_t off = __ldg(&g_edge_lo[e][0]) + g.nx * (__ldg(&g_edge_lo[e][1]) +
+                                                                              g.ny * __ldg(&g_edge_lo[e][2]));
+                        A.out_i[3 * (size_t)tstart + k] = (cell + off) * 3 + __ldg(&g_edge_axis[e]);
+                    }
                 } else {
                     atomicOr(A.err, DERR_CAPACITY);
                 }
