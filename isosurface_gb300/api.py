@@ -102,7 +102,10 @@ class Context:
         return lib().iso_ctx_kernel_launches(self.h)
 
     def program(self, source):
-        """Upload (once per distinct program) and return a Program."""
+        """Upload (once per distinct program) and return a Program (a Program
+        of this context is returned as it is)."""
+        if isinstance(source, Program) and source.ctx is self:
+            return source
         data = source if isinstance(source, (bytes, bytearray)) else lower(source)
         data = bytes(data)
         p = self._programs.get(data)

@@ -1,6 +1,7 @@
 // Contexts, programs, buffers and the C ABI entry points (include/isosurface_gpu.h).
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <utility>
 
 #include <algorithm>
@@ -29,6 +30,7 @@ iso_status set_device(iso_ctx* ctx) {
 
 iso_status ensure(iso_ctx* ctx, DevBuf& b, size_t bytes) {
     if (bytes <= b.bytes) return ISO_OK;
+    if (ctx->capturing) return fail(ctx, ISO_ERR_INVALID_ARG, "allocation while recording a graph");
     if (b.p) {
         // the buffer may still be read by queued work of this context
         cudaError_t e = cudaStreamSynchronize(ctx->stream);
@@ -205,6 +207,27 @@ void classify(iso_program* p) {
 
 }  // namespace
 
+namespace iso {
+
+iso_status sample_lattice(iso_ctx* ctx, const iso_program* prog, uint32_t size, Lattice* L) {
+    const uint32_t nx = size, ny = size, nz = size + 1;
+    const uint64_t pitch = default_pitch(nx);
+    const uint32_t W = words_per_row(nx);
+    iso_status s;
+    if ((s = ensure(ctx, ctx->field, 4ull * pitch * ny * nz)) != ISO_OK) return s;
+    if ((s = ensure(ctx, ctx->bits, 4ull * W * ny * nz)) != ISO_OK) return s;
+    const float inv = 1.0f / (float)(size - 1);
+    // marching cubes reads values only at the ends of crossing edges: the
+    // sampler may skip the values far from the surface
+    if ((s = launch_sample_grid(ctx, prog, nx, ny, nz, inv, (float*)ctx->field.p, pitch, (uint32_t*)ctx->bits.p,
+                                true)) != ISO_OK)
+        return s;
+    *L = Lattice{nx, ny, nz, pitch, (const float*)ctx->field.p, (const uint32_t*)ctx->bits.p, W, inv, nullptr};
+    return ISO_OK;
+}
+
+}  // namespace iso
+
 extern "C" {
 
 const char* iso_status_str(iso_status s) {
@@ -268,6 +291,7 @@ iso_status iso_ctx_destroy(iso_ctx* ctx) {
         cudaEventDestroy(p.b);
     }
     for (cudaEvent_t ev : ctx->event_pool) cudaEventDestroy(ev);
+    mc_plan_release(ctx);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
     return ISO_OK;
@@ -328,6 +352,8 @@ iso_status iso_program_create(iso_ctx* ctx, const uint8_t* bytes, size_t len, is
     iso_program* p = new (std::nothrow) iso_program();
     if (!p) return ISO_ERR_OUT_OF_MEMORY;
     p->ctx = ctx;
+    static std::atomic<uint64_t> next_uid{1};
+    p->uid = next_uid.fetch_add(1);
     p->ops.resize(h[1]);
     p->consts.resize(h[2]);
     std::memcpy(p->ops.data(), bytes + 16, 4ull * h[1]);
@@ -412,22 +438,6 @@ iso_status iso_mesh_device(iso_ctx* ctx, const float** vertices, const uint32_t*
     return ISO_OK;
 }
 
-static iso_status sample_into_ctx(iso_ctx* ctx, const iso_program* prog, uint32_t size, Lattice* L) {
-    const uint32_t nx = size, ny = size, nz = size + 1;
-    const uint64_t pitch = default_pitch(nx);
-    const uint32_t W = words_per_row(nx);
-    iso_status s;
-    if ((s = ensure(ctx, ctx->field, 4ull * pitch * ny * nz)) != ISO_OK) return s;
-    if ((s = ensure(ctx, ctx->bits, 4ull * W * ny * nz)) != ISO_OK) return s;
-    const float inv = 1.0f / (float)(size - 1);
-    // marching cubes reads values only at the ends of crossing edges: the
-    // sampler may skip the values far from the surface
-    if ((s = launch_sample_grid(ctx, prog, nx, ny, nz, inv, (float*)ctx->field.p, pitch, (uint32_t*)ctx->bits.p,
-                                true)) != ISO_OK)
-        return s;
-    *L = Lattice{nx, ny, nz, pitch, (const float*)ctx->field.p, (const uint32_t*)ctx->bits.p, W, inv, nullptr};
-    return ISO_OK;
-}
 
 static iso_status check_size(iso_ctx* ctx, const iso_program* prog, uint32_t size) {
     if (!ctx || !prog) return ISO_ERR_INVALID_ARG;
@@ -461,9 +471,7 @@ iso_status iso_mc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, 
         if (info) *info = ctx->last;
         return ISO_OK;
     }
-    Lattice L;
-    if ((s = sample_into_ctx(ctx, prog, size, &L)) != ISO_OK) return s;
-    if ((s = mc_extract_lattice(ctx, L, flags & ~(uint32_t)ISO_FLAG_NORMALS, info)) != ISO_OK) return s;
+    if ((s = mc_extract_program(ctx, prog, size, flags & ~(uint32_t)ISO_FLAG_NORMALS, info)) != ISO_OK) return s;
     return (flags & ISO_FLAG_NORMALS) ? attach_normals(ctx, prog) : ISO_OK;
 }
 
@@ -489,7 +497,7 @@ iso_status iso_mc_cases(iso_ctx* ctx, const iso_program* prog, uint32_t size, ui
     if (!cases_host) return fail(ctx, ISO_ERR_INVALID_ARG, "null output");
     if (size < 2) return ISO_OK;
     Lattice L;
-    if ((s = sample_into_ctx(ctx, prog, size, &L)) != ISO_OK) return s;
+    if ((s = sample_lattice(ctx, prog, size, &L)) != ISO_OK) return s;
     const uint64_t ncells = (uint64_t)(size - 1) * (size - 1) * size;
     if ((s = ensure(ctx, ctx->aux, ncells)) != ISO_OK) return s;
     if ((s = mc_cases_lattice(ctx, L, (uint8_t*)ctx->aux.p)) != ISO_OK) return s;
@@ -528,7 +536,7 @@ iso_status iso_point_cloud_extract(iso_ctx* ctx, const iso_program* prog, uint32
         ctx->last_vertex_floats = 3;
     } else {
         Lattice L;
-        if ((s = sample_into_ctx(ctx, prog, size, &L)) != ISO_OK) return s;
+        if ((s = sample_lattice(ctx, prog, size, &L)) != ISO_OK) return s;
         if ((s = point_cloud_lattice(ctx, L, nullptr)) != ISO_OK) return s;
     }
     if ((flags & ISO_FLAG_NORMALS) && (s = attach_normals(ctx, prog)) != ISO_OK) return s;

@@ -69,6 +69,18 @@ struct iso_ctx {
     std::vector<Pending> pending;
     double stage_ms[ISO_STAGE_COUNT] = {};
     uint64_t stage_launches[ISO_STAGE_COUNT] = {};
+    // steady-state MarchingCubes: the whole extraction recorded as one CUDA
+    // graph, replayed while the program, size, flags and buffers stay the same
+    bool capturing = false;  // no allocation while a stream capture records
+    struct McPlan {
+        cudaGraphExec_t exec = nullptr;
+        const iso_program* prog = nullptr;
+        uint64_t prog_uid = 0;
+        uint32_t size = 0, flags = 0;
+        void* bufs[12] = {};
+        uint64_t launches = 0;
+    } mc_plan;
+    uint64_t mc_last_key[3] = {};  // (program uid, size, flags) of the last eager extraction
 };
 
 namespace iso {
@@ -97,6 +109,7 @@ struct iso_program {
     bool has_domain = false;
     float domain[6] = {0, 0, 0, 0, 0, 0};
     uint32_t set_at = 0, set_n = 0;
+    uint64_t uid = 0;  // unique per program created in this process
     iso::ProgView view() const { return iso::ProgView{d_ops, d_consts, d_jump, (uint32_t)ops.size()}; }
 };
 
@@ -131,6 +144,14 @@ struct Lattice {
     const float4* positions; // DC: explicit xyz per point (w unused); null = regular grid
 };
 iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, iso_mesh_info* info);
+// iso_mc_extract without the normals sink: sampler + MarchingCubes, replaying
+// the context's recorded graph when it applies
+iso_status mc_extract_program(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t flags,
+                              iso_mesh_info* info);
+// the sampler half (signs everywhere, values near the surface) into the
+// context's field and sign buffers
+iso_status sample_lattice(iso_ctx* ctx, const iso_program* prog, uint32_t size, Lattice* L);
+void mc_plan_release(iso_ctx* ctx);
 iso_status mc_cases_lattice(iso_ctx* ctx, const Lattice& L, uint8_t* d_cases);
 // PointCloud::extract over a sampled lattice: active-cell centres into the context's mesh
 iso_status point_cloud_lattice(iso_ctx* ctx, const Lattice& L, iso_mesh_info* info);

@@ -592,14 +592,18 @@ cudaError_t emit_smem_attribute(size_t smem) {
 // back, the emit writing into the context's mesh buffers as sized by earlier
 // extractions (its writes are capacity-checked); the totals come back with
 // the final synchronisation, and an emit that ran out of room is repeated
-// into buffers of the exact size.
-iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, iso_mesh_info* info) {
-    ctx->last = iso_mesh_info{};
-    ctx->last_flags = flags;
-    ctx->last_vertex_floats = 3;
+// into buffers of the exact size.  With `record` the passes are only queued
+// (for a stream capture): no allocation, no synchronisation, no read-back.
+static iso_status mc_lattice_passes(iso_ctx* ctx, const Lattice& L, uint32_t flags, iso_mesh_info* info,
+                                    bool record) {
+    if (!record) {
+        ctx->last = iso_mesh_info{};
+        ctx->last_flags = flags;
+        ctx->last_vertex_floats = 3;
+    }
     if (L.nx < 2 || L.ny < 2 || L.nz < 2) {
         if (info) *info = ctx->last;
-        return ISO_OK;
+        return record ? fail(ctx, ISO_ERR_INVALID_ARG, "nothing to record") : ISO_OK;
     }
     const uint32_t ncx = L.nx - 1;
     const uint32_t CW = (ncx + 31) / 32;
@@ -616,6 +620,11 @@ iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, is
     if ((s = ensure(ctx, ctx->mesh_v, 12 * (size_t)65536)) != ISO_OK) return s;
     if ((s = ensure(ctx, ctx->mesh_i, 12 * (size_t)131072)) != ISO_OK) return s;
     if (keys && (s = ensure(ctx, ctx->mesh_k, 16 * (size_t)65536)) != ISO_OK) return s;
+    // the dense edge -> vertex map (4 B per lattice edge) when the edge
+    // indices fit 32 bits; otherwise the block emit resolves owners itself
+    const uint64_t nedges = 3ull * L.nx * L.ny * L.nz;
+    const bool edge_map = nedges < (1ull << 32) && L.positions == nullptr;
+    if (edge_map && (s = ensure(ctx, ctx->edges, 4 * nedges)) != ISO_OK) return s;
     uint2* local = (uint2*)ctx->rowtri.p;
     uint2* rangeagg = (uint2*)ctx->scan.p;
     uint2* rangepre = rangeagg + nranges;
@@ -633,11 +642,6 @@ iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, is
     }
     ctx->launches += 3;
     if ((s = check_launch(ctx, "mc_chunk_count")) != ISO_OK) return s;
-    // the dense edge -> vertex map (4 B per lattice edge) when the edge
-    // indices fit 32 bits; otherwise the block emit resolves owners itself
-    const uint64_t nedges = 3ull * L.nx * L.ny * L.nz;
-    const bool edge_map = nedges < (1ull << 32) && L.positions == nullptr;
-    if (edge_map && (s = ensure(ctx, ctx->edges, 4 * nedges)) != ISO_OK) return s;
     auto emit = [&]() -> iso_status {
         uint64_t cap_v = ctx->mesh_v.bytes / 12, cap_t = ctx->mesh_i.bytes / 12;
         if (keys) cap_v = std::min<uint64_t>(cap_v, ctx->mesh_k.bytes / 16);
@@ -660,10 +664,11 @@ iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, is
         if (st != ISO_OK) return st;
         cudaError_t ce = cudaMemcpyAsync(ctx->h_pinned, totals, 16, cudaMemcpyDeviceToHost, ctx->stream);
         if (ce == cudaSuccess) ce = cudaMemcpyAsync(ctx->h_pinned + 2, ctx->d_err, 4, cudaMemcpyDeviceToHost, ctx->stream);
-        if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+        if (ce == cudaSuccess && !record) ce = cudaStreamSynchronize(ctx->stream);
         return ce == cudaSuccess ? ISO_OK : cuda_fail(ctx, ce, "sync after emit");
     };
     if ((s = emit()) != ISO_OK) return s;
+    if (record) return ISO_OK;
     uint64_t nt = ctx->h_pinned[0], nv = ctx->h_pinned[1];
     uint32_t err = (uint32_t)ctx->h_pinned[2];
     if (nv >= (1ull << 31) || nt >= (1ull << 31)) {
@@ -690,6 +695,104 @@ iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, is
     return ISO_OK;
 }
 
+iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, iso_mesh_info* info) {
+    return mc_lattice_passes(ctx, L, flags, info, false);
+}
+
+void mc_plan_release(iso_ctx* ctx) {
+    if (ctx->mc_plan.exec) cudaGraphExecDestroy(ctx->mc_plan.exec);
+    ctx->mc_plan = iso_ctx::McPlan{};
+}
+
+// the buffers a recorded extraction has baked into its kernels' arguments
+static void plan_buffers(const iso_ctx* ctx, void** b) {
+    const DevBuf* bufs[12] = {&ctx->field, &ctx->bits, &ctx->rowtri, &ctx->scan,  &ctx->tiles, &ctx->edges,
+                              &ctx->mesh_v, &ctx->mesh_i, &ctx->mesh_k, &ctx->aux, &ctx->aux2, &ctx->aux3};
+    for (int i = 0; i < 12; ++i) b[i] = bufs[i]->p;
+}
+
+// MarchingCubes of a program: extractions run eagerly (sizing every buffer)
+// until the same (program, size, flags) comes twice in a row; it is then
+// recorded as one CUDA graph, and later extractions with the same buffers
+// replay it and synchronise once.  Whatever does not fit (a mesh that outgrew its buffers,
+// an error flag) falls back to the eager path, which records again.  Stage
+// timing (events) needs the eager path.
+iso_status mc_extract_program(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t flags,
+                              iso_mesh_info* info) {
+    iso_ctx::McPlan& P = ctx->mc_plan;
+    void* bufs[12];
+    plan_buffers(ctx, bufs);
+    const bool match = P.exec && !ctx->timing && P.prog == prog && P.prog_uid == prog->uid && P.size == size &&
+                       P.flags == flags && std::memcmp(P.bufs, bufs, sizeof(bufs)) == 0;
+    if (match) {
+        cudaError_t e = cudaGraphLaunch(P.exec, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "extraction graph");
+        ctx->launches += P.launches;
+        const uint64_t nt = ctx->h_pinned[0], nv = ctx->h_pinned[1];
+        const uint32_t err = (uint32_t)ctx->h_pinned[2];
+        const bool keys = (flags & ISO_FLAG_KEYS) != 0;
+        const bool fits = nv <= ctx->mesh_v.bytes / 12 && nt <= ctx->mesh_i.bytes / 12 &&
+                          (!keys || nv <= ctx->mesh_k.bytes / 16) && nv < (1ull << 31) && nt < (1ull << 31);
+        if (!err && fits) {
+            ctx->last = iso_mesh_info{nv, nt, (uint64_t)(size - 1) * (size - 1) * size};
+            ctx->last_flags = flags;
+            ctx->last_vertex_floats = 3;
+            if (info) *info = ctx->last;
+            return ISO_OK;
+        }
+        // the eager path below clears nothing it needs: it re-samples and re-counts
+        if (err) {
+            e = cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "clear error flags");
+        }
+        mc_plan_release(ctx);
+    }
+    Lattice L;
+    iso_status s = sample_lattice(ctx, prog, size, &L);
+    if (s != ISO_OK) return s;
+    if ((s = mc_lattice_passes(ctx, L, flags, info, false)) != ISO_OK) return s;
+    // record only a configuration that repeats (and not under stage timing)
+    const uint64_t key[3] = {prog->uid, size, flags};
+    const bool repeat = std::memcmp(key, ctx->mc_last_key, sizeof(key)) == 0;
+    std::memcpy(ctx->mc_last_key, key, sizeof(key));
+    if (ctx->timing || !repeat) return ISO_OK;
+    // record the same extraction (nothing runs while recording)
+    mc_plan_release(ctx);
+    const uint64_t launches0 = ctx->launches;
+    cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return ISO_OK;  // no graph: every call stays eager
+    }
+    ctx->capturing = true;
+    Lattice R;
+    const iso_mesh_info keep = ctx->last;
+    iso_status rs = sample_lattice(ctx, prog, size, &R);
+    if (rs == ISO_OK) rs = mc_lattice_passes(ctx, R, flags, nullptr, true);
+    ctx->capturing = false;
+    ctx->last = keep;
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(ctx->stream, &g);
+    const uint64_t recorded = ctx->launches - launches0;
+    ctx->launches = launches0;  // recording launched nothing
+    if (rs == ISO_OK && e == cudaSuccess && g) {
+        cudaGraphExec_t exec = nullptr;
+        if (cudaGraphInstantiate(&exec, g, 0) == cudaSuccess) {
+            P.exec = exec;
+            P.prog = prog;
+            P.prog_uid = prog->uid;
+            P.size = size;
+            P.flags = flags;
+            plan_buffers(ctx, P.bufs);
+            P.launches = recorded;
+        }
+    }
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();  // a failed recording only means no replay
+    ctx->last_error.clear();
+    return ISO_OK;
+}
 // ---- many grids in one launch (batch.cu) ----------------------------------
 size_t mc_grid_bytes() { return sizeof(Grid); }
 
