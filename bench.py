@@ -117,8 +117,9 @@ def cpu_baseline_port(src_bytes, budget_s=12.0, threads=1):
 def secondary_workloads(ctx, torch, steps, only=None):
     """The other workloads, timed with CUDA events on the library's stream:
     the 4096-chunk batch (one CUDA graph vs one extraction per chunk),
-    DualContouring at 256^3 and LinearHashedMarchingCubes at depth 8
-    (`only`: a set of names among batch, dc, lhmc to run just those)."""
+    DualContouring at 256^3, LinearHashedMarchingCubes at depth 8 and the
+    reference's own benchmark shapes (`only`: a set of names among refshapes,
+    batch, dc, lhmc to run just those)."""
     from isosurface_gb300 import scenes
     stream = torch.cuda.ExternalStream(ctx.stream)
 
@@ -133,6 +134,8 @@ def secondary_workloads(ctx, torch, steps, only=None):
 
     out = {}
     want = (lambda name: only is None or name in only)
+    if want("refshapes"):
+        out["reference_bench_shapes"] = _reference_bench_shapes(ctx, timed, steps)
     if want("batch"):
         out.update(_batch_workload(ctx, timed, steps))
     src = scenes.csg()
@@ -147,6 +150,33 @@ def secondary_workloads(ctx, torch, steps, only=None):
             info = ctx.lhmc_extract(src, 8)
         ms = timed(lambda: ctx.lhmc_extract(src, 8), max(steps, 3))
         out["lhmc_depth8"] = {"dual_cubes": int(info.num_cells), "ms": ms, "triangles": int(info.num_triangles)}
+    return out
+
+
+def _reference_bench_shapes(ctx, timed, steps):
+    """The reference's own benchmark shapes (benches/isosurface.rs): Torus(0.25,
+    0.1) at the origin, MarchingCubes::new(128) and LinearHashedMarchingCubes::
+    new(7), on the GPU and with the single-threaded oracle beside them."""
+    import oracle
+    from isosurface_gb300 import scenes
+    from isosurface_gb300 import source as S
+    src = scenes.bench_torus()
+    prog = ctx.program(src)
+    o = oracle.Program(S.lower(src))
+    out = {}
+    for _ in range(3):
+        info = ctx.mc_extract(prog, 128)
+    gpu_ms = timed(lambda: ctx.mc_extract(prog, 128), max(steps, 5))
+    secs, cells, _ = o.mc_timed(128, 0, 128, 1)
+    out["mc_128_torus"] = {"cells": int(info.num_cells), "gpu_ms": gpu_ms, "cpu_baseline_ms": 1e3 * secs,
+                           "cpu_threads": 1, "triangles": int(info.num_triangles)}
+    for _ in range(2):
+        info = ctx.lhmc_extract(prog, 7)
+    gpu_ms = timed(lambda: ctx.lhmc_extract(prog, 7), max(steps, 5))
+    t0 = time.time()
+    o.lhmc(7)
+    out["lhmc_7_torus"] = {"gpu_ms": gpu_ms, "cpu_baseline_ms": 1e3 * (time.time() - t0), "cpu_threads": 1,
+                           "triangles": int(info.num_triangles)}
     return out
 
 
@@ -297,7 +327,7 @@ def main():
     ap.add_argument("--no-secondary", action="store_true", help="skip the batch / DC / LHMC timings")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-surrogate workload")
     ap.add_argument("--secondary-only", default=None,
-                    help="comma list among batch,dc,lhmc,surrogate: run only these secondary workloads")
+                    help="comma list among refshapes,batch,dc,lhmc,surrogate: run only these secondary workloads")
     ap.add_argument("--surrogate-train-steps", type=int, default=4000)
     args = ap.parse_args()
     if args.warmup < 3:
