@@ -266,3 +266,37 @@ def test_sphere_union_near_only_values(ctx, size):
         want = oracle.Program(S.lower(src)).marching_cubes(size)
         assert np.array_equal(got.vertices, want.vertices)
         assert np.array_equal(got.indices, want.indices)
+
+
+def test_repeated_extractions_replay_the_recorded_graph(ctx):
+    """A (program, size) extracted twice in a row is recorded as one CUDA graph
+    and replayed afterwards: replays give the same bytes as the eager run,
+    also after other extractions, a keys flag change and a buffer regrowth
+    (which must force a new recording rather than a stale replay)."""
+    src = scenes.sphere_union()
+    want = oracle.Program(S.lower(src)).marching_cubes(97)
+    prog = ctx.program(src)
+
+    def check(keys=False):
+        got = ctx.download(ctx.mc_extract(prog, 97, keys=keys), keys=keys)
+        assert np.array_equal(got.vertices, want.vertices)
+        assert np.array_equal(got.indices, want.indices)
+        if keys:
+            assert np.array_equal(got.keys, want.keys)
+
+    for _ in range(4):  # eager, eager + record, replay, replay
+        check()
+    launches = ctx.kernel_launches
+    check()
+    assert ctx.kernel_launches > launches  # replays still count their kernels
+    ctx.mc_extract(scenes.bench_torus(), 97)  # another program in between
+    check()
+    check()
+    for _ in range(3):
+        check(keys=True)
+    check()
+    # a much larger mesh regrows the context's buffers; the recorded graph
+    # must not write into the freed ones
+    ctx.mc_extract(src, 301)
+    for _ in range(3):
+        check()
