@@ -61,7 +61,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -142,13 +142,13 @@ def secondary_workloads(ctx, torch, steps, only=None):
     if want("dc"):
         for _ in range(2):
             info = ctx.dc_extract(src, 257)
-        ms = timed(lambda: ctx.dc_extract(src, 257), max(steps, 3))
+        ms = timed(lambda: ctx.dc_extract(src, 257), max(3, min(steps, 20)))
         out["dc_256"] = {"cells": int(info.num_cells), "ms": ms, "cells_per_s": 256 * 256 * 257 / (ms / 1e3),
                          "triangles": int(info.num_triangles), "placer": "MinimiseQEF"}
     if want("lhmc"):
         for _ in range(2):
             info = ctx.lhmc_extract(src, 8)
-        ms = timed(lambda: ctx.lhmc_extract(src, 8), max(steps, 3))
+        ms = timed(lambda: ctx.lhmc_extract(src, 8), max(3, min(steps, 20)))
         out["lhmc_depth8"] = {"dual_cubes": int(info.num_cells), "ms": ms, "triangles": int(info.num_triangles)}
     return out
 
@@ -166,13 +166,13 @@ def _reference_bench_shapes(ctx, timed, steps):
     out = {}
     for _ in range(3):
         info = ctx.mc_extract(prog, 128)
-    gpu_ms = timed(lambda: ctx.mc_extract(prog, 128), max(steps, 5))
+    gpu_ms = timed(lambda: ctx.mc_extract(prog, 128), max(5, min(steps, 20)))
     secs, cells, _ = o.mc_timed(128, 0, 128, 1)
     out["mc_128_torus"] = {"cells": int(info.num_cells), "gpu_ms": gpu_ms, "cpu_baseline_ms": 1e3 * secs,
                            "cpu_threads": 1, "triangles": int(info.num_triangles)}
     for _ in range(2):
         info = ctx.lhmc_extract(prog, 7)
-    gpu_ms = timed(lambda: ctx.lhmc_extract(prog, 7), max(steps, 5))
+    gpu_ms = timed(lambda: ctx.lhmc_extract(prog, 7), max(5, min(steps, 20)))
     t0 = time.time()
     o.lhmc(7)
     out["lhmc_7_torus"] = {"gpu_ms": gpu_ms, "cpu_baseline_ms": 1e3 * (time.time() - t0), "cpu_threads": 1,
@@ -190,7 +190,7 @@ def _batch_workload(ctx, timed, steps):
     chosen = batch.autotune(cache)
     batch.run(graph=False)
     batch.run(graph=True)
-    graph_ms = timed(lambda: batch.run(graph=True), max(steps, 3))
+    graph_ms = timed(lambda: batch.run(graph=True), max(3, min(steps, 20)))
     info = batch.run(graph=True)
     per_ms = timed(batch.run_per_chunk, 2)
     cells = info.num_cells
@@ -295,7 +295,9 @@ def run_reference(args):
     # size each step to a few seconds of work
     mid = SIZE // 2
     secs, _, _ = prog.mc_timed(SIZE, mid, mid + threads, threads)
-    layers = max(threads, int(3.0 / max(secs, 1e-6)) * threads)
+    # each step a bounded sample: the whole run stays near a minute and a half
+    per_step = min(3.0, 90.0 / max(1, args.steps + args.warmup))
+    layers = max(threads, int(per_step / max(secs, 1e-6)) * threads)
     layers = min(layers, SIZE - 1)
     z0 = max(0, mid - layers // 2)
     for _ in range(args.warmup):
@@ -320,8 +322,8 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true", help="skip the batch / DC / LHMC timings")
