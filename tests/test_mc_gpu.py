@@ -300,3 +300,30 @@ def test_repeated_extractions_replay_the_recorded_graph(ctx):
     ctx.mc_extract(src, 301)
     for _ in range(3):
         check()
+
+
+def test_1024_cubed_block_emit_fallback(ctx):
+    """new(1025): 3.2e9 lattice edges do not fit the 32-bit edge map, so the
+    block emit resolves owners itself (on near-surface sampled values).  A
+    middle slab of cell layers must equal the oracle's traversal of that slab,
+    and every vertex must be used once per distinct lattice edge."""
+    src = scenes.sphere_union()
+    size = 1025
+    info = ctx.mc_extract(src, size, keys=True)
+    got = ctx.download(info, keys=True)
+    cases = ctx.mc_cases(src, size)
+    tri_count = np.array(json.load(open(os.path.join(GOLDEN, "mc_tables.json")))["TRIANGLE_CONNECTION"])
+    ntri = (tri_count[:, 0::3][:, :5] >= 0).sum(1)
+    per_layer = ntri[cases.reshape(size, -1)].sum(1)
+    del cases
+    assert per_layer.sum() == info.num_triangles
+    z0, z1 = 511, 513
+    t0, t1 = int(per_layer[:z0].sum()), int(per_layer[:z1].sum())
+    want = oracle.Program(S.lower(src)).marching_cubes_slab(size, z0, z1)
+    assert np.array_equal(got.keys[:, 0][got.indices[3 * t0:3 * t1]], want.keys[:, 0][want.indices])
+    gv = got.vertices[got.indices[3 * t0:3 * t1]]
+    wv = want.vertices[want.indices]
+    assert np.max(np.abs(gv - wv)) <= 1e-5 / (size - 1)
+    # every vertex is used and every key is distinct
+    assert len(np.unique(got.indices)) == info.num_vertices
+    assert len(np.unique(got.keys[:, 0])) == info.num_vertices
