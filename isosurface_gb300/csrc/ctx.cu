@@ -203,6 +203,44 @@ void classify(iso_program* p) {
         p->set_at = arg(set_pc);
         p->set_n = (uint32_t)p->consts[p->set_at];
     }
+    // [DOMAIN] TRANSLATE prim POP (TRANSLATE prim POP UNION)* [POP]: a left
+    // fold of hard unions over translated primitives, compiled to a flat list
+    // that the evaluator walks with the same operations in the same order
+    size_t i = 0;
+    int32_t dom = -1;
+    if (o.size() > 0 && op(0) == OP_PT_DOMAIN) {
+        dom = (int32_t)arg(0);
+        i = 1;
+    }
+    std::vector<float> prims;
+    bool ok = true;
+    size_t groups = 0;
+    while (ok && i + 3 <= o.size() && op(i) == OP_PT_TRANSLATE) {
+        const uint32_t pr = op(i + 1);
+        if (op(i + 2) != OP_PT_POP || !(pr == OP_SPHERE || pr == OP_BOX || pr == OP_CYLINDER || pr == OP_TORUS)) {
+            ok = false;
+            break;
+        }
+        if (groups > 0) {
+            if (i + 3 >= o.size() || op(i + 3) != OP_UNION) {
+                ok = false;
+                break;
+            }
+        }
+        const float* c = p->consts.data() + arg(i);
+        const float* a = p->consts.data() + arg(i + 1);
+        const int na = pr == OP_SPHERE ? 1 : (pr == OP_BOX ? 3 : 2);
+        float rec[8] = {c[0], c[1], c[2], 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        std::memcpy(&rec[3], &pr, 4);
+        for (int j = 0; j < na; ++j) rec[4 + j] = a[j];
+        prims.insert(prims.end(), rec, rec + 8);
+        i += groups > 0 ? 4 : 3;
+        ++groups;
+    }
+    if (ok && groups > 0 && ((dom < 0 && i == o.size()) || (dom >= 0 && i + 1 == o.size() && op(i) == OP_PT_POP))) {
+        p->prims = std::move(prims);
+        p->prim_dom_at = dom;
+    }
 }
 
 }  // namespace
@@ -385,6 +423,12 @@ iso_status iso_program_create(iso_ctx* ctx, const uint8_t* bytes, size_t len, is
             e = cudaMemcpy(d_set, p->consts.data() + p->set_at + 3, 16ull * p->set_n, cudaMemcpyHostToDevice);
         p->d_set = d_set;
     }
+    if (e == cudaSuccess && !p->prims.empty()) {
+        float4* d_prims = nullptr;
+        e = cudaMalloc(&d_prims, 4 * p->prims.size());
+        if (e == cudaSuccess) e = cudaMemcpy(d_prims, p->prims.data(), 4 * p->prims.size(), cudaMemcpyHostToDevice);
+        p->d_prims = d_prims;
+    }
     if (e != cudaSuccess) {
         iso_status r = cuda_fail(ctx, e, "program upload");
         iso_program_destroy(p);
@@ -401,6 +445,7 @@ iso_status iso_program_destroy(iso_program* p) {
     if (p->d_consts) cudaFree(p->d_consts);
     if (p->d_jump) cudaFree(p->d_jump);
     if (p->d_set) cudaFree(p->d_set);
+    if (p->d_prims) cudaFree(p->d_prims);
     delete p;
     return ISO_OK;
 }

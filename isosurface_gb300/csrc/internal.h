@@ -38,6 +38,11 @@ struct ProgView {
     const float* k;
     const int32_t* jump;  // CD_BEGIN -> index of its CD_END (others 0)
     uint32_t n_ops;
+    // compiled form of a hard union of translated primitives (null: run ops):
+    // two float4 per primitive {centre xyz, type bits}, {parameters}
+    const float4* prims = nullptr;
+    uint32_t nprims = 0;
+    int32_t dom_at = -1;  // constants of a leading domain map, or -1
 };
 
 }  // namespace iso
@@ -109,8 +114,15 @@ struct iso_program {
     bool has_domain = false;
     float domain[6] = {0, 0, 0, 0, 0, 0};
     uint32_t set_at = 0, set_n = 0;
+    // compiled union of translated primitives (see ProgView)
+    std::vector<float> prims;  // 8 floats per primitive
+    float4* d_prims = nullptr;
+    int32_t prim_dom_at = -1;
     uint64_t uid = 0;  // unique per program created in this process
-    iso::ProgView view() const { return iso::ProgView{d_ops, d_consts, d_jump, (uint32_t)ops.size()}; }
+    iso::ProgView view() const {
+        return iso::ProgView{d_ops, d_consts, d_jump, (uint32_t)ops.size(), d_prims, (uint32_t)(prims.size() / 8),
+                             prim_dom_at};
+    }
 };
 
 namespace iso {

@@ -90,29 +90,39 @@ __device__ __forceinline__ V3 pt_apply(uint32_t op, const float* k, V3 p) {
 }
 
 // Scalar evaluation of ops[begin, end) at p (one value left on the stack).
+// The top value and the current point live in registers; only the entries
+// below them are kept in (local-memory) stacks, so a primitive, a binary
+// operator and a point op each touch memory at most once.
 static __device__ __noinline__ float eval_range(const ProgView& pv, uint32_t begin, uint32_t end, V3 p) {
-    float vs[VSTACK];
-    V3 ps[PSTACK];
+    float vs[VSTACK];  // values below the top: vs[0 .. vsp-2]
+    V3 ps[PSTACK];     // points below the current one: ps[0 .. psp-1]
+    float tos = 0.0f;  // top value (vsp > 0)
+    V3 q = p;          // current point
     int vsp = 0, psp = 0;
-    ps[0] = p;
+    auto push = [&](float x) {
+        if (vsp > 0) vs[vsp - 1] = tos;
+        tos = x;
+        ++vsp;
+    };
     for (uint32_t pc = begin; pc < end; ++pc) {
-        uint32_t w = pv.ops[pc];
-        uint32_t op = w & 0xFFu;
+        const uint32_t w = __ldg(pv.ops + pc);
+        const uint32_t op = w & 0xFFu;
         const float* k = pv.k + (w >> 8);
-        V3 q = ps[psp];
         switch (op) {
         case OP_PT_DOMAIN: case OP_PT_TRANSLATE: case OP_PT_RIGID:
-            ps[++psp] = pt_apply(op, k, q);
+            ps[psp++] = q;
+            q = pt_apply(op, k, q);
             break;
-        case OP_PT_POP: --psp; break;
-        case OP_SPHERE: vs[vsp++] = sd_sphere(q, k[0]); break;
-        case OP_BOX: vs[vsp++] = sd_box(q, k[0], k[1], k[2]); break;
-        case OP_CYLINDER: vs[vsp++] = sd_cylinder(q, k[0], k[1]); break;
-        case OP_TORUS: vs[vsp++] = sd_torus(q, k[0], k[1]); break;
-        case OP_UNION: --vsp; vs[vsp - 1] = fminf(vs[vsp - 1], vs[vsp]); break;
-        case OP_INTERSECTION: --vsp; vs[vsp - 1] = fmaxf(vs[vsp - 1], vs[vsp]); break;
-        case OP_DIFFERENCE: --vsp; vs[vsp - 1] = fmaxf(vs[vsp], -vs[vsp - 1]); break;
-        case OP_SMOOTH_UNION: --vsp; vs[vsp - 1] = smooth_min(vs[vsp - 1], vs[vsp], k[0]); break;
+        case OP_PT_POP: q = ps[--psp]; break;
+        case OP_SPHERE: push(sd_sphere(q, k[0])); break;
+        case OP_BOX: push(sd_box(q, k[0], k[1], k[2])); break;
+        case OP_CYLINDER: push(sd_cylinder(q, k[0], k[1])); break;
+        case OP_TORUS: push(sd_torus(q, k[0], k[1])); break;
+        // binary operators: a = the entry below the top, b = the top
+        case OP_UNION: tos = fminf(vs[vsp - 2], tos); --vsp; break;
+        case OP_INTERSECTION: tos = fmaxf(vs[vsp - 2], tos); --vsp; break;
+        case OP_DIFFERENCE: tos = fmaxf(tos, -vs[vsp - 2]); --vsp; break;
+        case OP_SMOOTH_UNION: tos = smooth_min(vs[vsp - 2], tos, k[0]); --vsp; break;
         case OP_SPHERE_SET: {
             uint32_t n = (uint32_t)k[0];
             bool smooth = k[1] != 0.0f;
@@ -123,16 +133,37 @@ static __device__ __noinline__ float eval_range(const ProgView& pv, uint32_t beg
                 float d = vlen(v3(q.x - c[0], q.y - c[1], q.z - c[2])) - c[3];
                 v = (i == 0) ? d : (smooth ? smooth_min(v, d, kk) : fminf(v, d));
             }
-            vs[vsp++] = v;
+            push(v);
             break;
         }
         default: break;  // CD_BEGIN / CD_END are markers in scalar mode
         }
     }
-    return vs[0];
+    return tos;
 }
 
-__device__ __forceinline__ float eval_scalar(const ProgView& pv, V3 p) { return eval_range(pv, 0, pv.n_ops, p); }
+// A hard union of translated primitives (ProgView::prims): the same
+// translate, primitive and fminf operations as the ops, in the same order.
+static __device__ __noinline__ float eval_prims(const ProgView& pv, V3 p) {
+    const V3 q = pv.dom_at >= 0 ? pt_apply(OP_PT_DOMAIN, pv.k + pv.dom_at, p) : p;
+    float v = 0.0f;
+    for (uint32_t i = 0; i < pv.nprims; ++i) {
+        const float4 c = __ldg(pv.prims + 2 * i), a = __ldg(pv.prims + 2 * i + 1);
+        const V3 t = v3(q.x - c.x, q.y - c.y, q.z - c.z);
+        const uint32_t type = __float_as_uint(c.w);
+        float d;
+        if (type == OP_SPHERE) d = sd_sphere(t, a.x);
+        else if (type == OP_BOX) d = sd_box(t, a.x, a.y, a.z);
+        else if (type == OP_CYLINDER) d = sd_cylinder(t, a.x, a.y);
+        else d = sd_torus(t, a.x, a.y);
+        v = (i == 0) ? d : fminf(v, d);
+    }
+    return v;
+}
+
+__device__ __forceinline__ float eval_scalar(const ProgView& pv, V3 p) {
+    return pv.prims ? eval_prims(pv, p) : eval_range(pv, 0, pv.n_ops, p);
+}
 
 // Value and (unnormalised) normal: HermiteSource::sample_normal semantics.
 static __device__ __noinline__ float eval_hermite(const ProgView& pv, V3 p, V3* normal) {

@@ -54,6 +54,10 @@ def _sources():
         "sphere_set": S.unit_to_cube(S.SphereSet(sph)),
         "smooth_set": S.unit_to_cube(S.SphereSet(sph, smooth_k=0.05)),
         "set_nodomain": S.SphereSet(sph * np.float32([0.5, 0.5, 0.5, 0.5]) + np.float32([0.5, 0.5, 0.5, 0])),
+        # a left fold of unions over translated primitives: compiled to a flat list on the device
+        "prim_union": S.unit_to_cube(S.Union(S.Union(S.Union(
+            S.Translate(S.Sphere(0.3), (0.2, -0.1, 0.05)), S.Translate(S.RectangularPrism((0.2, 0.3, 0.15)), (-0.3, 0.2, 0.1))),
+            S.Translate(S.Torus(0.3, 0.08), (0.05, 0.35, -0.3))), S.Translate(S.Cylinder(0.12, 0.4), (-0.2, -0.4, 0.2)))),
     }
 
 
