@@ -636,7 +636,7 @@ static iso_status mc_lattice_passes(iso_ctx* ctx, const Lattice& L, uint32_t fla
     ChunkCountArgs ca{d_grid, nullptr, (uint32_t)chunks, local, rangeagg};
     {
         StageTimer timer(ctx, ISO_STAGE_CLASSIFY);
-        mc_chunk_count<<<nranges, 256, 0, ctx->stream>>>(ca);
+        mc_chunk_count<<<(nranges + 7) / 8, 256, 0, ctx->stream>>>(ca);
         mc_range_scan<<<1, 1024, 0, ctx->stream>>>(rangeagg, nranges, rangepre, totals, local, (uint32_t)chunks,
                                                    ctx->d_err);
     }
@@ -824,7 +824,7 @@ iso_status mc_extract_grids(iso_ctx* ctx, const void* d_grids, uint32_t ngrids, 
     ChunkCountArgs ca{grids, d_range_grid, chunks, local, rangeagg};
     {
         StageTimer timer(ctx, ISO_STAGE_CLASSIFY);
-        mc_chunk_count<<<nranges + 1, 256, 0, ctx->stream>>>(ca);
+        mc_chunk_count<<<(nranges + 1 + 7) / 8, 256, 0, ctx->stream>>>(ca);
         mc_range_scan<<<1, 1024, 0, ctx->stream>>>(rangeagg, nranges, rangepre, totals, local, chunks, ctx->d_err);
     }
     ctx->launches += 2;

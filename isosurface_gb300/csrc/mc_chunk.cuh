@@ -75,59 +75,96 @@ struct ChunkCountArgs {
     uint2* rangeagg;   // per range: (vertices, triangles)
 };
 
-// Pass 1: per-chunk counts and in-range prefixes.  One block per range of
-// 256 chunks, one warp per 32 of them (a single round each); the block scans
-// its eight warps' totals.
+// Pass 1: per-chunk counts and in-range prefixes.  One warp per range of 256
+// chunks, 32 per round (no barrier); the next round's corner words are loaded
+// while this round is counted, so the loads' latency overlaps the counting.
 __global__ void __launch_bounds__(256) mc_chunk_count(ChunkCountArgs A) {
     __shared__ uint8_t s_ntri[256];
     __shared__ uint16_t s_owned[8];
-    __shared__ uint32_t s_segt[8], s_segv[8];
+    __shared__ uint32_t s_tri[8][32];  // per warp: triangles of each of the round's chunks
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     s_ntri[threadIdx.x] = iso_tri_count[threadIdx.x];
     if (threadIdx.x < 8) s_owned[threadIdx.x] = iso_owned_mask[threadIdx.x];
-    const uint32_t range = blockIdx.x;
-    if (range * RANGE > A.chunks) return;  // block-uniform
     __syncthreads();
+    const uint32_t range = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (range * RANGE > A.chunks) return;  // warp-uniform
     const Grid g = A.grids[grid_of_range(A.range_grid, min(range, A.chunks / RANGE - (A.chunks % RANGE == 0)))];
     const uint32_t ncx = g.nx - 1;
-    const uint32_t ch = range * RANGE + warp * 32 + lane;
-    const uint32_t lc = ch - g.chunk0;
-    uint32_t t = 0, v = 0;
-    if (ch < A.chunks && lc < g.nchunks) {
-        const uint32_t row = fdiv(lc, g.div_cw);
-        const uint32_t c = lc - row * g.CW;
-        const uint32_t z = fdiv(row, g.div_ncy);
-        const uint32_t y = row - z * (g.ny - 1);
-        const Corners q = load_corners(g.bits, g.W, g.ny, y, z, c);
-        uint32_t act = active_cells(q, chunk_valid(c, ncx));
+    // corner words of chunk ch (zeros outside the grid)
+    auto fetch = [&](uint32_t ch, uint32_t& y, uint32_t& z, uint32_t& c, bool& in) {
+        const uint32_t lc = ch - g.chunk0;
+        in = ch < A.chunks && lc < g.nchunks;
+        Corners q;
+        if (in) {
+            const uint32_t row = fdiv(lc, g.div_cw);
+            c = lc - row * g.CW;
+            z = fdiv(row, g.div_ncy);
+            y = row - z * (g.ny - 1);
+            q = load_corners(g.bits, g.W, g.ny, y, z, c);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) q.k[k] = 0;
+            y = z = c = 0;
+        }
+        return q;
+    };
+    uint32_t agg_t = 0, agg_v = 0;
+    uint32_t ny_, nz_, nc_;
+    bool nin;
+    Corners qn = fetch(range * RANGE + lane, ny_, nz_, nc_, nin);
+    for (int r = 0; r < RANGE_ROUNDS; ++r) {
+        const uint32_t ch = range * RANGE + r * 32 + lane;
+        const Corners q = qn;
+        const uint32_t y = ny_, z = nz_, c = nc_;
+        const bool in = nin;
+        if (r + 1 < RANGE_ROUNDS) qn = fetch(ch + 32, ny_, nz_, nc_, nin);
+        uint32_t v = 0;
+        const uint32_t act = in ? active_cells(q, chunk_valid(c, ncx)) : 0u;
         if (act) {
-            const int cls = (y == 0 ? 2 : 0) | (z == 0 ? 4 : 0);
-            v = owned_count(q, act, s_owned[cls], s_owned[cls | 1], c == 0 ? 1u : 0u);
-            while (act) {
-                const uint32_t i = __ffs(act) - 1;
-                act &= act - 1;
-                t += s_ntri[case_at(q, i)];
+            if (y > 0 && z > 0) {
+                // interior row: cells own edges 5 (k5^k6), 6 (k6^k7), 10 (k2^k6);
+                // the row's x == 0 cell also owns 7 (k7^k4) and 11 (k3^k7)
+                v = __popc((q.k[5] ^ q.k[6]) & act) + __popc((q.k[6] ^ q.k[7]) & act) + __popc((q.k[2] ^ q.k[6]) & act);
+                if (c == 0 && (act & 1u)) v += ((q.k[7] ^ q.k[4]) & 1u) + ((q.k[3] ^ q.k[7]) & 1u);
+            } else {
+                const int cls = (y == 0 ? 2 : 0) | (z == 0 ? 4 : 0);
+                v = owned_count(q, act, s_owned[cls], s_owned[cls | 1], c == 0 ? 1u : 0u);
             }
         }
-    }
-    const uint32_t ti = warp_incl_scan(t, lane), vi = warp_incl_scan(v, lane);
-    if (lane == 31) {
-        s_segt[warp] = ti;
-        s_segv[warp] = vi;
-    }
-    __syncthreads();
-    uint32_t pt = 0, pv = 0, at = 0, av = 0;
+        // triangles: the round's active cells one per lane (in chunk order),
+        // their counts summed back per chunk in shared memory
+        s_tri[warp][lane] = 0;
+        const uint32_t n = __popc(act);
+        const uint32_t incl = warp_incl_scan(n, lane), excl = incl - n;
+        const uint32_t total = __shfl_sync(FULL, incl, 31);
+        __syncwarp();
+        for (uint32_t b0 = 0; b0 < total; b0 += 32) {
+            const uint32_t kk = b0 + lane;
+            uint32_t src = 0;
 #pragma unroll
-    for (int w = 0; w < 8; ++w) {
-        if (w < warp) {
-            pt += s_segt[w];
-            pv += s_segv[w];
+            for (uint32_t step = 16; step > 0; step >>= 1) {
+                const uint32_t cand = src + step;
+                const uint32_t e = __shfl_sync(FULL, excl, cand & 31);
+                if (cand < 32 && e <= kk) src = cand;
+            }
+            const uint32_t sact = __shfl_sync(FULL, act, src), sexcl = __shfl_sync(FULL, excl, src);
+            Corners cq;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) cq.k[k] = __shfl_sync(FULL, q.k[k], src);
+            if (kk < total) {
+                const uint32_t i = __fns(sact, 0, (int)(kk - sexcl) + 1);
+                atomicAdd(&s_tri[warp][src], (uint32_t)s_ntri[case_at(cq, i)]);
+            }
         }
-        at += s_segt[w];
-        av += s_segv[w];
+        __syncwarp();
+        const uint32_t t = s_tri[warp][lane];
+        __syncwarp();
+        const uint32_t ti = warp_incl_scan(t, lane), vi = warp_incl_scan(v, lane);
+        if (ch <= A.chunks) A.local[ch] = make_uint2(agg_v + vi - v, agg_t + ti - t);
+        agg_t += __shfl_sync(FULL, ti, 31);
+        agg_v += __shfl_sync(FULL, vi, 31);
     }
-    if (ch <= A.chunks) A.local[ch] = make_uint2(pv + vi - v, pt + ti - t);
-    if (threadIdx.x == 0 && range * RANGE < A.chunks) A.rangeagg[range] = make_uint2(av, at);
+    if (lane == 0 && range * RANGE < A.chunks) A.rangeagg[range] = make_uint2(agg_v, agg_t);
 }
 
 // Exclusive scan of the range totals (one block).  rangepre[nr] and totals
