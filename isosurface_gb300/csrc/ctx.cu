@@ -330,6 +330,7 @@ iso_status iso_ctx_destroy(iso_ctx* ctx) {
     }
     for (cudaEvent_t ev : ctx->event_pool) cudaEventDestroy(ev);
     mc_plan_release(ctx);
+    lhmc_plan_release(ctx);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
     return ISO_OK;

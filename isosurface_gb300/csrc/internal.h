@@ -86,6 +86,18 @@ struct iso_ctx {
         uint64_t launches = 0;
     } mc_plan;
     uint64_t mc_last_key[3] = {};  // (program uid, size, flags) of the last eager extraction
+    // the same for LinearHashedMarchingCubes (lhmc.cu), with the counts found
+    struct LhmcPlan {
+        cudaGraphExec_t exec = nullptr;
+        const iso_program* prog = nullptr;
+        uint64_t prog_uid = 0;
+        uint32_t depth = 0, flags = 0;
+        void* bufs[6] = {};
+        std::vector<uint32_t> nref;
+        uint32_t ncubes = 0, nt = 0, nv = 0;
+        uint64_t launches = 0;
+    } lhmc_plan;
+    uint64_t lhmc_last_key[3] = {};
 };
 
 namespace iso {
@@ -164,6 +176,7 @@ iso_status mc_extract_program(iso_ctx* ctx, const iso_program* prog, uint32_t si
 // context's field and sign buffers
 iso_status sample_lattice(iso_ctx* ctx, const iso_program* prog, uint32_t size, Lattice* L);
 void mc_plan_release(iso_ctx* ctx);
+void lhmc_plan_release(iso_ctx* ctx);
 iso_status mc_cases_lattice(iso_ctx* ctx, const Lattice& L, uint8_t* d_cases);
 // PointCloud::extract over a sampled lattice: active-cell centres into the context's mesh
 iso_status point_cloud_lattice(iso_ctx* ctx, const Lattice& L, iso_mesh_info* info);

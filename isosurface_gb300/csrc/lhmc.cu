@@ -29,6 +29,8 @@
 // deterministic.  Keys must fit 31 bits: max_depth <= 10.
 #include <cuda_runtime.h>
 
+#include <cstring>
+
 #include <algorithm>
 #include <vector>
 
@@ -221,6 +223,8 @@ __global__ void oct_eval(GenArgs A) {
     A.vals[A.off + i] = d;
     A.refine[A.off + i] = r ? 1u : 0u;
 }
+
+__global__ void set_root(unsigned long long* keys) { keys[0] = 1ull; }
 
 __global__ void oct_expand(unsigned long long* keys, const uint32_t* refine, const uint32_t* rank, uint32_t off,
                            uint32_t cnt, uint32_t next_off) {
@@ -523,17 +527,31 @@ inline size_t scan_sums_for(uint64_t n) { return (size_t)((n + 1023) / 1024) + 6
 
 }  // namespace
 
+// The counts an extraction discovered: the refined nodes of each generation,
+// the dual cubes, the triangles and vertices.  An eager run fills one; a run
+// recorded into a CUDA graph replays one (queueing everything, synchronising
+// nowhere) and copies each count it computes to pinned memory, so that the
+// replay can be checked against the trace.
+struct LhmcTrace {
+    std::vector<uint32_t> nref;
+    uint32_t ncubes = 0, nt = 0, nv = 0;
+};
+constexpr int LHMC_PIN_GEN = 8;  // h_pinned slots: [0] nt|nv, [2] stale, [3] error flags, [7] ncubes, [8+g] nref
+
 static iso_status lhmc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint32_t max_depth, uint32_t flags,
-                                       iso_mesh_info* info) {
+                                       iso_mesh_info* info, LhmcTrace* trace, const LhmcTrace* replay) {
     if (!ctx || !prog) return ISO_ERR_INVALID_ARG;
     if (prog->ctx != ctx) return fail(ctx, ISO_ERR_INVALID_ARG, "program belongs to another context");
     if (max_depth > 10) return fail(ctx, ISO_ERR_INVALID_ARG, "max_depth above 10 (Morton keys must fit 31 bits)");
     if (flags & ~(uint32_t)ISO_FLAG_KEYS) return fail(ctx, ISO_ERR_INVALID_ARG, "unsupported flags");
     iso_status s = set_device(ctx);
     if (s != ISO_OK) return s;
-    ctx->last = iso_mesh_info{};
-    ctx->last_flags = flags;
-    ctx->last_vertex_floats = 3;
+    const bool rec = replay != nullptr;
+    if (!rec) {
+        ctx->last = iso_mesh_info{};
+        ctx->last_flags = flags;
+        ctx->last_vertex_floats = 3;
+    }
     StageTimer timer(ctx, ISO_STAGE_OCTREE);
     // ---- 1. octree, generation by generation (root, then 8 per refined node)
     uint64_t max_nodes = 1;
@@ -546,8 +564,10 @@ static iso_status lhmc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint3
         }
     }
     // node arrays grow as generations are built
-    size_t node_cap = (size_t)std::min<uint64_t>(max_nodes, 1ull << 20);
     auto node_bytes = [](size_t cap) { return cap * (8 + 4 + 4 + 4) + 4 * scan_sums_for(cap) + 4 * 1024 + 4096; };
+    size_t node_cap = (size_t)std::min<uint64_t>(max_nodes, 1ull << 20);
+    // reuse an arena that earlier extractions grew
+    while (node_cap < max_nodes && node_bytes(2 * node_cap) <= ctx->aux.bytes) node_cap *= 2;
     if ((s = ensure(ctx, ctx->aux, node_bytes(node_cap))) != ISO_OK) return s;
     auto carve = [&](size_t cap, unsigned long long** keys, float** vals, uint32_t** refine, uint32_t** rank,
                      uint32_t** sums, uint32_t** total) {
@@ -563,20 +583,32 @@ static iso_status lhmc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint3
     float* nvals;
     uint32_t *refine, *rank, *sums, *total;
     carve(node_cap, &nkeys, &nvals, &refine, &rank, &sums, &total);
-    unsigned long long root = 1;
-    cudaError_t e = cudaMemcpyAsync(nkeys, &root, 8, cudaMemcpyHostToDevice, ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "root");
-    uint32_t off = 0, cnt = 1;
+    set_root<<<1, 1, 0, ctx->stream>>>(nkeys);
+    ctx->launches++;
+    cudaError_t e = cudaSuccess;
+    uint32_t off = 0, cnt = 1, gen_i = 0;
+    if (trace) *trace = LhmcTrace{};
     while (cnt > 0) {
         GenArgs ga{prog->view(), nkeys, nvals, refine, off, cnt, max_depth};
         oct_eval<<<(cnt + 127) / 128, 128, 0, ctx->stream>>>(ga);
         ctx->launches++;
         if ((s = scan_u32(ctx, refine + off, rank, cnt, sums, total)) != ISO_OK) return s;
         uint32_t nref = 0;
-        if ((s = read_u32(ctx, total, &nref)) != ISO_OK) return s;
+        if (rec) {
+            if (gen_i >= replay->nref.size() || LHMC_PIN_GEN + gen_i >= 512)
+                return fail(ctx, ISO_ERR_INVALID_ARG, "trace shorter than the octree");
+            nref = replay->nref[gen_i];
+            e = cudaMemcpyAsync(ctx->h_pinned + LHMC_PIN_GEN + gen_i, total, 4, cudaMemcpyDeviceToHost, ctx->stream);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "copy count");
+        } else {
+            if ((s = read_u32(ctx, total, &nref)) != ISO_OK) return s;
+            if (trace) trace->nref.push_back(nref);
+        }
+        ++gen_i;
         const uint64_t next = 8ull * nref;
         const uint64_t need = (uint64_t)off + cnt + next;
         if (need >= 0xFFFFFFF0ull) return fail(ctx, ISO_ERR_TOO_LARGE, "octree too large");
+        if (need > node_cap && rec) return fail(ctx, ISO_ERR_INVALID_ARG, "octree arena would grow while recording");
         if (need > node_cap) {
             // grow: copy the built prefix into a larger arena
             const size_t new_cap = (size_t)std::max<uint64_t>(need, 2 * node_cap);
@@ -645,7 +677,14 @@ static iso_status lhmc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint3
     leaf_write<<<(nodes + 255) / 256, 256, 0, ctx->stream>>>(la, offsets, pv_key, pv_level);
     ctx->launches++;
     uint32_t ncubes = 0;
-    if ((s = read_u32(ctx, total2, &ncubes)) != ISO_OK) return s;
+    if (rec) {
+        ncubes = replay->ncubes;
+        e = cudaMemcpyAsync(ctx->h_pinned + 7, total2, 4, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "copy count");
+    } else {
+        if ((s = read_u32(ctx, total2, &ncubes)) != ISO_OK) return s;
+        if (trace) trace->ncubes = ncubes;
+    }
 
     // ---- 3./4. dual cubes and their marching cubes
     const uint32_t hcap2 = pow2_at_least(8ull * ncubes + 1024);
@@ -681,13 +720,25 @@ static iso_status lhmc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint3
     }
     if ((s = scan_u32(ctx, tcount, tbase, ncubes, sums3, tot3)) != ISO_OK) return s;
     if ((s = scan_u32(ctx, vcount, vbase, ncubes, sums3 + scan_sums_for(ncubes), tot3 + 1)) != ISO_OK) return s;
-    e = cudaMemcpyAsync(ctx->h_pinned, tot3, 16, cudaMemcpyDeviceToHost, ctx->stream);
+    e = cudaMemcpyAsync(ctx->h_pinned, tot3, 8, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_pinned + 2, stale, 8, cudaMemcpyDeviceToHost, ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "read totals");
-    if ((s = read_device_errors(ctx)) != ISO_OK) return s;
-    const uint32_t nt = ((uint32_t*)ctx->h_pinned)[0], nv = ((uint32_t*)ctx->h_pinned)[1];
-    ctx->lhmc_stale = ctx->h_pinned[2];
+    uint32_t nt, nv;
+    if (rec) {
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "copy totals");
+        nt = replay->nt;
+        nv = replay->nv;
+    } else {
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "read totals");
+        if ((s = read_device_errors(ctx)) != ISO_OK) return s;
+        nt = ((uint32_t*)ctx->h_pinned)[0];
+        nv = ((uint32_t*)ctx->h_pinned)[1];
+        ctx->lhmc_stale = ctx->h_pinned[2];
+        if (trace) {
+            trace->nt = nt;
+            trace->nv = nv;
+        }
+    }
     const bool keys = (flags & ISO_FLAG_KEYS) != 0;
     if ((s = ensure(ctx, ctx->mesh_v, 12ull * std::max<uint32_t>(nv, 1))) != ISO_OK) return s;
     if ((s = ensure(ctx, ctx->mesh_i, 12ull * std::max<uint32_t>(nt, 1))) != ISO_OK) return s;
@@ -699,6 +750,10 @@ static iso_status lhmc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint3
         cube_emit<<<(ncubes + 127) / 128, 128, 0, ctx->stream>>>(ma);
         ctx->launches++;
         if ((s = check_launch(ctx, "cube_emit")) != ISO_OK) return s;
+    }
+    if (rec) {
+        e = cudaMemcpyAsync(ctx->h_pinned + 3, ctx->d_err, 4, cudaMemcpyDeviceToHost, ctx->stream);
+        return e == cudaSuccess ? ISO_OK : cuda_fail(ctx, e, "copy error flags");
     }
     e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "sync");
@@ -712,11 +767,100 @@ static iso_status lhmc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint3
 
 extern "C" uint64_t iso_lhmc_stale_corners(const iso_ctx* ctx) { return ctx ? ctx->lhmc_stale : 0; }
 
+static void lhmc_buffers(const iso_ctx* ctx, void** b) {
+    const DevBuf* bufs[6] = {&ctx->aux, &ctx->aux2, &ctx->aux3, &ctx->mesh_v, &ctx->mesh_i, &ctx->mesh_k};
+    for (int i = 0; i < 6; ++i) b[i] = bufs[i]->p;
+}
+
+void iso::lhmc_plan_release(iso_ctx* ctx) {
+    if (ctx->lhmc_plan.exec) cudaGraphExecDestroy(ctx->lhmc_plan.exec);
+    ctx->lhmc_plan = iso_ctx::LhmcPlan{};
+}
+
+// LinearHashedMarchingCubes of a program, replaying a recorded CUDA graph when
+// the same (program, depth, flags) repeats: the eager run's counts are baked
+// into the recording (no synchronisation between generations), and every
+// count the replay computes is checked against them before its mesh is
+// used; any difference (or an error flag) falls back to the eager path.
+static iso_status lhmc_planned(iso_ctx* ctx, const iso_program* prog, uint32_t depth, uint32_t flags,
+                               iso_mesh_info* info) {
+    if (!ctx || !prog) return ISO_ERR_INVALID_ARG;
+    iso_ctx::LhmcPlan& P = ctx->lhmc_plan;
+    void* bufs[6];
+    lhmc_buffers(ctx, bufs);
+    if (P.exec && !ctx->timing && P.prog == prog && P.prog_uid == prog->uid && P.depth == depth && P.flags == flags &&
+        std::memcmp(P.bufs, bufs, sizeof(bufs)) == 0 && set_device(ctx) == ISO_OK) {
+        cudaError_t e = cudaGraphLaunch(P.exec, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "octree graph");
+        const uint64_t* h = ctx->h_pinned;
+        bool same = (uint32_t)h[0] == P.nt && (uint32_t)(h[0] >> 32) == P.nv && (uint32_t)h[7] == P.ncubes &&
+                    (uint32_t)h[3] == 0;
+        for (size_t g = 0; same && g < P.nref.size(); ++g) same = (uint32_t)h[LHMC_PIN_GEN + g] == P.nref[g];
+        if (same) {
+            ctx->launches += P.launches;
+            ctx->last = iso_mesh_info{P.nv, P.nt, P.ncubes};
+            ctx->last_flags = flags;
+            ctx->last_vertex_floats = 3;
+            ctx->lhmc_stale = h[2];
+            if (info) *info = ctx->last;
+            return ISO_OK;
+        }
+        if ((uint32_t)h[3]) cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream);
+        lhmc_plan_release(ctx);
+    }
+    LhmcTrace tr;
+    iso_status s = lhmc_extract_impl(ctx, prog, depth, flags, info, &tr, nullptr);
+    if (s != ISO_OK) return s;
+    const uint64_t key[3] = {prog->uid, depth, flags};
+    const bool repeat = std::memcmp(key, ctx->lhmc_last_key, sizeof(key)) == 0;
+    std::memcpy(ctx->lhmc_last_key, key, sizeof(key));
+    if (ctx->timing || !repeat || tr.nref.size() + LHMC_PIN_GEN >= 512) return ISO_OK;
+    // record the same extraction with the counts just found
+    lhmc_plan_release(ctx);
+    const uint64_t launches0 = ctx->launches;
+    const iso_mesh_info keep = ctx->last;
+    const uint64_t keep_stale = ctx->lhmc_stale;
+    if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return ISO_OK;
+    }
+    ctx->capturing = true;
+    iso_status rs = lhmc_extract_impl(ctx, prog, depth, flags, nullptr, nullptr, &tr);
+    ctx->capturing = false;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    const uint64_t recorded = ctx->launches - launches0;
+    ctx->launches = launches0;
+    ctx->last = keep;
+    ctx->lhmc_stale = keep_stale;
+    if (rs == ISO_OK && e == cudaSuccess && g) {
+        cudaGraphExec_t exec = nullptr;
+        if (cudaGraphInstantiate(&exec, g, 0) == cudaSuccess) {
+            P.exec = exec;
+            P.prog = prog;
+            P.prog_uid = prog->uid;
+            P.depth = depth;
+            P.flags = flags;
+            lhmc_buffers(ctx, P.bufs);
+            P.nref = tr.nref;
+            P.ncubes = tr.ncubes;
+            P.nt = tr.nt;
+            P.nv = tr.nv;
+            P.launches = recorded;
+        }
+    }
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    ctx->last_error.clear();
+    return ISO_OK;
+}
+
 // ISO_FLAG_NORMALS: the *InterleavedNormals sinks, sample_normal at every vertex
 extern "C" iso_status iso_lhmc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t max_depth, uint32_t flags, iso_mesh_info* info) {
     if (!ctx || !prog) return ISO_ERR_INVALID_ARG;
     if (flags & ~(uint32_t)(ISO_FLAG_KEYS | ISO_FLAG_NORMALS)) return fail(ctx, ISO_ERR_INVALID_ARG, "unsupported flags");
-    iso_status s = lhmc_extract_impl(ctx, prog, max_depth, flags & ~(uint32_t)ISO_FLAG_NORMALS, info);
+    iso_status s = lhmc_planned(ctx, prog, max_depth, flags & ~(uint32_t)ISO_FLAG_NORMALS, info);
     if (s != ISO_OK || !(flags & ISO_FLAG_NORMALS)) return s;
     return attach_normals(ctx, prog);
 }

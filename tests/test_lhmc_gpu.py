@@ -96,3 +96,23 @@ def test_lhmc_interleaved_normals(ctx):
     assert np.array_equal(got.indices, plain.indices)
     o = oracle.Program(S.lower(src))
     assert np.array_equal(got.vertices[:, 3:], o.sample_normal(plain.vertices))
+
+
+def test_lhmc_repeated_extractions_replay(ctx):
+    """The same (program, depth) twice in a row is recorded as one CUDA graph
+    with its counts; replays must give the eager run's bytes, also after
+    another program in between and with keys."""
+    src = scenes.csg()
+    prog = ctx.program(src)
+    first = ctx.download(ctx.lhmc_extract(prog, 6))
+    for _ in range(4):  # eager, eager + record, replay, replay
+        got = ctx.download(ctx.lhmc_extract(prog, 6))
+        assert np.array_equal(got.vertices, first.vertices)
+        assert np.array_equal(got.indices, first.indices)
+    ctx.lhmc_extract(scenes.sphere(), 6)
+    for _ in range(3):
+        got = ctx.download(ctx.lhmc_extract(prog, 6, keys=True), keys=True)
+        assert np.array_equal(got.vertices, first.vertices)
+        assert np.array_equal(got.indices, first.indices)
+    want = oracle.Program(S.lower(src)).lhmc(6)
+    assert len(got.indices) == len(want.indices)
