@@ -339,14 +339,10 @@ def main():
         return
 
     import torch
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from isosurface_gb300 import replicas
+    world, rank, local = replicas.rank_env()
     torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    dist = replicas.init("nccl")
 
     from isosurface_gb300 import build as gbuild
     gbuild.build()
@@ -400,12 +396,8 @@ def main():
     lib().iso_ctx_stage_times(ctx.h, ms_buf, ln_buf)
     lib().iso_ctx_enable_stage_timing(ctx.h, 0)
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    ms = sum(step_ms) / len(step_ms)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * CELLS / (ms / 1e3)
+    ms = replicas.max_over_ranks(sum(step_ms) / len(step_ms), dist, "cuda")
+    value = replicas.whole_job_rate(CELLS, world, ms / 1e3)
 
     # per-stage device time (CUDA events on the launching stream) and roofline
     stages = {"sample": 0, "classify_scan": 1, "emit": 2}
@@ -463,12 +455,8 @@ def main():
         mi = e2e_step()
         e2e_times.append(time.perf_counter() - t0)
     barrier()
-    e2e_s = sum(e2e_times) / len(e2e_times)
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": world * CELLS / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": len(src_bytes),
+    e2e_s = replicas.max_over_ranks(sum(e2e_times) / len(e2e_times), dist, "cuda")
+    e2e = {"value": replicas.whole_job_rate(CELLS, world, e2e_s), "unit": "cells/s", "h2d_bytes_per_step": len(src_bytes),
            "d2h_bytes_per_step": 12 * mi.num_vertices + 12 * mi.num_triangles, "ms_per_step": 1e3 * e2e_s}
 
     secondary = None
