@@ -236,7 +236,7 @@ struct ChunkEmitArgs {
     uint64_t* out_k;
     uint64_t cap_v, cap_t;
     uint32_t* err;
-    uint32_t* edge_id;  // mc_cell_emit: vertex id per lattice edge, (lattice point * 3 + axis)
+    uint32_t* edge_id;  // mc_cell_emit: vertex id per lattice edge, keyed by (upper end point * 3 + axis)
 };
 
 __device__ __forceinline__ uint2 chunk_base(const ChunkEmitArgs& A, uint32_t ch) {
@@ -490,19 +490,46 @@ __global__ void __launch_bounds__(256) mc_block_emit(ChunkEmitArgs A, uint32_t m
     }
 }
 
-// Pass 2, cell-parallel.  Persistent blocks of 8 warps copy the tables to
-// shared memory once; each warp then takes whole ranges of 256 chunks, 32
-// chunks per round (lane = chunk).  The round's active cells are handed out
-// 32 at a time in chunk order (lane = cell: the owning chunk by a shuffle
-// search over the chunks' exclusive counts, the bit by __fns), so lanes stay
-// busy however the active cells are spread.  A cell's own output offsets are
-// the range's base plus a running warp scan of owned-vertex and triangle
-// counts in cell order (the reference's emission order).  Every owned vertex
-// also records its id in a dense per-lattice-edge map, and triangles are
-// written as lattice edge indices; mc_resolve_ids then replaces each index by
-// the id its owner recorded (no owner lookup in this pass; the map needs no
-// initialisation: every crossing edge has an owner, and only crossing edges
-// are referenced).
+// One vertex on lattice edge (pa, pb) with values (fa, fb): the crossing
+// point (Signed::find_crossing_point, distance.rs:64-69), its optional lattice
+// edge key (lower end point * 3 + axis), and its grid-local id in the edge map
+// under ``key``.
+__device__ __forceinline__ void put_vertex(const ChunkEmitArgs& A, const Grid& g, float fa, float fb, float pax,
+                                           float pay, float paz, float pbx, float pby, float pbz, uint32_t vid,
+                                           uint32_t key, uint32_t grid_v0, uint32_t lx, uint32_t ly, uint32_t lz,
+                                           uint32_t ax) {
+    const float delta = fb - fa;
+    const float tt = (delta == 0.0f) ? 0.5f : -fa / delta;
+    const float omt = 1.0f - tt;
+    if (vid < A.cap_v) {
+        A.out_v[3 * (size_t)vid + 0] = pax * omt + pbx * tt;
+        A.out_v[3 * (size_t)vid + 1] = pay * omt + pby * tt;
+        A.out_v[3 * (size_t)vid + 2] = paz * omt + pbz * tt;
+        if (A.out_k) {
+            A.out_k[2 * (size_t)vid] = (((uint64_t)lz * g.ny + ly) * g.nx + lx) * 3 + ax;
+            A.out_k[2 * (size_t)vid + 1] = 0;
+        }
+    } else {
+        atomicOr(A.err, DERR_CAPACITY);
+    }
+    A.edge_id[key] = vid - grid_v0;
+}
+
+// Pass 2, cell-parallel, for lattices given by values alone (no explicit
+// sample positions) whose edge count fits 32 bits.  Each warp takes one
+// segment of 32 chunks (lane = chunk: corner words and active cells).  The
+// segment's active cells are handed out 32 at a time in chunk order (lane =
+// cell: the owning chunk by a shuffle search over the chunks' exclusive
+// counts, the bit by __fns), so lanes stay busy however the active cells are
+// spread.  A cell's output offsets are the segment's base plus a running warp
+// scan of owned-vertex and triangle counts in cell order (the reference's
+// emission order).  Every owned vertex records its grid-local id in a dense
+// per-lattice-edge map, and triangles are written as map keys; mc_resolve_ids
+// then replaces each key by the id its owner recorded (no owner lookup in this
+// pass; the map needs no initialisation: every crossing edge has an owner, and
+// only crossing edges are referenced).  Keys are 3 * (upper end point) + axis,
+// so the (at most three) edges an interior cell owns, which all end at its
+// corner 6, share one 12-byte slot.
 __global__ void __launch_bounds__(256, 5) mc_cell_emit(ChunkEmitArgs A, uint32_t nranges) {
     const int lane = threadIdx.x & 31;
     const uint32_t seg = blockIdx.x * 8 + (threadIdx.x >> 5);  // 32 chunks per warp
@@ -516,7 +543,6 @@ __global__ void __launch_bounds__(256, 5) mc_cell_emit(ChunkEmitArgs A, uint32_t
     if (chunk_base(A, g.chunk0 + c_end).y == bb.y) return;  // no triangle in these chunks
     const uint32_t CW = g.CW, ncx = g.nx - 1, ncy = g.ny - 1;
     const uint32_t grid_v0 = chunk_base(A, g.chunk0).x;
-    const bool explicit_pos = g.positions != nullptr;
     uint32_t vcarry = bb.x, tcarry = bb.y;  // global offsets of the next cell's outputs
     {
         {
@@ -537,6 +563,15 @@ __global__ void __launch_bounds__(256, 5) mc_cell_emit(ChunkEmitArgs A, uint32_t
             const uint32_t n = __popc(act);
             const uint32_t incl = warp_incl_scan(n, lane), excl = incl - n;
             const uint32_t total = __shfl_sync(FULL, incl, 31);
+            // lane e < 12: edge-map key of cell edge e relative to 3 * (corner 0's
+            // lattice point); an edge's key is 3 * (its upper end point) + axis
+            uint32_t koff = 0;
+            if (lane < 12) {
+                const uint32_t ax = __ldg(&g_edge_axis[lane]);
+                const uint32_t hx = __ldg(&g_edge_lo[lane][0]) + (ax == 0), hy = __ldg(&g_edge_lo[lane][1]) + (ax == 1),
+                               hz = __ldg(&g_edge_lo[lane][2]) + (ax == 2);
+                koff = 3 * (hx + g.nx * (hy + g.ny * hz)) + ax;
+            }
             for (uint32_t b0 = 0; b0 < total; b0 += 32) {
                 // lane = cell number b0 + lane of these chunks, in chunk order
                 const uint32_t kk = b0 + lane;
@@ -571,63 +606,69 @@ __global__ void __launch_bounds__(256, 5) mc_cell_emit(ChunkEmitArgs A, uint32_t
                 const uint32_t vstart = vcarry + vi - nown, tstart = tcarry + ti - nt;
                 vcarry += __shfl_sync(FULL, vi, 31);
                 tcarry += __shfl_sync(FULL, ti, 31);
-                if (!have) continue;
-                const uint32_t own = __ldg(&iso_owned_mask[cls]);
-                const uint64_t ord = __ldg(&iso_edge_order[cs]);
-                const uint32_t ne = __ldg(&iso_edge_count[cs]);
-                const uint32_t cell = (z * g.ny + y) * g.nx + x;  // lattice point of corner 0
-                uint32_t r = 0;
-                for (uint32_t k = 0; k < ne; ++k) {
-                    const uint32_t e = (uint32_t)(ord >> (4 * k)) & 15u;
-                    if (!((own >> e) & 1u)) continue;  // its owner (an earlier cell) records the id
-                    const uint32_t lx = x + __ldg(&g_edge_lo[e][0]), ly = y + __ldg(&g_edge_lo[e][1]), lz = z + __ldg(&g_edge_lo[e][2]);
-                    const uint32_t idx = ((lz * g.ny + ly) * g.nx + lx) * 3 + __ldg(&g_edge_axis[e]);
-                    // owned: this cell writes the vertex (first use in visit order)
-                    const uint32_t u = __ldg(&iso_edge_connection[e][0]), v = __ldg(&iso_edge_connection[e][1]);
-                    const uint32_t ux = x + __ldg(&iso_corners[u][0]), uy = y + __ldg(&iso_corners[u][1]), uz = z + __ldg(&iso_corners[u][2]);
-                    const uint32_t vx = x + __ldg(&iso_corners[v][0]), vy = y + __ldg(&iso_corners[v][1]), vz = z + __ldg(&iso_corners[v][2]);
-                    const float fa = __ldg(g.values + ((size_t)uz * g.ny + uy) * g.pitch + ux);
-                    const float fb = __ldg(g.values + ((size_t)vz * g.ny + vy) * g.pitch + vx);
-                    float pax, pay, paz, pbx, pby, pbz;
-                    if (explicit_pos) {
-                        const float4 qa = __ldg(g.positions + ((size_t)uz * g.ny + uy) * g.nx + ux);
-                        const float4 qb = __ldg(g.positions + ((size_t)vz * g.ny + vy) * g.nx + vx);
-                        pax = qa.x; pay = qa.y; paz = qa.z; pbx = qb.x; pby = qb.y; pbz = qb.z;
-                    } else {
-                        pax = (float)ux * g.inv; pay = (float)uy * g.inv; paz = (float)uz * g.inv;
-                        pbx = (float)vx * g.inv; pby = (float)vy * g.inv; pbz = (float)vz * g.inv;
-                    }
-                    // Signed::find_crossing_point (distance.rs:64-69)
-                    const float delta = fb - fa;
-                    const float tt = (delta == 0.0f) ? 0.5f : -fa / delta;
-                    const float omt = 1.0f - tt;
-                    const uint32_t vid = vstart + r;
-                    ++r;
-                    if (vid < A.cap_v) {
-                        A.out_v[3 * (size_t)vid + 0] = pax * omt + pbx * tt;
-                        A.out_v[3 * (size_t)vid + 1] = pay * omt + pby * tt;
-                        A.out_v[3 * (size_t)vid + 2] = paz * omt + pbz * tt;
-                        if (A.out_k) {
-                            A.out_k[2 * (size_t)vid] = (((uint64_t)lz * g.ny + ly) * g.nx + lx) * 3 + __ldg(&g_edge_axis[e]);
-                            A.out_k[2 * (size_t)vid + 1] = 0;
-                        }
-                    } else {
-                        atomicOr(A.err, DERR_CAPACITY);
-                    }
-                    A.edge_id[idx] = vid - grid_v0;
+                uint32_t own = 0, cell = 0;
+                uint64_t tedges = 0;
+                if (have) {
+                    own = (uint32_t)__ldg(&iso_edge_mask[cs]) & __ldg(&iso_owned_mask[cls]);
+                    tedges = __ldg(&iso_tri_edges[cs]);
+                    cell = (z * g.ny + y) * g.nx + x;  // lattice point of corner 0
                 }
-                // triangles (march_cube, marching_cubes_impl.rs:102-117) as lattice
-                // edge indices: corner 0's lattice point plus the edge's lower end
-                const uint64_t tedges = __ldg(&iso_tri_edges[cs]);
-                if ((uint64_t)tstart + nt <= A.cap_t) {
-                    for (uint32_t k = 0; k < 3 * nt; ++k) {
-                        const uint32_t e = (uint32_t)(tedges >> (4 * k)) & 15u;
-                        const uint32_t off = __ldg(&g_edge_lo[e][0]) + g.nx * (__ldg(&g_edge_lo[e][1]) +
-                                                                              g.ny * __ldg(&g_edge_lo[e][2]));
-                        A.out_i[3 * (size_t)tstart + k] = (cell + off) * 3 + __ldg(&g_edge_axis[e]);
+                if (own) {
+                    // owned edges: this cell creates their vertices, numbered by
+                    // first use in the cell's visit order (rank table)
+                    const uint64_t rk = __ldg(&iso_owned_rank[cls][cs]);
+                    if (cls == 0) {
+                        // interior cell: its owned edges are among 5, 6 and 10, the
+                        // three edges ending at corner 6 = (x+1, y+1, z+1); all their
+                        // values are loaded before any vertex is formed
+                        const float* v6 = g.values + ((size_t)(z + 1) * g.ny + (y + 1)) * g.pitch + (x + 1);
+                        const bool e5 = (own >> 5) & 1u, e6 = (own >> 6) & 1u, e10 = (own >> 10) & 1u;
+                        const float f6 = __ldg(v6);
+                        const float f5 = e5 ? __ldg(v6 - g.pitch) : 0.0f;                    // corner 5
+                        const float f7 = e6 ? __ldg(v6 - 1) : 0.0f;                          // corner 7
+                        const float f2 = e10 ? __ldg(v6 - (size_t)g.ny * g.pitch) : 0.0f;    // corner 2
+                        const float X0 = (float)x * g.inv, X1 = (float)(x + 1) * g.inv;
+                        const float Y0 = (float)y * g.inv, Y1 = (float)(y + 1) * g.inv;
+                        const float Z0 = (float)z * g.inv, Z1 = (float)(z + 1) * g.inv;
+                        const uint32_t k6 = 3 * (cell + g.nx * (g.ny + 1) + 1);  // corner 6's key base
+                        if (e5)  // corners 5 -> 6, y axis
+                            put_vertex(A, g, f5, f6, X1, Y0, Z1, X1, Y1, Z1, vstart + (uint32_t)(rk >> 20 & 15u),
+                                       k6 + 1, grid_v0, x + 1, y, z + 1, 1);
+                        if (e6)  // corners 6 -> 7, x axis
+                            put_vertex(A, g, f6, f7, X1, Y1, Z1, X0, Y1, Z1, vstart + (uint32_t)(rk >> 24 & 15u),
+                                       k6 + 0, grid_v0, x, y + 1, z + 1, 0);
+                        if (e10)  // corners 2 -> 6, z axis
+                            put_vertex(A, g, f2, f6, X1, Y1, Z0, X1, Y1, Z1, vstart + (uint32_t)(rk >> 40 & 15u),
+                                       k6 + 2, grid_v0, x + 1, y + 1, z, 2);
+                    } else {
+                        for (uint32_t m = own; m; m &= m - 1) {
+                            const uint32_t e = __ffs(m) - 1;
+                            const uint32_t ax = __ldg(&g_edge_axis[e]);
+                            const uint32_t lx = x + __ldg(&g_edge_lo[e][0]), ly = y + __ldg(&g_edge_lo[e][1]),
+                                           lz = z + __ldg(&g_edge_lo[e][2]);
+                            const uint32_t hx = lx + (ax == 0), hy = ly + (ax == 1), hz = lz + (ax == 2);
+                            const uint32_t u = __ldg(&iso_edge_connection[e][0]), v = __ldg(&iso_edge_connection[e][1]);
+                            const uint32_t ux = x + __ldg(&iso_corners[u][0]), uy = y + __ldg(&iso_corners[u][1]),
+                                           uz = z + __ldg(&iso_corners[u][2]);
+                            const uint32_t vx = x + __ldg(&iso_corners[v][0]), vy = y + __ldg(&iso_corners[v][1]),
+                                           vz = z + __ldg(&iso_corners[v][2]);
+                            const float fa = __ldg(g.values + ((size_t)uz * g.ny + uy) * g.pitch + ux);
+                            const float fb = __ldg(g.values + ((size_t)vz * g.ny + vy) * g.pitch + vx);
+                            put_vertex(A, g, fa, fb, (float)ux * g.inv, (float)uy * g.inv, (float)uz * g.inv,
+                                       (float)vx * g.inv, (float)vy * g.inv, (float)vz * g.inv,
+                                       vstart + (uint32_t)(rk >> (4 * e) & 15u), ((hz * g.ny + hy) * g.nx + hx) * 3 + ax,
+                                       grid_v0, lx, ly, lz, ax);
+                        }
                     }
-                } else {
-                    atomicOr(A.err, DERR_CAPACITY);
+                }
+                // triangles (march_cube, marching_cubes_impl.rs:102-117) as edge-map
+                // keys, resolved to vertex ids once every owner has written its ids
+                const bool tfit = (uint64_t)tstart + nt <= A.cap_t;
+                if (have && !tfit) atomicOr(A.err, DERR_CAPACITY);
+                const uint32_t kmax = __reduce_max_sync(FULL, 3 * nt);
+                for (uint32_t k = 0; k < kmax; ++k) {
+                    const uint32_t ko = __shfl_sync(FULL, koff, (uint32_t)(tedges >> (4 * k)) & 15u);
+                    if (k < 3 * nt && tfit) A.out_i[3 * (size_t)tstart + k] = 3 * cell + ko;
                 }
             }
         }
