@@ -565,11 +565,6 @@ iso_status mc_cases_lattice(iso_ctx* ctx, const Lattice& L, uint8_t* d_cases) {
 namespace {
 __global__ void write_grid(Grid* dst, Grid g) { *dst = g; }
 
-// persistent grid for mc_cell_emit: a few blocks of 8 warps per SM, each warp
-// taking whole ranges
-unsigned emit_blocks(uint32_t nranges) {
-    return (unsigned)std::max<uint64_t>(1, nranges);  // 8 warps = one range of 256 chunks per block
-}
 
 // cudaFuncSetAttribute only when the size grows (per device; it costs a host round trip)
 cudaError_t emit_smem_attribute(size_t smem) {
@@ -613,6 +608,7 @@ static iso_status mc_lattice_passes(iso_ctx* ctx, const Lattice& L, uint32_t fla
     const size_t smem = block_emit_smem(CW);
     if (smem > 220 * 1024) return fail(ctx, ISO_ERR_INVALID_ARG, "rows too long for the emit pass");
     iso_status s;
+    // per-chunk prefixes (block emit) or per-segment records (cell emit)
     if ((s = ensure(ctx, ctx->rowtri, 8 * (chunks + 1))) != ISO_OK) return s;
     if ((s = ensure(ctx, ctx->scan, 16 * (size_t)nranges + 64 + sizeof(Grid) + 256)) != ISO_OK) return s;
     const bool keys = (flags & ISO_FLAG_KEYS) != 0;
@@ -632,13 +628,20 @@ static iso_status mc_lattice_passes(iso_ctx* ctx, const Lattice& L, uint32_t fla
     Grid* d_grid = (Grid*)(((uintptr_t)(totals + 4) + 255) & ~(uintptr_t)255);
     cudaError_t e = emit_smem_attribute(smem);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "emit smem attribute");
+    // the cell emit reads one record per 32-chunk segment; the block emit
+    // needs every chunk's prefix
+    const uint32_t nsegs = (uint32_t)((chunks + 31) / 32);
+    uint4* segs = edge_map ? (uint4*)ctx->rowtri.p : nullptr;
     write_grid<<<1, 1, 0, ctx->stream>>>(d_grid, make_grid(L, 0));
-    ChunkCountArgs ca{d_grid, nullptr, (uint32_t)chunks, local, rangeagg};
     {
         StageTimer timer(ctx, ISO_STAGE_CLASSIFY);
-        mc_chunk_count<<<(nranges + 7) / 8, 256, 0, ctx->stream>>>(ca);
-        mc_range_scan<<<1, 1024, 0, ctx->stream>>>(rangeagg, nranges, rangepre, totals, local, (uint32_t)chunks,
-                                                   ctx->d_err);
+        ChunkCountArgs ca{d_grid, nullptr, (uint32_t)chunks, edge_map ? nullptr : local, rangeagg, segs};
+        if (edge_map)
+            mc_chunk_count<true><<<(nranges + 7) / 8, 256, 0, ctx->stream>>>(ca);
+        else
+            mc_chunk_count<false><<<(nranges + 7) / 8, 256, 0, ctx->stream>>>(ca);
+        mc_range_scan<<<1, 1024, 0, ctx->stream>>>(rangeagg, nranges, rangepre, totals, edge_map ? nullptr : local,
+                                                   (uint32_t)chunks, ctx->d_err);
     }
     ctx->launches += 3;
     if ((s = check_launch(ctx, "mc_chunk_count")) != ISO_OK) return s;
@@ -651,8 +654,8 @@ static iso_status mc_lattice_passes(iso_ctx* ctx, const Lattice& L, uint32_t fla
         {
             StageTimer timer(ctx, ISO_STAGE_EMIT);
             if (edge_map) {
-                mc_cell_emit<<<emit_blocks(nranges), 256, 0, ctx->stream>>>(ea, nranges);
-                mc_resolve_ids<<<std::min<unsigned>(emit_blocks(nranges), 4096), 256, 0, ctx->stream>>>(
+                mc_cell_emit<<<(nsegs + 7) / 8, 256, 0, ctx->stream>>>(ea, segs, nsegs);
+                mc_resolve_ids<<<resolve_blocks(cap_t), 256, 0, ctx->stream>>>(
                     (uint32_t*)ctx->mesh_i.p, totals, cap_t, (const uint32_t*)ctx->edges.p, (uint32_t)nedges);
                 ctx->launches++;
             } else {
@@ -821,10 +824,10 @@ iso_status mc_extract_grids(iso_ctx* ctx, const void* d_grids, uint32_t ngrids, 
     uint2* rangeagg = local + ((chunks + 1 + 31) & ~31u);
     uint2* rangepre = rangeagg + nranges;
     const Grid* grids = (const Grid*)d_grids;
-    ChunkCountArgs ca{grids, d_range_grid, chunks, local, rangeagg};
+    ChunkCountArgs ca{grids, d_range_grid, chunks, local, rangeagg, nullptr};
     {
         StageTimer timer(ctx, ISO_STAGE_CLASSIFY);
-        mc_chunk_count<<<(nranges + 1 + 7) / 8, 256, 0, ctx->stream>>>(ca);
+        mc_chunk_count<false><<<(nranges + 1 + 7) / 8, 256, 0, ctx->stream>>>(ca);
         mc_range_scan<<<1, 1024, 0, ctx->stream>>>(rangeagg, nranges, rangepre, totals, local, chunks, ctx->d_err);
     }
     ctx->launches += 2;

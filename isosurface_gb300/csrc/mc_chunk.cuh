@@ -71,13 +71,17 @@ struct ChunkCountArgs {
     const Grid* grids;
     const uint32_t* range_grid;
     uint32_t chunks;   // global (padded) chunk count
-    uint2* local;      // chunks + 1: (vertex, triangle) exclusive prefix inside the range
+    uint2* local;      // chunk mode: chunks + 1 (vertex, triangle) exclusive prefixes inside the range
     uint2* rangeagg;   // per range: (vertices, triangles)
+    uint4* segs;       // segment mode: per 32 chunks (first vertex, first triangle) inside the range,
+                       // (vertices, triangles)
 };
 
-// Pass 1: per-chunk counts and in-range prefixes.  One warp per range of 256
-// chunks, 32 per round (no barrier); the next round's corner words are loaded
-// while this round is counted, so the loads' latency overlaps the counting.
+// Pass 1: per-chunk (SEG = false) or per-segment (32 chunks, SEG = true)
+// counts and in-range prefixes.  One warp per range of 256 chunks, 32 per
+// round (no barrier); the next round's corner words are loaded while this
+// round is counted, so the loads' latency overlaps the counting.
+template <bool SEG>
 __global__ void __launch_bounds__(256) mc_chunk_count(ChunkCountArgs A) {
     __shared__ uint8_t s_ntri[256];
     __shared__ uint16_t s_owned[8];
@@ -132,12 +136,14 @@ __global__ void __launch_bounds__(256) mc_chunk_count(ChunkCountArgs A) {
             }
         }
         // triangles: the round's active cells one per lane (in chunk order),
-        // their counts summed back per chunk in shared memory
-        s_tri[warp][lane] = 0;
+        // their counts summed back per chunk in shared memory (chunk mode) or
+        // over the round (segment mode)
+        if (!SEG) s_tri[warp][lane] = 0;
+        uint32_t tl = 0;
         const uint32_t n = __popc(act);
         const uint32_t incl = warp_incl_scan(n, lane), excl = incl - n;
         const uint32_t total = __shfl_sync(FULL, incl, 31);
-        __syncwarp();
+        if (!SEG) __syncwarp();
         for (uint32_t b0 = 0; b0 < total; b0 += 32) {
             const uint32_t kk = b0 + lane;
             uint32_t src = 0;
@@ -153,8 +159,18 @@ __global__ void __launch_bounds__(256) mc_chunk_count(ChunkCountArgs A) {
             for (int k = 0; k < 8; ++k) cq.k[k] = __shfl_sync(FULL, q.k[k], src);
             if (kk < total) {
                 const uint32_t i = __fns(sact, 0, (int)(kk - sexcl) + 1);
-                atomicAdd(&s_tri[warp][src], (uint32_t)s_ntri[case_at(cq, i)]);
+                if (SEG)
+                    tl += s_ntri[case_at(cq, i)];
+                else
+                    atomicAdd(&s_tri[warp][src], (uint32_t)s_ntri[case_at(cq, i)]);
             }
+        }
+        if (SEG) {
+            const uint32_t vr = __reduce_add_sync(FULL, v), tr = __reduce_add_sync(FULL, tl);
+            if (lane == 0 && ch - lane < A.chunks) A.segs[ch / 32] = make_uint4(agg_v, agg_t, vr, tr);
+            agg_v += vr;
+            agg_t += tr;
+            continue;
         }
         __syncwarp();
         const uint32_t t = s_tri[warp][lane];
@@ -167,21 +183,29 @@ __global__ void __launch_bounds__(256) mc_chunk_count(ChunkCountArgs A) {
     if (lane == 0 && range * RANGE < A.chunks) A.rangeagg[range] = make_uint2(agg_v, agg_t);
 }
 
-// Exclusive scan of the range totals (one block).  rangepre[nr] and totals
-// receive the grand totals; local[chunks] is cleared when `chunks` starts a
-// range that no warp counted.
+// Exclusive scan of the range totals (one block).  Each thread holds
+// SCAN_ITEMS consecutive ranges per pass (all loaded before any is used), so
+// 8K ranges take one pass of one block scan.  rangepre[nr] and totals
+// receive the grand totals; local[chunks] (chunk mode) is cleared when
+// `chunks` starts a range that no warp counted.
+constexpr int SCAN_ITEMS = 8;
+
 __global__ void __launch_bounds__(1024) mc_range_scan(const uint2* rangeagg, uint32_t nr, uint2* rangepre,
                                                       uint64_t* totals, uint2* local, uint32_t chunks, uint32_t* err) {
     __shared__ uint64_t s_wv[32], s_wt[32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint64_t carry_t = 0, carry_v = 0;
-    uint2 next = threadIdx.x < nr ? rangeagg[threadIdx.x] : make_uint2(0, 0);
-    for (uint32_t base = 0; base < nr; base += 1024) {
-        const uint32_t i = base + threadIdx.x;
-        const uint2 a = next;
-        // the next round's load overlaps this round's scan
-        next = i + 1024 < nr ? rangeagg[i + 1024] : make_uint2(0, 0);
-        uint64_t vi = a.x, ti = a.y;
+    for (uint32_t base = 0; base < nr; base += 1024 * SCAN_ITEMS) {
+        const uint32_t i0 = base + threadIdx.x * SCAN_ITEMS;
+        uint2 a[SCAN_ITEMS];
+        uint32_t sv = 0, st = 0;  // a range holds at most 256 * 32 * 5 triangles
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; ++k) {
+            a[k] = i0 + k < nr ? rangeagg[i0 + k] : make_uint2(0, 0);
+            sv += a[k].x;
+            st += a[k].y;
+        }
+        uint64_t vi = sv, ti = st;
         for (int o = 1; o < 32; o <<= 1) {
             const uint64_t tv = __shfl_up_sync(FULL, vi, o), tt = __shfl_up_sync(FULL, ti, o);
             if (lane >= o) {
@@ -207,11 +231,16 @@ __global__ void __launch_bounds__(1024) mc_range_scan(const uint2* rangeagg, uin
             s_wt[lane] = wt;
         }
         __syncthreads();
-        const uint64_t bv = warp ? s_wv[warp - 1] : 0, bt = warp ? s_wt[warp - 1] : 0;
-        const uint64_t ev = carry_v + bv + vi - a.x, et = carry_t + bt + ti - a.y;
-        if (i < nr) {
-            if (ev > 0xFFFFFFFFull || et > 0xFFFFFFFFull) atomicOr(err, DERR_CAPACITY);
-            rangepre[i] = make_uint2((uint32_t)ev, (uint32_t)et);
+        uint64_t ev = carry_v + (warp ? s_wv[warp - 1] : 0) + vi - sv;
+        uint64_t et = carry_t + (warp ? s_wt[warp - 1] : 0) + ti - st;
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; ++k) {
+            if (i0 + k < nr) {
+                if (ev > 0xFFFFFFFFull || et > 0xFFFFFFFFull) atomicOr(err, DERR_CAPACITY);
+                rangepre[i0 + k] = make_uint2((uint32_t)ev, (uint32_t)et);
+            }
+            ev += a[k].x;
+            et += a[k].y;
         }
         carry_v += s_wv[31];
         carry_t += s_wt[31];
@@ -221,7 +250,7 @@ __global__ void __launch_bounds__(1024) mc_range_scan(const uint2* rangeagg, uin
         totals[0] = carry_t;
         totals[1] = carry_v;
         rangepre[nr] = make_uint2((uint32_t)carry_v, (uint32_t)carry_t);
-        if (chunks % RANGE == 0) local[chunks] = make_uint2(0, 0);
+        if (local && chunks % RANGE == 0) local[chunks] = make_uint2(0, 0);
     }
 }
 
@@ -515,177 +544,203 @@ __device__ __forceinline__ void put_vertex(const ChunkEmitArgs& A, const Grid& g
     A.edge_id[key] = vid - grid_v0;
 }
 
-// Pass 2, cell-parallel, for lattices given by values alone (no explicit
-// sample positions) whose edge count fits 32 bits.  Each warp takes one
-// segment of 32 chunks (lane = chunk: corner words and active cells).  The
-// segment's active cells are handed out 32 at a time in chunk order (lane =
-// cell: the owning chunk by a shuffle search over the chunks' exclusive
-// counts, the bit by __fns), so lanes stay busy however the active cells are
-// spread.  A cell's output offsets are the segment's base plus a running warp
-// scan of owned-vertex and triangle counts in cell order (the reference's
-// emission order).  Every owned vertex records its grid-local id in a dense
-// per-lattice-edge map, and triangles are written as map keys; mc_resolve_ids
-// then replaces each key by the id its owner recorded (no owner lookup in this
-// pass; the map needs no initialisation: every crossing edge has an owner, and
-// only crossing edges are referenced).  Keys are 3 * (upper end point) + axis,
-// so the (at most three) edges an interior cell owns, which all end at its
-// corner 6, share one 12-byte slot.
-__global__ void __launch_bounds__(256, 5) mc_cell_emit(ChunkEmitArgs A, uint32_t nranges) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t seg = blockIdx.x * 8 + (threadIdx.x >> 5);  // 32 chunks per warp
-    const uint32_t range = seg / (RANGE / 32);
-    if (range >= nranges) return;
-    const Grid g = A.grids[grid_of_range(A.range_grid, range)];
-    const uint32_t gs0 = seg * 32;
-    if (gs0 - g.chunk0 >= g.nchunks) return;  // padding
-    const uint32_t rc = gs0 - g.chunk0, c_end = min(rc + 32, g.nchunks);
-    const uint2 bb = chunk_base(A, gs0);
-    if (chunk_base(A, g.chunk0 + c_end).y == bb.y) return;  // no triangle in these chunks
-    const uint32_t CW = g.CW, ncx = g.nx - 1, ncy = g.ny - 1;
-    const uint32_t grid_v0 = chunk_base(A, g.chunk0).x;
-    uint32_t vcarry = bb.x, tcarry = bb.y;  // global offsets of the next cell's outputs
-    {
-        {
-            // lane = chunk: corner bit-vectors and active cells
-            const uint32_t ch = rc + lane;
-            Corners q;
-            uint32_t act = 0;
-            if (ch < c_end) {
-                const uint32_t row = fdiv(ch, g.div_cw);
-                const uint32_t c = ch - row * CW;
-                const uint32_t z = fdiv(row, g.div_ncy);
-                q = load_corners(g.bits, g.W, g.ny, row - z * ncy, z, c);
-                act = active_cells(q, chunk_valid(c, ncx));
-            } else {
+// Pass 2, cell-parallel, for one lattice given by values alone (no explicit
+// sample positions) whose edge count fits 32 bits.  Warp = one segment of 32
+// chunks (lane = chunk: corner words and active cells), whose first vertex
+// and triangle come from pass 1's segment records.  The segment's active
+// cells are handed out 32 at a time in chunk order (lane = cell: the owning
+// chunk by a shuffle search over the chunks' exclusive counts, the bit by
+// __fns), so lanes stay busy however the active cells are spread.  A cell's
+// own offsets are the segment's base plus a running warp scan of owned-vertex
+// and triangle counts in cell order (the reference's emission order).  Every
+// owned vertex records its id in a dense per-lattice-edge map, and triangles
+// are written as map keys; mc_resolve_ids then replaces each key by the id
+// its owner recorded (the map needs no initialisation: every crossing edge
+// has an owner, and only crossing edges are referenced).  Keys are
+// 3 * (upper end point) + axis, so the (at most three) edges an interior
+// cell owns, which all end at its corner 6, share one 12-byte slot.
+// Active cell number kk (in chunk order) of the segment starting at grid
+// chunk rc; every lane calls it, have = kk < total.
+struct SegCell {
+    uint32_t x, y, z, cs, nown, nt;
+    int cls;
+    bool have;
+};
+
+__device__ __forceinline__ SegCell seg_cell(const Grid& g, uint32_t rc, uint32_t kk, uint32_t total, uint32_t act,
+                                            uint32_t excl, const Corners& q) {
+    SegCell c{0, 0, 0, 0, 0, 0, 0, kk < total};
+    uint32_t src = 0;
 #pragma unroll
-                for (int k = 0; k < 8; ++k) q.k[k] = 0;
-            }
-            const uint32_t n = __popc(act);
-            const uint32_t incl = warp_incl_scan(n, lane), excl = incl - n;
-            const uint32_t total = __shfl_sync(FULL, incl, 31);
-            // lane e < 12: edge-map key of cell edge e relative to 3 * (corner 0's
-            // lattice point); an edge's key is 3 * (its upper end point) + axis
-            uint32_t koff = 0;
-            if (lane < 12) {
-                const uint32_t ax = __ldg(&g_edge_axis[lane]);
-                const uint32_t hx = __ldg(&g_edge_lo[lane][0]) + (ax == 0), hy = __ldg(&g_edge_lo[lane][1]) + (ax == 1),
-                               hz = __ldg(&g_edge_lo[lane][2]) + (ax == 2);
-                koff = 3 * (hx + g.nx * (hy + g.ny * hz)) + ax;
-            }
-            for (uint32_t b0 = 0; b0 < total; b0 += 32) {
-                // lane = cell number b0 + lane of these chunks, in chunk order
-                const uint32_t kk = b0 + lane;
-                const bool have = kk < total;
-                uint32_t src = 0;
+    for (uint32_t step = 16; step > 0; step >>= 1) {
+        const uint32_t cand = src + step;
+        const uint32_t e = __shfl_sync(FULL, excl, cand & 31);
+        if (cand < 32 && e <= kk) src = cand;
+    }
+    const uint32_t sact = __shfl_sync(FULL, act, src);
+    const uint32_t sexcl = __shfl_sync(FULL, excl, src);
+    Corners cq;
 #pragma unroll
-                for (uint32_t step = 16; step > 0; step >>= 1) {
-                    const uint32_t cand = src + step;
-                    const uint32_t e = __shfl_sync(FULL, excl, cand & 31);
-                    if (cand < 32 && e <= kk) src = cand;
-                }
-                const uint32_t sact = __shfl_sync(FULL, act, src);
-                const uint32_t sexcl = __shfl_sync(FULL, excl, src);
-                Corners cq;
-#pragma unroll
-                for (int k = 0; k < 8; ++k) cq.k[k] = __shfl_sync(FULL, q.k[k], src);
-                uint32_t x = 0, y = 0, z = 0, cs = 0, nown = 0, nt = 0;
-                int cls = 0;
-                if (have) {
-                    const uint32_t i = __fns(sact, 0, (int)(kk - sexcl) + 1);
-                    const uint32_t cch = rc + src;
-                    const uint32_t row = fdiv(cch, g.div_cw);
-                    z = fdiv(row, g.div_ncy);
-                    y = row - z * ncy;
-                    x = 32 * (cch - row * CW) + i;
-                    cs = case_at(cq, i);
-                    cls = (x == 0 ? 1 : 0) | (y == 0 ? 2 : 0) | (z == 0 ? 4 : 0);
-                    nown = __popc((uint32_t)__ldg(&iso_edge_mask[cs]) & __ldg(&iso_owned_mask[cls]));
-                    nt = __ldg(&iso_tri_count[cs]);
-                }
-                const uint32_t vi = warp_incl_scan(nown, lane), ti = warp_incl_scan(nt, lane);
-                const uint32_t vstart = vcarry + vi - nown, tstart = tcarry + ti - nt;
-                vcarry += __shfl_sync(FULL, vi, 31);
-                tcarry += __shfl_sync(FULL, ti, 31);
-                uint32_t own = 0, cell = 0;
-                uint64_t tedges = 0;
-                if (have) {
-                    own = (uint32_t)__ldg(&iso_edge_mask[cs]) & __ldg(&iso_owned_mask[cls]);
-                    tedges = __ldg(&iso_tri_edges[cs]);
-                    cell = (z * g.ny + y) * g.nx + x;  // lattice point of corner 0
-                }
-                if (own) {
-                    // owned edges: this cell creates their vertices, numbered by
-                    // first use in the cell's visit order (rank table)
-                    const uint64_t rk = __ldg(&iso_owned_rank[cls][cs]);
-                    if (cls == 0) {
-                        // interior cell: its owned edges are among 5, 6 and 10, the
-                        // three edges ending at corner 6 = (x+1, y+1, z+1); all their
-                        // values are loaded before any vertex is formed
-                        const float* v6 = g.values + ((size_t)(z + 1) * g.ny + (y + 1)) * g.pitch + (x + 1);
-                        const bool e5 = (own >> 5) & 1u, e6 = (own >> 6) & 1u, e10 = (own >> 10) & 1u;
-                        const float f6 = __ldg(v6);
-                        const float f5 = e5 ? __ldg(v6 - g.pitch) : 0.0f;                    // corner 5
-                        const float f7 = e6 ? __ldg(v6 - 1) : 0.0f;                          // corner 7
-                        const float f2 = e10 ? __ldg(v6 - (size_t)g.ny * g.pitch) : 0.0f;    // corner 2
-                        const float X0 = (float)x * g.inv, X1 = (float)(x + 1) * g.inv;
-                        const float Y0 = (float)y * g.inv, Y1 = (float)(y + 1) * g.inv;
-                        const float Z0 = (float)z * g.inv, Z1 = (float)(z + 1) * g.inv;
-                        const uint32_t k6 = 3 * (cell + g.nx * (g.ny + 1) + 1);  // corner 6's key base
-                        if (e5)  // corners 5 -> 6, y axis
-                            put_vertex(A, g, f5, f6, X1, Y0, Z1, X1, Y1, Z1, vstart + (uint32_t)(rk >> 20 & 15u),
-                                       k6 + 1, grid_v0, x + 1, y, z + 1, 1);
-                        if (e6)  // corners 6 -> 7, x axis
-                            put_vertex(A, g, f6, f7, X1, Y1, Z1, X0, Y1, Z1, vstart + (uint32_t)(rk >> 24 & 15u),
-                                       k6 + 0, grid_v0, x, y + 1, z + 1, 0);
-                        if (e10)  // corners 2 -> 6, z axis
-                            put_vertex(A, g, f2, f6, X1, Y1, Z0, X1, Y1, Z1, vstart + (uint32_t)(rk >> 40 & 15u),
-                                       k6 + 2, grid_v0, x + 1, y + 1, z, 2);
-                    } else {
-                        for (uint32_t m = own; m; m &= m - 1) {
-                            const uint32_t e = __ffs(m) - 1;
-                            const uint32_t ax = __ldg(&g_edge_axis[e]);
-                            const uint32_t lx = x + __ldg(&g_edge_lo[e][0]), ly = y + __ldg(&g_edge_lo[e][1]),
-                                           lz = z + __ldg(&g_edge_lo[e][2]);
-                            const uint32_t hx = lx + (ax == 0), hy = ly + (ax == 1), hz = lz + (ax == 2);
-                            const uint32_t u = __ldg(&iso_edge_connection[e][0]), v = __ldg(&iso_edge_connection[e][1]);
-                            const uint32_t ux = x + __ldg(&iso_corners[u][0]), uy = y + __ldg(&iso_corners[u][1]),
-                                           uz = z + __ldg(&iso_corners[u][2]);
-                            const uint32_t vx = x + __ldg(&iso_corners[v][0]), vy = y + __ldg(&iso_corners[v][1]),
-                                           vz = z + __ldg(&iso_corners[v][2]);
-                            const float fa = __ldg(g.values + ((size_t)uz * g.ny + uy) * g.pitch + ux);
-                            const float fb = __ldg(g.values + ((size_t)vz * g.ny + vy) * g.pitch + vx);
-                            put_vertex(A, g, fa, fb, (float)ux * g.inv, (float)uy * g.inv, (float)uz * g.inv,
-                                       (float)vx * g.inv, (float)vy * g.inv, (float)vz * g.inv,
-                                       vstart + (uint32_t)(rk >> (4 * e) & 15u), ((hz * g.ny + hy) * g.nx + hx) * 3 + ax,
-                                       grid_v0, lx, ly, lz, ax);
-                        }
-                    }
-                }
-                // triangles (march_cube, marching_cubes_impl.rs:102-117) as edge-map
-                // keys, resolved to vertex ids once every owner has written its ids
-                const bool tfit = (uint64_t)tstart + nt <= A.cap_t;
-                if (have && !tfit) atomicOr(A.err, DERR_CAPACITY);
-                const uint32_t kmax = __reduce_max_sync(FULL, 3 * nt);
-                for (uint32_t k = 0; k < kmax; ++k) {
-                    const uint32_t ko = __shfl_sync(FULL, koff, (uint32_t)(tedges >> (4 * k)) & 15u);
-                    if (k < 3 * nt && tfit) A.out_i[3 * (size_t)tstart + k] = 3 * cell + ko;
-                }
+    for (int k = 0; k < 8; ++k) cq.k[k] = __shfl_sync(FULL, q.k[k], src);
+    if (c.have) {
+        const uint32_t i = __fns(sact, 0, (int)(kk - sexcl) + 1);
+        const uint32_t cch = rc + src;
+        const uint32_t row = fdiv(cch, g.div_cw);
+        c.z = fdiv(row, g.div_ncy);
+        c.y = row - c.z * (g.ny - 1);
+        c.x = 32 * (cch - row * g.CW) + i;
+        c.cs = case_at(cq, i);
+        c.cls = (c.x == 0 ? 1 : 0) | (c.y == 0 ? 2 : 0) | (c.z == 0 ? 4 : 0);
+        c.nown = __popc((uint32_t)__ldg(&iso_edge_mask[c.cs]) & __ldg(&iso_owned_mask[c.cls]));
+        c.nt = __ldg(&iso_tri_count[c.cs]);
+    }
+    return c;
+}
+
+// The vertices and triangles of one round of cells (every lane calls it).
+// koff (lane e < 12): the edge-map key of cell edge e relative to 3 * (corner
+// 0's lattice point).
+__device__ __forceinline__ void emit_cells(const ChunkEmitArgs& A, const Grid& g, const SegCell& c, uint32_t vstart,
+                                           uint32_t tstart, uint32_t koff, uint32_t grid_v0) {
+    uint32_t own = 0, cell = 0;
+    uint64_t tedges = 0;
+    if (c.have) {
+        own = (uint32_t)__ldg(&iso_edge_mask[c.cs]) & __ldg(&iso_owned_mask[c.cls]);
+        tedges = __ldg(&iso_tri_edges[c.cs]);
+        cell = (c.z * g.ny + c.y) * g.nx + c.x;  // lattice point of corner 0
+    }
+    if (own) {
+        // owned edges: this cell creates their vertices, numbered by
+        // first use in the cell's visit order (rank table)
+        const uint64_t rk = __ldg(&iso_owned_rank[c.cls][c.cs]);
+        if (c.cls == 0) {
+            // interior cell: its owned edges are among 5, 6 and 10, the
+            // three edges ending at corner 6 = (x+1, y+1, z+1); all their
+            // values are loaded before any vertex is formed
+            const float* v6 = g.values + ((size_t)(c.z + 1) * g.ny + (c.y + 1)) * g.pitch + (c.x + 1);
+            const bool e5 = (own >> 5) & 1u, e6 = (own >> 6) & 1u, e10 = (own >> 10) & 1u;
+            const float f6 = __ldg(v6);
+            const float f5 = e5 ? __ldg(v6 - g.pitch) : 0.0f;                    // corner 5
+            const float f7 = e6 ? __ldg(v6 - 1) : 0.0f;                          // corner 7
+            const float f2 = e10 ? __ldg(v6 - (size_t)g.ny * g.pitch) : 0.0f;    // corner 2
+            const float X0 = (float)c.x * g.inv, X1 = (float)(c.x + 1) * g.inv;
+            const float Y0 = (float)c.y * g.inv, Y1 = (float)(c.y + 1) * g.inv;
+            const float Z0 = (float)c.z * g.inv, Z1 = (float)(c.z + 1) * g.inv;
+            const uint32_t k6 = 3 * (cell + g.nx * (g.ny + 1) + 1);  // corner 6's key base
+            if (e5)  // corners 5 -> 6, y axis
+                put_vertex(A, g, f5, f6, X1, Y0, Z1, X1, Y1, Z1, vstart + (uint32_t)(rk >> 20 & 15u),
+                           k6 + 1, grid_v0, c.x + 1, c.y, c.z + 1, 1);
+            if (e6)  // corners 6 -> 7, x axis
+                put_vertex(A, g, f6, f7, X1, Y1, Z1, X0, Y1, Z1, vstart + (uint32_t)(rk >> 24 & 15u),
+                           k6 + 0, grid_v0, c.x, c.y + 1, c.z + 1, 0);
+            if (e10)  // corners 2 -> 6, z axis
+                put_vertex(A, g, f2, f6, X1, Y1, Z0, X1, Y1, Z1, vstart + (uint32_t)(rk >> 40 & 15u),
+                           k6 + 2, grid_v0, c.x + 1, c.y + 1, c.z, 2);
+        } else {
+            for (uint32_t m = own; m; m &= m - 1) {
+                const uint32_t e = __ffs(m) - 1;
+                const uint32_t ax = __ldg(&g_edge_axis[e]);
+                const uint32_t lx = c.x + __ldg(&g_edge_lo[e][0]), ly = c.y + __ldg(&g_edge_lo[e][1]),
+                               lz = c.z + __ldg(&g_edge_lo[e][2]);
+                const uint32_t hx = lx + (ax == 0), hy = ly + (ax == 1), hz = lz + (ax == 2);
+                const uint32_t u = __ldg(&iso_edge_connection[e][0]), v = __ldg(&iso_edge_connection[e][1]);
+                const uint32_t ux = c.x + __ldg(&iso_corners[u][0]), uy = c.y + __ldg(&iso_corners[u][1]),
+                               uz = c.z + __ldg(&iso_corners[u][2]);
+                const uint32_t vx = c.x + __ldg(&iso_corners[v][0]), vy = c.y + __ldg(&iso_corners[v][1]),
+                               vz = c.z + __ldg(&iso_corners[v][2]);
+                const float fa = __ldg(g.values + ((size_t)uz * g.ny + uy) * g.pitch + ux);
+                const float fb = __ldg(g.values + ((size_t)vz * g.ny + vy) * g.pitch + vx);
+                put_vertex(A, g, fa, fb, (float)ux * g.inv, (float)uy * g.inv, (float)uz * g.inv,
+                           (float)vx * g.inv, (float)vy * g.inv, (float)vz * g.inv,
+                           vstart + (uint32_t)(rk >> (4 * e) & 15u), ((hz * g.ny + hy) * g.nx + hx) * 3 + ax,
+                           grid_v0, lx, ly, lz, ax);
             }
         }
     }
+    // triangles (march_cube, marching_cubes_impl.rs:102-117) as edge-map
+    // keys, resolved to vertex ids once every owner has written its ids
+    const bool tfit = (uint64_t)tstart + c.nt <= A.cap_t;
+    if (c.have && !tfit) atomicOr(A.err, DERR_CAPACITY);
+    const uint32_t kmax = __reduce_max_sync(FULL, 3 * c.nt);
+    for (uint32_t k = 0; k < kmax; ++k) {
+        const uint32_t ko = __shfl_sync(FULL, koff, (uint32_t)(tedges >> (4 * k)) & 15u);
+        if (k < 3 * c.nt && tfit) A.out_i[3 * (size_t)tstart + k] = 3 * cell + ko;
+    }
 }
 
-// Triangle corners: lattice edge index -> vertex id recorded by the owner,
-// for the 3 * min(triangles, capacity) corners written (the count is read on
-// the device, so no host round trip is needed).  Indices outside the map
-// (corners of triangles an emit without room skipped) are left alone.
-__global__ void mc_resolve_ids(uint32_t* idx, const uint64_t* totals, uint64_t cap_t, const uint32_t* edge_id,
-                               uint32_t nedges) {
-    const uint64_t n = 3 * min(totals[0], cap_t);
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t v = idx[i];
-        if (v < nedges) idx[i] = __ldg(edge_id + v);
+__global__ void __launch_bounds__(256, 5) mc_cell_emit(ChunkEmitArgs A, const uint4* segs, uint32_t nsegs) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t seg = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (seg >= nsegs) return;
+    const uint4 sr = __ldg(&segs[seg]);  // (first vertex, first triangle) in the range, (vertices, triangles)
+    if (sr.w == 0) return;                // no triangle in the segment
+    const uint2 rp = __ldg(&A.rangepre[seg / (RANGE / 32)]);
+    const Grid g = A.grids[0];
+    const uint32_t rc = seg * 32, c_end = min(rc + 32, g.nchunks);
+    Corners q;
+    uint32_t act = 0;
+    if (rc + lane < c_end) {
+        const uint32_t ch = rc + lane;
+        const uint32_t row = fdiv(ch, g.div_cw);
+        const uint32_t cc = ch - row * g.CW;
+        const uint32_t z = fdiv(row, g.div_ncy);
+        q = load_corners(g.bits, g.W, g.ny, row - z * (g.ny - 1), z, cc);
+        act = active_cells(q, chunk_valid(cc, g.nx - 1));
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) q.k[k] = 0;
     }
+    const uint32_t n = __popc(act);
+    const uint32_t incl = warp_incl_scan(n, lane), excl = incl - n;
+    const uint32_t total = __shfl_sync(FULL, incl, 31);
+    uint32_t koff = 0;
+    if (lane < 12) {
+        const uint32_t ax = __ldg(&g_edge_axis[lane]);
+        const uint32_t hx = __ldg(&g_edge_lo[lane][0]) + (ax == 0), hy = __ldg(&g_edge_lo[lane][1]) + (ax == 1),
+                       hz = __ldg(&g_edge_lo[lane][2]) + (ax == 2);
+        koff = 3 * (hx + g.nx * (hy + g.ny * hz)) + ax;
+    }
+    uint32_t vcarry = rp.x + sr.x, tcarry = rp.y + sr.y;  // global offsets of the next cell's outputs
+    for (uint32_t b0 = 0; b0 < total; b0 += 32) {
+        const SegCell c = seg_cell(g, rc, b0 + lane, total, act, excl, q);
+        const uint32_t vi = warp_incl_scan(c.nown, lane), ti = warp_incl_scan(c.nt, lane);
+        const uint32_t vstart = vcarry + vi - c.nown, tstart = tcarry + ti - c.nt;
+        vcarry += __shfl_sync(FULL, vi, 31);
+        tcarry += __shfl_sync(FULL, ti, 31);
+        emit_cells(A, g, c, vstart, tstart, koff, 0u);
+    }
+}
+
+// Triangle corners: edge-map key -> vertex id recorded by the owner, for the
+// 3 * min(triangles, capacity) corners written (the count is read on the
+// device, so no host round trip is needed).  Four corners per thread and
+// step, so four independent gathers are in flight.  Keys outside the map
+// (corners of triangles an emit without room skipped) are left alone.
+__global__ void __launch_bounds__(256) mc_resolve_ids(uint32_t* __restrict__ idx, const uint64_t* totals,
+                                                      uint64_t cap_t, const uint32_t* __restrict__ edge_id,
+                                                      uint32_t nedges) {
+    const uint64_t n = 3 * min(totals[0], cap_t);
+    const uint64_t n4 = n / 4, stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t t0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint4* __restrict__ p = reinterpret_cast<uint4*>(idx);
+    for (uint64_t i = t0; i < n4; i += stride) {
+        uint4 v = p[i];
+        const uint32_t a = v.x < nedges ? __ldg(edge_id + v.x) : v.x;
+        const uint32_t b = v.y < nedges ? __ldg(edge_id + v.y) : v.y;
+        const uint32_t c = v.z < nedges ? __ldg(edge_id + v.z) : v.z;
+        const uint32_t d = v.w < nedges ? __ldg(edge_id + v.w) : v.w;
+        p[i] = make_uint4(a, b, c, d);
+    }
+    const uint64_t k = 4 * n4 + t0;  // the last n % 4 corners
+    if (k < n) {
+        const uint32_t v = idx[k];
+        if (v < nedges) idx[k] = __ldg(edge_id + v);
+    }
+}
+
+// grid of mc_resolve_ids for at most 3 * cap_t corners
+inline unsigned resolve_blocks(uint64_t cap_t) {
+    return (unsigned)std::min<uint64_t>(std::max<uint64_t>((3 * cap_t / 4 + 255) / 256, 1), 16384);
 }
 
 // Per-grid mesh extents: (first vertex, vertex count, first triangle, triangle count).
