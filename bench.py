@@ -441,12 +441,13 @@ def main():
     f32p, u32p = ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_uint32)
 
     def e2e_step():
+        # a program uploaded from host bytes and the mesh delivered into the
+        # caller's page-locked buffers, as a binding's extract() would do
         ph = ctypes.c_void_p()
         check(lib().iso_program_create(ctx.h, src_bytes, len(src_bytes), ctypes.byref(ph)), ctx.h)
         mi = MeshInfo()
-        check(lib().iso_mc_extract(ctx.h, ph, SIZE, 0, ctypes.byref(mi)), ctx.h)
-        check(lib().iso_mesh_download(ctx.h, ctypes.cast(vbuf.data_ptr(), f32p), vbuf.numel(),
-                                      ctypes.cast(ibuf.data_ptr(), u32p), ibuf.numel(), None, 0), ctx.h)
+        check(lib().iso_mc_extract_host(ctx.h, ph, SIZE, 0, ctypes.cast(vbuf.data_ptr(), f32p), vbuf.numel(),
+                                        ctypes.cast(ibuf.data_ptr(), u32p), ibuf.numel(), ctypes.byref(mi)), ctx.h)
         lib().iso_program_destroy(ph)
         return mi
 

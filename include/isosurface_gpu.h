@@ -194,6 +194,23 @@ ISO_API iso_status iso_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32
 ISO_API iso_status iso_mc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t flags,
                           iso_mesh_info* info);
 
+/* MarchingCubes::<Signed>::new(size).extract(&Sampler::new(&source),
+ * &mut IndexedVertices::new(&mut vertices, &mut indices)) into caller-owned
+ * host buffers: `vertices` (room for vertex_floats floats: 3 per vertex, 6
+ * with ISO_FLAG_NORMALS) and `indices` (room for index_count u32, 3 per
+ * triangle).  When both are page-locked (cudaHostAlloc, cudaHostRegister)
+ * and `indices` is 16-byte aligned, the extraction kernels write the mesh into
+ * them as they produce it, so the transfer overlaps the extraction; any other
+ * host memory receives an ordinary copy afterwards.  The mesh also stays on
+ * the device (iso_mesh_download, iso_mesh_device) and `info` receives its
+ * size.  If either buffer is too small, neither is written and the call
+ * returns ISO_ERR_CAPACITY (a caller can grow its buffers and call
+ * iso_mesh_download).  Replaces the crate's extract into Vec<f32>/Vec<u32>
+ * (src/marching_cubes.rs:59-82, src/extractor.rs:72-93). */
+ISO_API iso_status iso_mc_extract_host(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t flags,
+                               float* vertices, uint64_t vertex_floats, uint32_t* indices,
+                               uint64_t index_count, iso_mesh_info* info);
+
 /* Marching cubes over a caller-supplied device field laid out as
  * iso_sample_grid writes it (nx x ny x nz samples, row pitch `pitch` floats,
  * vertex positions (x/(nx-1)... ) as the reference computes them with

@@ -125,6 +125,29 @@ class Context:
         check(lib().iso_mc_extract(self.h, self.program(source).h, size, flags, ctypes.byref(info)), self.h)
         return info
 
+    def mc_extract_host(self, source, size, vertices, indices, normals=False):
+        """MarchingCubes straight into host buffers: `vertices` (f32, 3 or, with
+        normals, 6 per vertex) and `indices` (u32 / i32, 3 per triangle), numpy
+        arrays or CPU torch tensors.  Page-locked buffers (torch
+        ``pin_memory=True``) are filled by the extraction kernels themselves.
+        Returns the MeshInfo; raises IsoError (capacity) when a buffer is too
+        small, with the mesh left on the device for ``download``."""
+        def addr(a):
+            if hasattr(a, "data_ptr"):
+                if a.is_cuda or not a.is_contiguous():
+                    raise ValueError("host buffers must be contiguous CPU memory")
+                return a.data_ptr(), a.numel()
+            if not a.flags.c_contiguous:
+                raise ValueError("host buffers must be contiguous")
+            return a.ctypes.data, a.size
+        pv, nv = addr(vertices)
+        pi, ni = addr(indices)
+        info = MeshInfo()
+        flags = self._flags(False, normals)
+        check(lib().iso_mc_extract_host(self.h, self.program(source).h, size, flags, ctypes.c_void_p(pv), nv,
+                                        ctypes.c_void_p(pi), ni, ctypes.byref(info)), self.h)
+        return info
+
     def mc_extract_field(self, field_ptr, nx, ny, nz, pitch, keys=False):
         info = MeshInfo()
         flags = self._flags(keys, False)

@@ -298,6 +298,8 @@ iso_status iso_ctx_create(int device, iso_ctx** out) {
     iso_ctx* ctx = new (std::nothrow) iso_ctx();
     if (!ctx) return ISO_ERR_OUT_OF_MEMORY;
     ctx->device = device;
+    cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
+    if (ctx->sms < 1) ctx->sms = 1;
     iso_status s = set_device(ctx);
     cudaError_t e = cudaSuccess;
     if (s == ISO_OK) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
@@ -408,27 +410,31 @@ iso_status iso_program_create(iso_ctx* ctx, const uint8_t* bytes, size_t len, is
         delete p;
         return s;
     }
-    // sphere data of the fast path is re-based to a 16-byte boundary for float4 loads
+    // one device block holds every array (16-byte aligned pieces, so the
+    // sphere data of the fast path takes float4 loads): one allocation, one
+    // copy, one free per program
     const size_t nk = p->consts.size() + 4;
-    cudaError_t e = cudaMalloc(&p->d_ops, 4 * p->ops.size());
-    if (e == cudaSuccess) e = cudaMalloc(&p->d_consts, 4 * nk);
-    if (e == cudaSuccess) e = cudaMalloc(&p->d_jump, 4 * p->jump.size());
-    if (e == cudaSuccess) e = cudaMemcpy(p->d_ops, p->ops.data(), 4 * p->ops.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && !p->consts.empty())
-        e = cudaMemcpy(p->d_consts, p->consts.data(), 4 * p->consts.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(p->d_jump, p->jump.data(), 4 * p->jump.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && p->kind == PK_SPHERE_SET_HARD) {
-        float* d_set = nullptr;
-        e = cudaMalloc(&d_set, 16ull * p->set_n);
-        if (e == cudaSuccess)
-            e = cudaMemcpy(d_set, p->consts.data() + p->set_at + 3, 16ull * p->set_n, cudaMemcpyHostToDevice);
-        p->d_set = d_set;
-    }
-    if (e == cudaSuccess && !p->prims.empty()) {
-        float4* d_prims = nullptr;
-        e = cudaMalloc(&d_prims, 4 * p->prims.size());
-        if (e == cudaSuccess) e = cudaMemcpy(d_prims, p->prims.data(), 4 * p->prims.size(), cudaMemcpyHostToDevice);
-        p->d_prims = d_prims;
+    auto at16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
+    const size_t o_ops = 0, o_consts = at16(o_ops + 4 * p->ops.size()), o_jump = at16(o_consts + 4 * nk);
+    const size_t o_set = at16(o_jump + 4 * p->jump.size());
+    const size_t set_bytes = p->kind == PK_SPHERE_SET_HARD ? 16ull * p->set_n : 0;
+    const size_t o_prims = at16(o_set + set_bytes), total = at16(o_prims + 4 * p->prims.size());
+    std::vector<unsigned char> staged(total, 0);
+    std::memcpy(staged.data() + o_ops, p->ops.data(), 4 * p->ops.size());
+    if (!p->consts.empty()) std::memcpy(staged.data() + o_consts, p->consts.data(), 4 * p->consts.size());
+    if (!p->jump.empty()) std::memcpy(staged.data() + o_jump, p->jump.data(), 4 * p->jump.size());
+    if (set_bytes) std::memcpy(staged.data() + o_set, p->consts.data() + p->set_at + 3, set_bytes);
+    if (!p->prims.empty()) std::memcpy(staged.data() + o_prims, p->prims.data(), 4 * p->prims.size());
+    unsigned char* block = nullptr;
+    cudaError_t e = cudaMalloc(&block, total);
+    if (e == cudaSuccess) {
+        p->d_block = block;
+        p->d_ops = (uint32_t*)(block + o_ops);
+        p->d_consts = (float*)(block + o_consts);
+        p->d_jump = (int32_t*)(block + o_jump);
+        if (set_bytes) p->d_set = (float*)(block + o_set);
+        if (!p->prims.empty()) p->d_prims = (float4*)(block + o_prims);
+        e = cudaMemcpy(block, staged.data(), total, cudaMemcpyHostToDevice);
     }
     if (e != cudaSuccess) {
         iso_status r = cuda_fail(ctx, e, "program upload");
@@ -442,11 +448,7 @@ iso_status iso_program_create(iso_ctx* ctx, const uint8_t* bytes, size_t len, is
 iso_status iso_program_destroy(iso_program* p) {
     if (!p) return ISO_ERR_INVALID_ARG;
     if (p->ctx) cudaSetDevice(p->ctx->device);
-    if (p->d_ops) cudaFree(p->d_ops);
-    if (p->d_consts) cudaFree(p->d_consts);
-    if (p->d_jump) cudaFree(p->d_jump);
-    if (p->d_set) cudaFree(p->d_set);
-    if (p->d_prims) cudaFree(p->d_prims);
+    if (p->d_block) cudaFree(p->d_block);
     delete p;
     return ISO_OK;
 }
@@ -521,6 +523,51 @@ iso_status iso_mc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, 
     return (flags & ISO_FLAG_NORMALS) ? attach_normals(ctx, prog) : ISO_OK;
 }
 
+
+// the device-side address of page-locked host memory (null: pageable,
+// device memory or unknown)
+static void* pinned_device_view(const void* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+iso_status iso_mc_extract_host(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t flags, float* vertices,
+                               uint64_t vertex_floats, uint32_t* indices, uint64_t index_count, iso_mesh_info* info) {
+    if (!ctx) return ISO_ERR_INVALID_ARG;
+    if ((!vertices && vertex_floats) || (!indices && index_count))
+        return fail(ctx, ISO_ERR_INVALID_ARG, "null host buffer with nonzero room");
+    iso_status s = check_size(ctx, prog, size);
+    if (s != ISO_OK) return s;
+    if (flags & ~(uint32_t)(ISO_FLAG_KEYS | ISO_FLAG_NORMALS)) return fail(ctx, ISO_ERR_INVALID_ARG, "unknown flags");
+    void* dv = flags == 0 && size > 1 ? pinned_device_view(vertices) : nullptr;
+    void* di = dv ? pinned_device_view(indices) : nullptr;
+    const bool direct = dv && di && ((uintptr_t)di & 15) == 0;
+    iso_mesh_info mi{};
+    if (direct) {
+        ctx->host_out = iso_ctx::HostOut{(float*)dv, (uint32_t*)di, vertex_floats / 3, index_count / 3, false};
+        s = mc_extract_program(ctx, prog, size, 0, &mi);
+        const bool delivered = ctx->host_out.armed;
+        ctx->host_out = iso_ctx::HostOut{};
+        if (s != ISO_OK) return s;
+        if (info) *info = mi;
+        if (3 * mi.num_vertices > vertex_floats || 3 * mi.num_triangles > index_count)
+            return fail(ctx, ISO_ERR_CAPACITY, "host buffers too small for the mesh (its size is in info)");
+        if (delivered) return ISO_OK;
+        // the lattice went through the block emit, which writes only the device mesh
+        return iso_mesh_download(ctx, vertices, vertex_floats, indices, index_count, nullptr, 0);
+    }
+    if ((s = iso_mc_extract(ctx, prog, size, flags, &mi)) != ISO_OK) return s;
+    if (info) *info = mi;
+    const uint64_t vf = (flags & ISO_FLAG_NORMALS) ? 6 : 3;
+    if (vf * mi.num_vertices > vertex_floats || 3 * mi.num_triangles > index_count)
+        return fail(ctx, ISO_ERR_CAPACITY, "host buffers too small for the mesh (its size is in info)");
+    return iso_mesh_download(ctx, vertices, vertex_floats, indices, index_count, nullptr, 0);
+}
 
 iso_status iso_mc_extract_field(iso_ctx* ctx, const float* field, uint32_t nx, uint32_t ny, uint32_t nz, uint64_t pitch,
                                 uint32_t flags, iso_mesh_info* info) {

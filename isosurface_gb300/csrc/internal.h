@@ -49,6 +49,7 @@ struct ProgView {
 
 struct iso_ctx {
     int device = 0;
+    int sms = 1;  // streaming multiprocessors of the device
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     // work buffers (grow-only, reused across calls)
@@ -77,12 +78,25 @@ struct iso_ctx {
     // steady-state MarchingCubes: the whole extraction recorded as one CUDA
     // graph, replayed while the program, size, flags and buffers stay the same
     bool capturing = false;  // no allocation while a stream capture records
+    // page-locked host buffers (device-side pointers) that the MarchingCubes
+    // kernels fill alongside the device mesh (iso_mc_extract_host); `armed`
+    // reports whether the last lattice pass could deliver there
+    struct HostOut {
+        float* v = nullptr;
+        uint32_t* i = nullptr;
+        uint64_t cap_v = 0, cap_t = 0;  // vertices, triangles
+        bool armed = false;
+    } host_out;
     struct McPlan {
         cudaGraphExec_t exec = nullptr;
         const iso_program* prog = nullptr;
         uint64_t prog_uid = 0;
         uint32_t size = 0, flags = 0;
         void* bufs[12] = {};
+        float* host_v = nullptr;  // host buffers baked into the recorded kernels
+        uint32_t* host_i = nullptr;
+        uint64_t host_cap_v = 0, host_cap_t = 0;
+        bool host_armed = false;  // the recorded kernels deliver to the host buffers
         uint64_t launches = 0;
     } mc_plan;
     uint64_t mc_last_key[3] = {};  // (program uid, size, flags) of the last eager extraction
@@ -116,6 +130,7 @@ struct iso_program {
     std::vector<uint32_t> ops;
     std::vector<float> consts;
     std::vector<int32_t> jump;
+    void* d_block = nullptr;  // one device allocation holding the arrays below
     uint32_t* d_ops = nullptr;
     float* d_consts = nullptr;
     int32_t* d_jump = nullptr;

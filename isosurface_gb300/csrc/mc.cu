@@ -628,6 +628,8 @@ static iso_status mc_lattice_passes(iso_ctx* ctx, const Lattice& L, uint32_t fla
     Grid* d_grid = (Grid*)(((uintptr_t)(totals + 4) + 255) & ~(uintptr_t)255);
     cudaError_t e = emit_smem_attribute(smem);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "emit smem attribute");
+    // only the cell emit delivers to host buffers
+    ctx->host_out.armed = edge_map && ctx->host_out.v && ctx->host_out.i;
     // the cell emit reads one record per 32-chunk segment; the block emit
     // needs every chunk's prefix
     const uint32_t nsegs = (uint32_t)((chunks + 31) / 32);
@@ -648,15 +650,17 @@ static iso_status mc_lattice_passes(iso_ctx* ctx, const Lattice& L, uint32_t fla
     auto emit = [&]() -> iso_status {
         uint64_t cap_v = ctx->mesh_v.bytes / 12, cap_t = ctx->mesh_i.bytes / 12;
         if (keys) cap_v = std::min<uint64_t>(cap_v, ctx->mesh_k.bytes / 16);
+        const iso_ctx::HostOut& H = ctx->host_out;
         ChunkEmitArgs ea{d_grid, nullptr, (uint32_t)chunks, local, rangepre, (float*)ctx->mesh_v.p,
                          (uint32_t*)ctx->mesh_i.p, keys ? (uint64_t*)ctx->mesh_k.p : nullptr, cap_v, cap_t,
-                         ctx->d_err, (uint32_t*)ctx->edges.p};
+                         ctx->d_err, (uint32_t*)ctx->edges.p, H.v, H.i, H.cap_v, H.cap_t, totals};
         {
             StageTimer timer(ctx, ISO_STAGE_EMIT);
             if (edge_map) {
                 mc_cell_emit<<<(nsegs + 7) / 8, 256, 0, ctx->stream>>>(ea, segs, nsegs);
                 mc_resolve_ids<<<resolve_blocks(cap_t), 256, 0, ctx->stream>>>(
-                    (uint32_t*)ctx->mesh_i.p, totals, cap_t, (const uint32_t*)ctx->edges.p, (uint32_t)nedges);
+                    (uint32_t*)ctx->mesh_i.p, totals, cap_t, (const uint32_t*)ctx->edges.p, (uint32_t)nedges, H.i,
+                    H.cap_v, H.cap_t, cap_v);
                 ctx->launches++;
             } else {
                 mc_block_emit<<<(unsigned)((chunks + 255) / 256), 256, smem, ctx->stream>>>(ea, CW);
@@ -725,8 +729,10 @@ iso_status mc_extract_program(iso_ctx* ctx, const iso_program* prog, uint32_t si
     iso_ctx::McPlan& P = ctx->mc_plan;
     void* bufs[12];
     plan_buffers(ctx, bufs);
+    const iso_ctx::HostOut& H = ctx->host_out;
     const bool match = P.exec && !ctx->timing && P.prog == prog && P.prog_uid == prog->uid && P.size == size &&
-                       P.flags == flags && std::memcmp(P.bufs, bufs, sizeof(bufs)) == 0;
+                       P.flags == flags && std::memcmp(P.bufs, bufs, sizeof(bufs)) == 0 && P.host_v == H.v &&
+                       P.host_i == H.i && P.host_cap_v == H.cap_v && P.host_cap_t == H.cap_t;
     if (match) {
         cudaError_t e = cudaGraphLaunch(P.exec, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -738,6 +744,7 @@ iso_status mc_extract_program(iso_ctx* ctx, const iso_program* prog, uint32_t si
         const bool fits = nv <= ctx->mesh_v.bytes / 12 && nt <= ctx->mesh_i.bytes / 12 &&
                           (!keys || nv <= ctx->mesh_k.bytes / 16) && nv < (1ull << 31) && nt < (1ull << 31);
         if (!err && fits) {
+            ctx->host_out.armed = P.host_armed;
             ctx->last = iso_mesh_info{nv, nt, (uint64_t)(size - 1) * (size - 1) * size};
             ctx->last_flags = flags;
             ctx->last_vertex_floats = 3;
@@ -788,6 +795,11 @@ iso_status mc_extract_program(iso_ctx* ctx, const iso_program* prog, uint32_t si
             P.size = size;
             P.flags = flags;
             plan_buffers(ctx, P.bufs);
+            P.host_v = H.v;
+            P.host_i = H.i;
+            P.host_cap_v = H.cap_v;
+            P.host_cap_t = H.cap_t;
+            P.host_armed = H.armed;
             P.launches = recorded;
         }
     }

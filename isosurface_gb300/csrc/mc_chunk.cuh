@@ -266,7 +266,22 @@ struct ChunkEmitArgs {
     uint64_t cap_v, cap_t;
     uint32_t* err;
     uint32_t* edge_id;  // mc_cell_emit: vertex id per lattice edge, keyed by (upper end point * 3 + axis)
+    // mc_cell_emit / mc_resolve_ids: page-locked host buffers (device-side
+    // pointers, null: none) that also receive the mesh when all of it fits
+    // both them and the device buffers (`totals` = triangles, vertices)
+    float* host_v;
+    uint32_t* host_i;
+    uint64_t host_cap_v, host_cap_t;
+    const uint64_t* totals;
 };
+
+// whether this launch copies the mesh to the host buffers
+__device__ __forceinline__ bool mesh_to_host(const float* host, const uint64_t* totals, uint64_t host_cap_v,
+                                             uint64_t host_cap_t, uint64_t cap_v, uint64_t cap_t) {
+    if (!host) return false;
+    const uint64_t nt = totals[0], nv = totals[1];
+    return nv <= host_cap_v && nt <= host_cap_t && nv <= cap_v && nt <= cap_t;
+}
 
 __device__ __forceinline__ uint2 chunk_base(const ChunkEmitArgs& A, uint32_t ch) {
     const uint2 l = __ldg(&A.local[ch]);
@@ -709,17 +724,29 @@ __global__ void __launch_bounds__(256, 5) mc_cell_emit(ChunkEmitArgs A, const ui
         tcarry += __shfl_sync(FULL, ti, 31);
         emit_cells(A, g, c, vstart, tstart, koff, 0u);
     }
+    if (mesh_to_host(A.host_v, A.totals, A.host_cap_v, A.host_cap_t, A.cap_v, A.cap_t)) {
+        // the segment's vertices, just written by this warp, in whole lines
+        // to the host (the warp's own stores are ordered before its reads)
+        __syncwarp();
+        const size_t f0 = 3 * (size_t)(rp.x + sr.x), f1 = f0 + 3 * (size_t)sr.z;
+        for (size_t f = f0 + lane; f < f1; f += 32) A.host_v[f] = __ldcg(A.out_v + f);
+    }
 }
 
 // Triangle corners: edge-map key -> vertex id recorded by the owner, for the
 // 3 * min(triangles, capacity) corners written (the count is read on the
 // device, so no host round trip is needed).  Four corners per thread and
-// step, so four independent gathers are in flight.  Keys outside the map
-// (corners of triangles an emit without room skipped) are left alone.
+// step, so four independent gathers are in flight; the resolved corners also
+// go to the page-locked host buffer when the mesh is delivered there.  Keys
+// outside the map (corners of triangles an emit without room skipped) are
+// left alone.
 __global__ void __launch_bounds__(256) mc_resolve_ids(uint32_t* __restrict__ idx, const uint64_t* totals,
                                                       uint64_t cap_t, const uint32_t* __restrict__ edge_id,
-                                                      uint32_t nedges) {
+                                                      uint32_t nedges, uint32_t* host_i, uint64_t host_cap_v,
+                                                      uint64_t host_cap_t, uint64_t cap_v) {
     const uint64_t n = 3 * min(totals[0], cap_t);
+    const bool to_host = mesh_to_host(reinterpret_cast<const float*>(host_i), totals, host_cap_v, host_cap_t, cap_v,
+                                      cap_t);
     const uint64_t n4 = n / 4, stride = (uint64_t)gridDim.x * blockDim.x;
     const uint64_t t0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint4* __restrict__ p = reinterpret_cast<uint4*>(idx);
@@ -729,12 +756,15 @@ __global__ void __launch_bounds__(256) mc_resolve_ids(uint32_t* __restrict__ idx
         const uint32_t b = v.y < nedges ? __ldg(edge_id + v.y) : v.y;
         const uint32_t c = v.z < nedges ? __ldg(edge_id + v.z) : v.z;
         const uint32_t d = v.w < nedges ? __ldg(edge_id + v.w) : v.w;
-        p[i] = make_uint4(a, b, c, d);
+        v = make_uint4(a, b, c, d);
+        p[i] = v;
+        if (to_host) reinterpret_cast<uint4*>(host_i)[i] = v;
     }
     const uint64_t k = 4 * n4 + t0;  // the last n % 4 corners
     if (k < n) {
-        const uint32_t v = idx[k];
-        if (v < nedges) idx[k] = __ldg(edge_id + v);
+        uint32_t v = idx[k];
+        if (v < nedges) idx[k] = v = __ldg(edge_id + v);
+        if (to_host) host_i[k] = v;
     }
 }
 

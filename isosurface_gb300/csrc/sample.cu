@@ -464,7 +464,9 @@ __global__ void set_thresholds(SetArgs A, float4* thr) {
 // persistent: warps stride over (mixed tile, row) items.  A row is first
 // bounded against the tile's kept spheres alone (they decide the minimum
 // everywhere in the tile): a row wholly beyond reach writes its sign words.
-__global__ void __launch_bounds__(256, 3) set_rows(SetArgs A, uint32_t tiles_y, const TileRec* recs,
+constexpr int SET_ROWS_BLOCKS = 3;  // resident blocks of set_rows per SM (4 measured slower)
+
+__global__ void __launch_bounds__(256, SET_ROWS_BLOCKS) set_rows(SetArgs A, uint32_t tiles_y, const TileRec* recs,
                                                    const uint32_t* mixed, const uint32_t* nmixed, const float4* thr_all) {
     __shared__ float4 s_keep[8][KEEP_MAX];
     __shared__ float4 s_thr[8][KEEP_MAX];
@@ -611,9 +613,6 @@ iso_status launch_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t nx
             float4* thr = (float4*)((char*)nmixed + 256);
             cudaError_t e = cudaMemsetAsync(nmixed, 0, 4, ctx->stream);
             if (e != cudaSuccess) return cuda_fail(ctx, e, "mixed-tile count");
-            int dev = 0, sms = 0;
-            cudaGetDevice(&dev);
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
             StageTimer timer(ctx, ISO_STAGE_SAMPLE);
             if (near_only) {
                 set_thresholds<<<(prog->set_n + 127) / 128, 128, 0, ctx->stream>>>(a, thr);
@@ -621,7 +620,7 @@ iso_status launch_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t nx
             }
             set_tiles<<<(unsigned)((tiles + TILE_WARPS - 1) / TILE_WARPS), 32 * TILE_WARPS, 0, ctx->stream>>>(
                 a, ty, tz, recs, mixed, nmixed);
-            set_rows<<<(unsigned)sms * 3, 256, 0, ctx->stream>>>(a, ty, recs, mixed, nmixed, thr);
+            set_rows<<<(unsigned)ctx->sms * SET_ROWS_BLOCKS, 256, 0, ctx->stream>>>(a, ty, recs, mixed, nmixed, thr);
             ctx->launches++;
         } else {
             dim3 grid(W, (ny + 7) / 8, (nz + TZ - 1) / TZ);

@@ -331,3 +331,84 @@ def test_1024_cubed_block_emit_fallback(ctx):
     # every vertex is used and every key is distinct
     assert len(np.unique(got.indices)) == info.num_vertices
     assert len(np.unique(got.keys[:, 0])) == info.num_vertices
+
+
+def _pinned(n, dtype):
+    import torch
+    return torch.empty(n, dtype=dtype, pin_memory=True)
+
+
+def test_extract_into_host_buffers(ctx):
+    """iso_mc_extract_host: page-locked buffers are filled by the extraction
+    kernels themselves (eager, recording and replayed runs), pageable ones by
+    a copy; both give the oracle's bytes, and the mesh stays on the device."""
+    import torch
+    src = scenes.sphere_union()
+    size = 161
+    want = oracle.Program(S.lower(src)).marching_cubes(size)
+    nv, nt = len(want.vertices), len(want.indices) // 3
+    prog = ctx.program(src)
+    pv, pi = _pinned(3 * nv + 7, torch.float32), _pinned(3 * nt + 5, torch.int32)
+    for _ in range(4):  # eager, eager + record, replay, replay
+        pv.fill_(-1.0)
+        pi.fill_(-1)
+        info = ctx.mc_extract_host(prog, size, pv, pi)
+        assert (info.num_vertices, info.num_triangles) == (nv, nt)
+        assert np.array_equal(pv.numpy()[:3 * nv].reshape(-1, 3), want.vertices)
+        assert np.array_equal(pi.numpy()[:3 * nt].view(np.uint32), want.indices)
+        assert (pv.numpy()[3 * nv:] == -1.0).all() and (pi.numpy()[3 * nt:] == -1).all()
+    on_dev = ctx.download(info)
+    assert np.array_equal(on_dev.vertices, want.vertices) and np.array_equal(on_dev.indices, want.indices)
+    # other page-locked buffers after the recording: no replay into the old ones
+    qv, qi = _pinned(3 * nv, torch.float32), _pinned(3 * nt, torch.int32)
+    pv.fill_(-1.0)
+    for _ in range(3):
+        ctx.mc_extract_host(prog, size, qv, qi)
+        assert np.array_equal(qv.numpy().reshape(-1, 3), want.vertices)
+        assert np.array_equal(qi.numpy().view(np.uint32), want.indices)
+    assert (pv.numpy() == -1.0).all()
+    # pageable numpy buffers take the copy path
+    v = np.zeros((nv, 3), np.float32)
+    i = np.zeros(3 * nt, np.uint32)
+    ctx.mc_extract_host(prog, size, v, i)
+    assert np.array_equal(v, want.vertices) and np.array_equal(i, want.indices)
+
+
+def test_extract_into_host_buffers_too_small(ctx):
+    """Buffers one element short: ISO_ERR_CAPACITY, nothing written, the
+    sizes reported and the mesh downloadable afterwards."""
+    import ctypes
+
+    import torch
+    from isosurface_gb300._capi import MeshInfo, lib
+    src = scenes.sphere_union()
+    size = 97
+    want = oracle.Program(S.lower(src)).marching_cubes(size)
+    nv, nt = len(want.vertices), len(want.indices) // 3
+    prog = ctx.program(src)
+    for short_v in (True, False):
+        pv = _pinned(3 * nv - (1 if short_v else 0), torch.float32).fill_(7.0)
+        pi = _pinned(3 * nt - (0 if short_v else 1), torch.int32).fill_(7)
+        for _ in range(3):
+            info = MeshInfo()
+            st = lib().iso_mc_extract_host(ctx.h, prog.h, size, 0, ctypes.c_void_p(pv.data_ptr()), pv.numel(),
+                                           ctypes.c_void_p(pi.data_ptr()), pi.numel(), ctypes.byref(info))
+            assert st == 2  # ISO_ERR_CAPACITY
+            assert (info.num_vertices, info.num_triangles) == (nv, nt)
+            assert (pv.numpy() == 7.0).all() and (pi.numpy() == 7).all()
+        got = ctx.download(info)
+        assert np.array_equal(got.vertices, want.vertices) and np.array_equal(got.indices, want.indices)
+
+
+def test_extract_into_host_buffers_with_normals(ctx):
+    import torch
+    src = scenes.csg()
+    size = 65
+    want = oracle.Program(S.lower(src)).marching_cubes(size, normals=True)
+    nv, nt = len(want.vertices), len(want.indices) // 3
+    pv, pi = _pinned(6 * nv, torch.float32), _pinned(3 * nt, torch.int32)
+    info = ctx.mc_extract_host(src, size, pv, pi, normals=True)
+    assert (info.num_vertices, info.num_triangles) == (nv, nt)
+    got = pv.numpy().reshape(-1, 6)
+    assert np.array_equal(got[:, :3], want.vertices) and np.array_equal(got[:, 3:], want.normals)
+    assert np.array_equal(pi.numpy().view(np.uint32), want.indices)
