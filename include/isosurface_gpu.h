@@ -211,6 +211,14 @@ ISO_API iso_status iso_mc_extract_host(iso_ctx* ctx, const iso_program* prog, ui
                                float* vertices, uint64_t vertex_floats, uint32_t* indices,
                                uint64_t index_count, iso_mesh_info* info);
 
+/* Page-lock `bytes` of caller host memory at `p` (cudaHostRegister, mapped
+ * and portable), so that iso_mc_extract_host can deliver into it directly;
+ * for callers whose vectors come from an ordinary allocator.  The range stays
+ * registered until iso_host_unregister(p).  ISO_ERR_INVALID_ARG for a null
+ * or empty range or one that is already registered, ISO_ERR_CUDA otherwise. */
+ISO_API iso_status iso_host_register(void* p, uint64_t bytes);
+ISO_API iso_status iso_host_unregister(void* p);
+
 /* Marching cubes over a caller-supplied device field laid out as
  * iso_sample_grid writes it (nx x ny x nz samples, row pitch `pitch` floats,
  * vertex positions (x/(nx-1)... ) as the reference computes them with

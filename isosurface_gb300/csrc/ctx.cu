@@ -536,6 +536,22 @@ static void* pinned_device_view(const void* p) {
     return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
+iso_status iso_host_register(void* p, uint64_t bytes) {
+    if (!p || !bytes) return ISO_ERR_INVALID_ARG;
+    const cudaError_t e = cudaHostRegister(p, bytes, cudaHostRegisterMapped | cudaHostRegisterPortable);
+    if (e == cudaSuccess) return ISO_OK;
+    cudaGetLastError();
+    return e == cudaErrorHostMemoryAlreadyRegistered ? ISO_ERR_INVALID_ARG : ISO_ERR_CUDA;
+}
+
+iso_status iso_host_unregister(void* p) {
+    if (!p) return ISO_ERR_INVALID_ARG;
+    const cudaError_t e = cudaHostUnregister(p);
+    if (e == cudaSuccess) return ISO_OK;
+    cudaGetLastError();
+    return e == cudaErrorHostMemoryNotRegistered ? ISO_ERR_INVALID_ARG : ISO_ERR_CUDA;
+}
+
 iso_status iso_mc_extract_host(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t flags, float* vertices,
                                uint64_t vertex_floats, uint32_t* indices, uint64_t index_count, iso_mesh_info* info) {
     if (!ctx) return ISO_ERR_INVALID_ARG;

@@ -610,7 +610,10 @@ static iso_status mc_lattice_passes(iso_ctx* ctx, const Lattice& L, uint32_t fla
     iso_status s;
     // per-chunk prefixes (block emit) or per-segment records (cell emit)
     if ((s = ensure(ctx, ctx->rowtri, 8 * (chunks + 1))) != ISO_OK) return s;
-    if ((s = ensure(ctx, ctx->scan, 16 * (size_t)nranges + 64 + sizeof(Grid) + 256)) != ISO_OK) return s;
+    const uint32_t nblocks = (nranges + 7) / 8;  // counting blocks of 8 ranges
+    if ((s = ensure(ctx, ctx->scan, 16 * (size_t)nranges + 64 + sizeof(Grid) + 256 + 16 * ((size_t)nblocks + 1) + 256)) !=
+        ISO_OK)
+        return s;
     const bool keys = (flags & ISO_FLAG_KEYS) != 0;
     // a first extraction starts from a modest guess; later ones reuse what grew
     if ((s = ensure(ctx, ctx->mesh_v, 12 * (size_t)65536)) != ISO_OK) return s;
@@ -626,6 +629,8 @@ static iso_status mc_lattice_passes(iso_ctx* ctx, const Lattice& L, uint32_t fla
     uint2* rangepre = rangeagg + nranges;
     uint64_t* totals = (uint64_t*)(rangepre + nranges + 2);
     Grid* d_grid = (Grid*)(((uintptr_t)(totals + 4) + 255) & ~(uintptr_t)255);
+    uint2* blockagg = (uint2*)(((uintptr_t)(d_grid + 1) + 255) & ~(uintptr_t)255);  // segment mode
+    uint2* blockpre = blockagg + nblocks;
     cudaError_t e = emit_smem_attribute(smem);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "emit smem attribute");
     // only the cell emit delivers to host buffers
@@ -637,13 +642,17 @@ static iso_status mc_lattice_passes(iso_ctx* ctx, const Lattice& L, uint32_t fla
     write_grid<<<1, 1, 0, ctx->stream>>>(d_grid, make_grid(L, 0));
     {
         StageTimer timer(ctx, ISO_STAGE_CLASSIFY);
-        ChunkCountArgs ca{d_grid, nullptr, (uint32_t)chunks, edge_map ? nullptr : local, rangeagg, segs};
-        if (edge_map)
-            mc_chunk_count<true><<<(nranges + 7) / 8, 256, 0, ctx->stream>>>(ca);
-        else
-            mc_chunk_count<false><<<(nranges + 7) / 8, 256, 0, ctx->stream>>>(ca);
-        mc_range_scan<<<1, 1024, 0, ctx->stream>>>(rangeagg, nranges, rangepre, totals, edge_map ? nullptr : local,
-                                                   (uint32_t)chunks, ctx->d_err);
+        ChunkCountArgs ca{d_grid, nullptr, (uint32_t)chunks, edge_map ? nullptr : local, rangeagg, segs, blockagg};
+        if (edge_map) {
+            // range prefixes inside blocks of 8 ranges; one scan over the block totals
+            mc_chunk_count<true><<<nblocks, 256, 0, ctx->stream>>>(ca);
+            mc_range_scan<<<1, 1024, 0, ctx->stream>>>(blockagg, nblocks, blockpre, totals, nullptr, (uint32_t)chunks,
+                                                       ctx->d_err);
+        } else {
+            mc_chunk_count<false><<<nblocks, 256, 0, ctx->stream>>>(ca);
+            mc_range_scan<<<1, 1024, 0, ctx->stream>>>(rangeagg, nranges, rangepre, totals, local, (uint32_t)chunks,
+                                                       ctx->d_err);
+        }
     }
     ctx->launches += 3;
     if ((s = check_launch(ctx, "mc_chunk_count")) != ISO_OK) return s;
@@ -651,9 +660,10 @@ static iso_status mc_lattice_passes(iso_ctx* ctx, const Lattice& L, uint32_t fla
         uint64_t cap_v = ctx->mesh_v.bytes / 12, cap_t = ctx->mesh_i.bytes / 12;
         if (keys) cap_v = std::min<uint64_t>(cap_v, ctx->mesh_k.bytes / 16);
         const iso_ctx::HostOut& H = ctx->host_out;
-        ChunkEmitArgs ea{d_grid, nullptr, (uint32_t)chunks, local, rangepre, (float*)ctx->mesh_v.p,
-                         (uint32_t*)ctx->mesh_i.p, keys ? (uint64_t*)ctx->mesh_k.p : nullptr, cap_v, cap_t,
-                         ctx->d_err, (uint32_t*)ctx->edges.p, H.v, H.i, H.cap_v, H.cap_t, totals};
+        ChunkEmitArgs ea{d_grid, nullptr, (uint32_t)chunks, local, edge_map ? rangeagg : rangepre,
+                         (float*)ctx->mesh_v.p, (uint32_t*)ctx->mesh_i.p, keys ? (uint64_t*)ctx->mesh_k.p : nullptr,
+                         cap_v, cap_t, ctx->d_err, (uint32_t*)ctx->edges.p, H.v, H.i, H.cap_v, H.cap_t, totals,
+                         blockpre};
         {
             StageTimer timer(ctx, ISO_STAGE_EMIT);
             if (edge_map) {
@@ -836,7 +846,7 @@ iso_status mc_extract_grids(iso_ctx* ctx, const void* d_grids, uint32_t ngrids, 
     uint2* rangeagg = local + ((chunks + 1 + 31) & ~31u);
     uint2* rangepre = rangeagg + nranges;
     const Grid* grids = (const Grid*)d_grids;
-    ChunkCountArgs ca{grids, d_range_grid, chunks, local, rangeagg, nullptr};
+    ChunkCountArgs ca{grids, d_range_grid, chunks, local, rangeagg, nullptr, nullptr};
     {
         StageTimer timer(ctx, ISO_STAGE_CLASSIFY);
         mc_chunk_count<false><<<(nranges + 1 + 7) / 8, 256, 0, ctx->stream>>>(ca);

@@ -74,7 +74,9 @@ struct ChunkCountArgs {
     uint2* local;      // chunk mode: chunks + 1 (vertex, triangle) exclusive prefixes inside the range
     uint2* rangeagg;   // per range: (vertices, triangles)
     uint4* segs;       // segment mode: per 32 chunks (first vertex, first triangle) inside the range,
-                       // (vertices, triangles)
+                       // (vertices, triangles); rangeagg then holds each range's prefix inside
+                       // its block of 8 ranges and blockagg each block's totals
+    uint2* blockagg;
 };
 
 // Pass 1: per-chunk (SEG = false) or per-segment (32 chunks, SEG = true)
@@ -91,96 +93,117 @@ __global__ void __launch_bounds__(256) mc_chunk_count(ChunkCountArgs A) {
     if (threadIdx.x < 8) s_owned[threadIdx.x] = iso_owned_mask[threadIdx.x];
     __syncthreads();
     const uint32_t range = blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (range * RANGE > A.chunks) return;  // warp-uniform
-    const Grid g = A.grids[grid_of_range(A.range_grid, min(range, A.chunks / RANGE - (A.chunks % RANGE == 0)))];
-    const uint32_t ncx = g.nx - 1;
-    // corner words of chunk ch (zeros outside the grid)
-    auto fetch = [&](uint32_t ch, uint32_t& y, uint32_t& z, uint32_t& c, bool& in) {
-        const uint32_t lc = ch - g.chunk0;
-        in = ch < A.chunks && lc < g.nchunks;
-        Corners q;
-        if (in) {
-            const uint32_t row = fdiv(lc, g.div_cw);
-            c = lc - row * g.CW;
-            z = fdiv(row, g.div_ncy);
-            y = row - z * (g.ny - 1);
-            q = load_corners(g.bits, g.W, g.ny, y, z, c);
-        } else {
-#pragma unroll
-            for (int k = 0; k < 8; ++k) q.k[k] = 0;
-            y = z = c = 0;
-        }
-        return q;
-    };
+    const bool live = range * RANGE <= A.chunks;  // warp-uniform
+    if (!SEG && !live) return;
     uint32_t agg_t = 0, agg_v = 0;
-    uint32_t ny_, nz_, nc_;
-    bool nin;
-    Corners qn = fetch(range * RANGE + lane, ny_, nz_, nc_, nin);
-    for (int r = 0; r < RANGE_ROUNDS; ++r) {
-        const uint32_t ch = range * RANGE + r * 32 + lane;
-        const Corners q = qn;
-        const uint32_t y = ny_, z = nz_, c = nc_;
-        const bool in = nin;
-        if (r + 1 < RANGE_ROUNDS) qn = fetch(ch + 32, ny_, nz_, nc_, nin);
-        uint32_t v = 0;
-        const uint32_t act = in ? active_cells(q, chunk_valid(c, ncx)) : 0u;
-        if (act) {
-            if (y > 0 && z > 0) {
-                // interior row: cells own edges 5 (k5^k6), 6 (k6^k7), 10 (k2^k6);
-                // the row's x == 0 cell also owns 7 (k7^k4) and 11 (k3^k7)
-                v = __popc((q.k[5] ^ q.k[6]) & act) + __popc((q.k[6] ^ q.k[7]) & act) + __popc((q.k[2] ^ q.k[6]) & act);
-                if (c == 0 && (act & 1u)) v += ((q.k[7] ^ q.k[4]) & 1u) + ((q.k[3] ^ q.k[7]) & 1u);
+    if (live) {
+        const Grid g = A.grids[grid_of_range(A.range_grid, min(range, A.chunks / RANGE - (A.chunks % RANGE == 0)))];
+        const uint32_t ncx = g.nx - 1;
+        // corner words of chunk ch (zeros outside the grid)
+        auto fetch = [&](uint32_t ch, uint32_t& y, uint32_t& z, uint32_t& c, bool& in) {
+            const uint32_t lc = ch - g.chunk0;
+            in = ch < A.chunks && lc < g.nchunks;
+            Corners q;
+            if (in) {
+                const uint32_t row = fdiv(lc, g.div_cw);
+                c = lc - row * g.CW;
+                z = fdiv(row, g.div_ncy);
+                y = row - z * (g.ny - 1);
+                q = load_corners(g.bits, g.W, g.ny, y, z, c);
             } else {
-                const int cls = (y == 0 ? 2 : 0) | (z == 0 ? 4 : 0);
-                v = owned_count(q, act, s_owned[cls], s_owned[cls | 1], c == 0 ? 1u : 0u);
+    #pragma unroll
+                for (int k = 0; k < 8; ++k) q.k[k] = 0;
+                y = z = c = 0;
             }
-        }
-        // triangles: the round's active cells one per lane (in chunk order),
-        // their counts summed back per chunk in shared memory (chunk mode) or
-        // over the round (segment mode)
-        if (!SEG) s_tri[warp][lane] = 0;
-        uint32_t tl = 0;
-        const uint32_t n = __popc(act);
-        const uint32_t incl = warp_incl_scan(n, lane), excl = incl - n;
-        const uint32_t total = __shfl_sync(FULL, incl, 31);
-        if (!SEG) __syncwarp();
-        for (uint32_t b0 = 0; b0 < total; b0 += 32) {
-            const uint32_t kk = b0 + lane;
-            uint32_t src = 0;
-#pragma unroll
-            for (uint32_t step = 16; step > 0; step >>= 1) {
-                const uint32_t cand = src + step;
-                const uint32_t e = __shfl_sync(FULL, excl, cand & 31);
-                if (cand < 32 && e <= kk) src = cand;
+            return q;
+        };
+        uint32_t ny_, nz_, nc_;
+        bool nin;
+        Corners qn = fetch(range * RANGE + lane, ny_, nz_, nc_, nin);
+        for (int r = 0; r < RANGE_ROUNDS; ++r) {
+            const uint32_t ch = range * RANGE + r * 32 + lane;
+            const Corners q = qn;
+            const uint32_t y = ny_, z = nz_, c = nc_;
+            const bool in = nin;
+            if (r + 1 < RANGE_ROUNDS) qn = fetch(ch + 32, ny_, nz_, nc_, nin);
+            uint32_t v = 0;
+            const uint32_t act = in ? active_cells(q, chunk_valid(c, ncx)) : 0u;
+            if (act) {
+                if (y > 0 && z > 0) {
+                    // interior row: cells own edges 5 (k5^k6), 6 (k6^k7), 10 (k2^k6);
+                    // the row's x == 0 cell also owns 7 (k7^k4) and 11 (k3^k7)
+                    v = __popc((q.k[5] ^ q.k[6]) & act) + __popc((q.k[6] ^ q.k[7]) & act) + __popc((q.k[2] ^ q.k[6]) & act);
+                    if (c == 0 && (act & 1u)) v += ((q.k[7] ^ q.k[4]) & 1u) + ((q.k[3] ^ q.k[7]) & 1u);
+                } else {
+                    const int cls = (y == 0 ? 2 : 0) | (z == 0 ? 4 : 0);
+                    v = owned_count(q, act, s_owned[cls], s_owned[cls | 1], c == 0 ? 1u : 0u);
+                }
             }
-            const uint32_t sact = __shfl_sync(FULL, act, src), sexcl = __shfl_sync(FULL, excl, src);
-            Corners cq;
-#pragma unroll
-            for (int k = 0; k < 8; ++k) cq.k[k] = __shfl_sync(FULL, q.k[k], src);
-            if (kk < total) {
-                const uint32_t i = __fns(sact, 0, (int)(kk - sexcl) + 1);
-                if (SEG)
-                    tl += s_ntri[case_at(cq, i)];
-                else
-                    atomicAdd(&s_tri[warp][src], (uint32_t)s_ntri[case_at(cq, i)]);
+            // triangles: the round's active cells one per lane (in chunk order),
+            // their counts summed back per chunk in shared memory (chunk mode) or
+            // over the round (segment mode)
+            if (!SEG) s_tri[warp][lane] = 0;
+            uint32_t tl = 0;
+            const uint32_t n = __popc(act);
+            const uint32_t incl = warp_incl_scan(n, lane), excl = incl - n;
+            const uint32_t total = __shfl_sync(FULL, incl, 31);
+            if (!SEG) __syncwarp();
+            for (uint32_t b0 = 0; b0 < total; b0 += 32) {
+                const uint32_t kk = b0 + lane;
+                uint32_t src = 0;
+    #pragma unroll
+                for (uint32_t step = 16; step > 0; step >>= 1) {
+                    const uint32_t cand = src + step;
+                    const uint32_t e = __shfl_sync(FULL, excl, cand & 31);
+                    if (cand < 32 && e <= kk) src = cand;
+                }
+                const uint32_t sact = __shfl_sync(FULL, act, src), sexcl = __shfl_sync(FULL, excl, src);
+                Corners cq;
+    #pragma unroll
+                for (int k = 0; k < 8; ++k) cq.k[k] = __shfl_sync(FULL, q.k[k], src);
+                if (kk < total) {
+                    const uint32_t i = __fns(sact, 0, (int)(kk - sexcl) + 1);
+                    if (SEG)
+                        tl += s_ntri[case_at(cq, i)];
+                    else
+                        atomicAdd(&s_tri[warp][src], (uint32_t)s_ntri[case_at(cq, i)]);
+                }
             }
+            if (SEG) {
+                const uint32_t vr = __reduce_add_sync(FULL, v), tr = __reduce_add_sync(FULL, tl);
+                if (lane == 0 && ch - lane < A.chunks) A.segs[ch / 32] = make_uint4(agg_v, agg_t, vr, tr);
+                agg_v += vr;
+                agg_t += tr;
+                continue;
+            }
+            __syncwarp();
+            const uint32_t t = s_tri[warp][lane];
+            __syncwarp();
+            const uint32_t ti = warp_incl_scan(t, lane), vi = warp_incl_scan(v, lane);
+            if (ch <= A.chunks) A.local[ch] = make_uint2(agg_v + vi - v, agg_t + ti - t);
+            agg_t += __shfl_sync(FULL, ti, 31);
+            agg_v += __shfl_sync(FULL, vi, 31);
         }
-        if (SEG) {
-            const uint32_t vr = __reduce_add_sync(FULL, v), tr = __reduce_add_sync(FULL, tl);
-            if (lane == 0 && ch - lane < A.chunks) A.segs[ch / 32] = make_uint4(agg_v, agg_t, vr, tr);
-            agg_v += vr;
-            agg_t += tr;
-            continue;
-        }
-        __syncwarp();
-        const uint32_t t = s_tri[warp][lane];
-        __syncwarp();
-        const uint32_t ti = warp_incl_scan(t, lane), vi = warp_incl_scan(v, lane);
-        if (ch <= A.chunks) A.local[ch] = make_uint2(agg_v + vi - v, agg_t + ti - t);
-        agg_t += __shfl_sync(FULL, ti, 31);
-        agg_v += __shfl_sync(FULL, vi, 31);
     }
-    if (lane == 0 && range * RANGE < A.chunks) A.rangeagg[range] = make_uint2(agg_v, agg_t);
+    if (!SEG) {
+        if (lane == 0 && range * RANGE < A.chunks) A.rangeagg[range] = make_uint2(agg_v, agg_t);
+        return;
+    }
+    // segment mode: each range's exclusive prefix inside the block's eight
+    // ranges, and the block's totals (scanned across blocks by mc_range_scan)
+    __shared__ uint2 s_agg[8];
+    if (lane == 0) s_agg[warp] = range * RANGE < A.chunks ? make_uint2(agg_v, agg_t) : make_uint2(0, 0);
+    __syncthreads();
+    if (threadIdx.x < 8) {  // thread w: range blockIdx.x * 8 + w
+        const uint32_t r = blockIdx.x * 8 + threadIdx.x;
+        uint2 pre = make_uint2(0, 0);
+        for (uint32_t w = 0; w < threadIdx.x; ++w) {
+            pre.x += s_agg[w].x;
+            pre.y += s_agg[w].y;
+        }
+        if (r * RANGE < A.chunks) A.rangeagg[r] = pre;
+        if (threadIdx.x == 7) A.blockagg[blockIdx.x] = make_uint2(pre.x + s_agg[7].x, pre.y + s_agg[7].y);
+    }
 }
 
 // Exclusive scan of the range totals (one block).  Each thread holds
@@ -273,6 +296,9 @@ struct ChunkEmitArgs {
     uint32_t* host_i;
     uint64_t host_cap_v, host_cap_t;
     const uint64_t* totals;
+    // mc_cell_emit: rangepre holds each range's prefix inside its block of 8
+    // ranges, blockpre each block's exclusive prefix
+    const uint2* blockpre;
 };
 
 // whether this launch copies the mesh to the host buffers
@@ -689,7 +715,9 @@ __global__ void __launch_bounds__(256, 5) mc_cell_emit(ChunkEmitArgs A, const ui
     if (seg >= nsegs) return;
     const uint4 sr = __ldg(&segs[seg]);  // (first vertex, first triangle) in the range, (vertices, triangles)
     if (sr.w == 0) return;                // no triangle in the segment
-    const uint2 rp = __ldg(&A.rangepre[seg / (RANGE / 32)]);
+    const uint32_t range = seg / (RANGE / 32);
+    const uint2 rin = __ldg(&A.rangepre[range]), rb = __ldg(&A.blockpre[range / 8]);
+    const uint32_t vbase = rb.x + rin.x + sr.x, tbase = rb.y + rin.y + sr.y;
     const Grid g = A.grids[0];
     const uint32_t rc = seg * 32, c_end = min(rc + 32, g.nchunks);
     Corners q;
@@ -715,7 +743,7 @@ __global__ void __launch_bounds__(256, 5) mc_cell_emit(ChunkEmitArgs A, const ui
                        hz = __ldg(&g_edge_lo[lane][2]) + (ax == 2);
         koff = 3 * (hx + g.nx * (hy + g.ny * hz)) + ax;
     }
-    uint32_t vcarry = rp.x + sr.x, tcarry = rp.y + sr.y;  // global offsets of the next cell's outputs
+    uint32_t vcarry = vbase, tcarry = tbase;  // global offsets of the next cell's outputs
     for (uint32_t b0 = 0; b0 < total; b0 += 32) {
         const SegCell c = seg_cell(g, rc, b0 + lane, total, act, excl, q);
         const uint32_t vi = warp_incl_scan(c.nown, lane), ti = warp_incl_scan(c.nt, lane);
@@ -728,7 +756,7 @@ __global__ void __launch_bounds__(256, 5) mc_cell_emit(ChunkEmitArgs A, const ui
         // the segment's vertices, just written by this warp, in whole lines
         // to the host (the warp's own stores are ordered before its reads)
         __syncwarp();
-        const size_t f0 = 3 * (size_t)(rp.x + sr.x), f1 = f0 + 3 * (size_t)sr.z;
+        const size_t f0 = 3 * (size_t)vbase, f1 = f0 + 3 * (size_t)sr.z;
         for (size_t f = f0 + lane; f < f1; f += 32) A.host_v[f] = __ldcg(A.out_v + f);
     }
 }

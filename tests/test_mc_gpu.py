@@ -412,3 +412,28 @@ def test_extract_into_host_buffers_with_normals(ctx):
     got = pv.numpy().reshape(-1, 6)
     assert np.array_equal(got[:, :3], want.vertices) and np.array_equal(got[:, 3:], want.normals)
     assert np.array_equal(pi.numpy().view(np.uint32), want.indices)
+
+
+def test_extract_into_registered_numpy_buffers(ctx):
+    """Ordinary host arrays page-locked with iso_host_register take the
+    direct path and give the oracle's bytes; registering twice is refused."""
+    import ctypes
+
+    from isosurface_gb300._capi import lib
+    src = scenes.sphere_union()
+    size = 129
+    want = oracle.Program(S.lower(src)).marching_cubes(size)
+    v = np.zeros((len(want.vertices) + 3, 3), np.float32)
+    i = np.zeros(len(want.indices) + 8, np.uint32)
+    for a in (v, i):
+        assert lib().iso_host_register(ctypes.c_void_p(a.ctypes.data), a.nbytes) == 0
+    try:
+        assert lib().iso_host_register(ctypes.c_void_p(v.ctypes.data), v.nbytes) == 1
+        for _ in range(3):
+            info = ctx.mc_extract_host(src, size, v, i)
+            assert np.array_equal(v[:info.num_vertices], want.vertices)
+            assert np.array_equal(i[:3 * info.num_triangles], want.indices)
+    finally:
+        for a in (v, i):
+            assert lib().iso_host_unregister(ctypes.c_void_p(a.ctypes.data)) == 0
+    assert lib().iso_host_unregister(ctypes.c_void_p(v.ctypes.data)) == 1
