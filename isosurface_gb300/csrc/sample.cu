@@ -49,7 +49,6 @@ __global__ void __launch_bounds__(256) sample_generic(ProgView pv, uint32_t nx, 
 // tile (the margin covers f32 rounding of both bounds and values), and min is
 // exact, so the field equals the full fold over all spheres bit for bit.
 constexpr int TZ = 16;
-constexpr int KEEP_REGS = 4;  // kept spheres held in registers (more: shared-memory loop)
 
 struct SetArgs {
     const float* spheres;  // n x (cx, cy, cz, r)
@@ -97,28 +96,89 @@ __device__ __forceinline__ float4 sphere_thresholds(float r, float reach) {
     return make_float4(T, U, L, 0.0f);
 }
 
-// Exact values of `count` queued samples of row y (entry = N squared
-// distances + (z << 5 | x - x0)): the same fold as the inline path.
-template <int N>
-__device__ __forceinline__ void near_flush(const SetArgs& A, const float* queue, const float* cr, uint32_t y,
-                                           uint32_t x0, int lane, uint32_t count) {
-    if ((uint32_t)lane >= count) return;
-    const uint32_t e = reinterpret_cast<const uint32_t*>(queue + 32 * N)[lane];
-    float v = sqrtf(queue[lane]) - cr[0];
-#pragma unroll
-    for (int i = 1; i < N; ++i) v = fminf(v, sqrtf(queue[32 * i + lane]) - cr[i]);
-    A.field[((size_t)(e >> 5) * A.ny + y) * A.pitch + x0 + (e & 31u)] = v;
+__device__ __forceinline__ uint32_t lane_incl_scan(uint32_t v, int lane) {
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(FULL, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
 }
 
-// One thread's z column with the N kept spheres in registers.  (dx*dx + dy*dy)
-// is shared by the whole column and is exactly len_sq's first partial sum.
-// Full mode: the exact value of every sample.  Near-only mode: the sign of
-// every sample from the thresholds, and the exact value (the same fold) only
-// where some sphere puts the sample within reach of the surface.
+// Near-only mode, one warp on 32 columns (lane = x) of row y, layers z0..z1
+// (at most TZ): the sign of every sample from the thresholds, collected as the
+// layers' sign words in lanes 0..z1-z0 and stored once; each lane notes its
+// samples within reach (some sphere with s <= U and none with s < L) in a bit
+// mask, and after the layers the warp evaluates those samples 32 at a time
+// (lane = sample, found by a shuffle search over the lanes' counts) with the
+// same fold as the full field.  (dx*dx + dy*dy) is shared by a column and is
+// exactly len_sq's first partial sum.
+template <int N, bool FULL_TILE>
+__device__ __forceinline__ void near_column(const SetArgs& A, const float* dxy, const float* cz, const float* cr,
+                                            const float* T, const float* U, const float* L, uint32_t x, uint32_t y,
+                                            uint32_t z0, uint32_t z1, bool valid, int lane, uint32_t wx) {
+    const uint32_t nzt = FULL_TILE ? (uint32_t)TZ : z1 - z0 + 1;
+    const float pzl = world((float)(z0 + lane) * A.inv, A.sz, A.oz, A.domain);  // lane k: layer z0 + k
+    uint32_t nearmask = 0, word = 0;
+    auto layer = [&](uint32_t k) {
+        const float pz = __shfl_sync(FULL, pzl, k);
+        bool in = false, hi = false, deep = false;
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            const float dz = pz - cz[i];
+            const float sq = dxy[i] + dz * dz;
+            in |= sq <= T[i];
+            hi |= sq <= U[i];
+            deep |= sq < L[i];
+        }
+        nearmask |= (uint32_t)(valid && hi && !deep) << k;
+        const uint32_t b = __ballot_sync(FULL, valid && in);
+        if ((uint32_t)lane == k) word = b;
+    };
+    if (FULL_TILE) {
+#pragma unroll
+        for (uint32_t k = 0; k < (uint32_t)TZ; ++k) layer(k);
+    } else {
+        for (uint32_t k = 0; k < nzt; ++k) layer(k);
+    }
+    if ((uint32_t)lane < nzt) A.bits[((size_t)(z0 + lane) * A.ny + y) * A.W + wx] = word;
+    const uint32_t cnt = __popc(nearmask);
+    const uint32_t incl = lane_incl_scan(cnt, lane), excl = incl - cnt;
+    const uint32_t total = __shfl_sync(FULL, incl, 31);
+    for (uint32_t b0 = 0; b0 < total; b0 += 32) {
+        const uint32_t kk = b0 + lane;
+        uint32_t src = 0;
+#pragma unroll
+        for (uint32_t step = 16; step > 0; step >>= 1) {
+            const uint32_t cand = src + step;
+            const uint32_t e = __shfl_sync(FULL, excl, cand & 31);
+            if (cand < 32 && e <= kk) src = cand;
+        }
+        const uint32_t smask = __shfl_sync(FULL, nearmask, src), sexcl = __shfl_sync(FULL, excl, src);
+        float sdxy[N];
+#pragma unroll
+        for (int i = 0; i < N; ++i) sdxy[i] = __shfl_sync(FULL, dxy[i], src);
+        if (kk < total) {
+            const uint32_t z = z0 + __fns(smask, 0, (int)(kk - sexcl) + 1);
+            const float pz = world((float)z * A.inv, A.sz, A.oz, A.domain);
+            float dz = pz - cz[0];
+            float v = sqrtf(sdxy[0] + dz * dz) - cr[0];
+#pragma unroll
+            for (int i = 1; i < N; ++i) {
+                dz = pz - cz[i];
+                v = fminf(v, sqrtf(sdxy[i] + dz * dz) - cr[i]);
+            }
+            A.field[((size_t)z * A.ny + y) * A.pitch + (x - lane + src)] = v;
+        }
+    }
+}
+
+// One thread's z column with the N kept spheres in registers (one warp on 32
+// columns of a row).  Full mode: the exact value of every sample.  Near-only
+// mode: near_column.
 template <int N>
 __device__ __forceinline__ void sphere_column(const SetArgs& A, const float4* keep, const float4* thr, float px,
                                               float py, uint32_t x, uint32_t y, uint32_t z0, uint32_t z1, bool valid,
-                                              int lane, uint32_t wx, float* queue) {
+                                              int lane, uint32_t wx) {
     float dxy[N], cz[N], cr[N], T[N], U[N], L[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) {
@@ -134,77 +194,27 @@ __device__ __forceinline__ void sphere_column(const SetArgs& A, const float4* ke
             L[i] = t.z;
         }
     }
-    uint32_t qn = 0;  // queued near samples (warp-uniform)
+    if (A.near_only) {
+        if (z1 - z0 + 1 == (uint32_t)TZ)
+            near_column<N, true>(A, dxy, cz, cr, T, U, L, x, y, z0, z1, valid, lane, wx);
+        else
+            near_column<N, false>(A, dxy, cz, cr, T, U, L, x, y, z0, z1, valid, lane, wx);
+        return;
+    }
 #pragma unroll 2
     for (uint32_t z = z0; z <= z1; ++z) {
         const float pz = world((float)z * A.inv, A.sz, A.oz, A.domain);
         const size_t row = (size_t)z * A.ny + y;
-        bool inside;
-        if (A.near_only) {
-            float sq[N];
-            bool in = false, hi = false, deep = false;
+        float dz = pz - cz[0];
+        float v = sqrtf(dxy[0] + dz * dz) - cr[0];
 #pragma unroll
-            for (int i = 0; i < N; ++i) {
-                const float dz = pz - cz[i];
-                sq[i] = dxy[i] + dz * dz;
-                in |= sq[i] <= T[i];
-                hi |= sq[i] <= U[i];
-                deep |= sq[i] < L[i];
-            }
-            inside = in;
-            const bool near = valid && hi && !deep;
-            if (!queue) {
-                if (near) {
-                    float v = sqrtf(sq[0]) - cr[0];
-#pragma unroll
-                    for (int i = 1; i < N; ++i) v = fminf(v, sqrtf(sq[i]) - cr[i]);
-                    A.field[row * A.pitch + x] = v;
-                }
-            } else {
-                // near samples queue up (squared distances + position); a full
-                // queue is evaluated by the whole warp, one entry per lane
-                const uint32_t m = __ballot_sync(FULL, near);
-                if (m) {
-                    const uint32_t cnt = __popc(m), pos = qn + __popc(m & ((1u << lane) - 1u));
-                    uint32_t* qpos = reinterpret_cast<uint32_t*>(queue + 32 * N);
-                    if (near && pos < 32) {
-#pragma unroll
-                        for (int i = 0; i < N; ++i) queue[32 * i + pos] = sq[i];
-                        qpos[pos] = (z << 5) | (uint32_t)lane;
-                    }
-                    if (qn + cnt >= 32) {
-                        __syncwarp();
-                        near_flush<N>(A, queue, cr, y, x - lane, lane, 32);
-                        __syncwarp();
-                        if (near && pos >= 32) {
-#pragma unroll
-                            for (int i = 0; i < N; ++i) queue[32 * i + pos - 32] = sq[i];
-                            qpos[pos - 32] = (z << 5) | (uint32_t)lane;
-                        }
-                        qn = qn + cnt - 32;
-                    } else {
-                        qn += cnt;
-                    }
-                }
-            }
-        } else {
-            float dz = pz - cz[0];
-            float v = sqrtf(dxy[0] + dz * dz) - cr[0];
-#pragma unroll
-            for (int i = 1; i < N; ++i) {
-                dz = pz - cz[i];
-                v = fminf(v, sqrtf(dxy[i] + dz * dz) - cr[i]);
-            }
-            if (valid) A.field[row * A.pitch + x] = v;
-            inside = !(v > 0.0f);
+        for (int i = 1; i < N; ++i) {
+            dz = pz - cz[i];
+            v = fminf(v, sqrtf(dxy[i] + dz * dz) - cr[i]);
         }
-        const uint32_t b = __ballot_sync(0xFFFFFFFFu, valid && inside);
+        if (valid) A.field[row * A.pitch + x] = v;
+        const uint32_t b = __ballot_sync(0xFFFFFFFFu, valid && !(v > 0.0f));
         if (lane == 0) A.bits[row * A.W + wx] = b;
-    }
-    if (queue && qn) {
-        __syncwarp();
-        near_flush<N>(A, queue, cr, y, x - lane, lane, qn);
-        __syncwarp();
     }
 }
 
@@ -212,12 +222,12 @@ __device__ __forceinline__ void sphere_column(const SetArgs& A, const float4* ke
 // sign words go to word wx of each row.
 __device__ __forceinline__ void sample_column(const SetArgs& A, const float4* keep, const float4* thr, uint32_t nk,
                                               float px, float py, uint32_t x, uint32_t y, uint32_t z0, uint32_t z1,
-                                              bool valid, int lane, uint32_t wx, float* queue = nullptr) {
+                                              bool valid, int lane, uint32_t wx) {
     switch (nk) {
-    case 1: sphere_column<1>(A, keep, thr, px, py, x, y, z0, z1, valid, lane, wx, queue); return;
-    case 2: sphere_column<2>(A, keep, thr, px, py, x, y, z0, z1, valid, lane, wx, queue); return;
-    case 3: sphere_column<3>(A, keep, thr, px, py, x, y, z0, z1, valid, lane, wx, queue); return;
-    case 4: sphere_column<4>(A, keep, thr, px, py, x, y, z0, z1, valid, lane, wx, queue); return;
+    case 1: sphere_column<1>(A, keep, thr, px, py, x, y, z0, z1, valid, lane, wx); return;
+    case 2: sphere_column<2>(A, keep, thr, px, py, x, y, z0, z1, valid, lane, wx); return;
+    case 3: sphere_column<3>(A, keep, thr, px, py, x, y, z0, z1, valid, lane, wx); return;
+    case 4: sphere_column<4>(A, keep, thr, px, py, x, y, z0, z1, valid, lane, wx); return;
     default: break;
     }
     for (uint32_t z = z0; z <= z1; ++z) {
@@ -470,7 +480,6 @@ __global__ void __launch_bounds__(256, SET_ROWS_BLOCKS) set_rows(SetArgs A, uint
                                                    const uint32_t* mixed, const uint32_t* nmixed, const float4* thr_all) {
     __shared__ float4 s_keep[8][KEEP_MAX];
     __shared__ float4 s_thr[8][KEEP_MAX];
-    __shared__ float s_queue[8][32 * (KEEP_REGS + 1)];  // near-sample queue per warp
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const float4* sp = reinterpret_cast<const float4*>(A.spheres);
     const uint32_t items = 8 * *nmixed;
@@ -526,7 +535,7 @@ __global__ void __launch_bounds__(256, SET_ROWS_BLOCKS) set_rows(SetArgs A, uint
             }
         }
         __syncwarp();
-        sample_column(A, s_keep[warp], s_thr[warp], nk, px, py, x, y, tb.z0, tb.z1, valid, lane, wx, s_queue[warp]);
+        sample_column(A, s_keep[warp], s_thr[warp], nk, px, py, x, y, tb.z0, tb.z1, valid, lane, wx);
     }
 }
 
