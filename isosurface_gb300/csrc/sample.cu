@@ -112,11 +112,11 @@ __device__ __forceinline__ uint32_t lane_incl_scan(uint32_t v, int lane) {
 // (lane = sample, found by a shuffle search over the lanes' counts) with the
 // same fold as the full field.  (dx*dx + dy*dy) is shared by a column and is
 // exactly len_sq's first partial sum.
-template <int N, bool FULL_TILE>
+template <int N>
 __device__ __forceinline__ void near_column(const SetArgs& A, const float* dxy, const float* cz, const float* cr,
                                             const float* T, const float* U, const float* L, uint32_t x, uint32_t y,
                                             uint32_t z0, uint32_t z1, bool valid, int lane, uint32_t wx) {
-    const uint32_t nzt = FULL_TILE ? (uint32_t)TZ : z1 - z0 + 1;
+    const uint32_t nzt = z1 - z0 + 1;
     const float pzl = world((float)(z0 + lane) * A.inv, A.sz, A.oz, A.domain);  // lane k: layer z0 + k
     uint32_t nearmask = 0, word = 0;
     auto layer = [&](uint32_t k) {
@@ -134,12 +134,8 @@ __device__ __forceinline__ void near_column(const SetArgs& A, const float* dxy, 
         const uint32_t b = __ballot_sync(FULL, valid && in);
         if ((uint32_t)lane == k) word = b;
     };
-    if (FULL_TILE) {
-#pragma unroll
-        for (uint32_t k = 0; k < (uint32_t)TZ; ++k) layer(k);
-    } else {
-        for (uint32_t k = 0; k < nzt; ++k) layer(k);
-    }
+#pragma unroll 4
+    for (uint32_t k = 0; k < nzt; ++k) layer(k);
     if ((uint32_t)lane < nzt) A.bits[((size_t)(z0 + lane) * A.ny + y) * A.W + wx] = word;
     const uint32_t cnt = __popc(nearmask);
     const uint32_t incl = lane_incl_scan(cnt, lane), excl = incl - cnt;
@@ -195,10 +191,7 @@ __device__ __forceinline__ void sphere_column(const SetArgs& A, const float4* ke
         }
     }
     if (A.near_only) {
-        if (z1 - z0 + 1 == (uint32_t)TZ)
-            near_column<N, true>(A, dxy, cz, cr, T, U, L, x, y, z0, z1, valid, lane, wx);
-        else
-            near_column<N, false>(A, dxy, cz, cr, T, U, L, x, y, z0, z1, valid, lane, wx);
+        near_column<N>(A, dxy, cz, cr, T, U, L, x, y, z0, z1, valid, lane, wx);
         return;
     }
 #pragma unroll 2
