@@ -173,6 +173,22 @@ def write_device_header(t, path):
           "// Per case, 4 bits per triangle vertex: index of its edge in the first-use order.",
           "ISO_TABLE uint64_t iso_tri_slot[256] = {",
           fmt_rows(slot, 4, lambda v: "0x%015xull" % v),
+          "};"]
+    # what an interior cell needs, in one 16-byte entry: the triangle edge
+    # list, then crossing mask | triangle count << 12 | first-use rank of owned
+    # edges 5, 6 and 10 (class 0) at bits 16, 20, 24
+    pack = []
+    for c in range(256):
+        r = rank[0][c]
+        info = masks[c] | (counts[c] << 12) | (((r >> 20) & 15) << 16) | (((r >> 24) & 15) << 20) | (((r >> 40) & 15) << 24)
+        pack.append((packed[c] & 0xFFFFFFFF, packed[c] >> 32, info, 0))
+    s += ["// Per case, for interior cells: {triangle edges low, high, crossing mask | triangle count << 12 |",
+          "// rank of owned edge 5 << 16 | of edge 6 << 20 | of edge 10 << 24, 0}, one 16-byte load.",
+          "struct alignas(16) IsoCasePack {",
+          "    uint32_t w[4];",
+          "};",
+          "ISO_TABLE IsoCasePack iso_case_pack[256] = {",
+          fmt_rows(pack, 2, lambda v: "{{0x%08x, 0x%08x, 0x%08x, 0}}" % v[:3]),
           "};", ""]
     open(path, "w").write("\n".join(s))
 

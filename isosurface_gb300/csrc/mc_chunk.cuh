@@ -606,11 +606,12 @@ struct SegCell {
     uint32_t x, y, z, cs, nown, nt;
     int cls;
     bool have;
+    uint4 pk;  // interior cells: the case's packed entry (iso_case_pack)
 };
 
 __device__ __forceinline__ SegCell seg_cell(const Grid& g, uint32_t rc, uint32_t kk, uint32_t total, uint32_t act,
                                             uint32_t excl, const Corners& q) {
-    SegCell c{0, 0, 0, 0, 0, 0, 0, kk < total};
+    SegCell c{0, 0, 0, 0, 0, 0, 0, kk < total, make_uint4(0, 0, 0, 0)};
     uint32_t src = 0;
 #pragma unroll
     for (uint32_t step = 16; step > 0; step >>= 1) {
@@ -632,8 +633,14 @@ __device__ __forceinline__ SegCell seg_cell(const Grid& g, uint32_t rc, uint32_t
         c.x = 32 * (cch - row * g.CW) + i;
         c.cs = case_at(cq, i);
         c.cls = (c.x == 0 ? 1 : 0) | (c.y == 0 ? 2 : 0) | (c.z == 0 ? 4 : 0);
-        c.nown = __popc((uint32_t)__ldg(&iso_edge_mask[c.cs]) & __ldg(&iso_owned_mask[c.cls]));
-        c.nt = __ldg(&iso_tri_count[c.cs]);
+        if (c.cls == 0) {
+            c.pk = __ldg(reinterpret_cast<const uint4*>(&iso_case_pack[c.cs]));
+            c.nown = __popc(c.pk.z & 0x460u);  // owned edges 5, 6, 10
+            c.nt = (c.pk.z >> 12) & 7u;
+        } else {
+            c.nown = __popc((uint32_t)__ldg(&iso_edge_mask[c.cs]) & __ldg(&iso_owned_mask[c.cls]));
+            c.nt = __ldg(&iso_tri_count[c.cs]);
+        }
     }
     return c;
 }
@@ -646,14 +653,18 @@ __device__ __forceinline__ void emit_cells(const ChunkEmitArgs& A, const Grid& g
     uint32_t own = 0, cell = 0;
     uint64_t tedges = 0;
     if (c.have) {
-        own = (uint32_t)__ldg(&iso_edge_mask[c.cs]) & __ldg(&iso_owned_mask[c.cls]);
-        tedges = __ldg(&iso_tri_edges[c.cs]);
         cell = (c.z * g.ny + c.y) * g.nx + c.x;  // lattice point of corner 0
+        if (c.cls == 0) {
+            own = c.pk.z & 0x460u;
+            tedges = ((uint64_t)c.pk.y << 32) | c.pk.x;
+        } else {
+            own = (uint32_t)__ldg(&iso_edge_mask[c.cs]) & __ldg(&iso_owned_mask[c.cls]);
+            tedges = __ldg(&iso_tri_edges[c.cs]);
+        }
     }
     if (own) {
         // owned edges: this cell creates their vertices, numbered by
         // first use in the cell's visit order (rank table)
-        const uint64_t rk = __ldg(&iso_owned_rank[c.cls][c.cs]);
         if (c.cls == 0) {
             // interior cell: its owned edges are among 5, 6 and 10, the
             // three edges ending at corner 6 = (x+1, y+1, z+1); all their
@@ -669,15 +680,16 @@ __device__ __forceinline__ void emit_cells(const ChunkEmitArgs& A, const Grid& g
             const float Z0 = (float)c.z * g.inv, Z1 = (float)(c.z + 1) * g.inv;
             const uint32_t k6 = 3 * (cell + g.nx * (g.ny + 1) + 1);  // corner 6's key base
             if (e5)  // corners 5 -> 6, y axis
-                put_vertex(A, g, f5, f6, X1, Y0, Z1, X1, Y1, Z1, vstart + (uint32_t)(rk >> 20 & 15u),
-                           k6 + 1, grid_v0, c.x + 1, c.y, c.z + 1, 1);
+                put_vertex(A, g, f5, f6, X1, Y0, Z1, X1, Y1, Z1, vstart + (c.pk.z >> 16 & 15u), k6 + 1, grid_v0,
+                           c.x + 1, c.y, c.z + 1, 1);
             if (e6)  // corners 6 -> 7, x axis
-                put_vertex(A, g, f6, f7, X1, Y1, Z1, X0, Y1, Z1, vstart + (uint32_t)(rk >> 24 & 15u),
-                           k6 + 0, grid_v0, c.x, c.y + 1, c.z + 1, 0);
+                put_vertex(A, g, f6, f7, X1, Y1, Z1, X0, Y1, Z1, vstart + (c.pk.z >> 20 & 15u), k6 + 0, grid_v0,
+                           c.x, c.y + 1, c.z + 1, 0);
             if (e10)  // corners 2 -> 6, z axis
-                put_vertex(A, g, f2, f6, X1, Y1, Z0, X1, Y1, Z1, vstart + (uint32_t)(rk >> 40 & 15u),
-                           k6 + 2, grid_v0, c.x + 1, c.y + 1, c.z, 2);
+                put_vertex(A, g, f2, f6, X1, Y1, Z0, X1, Y1, Z1, vstart + (c.pk.z >> 24 & 15u), k6 + 2, grid_v0,
+                           c.x + 1, c.y + 1, c.z, 2);
         } else {
+            const uint64_t rk = __ldg(&iso_owned_rank[c.cls][c.cs]);
             for (uint32_t m = own; m; m &= m - 1) {
                 const uint32_t e = __ffs(m) - 1;
                 const uint32_t ax = __ldg(&g_edge_axis[e]);
