@@ -437,3 +437,25 @@ def test_extract_into_registered_numpy_buffers(ctx):
         for a in (v, i):
             assert lib().iso_host_unregister(ctypes.c_void_p(a.ctypes.data)) == 0
     assert lib().iso_host_unregister(ctypes.c_void_p(v.ctypes.data)) == 1
+
+
+def test_extract_into_host_buffers_257(ctx):
+    """Delivery to page-locked buffers at 257^3 (16K segments, several
+    resolve steps per thread): eager, recorded and replayed runs give the
+    oracle's bytes."""
+    import torch
+    src = scenes.sphere_union()
+    size = 257
+    want = oracle.Program(S.lower(src)).marching_cubes(size)
+    nv, nt = len(want.vertices), len(want.indices) // 3
+    prog = ctx.program(src)
+    pv, pi = _pinned(3 * nv, torch.float32), _pinned(3 * nt, torch.int32)
+    for _ in range(4):
+        pv.fill_(0.0)
+        pi.fill_(0)
+        info = ctx.mc_extract_host(prog, size, pv, pi)
+        assert (info.num_vertices, info.num_triangles) == (nv, nt)
+        assert np.array_equal(pv.numpy().reshape(-1, 3), want.vertices)
+        assert np.array_equal(pi.numpy().view(np.uint32), want.indices)
+    got = ctx.download(info)
+    assert np.array_equal(got.indices, want.indices)
