@@ -8,8 +8,15 @@ grid (the reference's traversal visits 513 cell layers): sampling, cell
 classification + scan, vertex/index emission.  `value` is timed with CUDA
 events on the library's stream with the program already resident and the
 mesh left on the device; `e2e` times the public C ABI with host buffers
-(program upload H2D, mesh download D2H into pinned memory) on the host clock.
-L2 is flushed (a 256 MiB write) before every timed step.
+(program upload H2D from host bytes, iso_mc_extract_host into page-locked
+host buffers) on the host clock.  L2 is flushed (a 256 MiB write) before
+every timed step.
+
+`roofline` covers the extraction pass (counting, scan, emission, resolve):
+achieved = (4 B per sample for the field read once + 12 B per vertex + 12 B
+per triangle) / that pass's event-timed duration, against the measured HBM
+copy bandwidth; `traffic` is the DRAM bytes ncu measured for the same
+kernels (profiles/traffic.json).
 
 --impl reference times the oracle (the C++ restatement of the reference's
 single-threaded Rust CPU path; Rust does not build here) on all host cores,
@@ -399,40 +406,37 @@ def main():
     ms = replicas.max_over_ranks(sum(step_ms) / len(step_ms), dist, "cuda")
     value = replicas.whole_job_rate(CELLS, world, ms / 1e3)
 
-    # per-stage device time (CUDA events on the launching stream) and roofline.
-    # The library counts, scans and emits in one pass for this lattice, so the
-    # classify stage launches nothing and its bytes belong to the emit stage.
-    stages = {"sample": 0, "classify_scan": 1, "emit": 2}
-    if int(ln_buf[1]) == 0:
-        del stages["classify_scan"]
+    # per-stage device time (CUDA events on the launching stream) and the
+    # roofline of the extraction pass (counting, scan, emission, resolve): the
+    # unit the workload's bytes are defined for -- the field read once (4 B per
+    # sample) plus the mesh written (12 B per vertex, 12 B per triangle).  The
+    # library reads sign bits and near-surface values instead of the field, so
+    # its measured traffic is below that figure.
     nv, nt = info.num_vertices, info.num_triangles
     samples = SIZE * SIZE * (SIZE + 1)
     words = (SIZE + 31) // 32
-    sign_bytes = 4 * words * SIZE * (SIZE + 1)  # one sign bit per sample, rows padded to 32-bit words
-    algo_bytes = {
-        # sign bits written once + the two crossing values of each vertex
-        "sample": sign_bytes + 8 * nv,
-        # sign-bit volume read once + two u32 offsets per cell row
-        "classify_scan": sign_bytes + 8 * (SIZE - 1) * SIZE,
-        # mesh written (12 B per vertex, 12 B per triangle) + 2 field samples read
-        # per vertex (+ the sign-bit volume when counting is fused in)
-        "emit": 12 * nv + 12 * nt + 8 * nv + (0 if "classify_scan" in stages else sign_bytes),
-    }
+    stage_ix = {"sample": 0, "classify_scan": 1, "emit": 2}
     per_stage = {}
-    for name, i in stages.items():
+    total_ms = max(sum(ms_buf[i] for i in stage_ix.values()), 1e-9)
+    for name, i in stage_ix.items():
         n = max(int(ln_buf[i]), 1)
-        per_stage[name] = {"ms_per_launch": ms_buf[i] / n, "launches": int(ln_buf[i]),
-                           "share": ms_buf[i] / max(sum(ms_buf[j] for j in stages.values()), 1e-9)}
-    dom = max(stages, key=lambda s: ms_buf[stages[s]])
+        per_stage[name] = {"ms_per_launch": ms_buf[i] / n, "launches": int(ln_buf[i]), "share": ms_buf[i] / total_ms}
+    extract_ms = per_stage["classify_scan"]["ms_per_launch"] + per_stage["emit"]["ms_per_launch"]
+    algo = 4 * samples + 12 * nv + 12 * nt
     peak, peak_kind = peaks()
-    achieved = algo_bytes[dom] / (per_stage[dom]["ms_per_launch"] / 1e3) / 1e9
+    achieved = algo / (extract_ms / 1e3) / 1e9
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
-        traffic = json.load(open(tpath)).get(dom)
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
-                "algorithmic_bytes": algo_bytes[dom]}
+        t = json.load(open(tpath))
+        if "classify_scan" in t and "emit" in t:
+            traffic = t["classify_scan"] + t["emit"]
+    roofline = {"bound": "hbm", "kernel": "extraction (mc_chunk_count, mc_range_scan, mc_cell_emit, mc_resolve_ids)",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": traffic, "algorithmic_bytes": algo, "ms_per_launch": extract_ms,
+                "sampler": {"ms_per_launch": per_stage["sample"]["ms_per_launch"],
+                            "bytes_written": 4 * words * SIZE * (SIZE + 1) + 8 * nv,
+                            "note": "sign bits of every sample and exact values only near the surface"}}
 
     # e2e through the public C ABI with host buffers
     from isosurface_gb300._capi import MeshInfo, check
