@@ -667,7 +667,7 @@ static iso_status mc_lattice_passes(iso_ctx* ctx, const Lattice& L, uint32_t fla
         {
             StageTimer timer(ctx, ISO_STAGE_EMIT);
             if (edge_map) {
-                mc_cell_emit<<<(nsegs + 7) / 8, 256, 0, ctx->stream>>>(ea, segs, nsegs);
+                mc_cell_emit<<<(nsegs + 8 * EMIT_SEGS - 1) / (8 * EMIT_SEGS), 256, 0, ctx->stream>>>(ea, segs, nsegs);
                 mc_resolve_ids<<<resolve_blocks(cap_t), 256, 0, ctx->stream>>>(
                     (uint32_t*)ctx->mesh_i.p, totals, cap_t, (const uint32_t*)ctx->edges.p, (uint32_t)nedges, H.i,
                     H.cap_v, H.cap_t, cap_v);

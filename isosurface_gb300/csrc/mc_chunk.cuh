@@ -600,8 +600,23 @@ __device__ __forceinline__ void put_vertex(const ChunkEmitArgs& A, const Grid& g
 // has an owner, and only crossing edges are referenced).  Keys are
 // 3 * (upper end point) + axis, so the (at most three) edges an interior
 // cell owns, which all end at its corner 6, share one 12-byte slot.
-// Active cell number kk (in chunk order) of the segment starting at grid
-// chunk rc; every lane calls it, have = kk < total.
+// Segments of 32 chunks per warp in mc_cell_emit: a segment (two cell rows at
+// 513^3) holds a dozen or two active cells, so a warp takes several and hands
+// out their active cells together.
+constexpr int EMIT_SEGS = 2;
+constexpr int EMIT_CH = 32 * EMIT_SEGS;  // chunks per warp
+
+// A warp's chunks in shared memory: corner words (padded to 9 words, so that
+// lanes reading different chunks hit different banks), active-cell masks and
+// the exclusive prefix of their counts in chunk order.
+struct EmitChunks {
+    uint32_t q[EMIT_CH][9];
+    uint32_t act[EMIT_CH];
+    uint32_t excl[EMIT_CH];
+};
+
+// Active cell number kk (in chunk order) of the warp's chunks starting at
+// grid chunk rc; every lane calls it, have = kk < total.
 struct SegCell {
     uint32_t x, y, z, cs, nown, nt;
     int cls;
@@ -609,38 +624,32 @@ struct SegCell {
     uint4 pk;  // interior cells: the case's packed entry (iso_case_pack)
 };
 
-__device__ __forceinline__ SegCell seg_cell(const Grid& g, uint32_t rc, uint32_t kk, uint32_t total, uint32_t act,
-                                            uint32_t excl, const Corners& q) {
+__device__ __forceinline__ SegCell seg_cell(const Grid& g, uint32_t rc, uint32_t kk, uint32_t total,
+                                            const EmitChunks& S) {
     SegCell c{0, 0, 0, 0, 0, 0, 0, kk < total, make_uint4(0, 0, 0, 0)};
-    uint32_t src = 0;
+    if (!c.have) return c;
+    uint32_t j = 0;  // the last chunk whose prefix is <= kk
 #pragma unroll
-    for (uint32_t step = 16; step > 0; step >>= 1) {
-        const uint32_t cand = src + step;
-        const uint32_t e = __shfl_sync(FULL, excl, cand & 31);
-        if (cand < 32 && e <= kk) src = cand;
-    }
-    const uint32_t sact = __shfl_sync(FULL, act, src);
-    const uint32_t sexcl = __shfl_sync(FULL, excl, src);
+    for (uint32_t step = EMIT_CH / 2; step > 0; step >>= 1)
+        if (S.excl[j + step] <= kk) j += step;
     Corners cq;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) cq.k[k] = __shfl_sync(FULL, q.k[k], src);
-    if (c.have) {
-        const uint32_t i = __fns(sact, 0, (int)(kk - sexcl) + 1);
-        const uint32_t cch = rc + src;
-        const uint32_t row = fdiv(cch, g.div_cw);
-        c.z = fdiv(row, g.div_ncy);
-        c.y = row - c.z * (g.ny - 1);
-        c.x = 32 * (cch - row * g.CW) + i;
-        c.cs = case_at(cq, i);
-        c.cls = (c.x == 0 ? 1 : 0) | (c.y == 0 ? 2 : 0) | (c.z == 0 ? 4 : 0);
-        if (c.cls == 0) {
-            c.pk = __ldg(reinterpret_cast<const uint4*>(&iso_case_pack[c.cs]));
-            c.nown = __popc(c.pk.z & 0x460u);  // owned edges 5, 6, 10
-            c.nt = (c.pk.z >> 12) & 7u;
-        } else {
-            c.nown = __popc((uint32_t)__ldg(&iso_edge_mask[c.cs]) & __ldg(&iso_owned_mask[c.cls]));
-            c.nt = __ldg(&iso_tri_count[c.cs]);
-        }
+    for (int k = 0; k < 8; ++k) cq.k[k] = S.q[j][k];
+    const uint32_t i = __fns(S.act[j], 0, (int)(kk - S.excl[j]) + 1);
+    const uint32_t cch = rc + j;
+    const uint32_t row = fdiv(cch, g.div_cw);
+    c.z = fdiv(row, g.div_ncy);
+    c.y = row - c.z * (g.ny - 1);
+    c.x = 32 * (cch - row * g.CW) + i;
+    c.cs = case_at(cq, i);
+    c.cls = (c.x == 0 ? 1 : 0) | (c.y == 0 ? 2 : 0) | (c.z == 0 ? 4 : 0);
+    if (c.cls == 0) {
+        c.pk = __ldg(reinterpret_cast<const uint4*>(&iso_case_pack[c.cs]));
+        c.nown = __popc(c.pk.z & 0x460u);  // owned edges 5, 6, 10
+        c.nt = (c.pk.z >> 12) & 7u;
+    } else {
+        c.nown = __popc((uint32_t)__ldg(&iso_edge_mask[c.cs]) & __ldg(&iso_owned_mask[c.cls]));
+        c.nt = __ldg(&iso_tri_count[c.cs]);
     }
     return c;
 }
@@ -722,32 +731,53 @@ __device__ __forceinline__ void emit_cells(const ChunkEmitArgs& A, const Grid& g
 }
 
 __global__ void __launch_bounds__(256, 5) mc_cell_emit(ChunkEmitArgs A, const uint4* segs, uint32_t nsegs) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t seg = blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (seg >= nsegs) return;
-    const uint4 sr = __ldg(&segs[seg]);  // (first vertex, first triangle) in the range, (vertices, triangles)
-    if (sr.w == 0) return;                // no triangle in the segment
-    const uint32_t range = seg / (RANGE / 32);
+    __shared__ EmitChunks s_ch[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t seg0 = (blockIdx.x * 8 + warp) * EMIT_SEGS;  // the warp's first segment
+    if (seg0 >= nsegs) return;
+    // records: (first vertex, first triangle) in the range, (vertices, triangles)
+    const uint4 sr = __ldg(&segs[seg0]);
+    uint32_t nv_w = sr.z, nt_w = sr.w;
+#pragma unroll
+    for (int h = 1; h < EMIT_SEGS; ++h)
+        if (seg0 + h < nsegs) {
+            const uint4 r = __ldg(&segs[seg0 + h]);
+            nv_w += r.z;
+            nt_w += r.w;
+        }
+    if (nt_w == 0) return;  // no triangle in the warp's segments
+    const uint32_t range = seg0 / (RANGE / 32);  // EMIT_SEGS divides the 8 segments of a range
     const uint2 rin = __ldg(&A.rangepre[range]), rb = __ldg(&A.blockpre[range / 8]);
     const uint32_t vbase = rb.x + rin.x + sr.x, tbase = rb.y + rin.y + sr.y;
     const Grid g = A.grids[0];
-    const uint32_t rc = seg * 32, c_end = min(rc + 32, g.nchunks);
-    Corners q;
-    uint32_t act = 0;
-    if (rc + lane < c_end) {
-        const uint32_t ch = rc + lane;
-        const uint32_t row = fdiv(ch, g.div_cw);
-        const uint32_t cc = ch - row * g.CW;
-        const uint32_t z = fdiv(row, g.div_ncy);
-        q = load_corners(g.bits, g.W, g.ny, row - z * (g.ny - 1), z, cc);
-        act = active_cells(q, chunk_valid(cc, g.nx - 1));
-    } else {
+    const uint32_t rc = seg0 * 32, c_end = min(rc + (uint32_t)EMIT_CH, g.nchunks);
+    EmitChunks& S = s_ch[warp];
+    // lane = chunk, EMIT_SEGS times: corner bit-vectors, active cells, prefix
+    uint32_t total = 0;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) q.k[k] = 0;
+    for (int h = 0; h < EMIT_SEGS; ++h) {
+        const uint32_t ch = rc + 32 * h + lane;
+        Corners q;
+        uint32_t act = 0;
+        if (ch < c_end) {
+            const uint32_t row = fdiv(ch, g.div_cw);
+            const uint32_t cc = ch - row * g.CW;
+            const uint32_t z = fdiv(row, g.div_ncy);
+            q = load_corners(g.bits, g.W, g.ny, row - z * (g.ny - 1), z, cc);
+            act = active_cells(q, chunk_valid(cc, g.nx - 1));
+        } else {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) q.k[k] = 0;
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) S.q[32 * h + lane][k] = q.k[k];
+        S.act[32 * h + lane] = act;
+        const uint32_t n = __popc(act);
+        const uint32_t incl = warp_incl_scan(n, lane);
+        S.excl[32 * h + lane] = total + incl - n;
+        total += __shfl_sync(FULL, incl, 31);
     }
-    const uint32_t n = __popc(act);
-    const uint32_t incl = warp_incl_scan(n, lane), excl = incl - n;
-    const uint32_t total = __shfl_sync(FULL, incl, 31);
+    __syncwarp();
     uint32_t koff = 0;
     if (lane < 12) {
         const uint32_t ax = __ldg(&g_edge_axis[lane]);
@@ -757,7 +787,7 @@ __global__ void __launch_bounds__(256, 5) mc_cell_emit(ChunkEmitArgs A, const ui
     }
     uint32_t vcarry = vbase, tcarry = tbase;  // global offsets of the next cell's outputs
     for (uint32_t b0 = 0; b0 < total; b0 += 32) {
-        const SegCell c = seg_cell(g, rc, b0 + lane, total, act, excl, q);
+        const SegCell c = seg_cell(g, rc, b0 + lane, total, S);
         const uint32_t vi = warp_incl_scan(c.nown, lane), ti = warp_incl_scan(c.nt, lane);
         const uint32_t vstart = vcarry + vi - c.nown, tstart = tcarry + ti - c.nt;
         vcarry += __shfl_sync(FULL, vi, 31);
@@ -765,10 +795,10 @@ __global__ void __launch_bounds__(256, 5) mc_cell_emit(ChunkEmitArgs A, const ui
         emit_cells(A, g, c, vstart, tstart, koff, 0u);
     }
     if (mesh_to_host(A.host_v, A.totals, A.host_cap_v, A.host_cap_t, A.cap_v, A.cap_t)) {
-        // the segment's vertices, just written by this warp, in whole lines
+        // the segments' vertices, just written by this warp, in whole lines
         // to the host (the warp's own stores are ordered before its reads)
         __syncwarp();
-        const size_t f0 = 3 * (size_t)vbase, f1 = f0 + 3 * (size_t)sr.z;
+        const size_t f0 = 3 * (size_t)vbase, f1 = f0 + 3 * (size_t)nv_w;
         for (size_t f = f0 + lane; f < f1; f += 32) A.host_v[f] = __ldcg(A.out_v + f);
     }
 }
