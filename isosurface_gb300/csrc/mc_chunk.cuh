@@ -79,6 +79,32 @@ struct ChunkCountArgs {
     uint2* blockagg;
 };
 
+// Segments of 32 chunks per warp in mc_cell_emit: a segment (two cell rows at
+// 513^3) holds a dozen or two active cells, so a warp takes several and hands
+// out their active cells together.
+constexpr int EMIT_SEGS = 2;
+constexpr int EMIT_CH = 32 * EMIT_SEGS;  // chunks per warp
+
+// N chunks of a warp in shared memory: corner words (padded to 9 words, so
+// that lanes reading different chunks hit different banks), active-cell masks
+// and the exclusive prefix of their counts in chunk order.
+template <int N>
+struct ChunkStage {
+    uint32_t q[N][9];
+    uint32_t act[N];
+    uint32_t excl[N];
+    // the chunk holding active cell number kk (kk < the chunks' total): the
+    // last one whose prefix is <= kk
+    __device__ __forceinline__ uint32_t find(uint32_t kk) const {
+        uint32_t j = 0;
+#pragma unroll
+        for (uint32_t step = N / 2; step > 0; step >>= 1)
+            if (excl[j + step] <= kk) j += step;
+        return j;
+    }
+};
+using EmitChunks = ChunkStage<EMIT_CH>;
+
 // Pass 1: per-chunk (SEG = false) or per-segment (32 chunks, SEG = true)
 // counts and in-range prefixes.  One warp per range of 256 chunks, 32 per
 // round (no barrier); the next round's corner words are loaded while this
@@ -87,7 +113,8 @@ template <bool SEG>
 __global__ void __launch_bounds__(256) mc_chunk_count(ChunkCountArgs A) {
     __shared__ uint8_t s_ntri[256];
     __shared__ uint16_t s_owned[8];
-    __shared__ uint32_t s_tri[8][32];  // per warp: triangles of each of the round's chunks
+    __shared__ uint32_t s_tri[8][32];  // chunk mode, per warp: triangles of each of the round's chunks
+    __shared__ ChunkStage<SEG ? 64 : 2> s_pair[8];  // segment mode, per warp: two rounds of chunks
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     s_ntri[threadIdx.x] = iso_tri_count[threadIdx.x];
     if (threadIdx.x < 8) s_owned[threadIdx.x] = iso_owned_mask[threadIdx.x];
@@ -119,6 +146,7 @@ __global__ void __launch_bounds__(256) mc_chunk_count(ChunkCountArgs A) {
         };
         uint32_t ny_, nz_, nc_;
         bool nin;
+        uint32_t pair_total = 0, vr_first = 0;  // segment mode
         Corners qn = fetch(range * RANGE + lane, ny_, nz_, nc_, nin);
         for (int r = 0; r < RANGE_ROUNDS; ++r) {
             const uint32_t ch = range * RANGE + r * 32 + lane;
@@ -139,15 +167,59 @@ __global__ void __launch_bounds__(256) mc_chunk_count(ChunkCountArgs A) {
                     v = owned_count(q, act, s_owned[cls], s_owned[cls | 1], c == 0 ? 1u : 0u);
                 }
             }
+            if constexpr (SEG) {
+                // two rounds (two segments) at a time: the chunks go to shared
+                // memory, and the pair's active cells are handed out one per
+                // lane in chunk order, their triangles summed per segment
+                const uint32_t h = r & 1;
+                ChunkStage<64>& P = s_pair[warp];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) P.q[32 * h + lane][k] = q.k[k];
+                P.act[32 * h + lane] = act;
+                const uint32_t n = __popc(act);
+                const uint32_t incl = warp_incl_scan(n, lane);
+                P.excl[32 * h + lane] = pair_total + incl - n;
+                pair_total += __shfl_sync(FULL, incl, 31);
+                const uint32_t vr = __reduce_add_sync(FULL, v);
+                if (h == 0) {
+                    vr_first = vr;
+                    continue;
+                }
+                __syncwarp();
+                uint32_t t0 = 0, t1 = 0;
+                for (uint32_t b0 = 0; b0 < pair_total; b0 += 32) {
+                    const uint32_t kk = b0 + lane;
+                    if (kk < pair_total) {
+                        const uint32_t j = P.find(kk);
+                        Corners cq;
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) cq.k[k] = P.q[j][k];
+                        const uint32_t t = s_ntri[case_at(cq, __fns(P.act[j], 0, (int)(kk - P.excl[j]) + 1))];
+                        if (j < 32)
+                            t0 += t;
+                        else
+                            t1 += t;
+                    }
+                }
+                const uint32_t tr0 = __reduce_add_sync(FULL, t0), tr1 = __reduce_add_sync(FULL, t1);
+                const uint32_t first = ch - lane - 32;  // the pair's first chunk
+                if (lane == 0 && first < A.chunks) A.segs[first / 32] = make_uint4(agg_v, agg_t, vr_first, tr0);
+                agg_v += vr_first;
+                agg_t += tr0;
+                if (lane == 0 && first + 32 < A.chunks) A.segs[first / 32 + 1] = make_uint4(agg_v, agg_t, vr, tr1);
+                agg_v += vr;
+                agg_t += tr1;
+                pair_total = 0;
+                __syncwarp();  // the pair's chunks are read before the next pair overwrites them
+                continue;
+            }
             // triangles: the round's active cells one per lane (in chunk order),
-            // their counts summed back per chunk in shared memory (chunk mode) or
-            // over the round (segment mode)
-            if (!SEG) s_tri[warp][lane] = 0;
-            uint32_t tl = 0;
+            // their counts summed back per chunk in shared memory
+            s_tri[warp][lane] = 0;
             const uint32_t n = __popc(act);
             const uint32_t incl = warp_incl_scan(n, lane), excl = incl - n;
             const uint32_t total = __shfl_sync(FULL, incl, 31);
-            if (!SEG) __syncwarp();
+            __syncwarp();
             for (uint32_t b0 = 0; b0 < total; b0 += 32) {
                 const uint32_t kk = b0 + lane;
                 uint32_t src = 0;
@@ -163,18 +235,8 @@ __global__ void __launch_bounds__(256) mc_chunk_count(ChunkCountArgs A) {
                 for (int k = 0; k < 8; ++k) cq.k[k] = __shfl_sync(FULL, q.k[k], src);
                 if (kk < total) {
                     const uint32_t i = __fns(sact, 0, (int)(kk - sexcl) + 1);
-                    if (SEG)
-                        tl += s_ntri[case_at(cq, i)];
-                    else
-                        atomicAdd(&s_tri[warp][src], (uint32_t)s_ntri[case_at(cq, i)]);
+                    atomicAdd(&s_tri[warp][src], (uint32_t)s_ntri[case_at(cq, i)]);
                 }
-            }
-            if (SEG) {
-                const uint32_t vr = __reduce_add_sync(FULL, v), tr = __reduce_add_sync(FULL, tl);
-                if (lane == 0 && ch - lane < A.chunks) A.segs[ch / 32] = make_uint4(agg_v, agg_t, vr, tr);
-                agg_v += vr;
-                agg_t += tr;
-                continue;
             }
             __syncwarp();
             const uint32_t t = s_tri[warp][lane];
@@ -600,21 +662,6 @@ __device__ __forceinline__ void put_vertex(const ChunkEmitArgs& A, const Grid& g
 // has an owner, and only crossing edges are referenced).  Keys are
 // 3 * (upper end point) + axis, so the (at most three) edges an interior
 // cell owns, which all end at its corner 6, share one 12-byte slot.
-// Segments of 32 chunks per warp in mc_cell_emit: a segment (two cell rows at
-// 513^3) holds a dozen or two active cells, so a warp takes several and hands
-// out their active cells together.
-constexpr int EMIT_SEGS = 2;
-constexpr int EMIT_CH = 32 * EMIT_SEGS;  // chunks per warp
-
-// A warp's chunks in shared memory: corner words (padded to 9 words, so that
-// lanes reading different chunks hit different banks), active-cell masks and
-// the exclusive prefix of their counts in chunk order.
-struct EmitChunks {
-    uint32_t q[EMIT_CH][9];
-    uint32_t act[EMIT_CH];
-    uint32_t excl[EMIT_CH];
-};
-
 // Active cell number kk (in chunk order) of the warp's chunks starting at
 // grid chunk rc; every lane calls it, have = kk < total.
 struct SegCell {
@@ -628,10 +675,7 @@ __device__ __forceinline__ SegCell seg_cell(const Grid& g, uint32_t rc, uint32_t
                                             const EmitChunks& S) {
     SegCell c{0, 0, 0, 0, 0, 0, 0, kk < total, make_uint4(0, 0, 0, 0)};
     if (!c.have) return c;
-    uint32_t j = 0;  // the last chunk whose prefix is <= kk
-#pragma unroll
-    for (uint32_t step = EMIT_CH / 2; step > 0; step >>= 1)
-        if (S.excl[j + step] <= kk) j += step;
+    const uint32_t j = S.find(kk);
     Corners cq;
 #pragma unroll
     for (int k = 0; k < 8; ++k) cq.k[k] = S.q[j][k];
