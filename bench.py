@@ -302,8 +302,8 @@ def run_reference(args):
     # size each step to a few seconds of work
     mid = SIZE // 2
     secs, _, _ = prog.mc_timed(SIZE, mid, mid + threads, threads)
-    # each step a bounded sample: the whole run stays near a minute and a half
-    per_step = min(3.0, 90.0 / max(1, args.steps + args.warmup))
+    # each step a bounded sample: the whole run stays near the budget
+    per_step = min(3.0, args.reference_budget / max(1, args.steps + args.warmup))
     layers = max(threads, int(per_step / max(secs, 1e-6)) * threads)
     layers = min(layers, SIZE - 1)
     z0 = max(0, mid - layers // 2)
@@ -333,6 +333,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--reference-budget", type=float, default=90.0,
+                    help="--impl reference: seconds of oracle work across all steps (each step at most 3 s)")
     ap.add_argument("--no-secondary", action="store_true", help="skip the batch / DC / LHMC timings")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-surrogate workload")
     ap.add_argument("--secondary-only", default=None,
