@@ -14,17 +14,27 @@
 //   cell's triangles -- checked when the tables are generated), so each cell
 //   knows which of its crossing edges it "owns": interior cells own the three
 //   edges at their far corner; cells on the x=0 / y=0 / z=0 faces own more.
-// * Pass 1 (mc_count_scan) classifies every cell from packed sign bits and
-//   scans, per x-row of cells, the triangle count and the owned-vertex count
-//   with a single-pass decoupled look-back scan: rowtri[r], rowvert[r] are the
-//   exclusive output offsets of row r (r = z*(ny-1) + y).
-// * Pass 2 (mc_emit) re-derives, for a strip of rows of one z layer and the
-//   rows at y-1 and z-1 that own the strip's other edges, each cell's case and
-//   in-row prefix of owned vertices in shared memory.  A vertex id is then the
-//   owner row's offset + the owner cell's in-row prefix + the edge's rank in
-//   the owner's first-use order.  The owner computes the crossing with its
-//   own edge direction, as the reference's first visitor does, so positions
-//   are bit-identical.
+// * Extractions with a context use the chunk passes of mc_chunk.cuh (a chunk
+//   is 32 cells of a row): mc_chunk_count classifies every cell from packed
+//   sign bits and counts triangles and owned vertices per 32-chunk segment
+//   (or per chunk for the block emit), mc_range_scan turns the totals into
+//   offsets, and mc_cell_emit writes the vertices, records each owned
+//   vertex's id in a dense per-edge map and writes the triangles as map keys,
+//   which mc_resolve_ids turns into vertex ids.  Dual lattices, chunk batches
+//   and grids whose edge count exceeds 32 bits use mc_block_emit instead,
+//   which finds each owner's id from per-chunk prefixes in shared memory.
+// * The allocation-free entry point (iso_mc_extract_field_noalloc) keeps the
+//   row passes below: mc_count_scan classifies every cell and scans, per
+//   x-row of cells, the triangle count and the owned-vertex count with a
+//   single-pass decoupled look-back scan (rowtri[r], rowvert[r] are the
+//   exclusive output offsets of row r = z*(ny-1) + y); mc_emit re-derives,
+//   for a strip of rows of one z layer and the rows at y-1 and z-1 that own
+//   the strip's other edges, each cell's case and in-row prefix of owned
+//   vertices in shared memory.  A vertex id is then the owner row's offset +
+//   the owner cell's in-row prefix + the edge's rank in the owner's
+//   first-use order.
+// * Either way the owner computes the crossing with its own edge direction,
+//   as the reference's first visitor does, so positions are bit-identical.
 #include <cuda_runtime.h>
 
 #include <atomic>
