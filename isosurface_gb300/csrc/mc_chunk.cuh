@@ -7,13 +7,18 @@
 // funnel shifts, so activity and owned-vertex counts cost a few dozen bit
 // operations per 32 cells.
 //
-// Several grids can be processed by one launch: each grid's chunks occupy a
-// run of whole RANGEs (256 chunks) of a global chunk index space, and
-// range_grid maps a range to its grid (a null map means one grid).  Offsets:
-// pass 1 gives every chunk its exclusive prefix inside its range plus each
-// range's total; a one-block scan turns range totals into range offsets;
-// chunk base = range offset + in-range prefix.  Vertex indices are written
-// relative to the grid's first vertex, so each grid gets its own mesh.
+// Offsets come in two forms.  Chunk mode (the block emit): pass 1 gives every
+// chunk its exclusive prefix inside its range of 256 chunks plus each range's
+// total; a one-block scan turns range totals into range offsets; chunk base =
+// range offset + in-range prefix.  Several grids can be processed by one
+// launch in this mode: each grid's chunks occupy a run of whole ranges of a
+// global chunk index space, range_grid maps a range to its grid (a null map
+// means one grid), and vertex indices are written relative to the grid's
+// first vertex, so each grid gets its own mesh.  Segment mode (the cell emit,
+// one grid): pass 1 writes one record per 32-chunk segment (prefix inside
+// its range, own counts), each range's prefix inside its block of 8 ranges
+// and each block's totals; the one-block scan runs over the block totals;
+// segment base = block offset + in-block range prefix + in-range prefix.
 // Corners, load_corners, case_at, chunk_valid, active_cells and owned_count
 // are defined in mc.cu above the include.
 
