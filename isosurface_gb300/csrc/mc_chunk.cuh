@@ -652,21 +652,6 @@ __device__ __forceinline__ void put_vertex(const ChunkEmitArgs& A, const Grid& g
     A.edge_id[key] = vid - grid_v0;
 }
 
-// Pass 2, cell-parallel, for one lattice given by values alone (no explicit
-// sample positions) whose edge count fits 32 bits.  Warp = one segment of 32
-// chunks (lane = chunk: corner words and active cells), whose first vertex
-// and triangle come from pass 1's segment records.  The segment's active
-// cells are handed out 32 at a time in chunk order (lane = cell: the owning
-// chunk by a shuffle search over the chunks' exclusive counts, the bit by
-// __fns), so lanes stay busy however the active cells are spread.  A cell's
-// own offsets are the segment's base plus a running warp scan of owned-vertex
-// and triangle counts in cell order (the reference's emission order).  Every
-// owned vertex records its id in a dense per-lattice-edge map, and triangles
-// are written as map keys; mc_resolve_ids then replaces each key by the id
-// its owner recorded (the map needs no initialisation: every crossing edge
-// has an owner, and only crossing edges are referenced).  Keys are
-// 3 * (upper end point) + axis, so the (at most three) edges an interior
-// cell owns, which all end at its corner 6, share one 12-byte slot.
 // Active cell number kk (in chunk order) of the warp's chunks starting at
 // grid chunk rc; every lane calls it, have = kk < total.
 struct SegCell {
@@ -779,6 +764,22 @@ __device__ __forceinline__ void emit_cells(const ChunkEmitArgs& A, const Grid& g
     }
 }
 
+// Pass 2, cell-parallel, for one lattice given by values alone (no explicit
+// sample positions) whose edge count fits 32 bits.  Warp = EMIT_SEGS
+// consecutive segments of 32 chunks, whose first vertex and triangle come
+// from pass 1's segment records.  Lane = chunk, once per segment: corner
+// words and active cells, staged in shared memory with their count prefix.
+// The chunks' active cells are then handed out 32 at a time in chunk order
+// (lane = cell: the owning chunk by a binary search over the prefix, the bit
+// by __fns), so lanes stay busy however the active cells are spread.  A
+// cell's own offsets are the warp's base plus a running warp scan of
+// owned-vertex and triangle counts in cell order (the reference's emission
+// order).  Every owned vertex records its id in a dense per-lattice-edge map,
+// and triangles are written as map keys; mc_resolve_ids then replaces each
+// key by the id its owner recorded (the map needs no initialisation: every
+// crossing edge has an owner, and only crossing edges are referenced).  Keys
+// are 3 * (upper end point) + axis, so the (at most three) edges an interior
+// cell owns, which all end at its corner 6, share one 12-byte slot.
 __global__ void __launch_bounds__(256, 5) mc_cell_emit(ChunkEmitArgs A, const uint4* segs, uint32_t nsegs) {
     __shared__ EmitChunks s_ch[8];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
