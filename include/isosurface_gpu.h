@@ -102,7 +102,8 @@ ISO_API iso_status iso_ctx_stage_times(iso_ctx* ctx, double* ms, uint64_t* launc
 /* ------------------------------------------------------------------------ */
 /*
  * An implicit source (a Sampler over a Source tree: src/sampler.rs,
- * src/source.rs, src/implicit/*.rs) is handed to the library as a program:
+ * src/source.rs and the primitives under src/implicit/) is handed to the
+ * library as a program:
  *
  *   u32 magic     = 0x314F5349 ("ISO1" little-endian)
  *   u32 n_ops

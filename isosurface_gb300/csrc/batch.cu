@@ -129,12 +129,6 @@ struct iso_batch {
 
 namespace {
 
-uint32_t size_class(uint32_t size) {
-    uint32_t c = 0;
-    while ((1u << (c + 1)) < size) ++c;
-    return c;  // 17 -> 4, 33 -> 5, 65 -> 6
-}
-
 iso_status build_tiles(iso_batch* b) {
     std::vector<std::pair<double, Tile>> t;
     for (uint32_t i = 0; i < b->chunks.size(); ++i) {

@@ -73,7 +73,6 @@ __host__ __device__ inline int level(uint64_t k) {
     return lv;
 }
 __device__ inline uint64_t parent(uint64_t k) { return max(k >> 3, (uint64_t)1); }
-__device__ inline float size(uint64_t k) { return 1.0f / (float)((uint64_t)2 << level(k)); }
 __device__ inline uint64_t add(uint64_t a, uint64_t b) {  // morton.rs:147-157
     return (((a | DILATE_T1) + (b & DILATE_TZ)) & DILATE_TZ) | (((a | DILATE_T2) + (b & DILATE_TY)) & DILATE_TY) |
            (((a | DILATE_T3) + (b & DILATE_TX)) & DILATE_TX);

@@ -880,8 +880,9 @@ iso_status mc_extract_grids(iso_ctx* ctx, const void* d_grids, uint32_t ngrids, 
     const size_t smem = block_emit_smem(max_cw);
     cudaError_t e = emit_smem_attribute(smem);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "emit smem attribute");
-    ChunkEmitArgs ea{grids, d_range_grid, chunks, local, rangepre, out_v, out_i, nullptr, cap_v, cap_t, ctx->d_err,
-                     nullptr};
+    // the block emit: no edge map, no delivery to host buffers, no block prefixes
+    ChunkEmitArgs ea{grids,   d_range_grid, chunks,  local, rangepre, out_v,   out_i,  nullptr, cap_v,
+                     cap_t,   ctx->d_err,   nullptr, nullptr, nullptr, 0,       0,      totals,  nullptr};
     {
         StageTimer timer(ctx, ISO_STAGE_EMIT);
         mc_block_emit<<<nranges, 256, smem, ctx->stream>>>(ea, max_cw);

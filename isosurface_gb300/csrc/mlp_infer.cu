@@ -480,7 +480,7 @@ static iso_status ready(iso_mlp* net, MlpImages** out) {
 
 iso_status mlp_infer_launch(iso_mlp* net, const float* d_pts, uint64_t n, const MlpGrid* grid, float* d_out) {
     iso_ctx* ctx = net->ctx;
-    MlpImages* m;
+    MlpImages* m = nullptr;
     iso_status s = ready(net, &m);
     if (s != ISO_OK) return s;
     InferArgs a{};
