@@ -115,6 +115,27 @@ def test_mc_sphere_is_closed_genus0():
     assert len(np.unique(keys)) == len(keys)
 
 
+@pytest.mark.parametrize("seed", [1, 2, 3, 4])
+def test_mc_random_unions_are_watertight(seed):
+    """Seeded sphere unions strictly inside the sampled domain: the oracle's
+    MarchingCubes mesh is closed and consistently oriented, every vertex is
+    referenced, no triangle repeats a vertex, and each vertex lies within a
+    cell of the surface."""
+    from isosurface_gb300.scenes import random_spheres
+    sp = random_spheres(seed, 12, 0.6, (0.08, 0.25))
+    for size in (24, 41):
+        p = oracle.Program(S.lower(S.unit_to_cube(S.SphereSet(sp))))
+        m = p.marching_cubes(size)
+        tris = m.triangles
+        assert len(tris) > 0
+        _, bad, dup = edge_manifold_stats(tris)
+        assert bad == 0 and dup == 0
+        assert np.array_equal(np.unique(tris), np.arange(len(m.vertices)))
+        assert np.all((tris[:, 0] != tris[:, 1]) & (tris[:, 1] != tris[:, 2]) & (tris[:, 0] != tris[:, 2]))
+        cell = 2.0 / (size - 1)  # the domain map stretches [0,1] over [-1,1]
+        assert np.max(np.abs(p.sample_scalar(m.vertices))) < cell
+
+
 def test_mc_cases_match_grid_signs():
     p = oracle.Program(S.lower(scenes.csg()))
     g = p.sample_grid(17)
