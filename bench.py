@@ -124,9 +124,10 @@ def cpu_baseline_port(src_bytes, budget_s=12.0, threads=1):
 def secondary_workloads(ctx, torch, steps, only=None):
     """The other workloads, timed with CUDA events on the library's stream:
     the 4096-chunk batch (one CUDA graph vs one extraction per chunk),
-    DualContouring at 256^3, LinearHashedMarchingCubes at depth 8 and the
-    reference's own benchmark shapes (`only`: a set of names among refshapes,
-    batch, dc, lhmc to run just those)."""
+    DualContouring at 256^3, LinearHashedMarchingCubes at depth 8, the
+    reference's own benchmark shapes and the deferred point-splat frame
+    (`only`: a set of names among refshapes, batch, dc, lhmc, splat to run
+    just those)."""
     from isosurface_gb300 import scenes
     stream = torch.cuda.ExternalStream(ctx.stream)
 
@@ -157,7 +158,26 @@ def secondary_workloads(ctx, torch, steps, only=None):
             info = ctx.lhmc_extract(src, 8)
         ms = timed(lambda: ctx.lhmc_extract(src, 8), max(3, min(steps, 20)))
         out["lhmc_depth8"] = {"dual_cubes": int(info.num_cells), "ms": ms, "triangles": int(info.num_triangles)}
+    if want("splat"):
+        out["point_splat_1024x768"] = _point_splat_frame(ctx, steps)
     return out
+
+
+def _point_splat_frame(ctx, steps):
+    """The deferred-rasterisation example's frame (examples/deferred_rasterisation.rs):
+    PointCloud::new(64) of the centred torus with normals, splatted and
+    gathered at 1024 x 768 into a host image; host-timed per frame,
+    including the 12.6 MB image readback."""
+    from isosurface_gb300 import scenes
+    info = ctx.point_cloud_extract(scenes.demo_torus(), 64, normals=True)
+    for _ in range(3):
+        img = ctx.point_splat(1024, 768, 0.5 / 64)
+    reps = max(5, min(steps, 50))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        img = ctx.point_splat(1024, 768, 0.5 / 64)
+    ms = 1e3 * (time.perf_counter() - t0) / reps
+    return {"points": int(info.num_vertices), "ms_per_frame": ms, "lit_pixels": int((img[..., 3] == 1.0).sum())}
 
 
 def _reference_bench_shapes(ctx, timed, steps):
@@ -338,7 +358,7 @@ def main():
     ap.add_argument("--no-secondary", action="store_true", help="skip the batch / DC / LHMC timings")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-surrogate workload")
     ap.add_argument("--secondary-only", default=None,
-                    help="comma list among refshapes,batch,dc,lhmc,surrogate: run only these secondary workloads")
+                    help="comma list among refshapes,batch,dc,lhmc,splat,surrogate: run only these secondary workloads")
     ap.add_argument("--surrogate-train-steps", type=int, default=4000)
     args = ap.parse_args()
     if args.warmup < 3:

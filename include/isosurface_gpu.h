@@ -411,6 +411,23 @@ ISO_API iso_status iso_field_case_disagreement(iso_ctx* ctx, const float* fa, co
 ISO_API iso_status iso_point_cloud_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t flags,
                                            iso_mesh_info* info);
 
+/* Deferred point-splat rendering of the last extraction, which must be a
+ * PointCloud with ISO_FLAG_NORMALS: the technique of the reference's
+ * examples/deferred_rasterisation.rs (a depth-tested one-pixel splat of every
+ * point into position and normal buffers, three gathers of 16 taps either
+ * side along x, y, x that keep, per pixel, the nearest cube of half-size
+ * `voxel_half` around a gathered point that the pixel's eye ray hits, and a
+ * last gather along y that shades with the example's hemisphere term),
+ * written as a headless image instead of a GL framebuffer.  `view_proj` and
+ * `view_proj_inverse` are 4x4 column-major matrices (projection * view, the
+ * model being the identity, and its inverse); `clear_rgb` is the background.
+ * `rgba` (host memory, width * height * 4 floats, row 0 at the bottom)
+ * receives the composited image: the shaded colour and alpha 1 where a point
+ * was hit, the clear colour and alpha 0 elsewhere. */
+ISO_API iso_status iso_point_splat_render(iso_ctx* ctx, const float* view_proj, const float* view_proj_inverse,
+                                          uint32_t width, uint32_t height, float voxel_half, const float* clear_rgb,
+                                          float* rgba);
+
 /* ------------------------------------------------------------------------ */
 /* Host-side sampling helpers                                                */
 /* ------------------------------------------------------------------------ */

@@ -77,6 +77,7 @@ SIGNATURES = {
     "iso_sample_grid": (i32, [vp, vp, u32, vp, u64]),
     "iso_mc_extract": (i32, [vp, vp, u32, u32, ctypes.POINTER(MeshInfo)]),
     "iso_mc_extract_host": (i32, [vp, vp, u32, u32, vp, u64, vp, u64, ctypes.POINTER(MeshInfo)]),
+    "iso_point_splat_render": (i32, [vp, vp, vp, u32, u32, ctypes.c_float, vp, vp]),
     "iso_host_register": (i32, [vp, u64]),
     "iso_host_unregister": (i32, [vp]),
     "iso_mc_extract_field": (i32, [vp, vp, u32, u32, u32, u64, u32, ctypes.POINTER(MeshInfo)]),

@@ -183,6 +183,24 @@ class Context:
         check(lib().iso_point_cloud_extract(self.h, self.program(source).h, size, flags, ctypes.byref(info)), self.h)
         return info
 
+    def point_splat(self, width, height, voxel_half, view_proj=None, view_proj_inverse=None, clear=None):
+        """Deferred point-splat image of the last PointCloud extraction with
+        normals (examples/deferred_rasterisation.rs), (height, width, 4)
+        float32, row 0 at the bottom.  Without matrices, the example's camera
+        (isosurface_gb300.render.splat_camera)."""
+        from . import render
+        if view_proj is None or view_proj_inverse is None:
+            view_proj, view_proj_inverse = render.splat_camera(width, height)
+        vp = np.ascontiguousarray(view_proj, np.float32).reshape(16)
+        vpi = np.ascontiguousarray(view_proj_inverse, np.float32).reshape(16)
+        col = np.ascontiguousarray(render.CLEAR_RGB if clear is None else clear, np.float32).reshape(3)
+        out = np.empty((height, width, 4), np.float32)
+        f32p = ctypes.POINTER(ctypes.c_float)
+        check(lib().iso_point_splat_render(self.h, vp.ctypes.data_as(f32p), vpi.ctypes.data_as(f32p), width, height,
+                                           float(voxel_half), col.ctypes.data_as(f32p), out.ctypes.data_as(f32p)),
+              self.h)
+        return out
+
     def sample_grid(self, source, size, field_ptr, pitch):
         check(lib().iso_sample_grid(self.h, self.program(source).h, size, ctypes.c_void_p(field_ptr), pitch), self.h)
 

@@ -31,6 +31,7 @@ UNITS = {
     "mlp.cu": [],
     "mlp_infer.cu": [],
     "surrogate.cu": ["-fmad=false"],
+    "splat.cu": ["-fmad=false"],
 }
 HEADERS = ["internal.h", "vm.cuh", "mc_tables.h", "mc_chunk.cuh", "qef.cuh", "mlp.h"]
 

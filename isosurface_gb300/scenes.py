@@ -16,11 +16,13 @@ generators", 2014), so the CPU and GPU sides see identical f32 parameters.
                        U[-0.9,0.9]^3, radii U[0.01,0.08]
 * ``bench_torus``      the reference benchmark's source, Torus(0.25, 0.1) at the
                        origin of the [0,1]^3 sample frame (benches/isosurface.rs:21-31)
+* ``demo_torus``       the deferred-rasterisation example's source: the same torus
+                       moved to the frame's centre, with central-difference normals
 """
 import numpy as np
 
-from .source import (Difference, RectangularPrism, Rigid, Sphere, SphereSet, Torus, Translate, Union,
-                     unit_to_cube)
+from .source import (CentralDifference, Difference, RectangularPrism, Rigid, Sphere, SphereSet, Torus, Translate,
+                     Union, unit_to_cube)
 
 MASK64 = (1 << 64) - 1
 
@@ -125,3 +127,10 @@ def smooth_spheres(seed=99, count=4096, k=0.05):
 
 def bench_torus():
     return Torus(0.25, 0.1)
+
+
+def demo_torus():
+    """The deferred-rasterisation example's source: CentralDifference over
+    DemoSource(Torus(0.25, 0.1)), DemoSource sampling its source at p - 0.5
+    (examples/deferred_rasterisation.rs:78-80, examples/common/sources.rs:38-57)."""
+    return CentralDifference(Translate(Torus(0.25, 0.1), (0.5, 0.5, 0.5)))
