@@ -21,6 +21,7 @@ import numpy as np
 F = np.float32
 TAPS = 16
 NO_HIT = F(9999999.0)
+# hemisphere colours: C1 where N.L = -1, C2 where N.L = 1
 C1 = (F(0.886), F(0.757), F(0.337))
 C2 = (F(0.518), F(0.169), F(0.0))
 LIGHT = (F(0.1), F(-1.0), F(0.0))

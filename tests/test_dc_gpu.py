@@ -1,7 +1,7 @@
 """GPU parity of DualContouring (MinimiseQEF and ParticleBasedMinimisation
 placers) against the oracle, through the C ABI.
 
-The spec bar is positions within 1e-4 of a cell; the library follows the
+The required bar is DC vertex positions within 1e-4 of a cell; the library follows the
 reference's f32 and f64 operation order (the SVD of src/math/svd.rs included),
 so the tests assert the stricter byte-identical output and report the
 position difference if that ever fails."""

@@ -94,7 +94,7 @@ def test_mc_sphere_is_closed_genus0():
     ne, bad, dup = edge_manifold_stats(tris)
     assert bad == 0 and dup == 0
     assert len(m.vertices) - ne + len(tris) == 2
-    # Q1: MarchingCubes::new(n) visits (n-1) x (n-1) x n cells
+    # the reference's extra z layer: MarchingCubes::new(n) visits (n-1) x (n-1) x n cells
     assert m.cells == 64 * 64 * 65
     # every vertex lies on its lattice edge, between samples of opposite sign
     keys = m.keys[:, 0]
