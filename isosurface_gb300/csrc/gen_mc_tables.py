@@ -18,6 +18,14 @@ carried over unchanged; everything else in the headers is derived here:
 The generator also checks that every crossing edge of a case is used by one of
 its triangles and that no triangle uses a non-crossing edge: the GPU's
 vertex-ownership rule relies on it.
+
+EDGE_LOOPS (ExtendedMarchingCubes' triangle fans, marching_cubes_tables.rs:
+333-594: loop count, the length of each loop, then the loops' edges) goes to
+the oracle's header as declared.  Checked here: every loop has at least three
+edges, all of them crossing edges, and the loops of a case together use
+exactly its crossing edges.  Rows 167, 181 and 229 hold stray entries after
+their last loop; the reference reads each row only as far as its loop lengths
+reach, so those entries are never used.
 """
 import json
 import os
@@ -193,6 +201,28 @@ def write_device_header(t, path):
     open(path, "w").write("\n".join(s))
 
 
+def check_edge_loops(t):
+    """The structure the fans of ExtendedMarchingCubes rely on; returns the
+    cases whose rows hold entries after their last loop."""
+    stray = []
+    for case in range(256):
+        row = t["EDGE_LOOPS"][case]
+        n = row[0]
+        lengths = row[1:1 + n]
+        at = 1 + n
+        used = 0
+        for k in lengths:
+            assert k >= 3, case
+            for e in row[at:at + k]:
+                assert 0 <= e < 12 and (t["EDGE_CROSSING_MASK"][case] >> e) & 1, (case, e)
+                used |= 1 << e
+            at += k
+        assert at <= 17 and used == t["EDGE_CROSSING_MASK"][case], case
+        if any(v != -1 for v in row[at:]):
+            stray.append(case)
+    return stray
+
+
 def write_oracle_header(t, path):
     s = [LICENSE, "#pragma once", "#include <stdint.h>", "",
          "namespace ref_tables {",
@@ -206,6 +236,11 @@ def write_oracle_header(t, path):
     for row in t["TRIANGLE_CONNECTION"]:
         s.append("    {" + ", ".join(str(v) for v in row) + "},")
     s.append("};")
+    s.append("// loop count, each loop's length, then the loops' edges")
+    s.append("static const int8_t EDGE_LOOPS[256][17] = {")
+    for row in t["EDGE_LOOPS"]:
+        s.append("    {" + ", ".join(str(v) for v in row) + "},")
+    s.append("};")
     s.append("}  // namespace ref_tables")
     open(path, "w").write("\n".join(s) + "\n")
 
@@ -213,6 +248,7 @@ def write_oracle_header(t, path):
 def main():
     src = sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "tests", "golden", "mc_tables.json")
     t = json.load(open(src))
+    assert check_edge_loops(t) == [167, 181, 229]
     write_device_header(t, os.path.join(HERE, "mc_tables.h"))
     write_oracle_header(t, os.path.join(ROOT, "oracle", "ref_tables.h"))
     print("wrote mc_tables.h and oracle/ref_tables.h")

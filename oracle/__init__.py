@@ -26,6 +26,9 @@ def lib():
             "oracle_program_create": (vp, [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t]),
             "oracle_program_destroy": (None, [vp]),
             "oracle_program_has_normal": (ctypes.c_int, [vp]),
+            "oracle_program_has_vector": (ctypes.c_int, [vp]),
+            "oracle_sample_vector": (None, [vp, f32p, ctypes.c_uint64, f32p]),
+            "oracle_emc": (vp, [vp, ctypes.c_uint32, ctypes.c_int, u64p]),
             "oracle_sample_scalar": (None, [vp, f32p, ctypes.c_uint64, f32p]),
             "oracle_sample_normal": (None, [vp, f32p, ctypes.c_uint64, f32p]),
             "oracle_sample_grid": (None, [vp, ctypes.c_uint32, f32p]),
@@ -115,6 +118,29 @@ class Program:
         out = np.empty((len(pts), 3), np.float32)
         lib().oracle_sample_normal(self.h, _ptr(pts, ctypes.c_float), len(pts), _ptr(out, ctypes.c_float))
         return out
+
+    @property
+    def has_vector(self):
+        """Whether the source defines the Directed metric (sample_vector)."""
+        return bool(lib().oracle_program_has_vector(self.h))
+
+    def sample_vector(self, pts):
+        pts = np.ascontiguousarray(pts, np.float32).reshape(-1, 3)
+        out = np.empty((len(pts), 3), np.float32)
+        lib().oracle_sample_vector(self.h, _ptr(pts, ctypes.c_float), len(pts), _ptr(out, ctypes.c_float))
+        return out
+
+    def extended_marching_cubes(self, size, normals=False):
+        """ExtendedMarchingCubes::new(size).extract; the mesh carries
+        `features` (feature vertices), `flips` (edges rotated) and
+        `conflicts` (flips whose result would depend on their order)."""
+        if not self.has_vector:
+            raise ValueError("ExtendedMarchingCubes needs a source with the Directed metric")
+        stats = np.zeros(3, np.uint64)
+        m = Mesh(lib().oracle_emc(self.h, size, 1 if normals else 0, _ptr(stats, ctypes.c_uint64)),
+                 with_normals=normals)
+        m.features, m.flips, m.conflicts = (int(v) for v in stats)
+        return m
 
     def sample_grid(self, size):
         out = np.empty((size + 1, size, size), np.float32)

@@ -102,6 +102,23 @@ struct MeshBuilder {
         }
         return idx;
     }
+    // add_vertex(None, v): a vertex no key refers to (the feature points of
+    // ExtendedMarchingCubes); its dedup key reads as all ones
+    uint32_t add_unkeyed(const Vec3& v) {
+        uint32_t idx = next_vertex++;
+        mesh->vertices.push_back(v.x);
+        mesh->vertices.push_back(v.y);
+        mesh->vertices.push_back(v.z);
+        mesh->keys.push_back(~0ull);
+        mesh->keys.push_back(~0ull);
+        if (normal_source) {
+            Vec3 n = normal_source->normal(v);
+            mesh->normals.push_back(n.x);
+            mesh->normals.push_back(n.y);
+            mesh->normals.push_back(n.z);
+        }
+        return idx;
+    }
     void edge(uint32_t u, uint32_t v, uint32_t face) {
         std::pair<uint32_t, uint32_t> e = u > v ? std::make_pair(v, u) : std::make_pair(u, v);
         edges.insert(e);
@@ -187,23 +204,25 @@ inline Key2 grid_key(const LatticeKeys& lk, const uint32_t (*keys)[3], int edge)
 // the cell layers [z_begin, z_end) so that a bounded slab can be timed.  The
 // full traversal is z_begin = 0, z_end = size.
 // ===========================================================================
-template <class C>
-void primal_traverse(const Source& src, uint32_t size, uint32_t z_begin, uint32_t z_end, C&& callback) {
+// `V` is the distance type (f32 for Signed, Vec3 for Directed) and `sample`
+// the Sample<D> of the source.
+template <class V, class S, class C>
+void primal_grid(uint32_t size, uint32_t z_begin, uint32_t z_end, S&& sample, C&& callback) {
     const uint32_t n = size;
     const float one_over_size = 1.0f / (float)(size - 1);
     std::vector<Vec3> pos[2] = {std::vector<Vec3>((size_t)n * n), std::vector<Vec3>((size_t)n * n)};
-    std::vector<float> val[2] = {std::vector<float>((size_t)n * n), std::vector<float>((size_t)n * n)};
+    std::vector<V> val[2] = {std::vector<V>((size_t)n * n), std::vector<V>((size_t)n * n)};
     // layer z_begin (layer 0 in the reference)
     for (uint32_t y = 0; y < n; ++y)
         for (uint32_t x = 0; x < n; ++x) {
             Vec3 c((float)x * one_over_size, (float)y * one_over_size,
                    z_begin == 0 ? 0.0f : (float)z_begin * one_over_size);
             pos[0][(size_t)y * n + x] = c;
-            val[0][(size_t)y * n + x] = src.scalar(c);
+            val[0][(size_t)y * n + x] = sample(c);
         }
     uint32_t keys[8][3];
     Vec3 corners[8];
-    float values[8];
+    V values[8];
     int cur = 0;
     for (uint32_t z = z_begin; z < z_end; ++z) {
         int nxt = cur ^ 1;
@@ -211,7 +230,7 @@ void primal_traverse(const Source& src, uint32_t size, uint32_t z_begin, uint32_
             for (uint32_t x = 0; x < n; ++x) {
                 Vec3 c((float)x * one_over_size, (float)y * one_over_size, (float)(z + 1) * one_over_size);
                 pos[nxt][(size_t)y * n + x] = c;
-                val[nxt][(size_t)y * n + x] = src.scalar(c);
+                val[nxt][(size_t)y * n + x] = sample(c);
             }
         for (uint32_t y = 0; y + 1 < n; ++y)
             for (uint32_t x = 0; x + 1 < n; ++x) {
@@ -228,6 +247,11 @@ void primal_traverse(const Source& src, uint32_t size, uint32_t z_begin, uint32_
             }
         cur = nxt;
     }
+}
+
+template <class C>
+void primal_traverse(const Source& src, uint32_t size, uint32_t z_begin, uint32_t z_end, C&& callback) {
+    primal_grid<float>(size, z_begin, z_end, [&](const Vec3& c) { return src.scalar(c); }, callback);
 }
 
 // MarchingCubes::extract (src/marching_cubes.rs:59-82)
@@ -691,19 +715,22 @@ const float FEATURE_ANGLE = 0.8660254037844387f;  // feature/mod.rs:22
 enum Topology { PLANAR, EDGE, CORNER };
 
 struct Planes {
-    Vec3 normal[8];
-    float d[8];
+    Vec3 normal[12];
+    float d[12];
+    int n;
     Vec3 center_of_mass;
     Topology feature;
 };
 
-// TangentPlanes::new (feature/mod.rs:91-148) over the 8 cell corners
-void tangent_planes(const Vec3* vertices, const Vec3* normals, Planes* t) {
+// TangentPlanes::new (feature/mod.rs:91-148) over n points: the 8 cell
+// corners (from_corners, DualContouring) or a cell's 3-12 edge crossings
+// (from_edge_crossings, ExtendedMarchingCubes)
+void tangent_planes(const Vec3* vertices, const Vec3* normals, int n, Planes* t) {
     Vec3 com, axis;
     float min_angle = 3.40282347e+38f;
     float count = 0.0f;
-    for (int i = 0; i < 8; ++i) {
-        for (int j = 0; j < 8; ++j) {
+    for (int i = 0; i < n; ++i) {
+        for (int j = 0; j < n; ++j) {
             float angle = normals[i].dot(normals[j]);
             if (angle < min_angle) {
                 axis = normals[i].cross(normals[j]);
@@ -720,7 +747,7 @@ void tangent_planes(const Vec3* vertices, const Vec3* normals, Planes* t) {
     } else {
         axis = axis.normalised_or_zero();
         float min_c = 1.0f, max_c = -1.0f;
-        for (int i = 0; i < 8; ++i) {
+        for (int i = 0; i < n; ++i) {
             float c = axis.dot(normals[i]);
             min_c = std::fmin(min_c, c);
             max_c = std::fmax(max_c, c);
@@ -729,10 +756,11 @@ void tangent_planes(const Vec3* vertices, const Vec3* normals, Planes* t) {
         c = std::sqrt(1.0f - c * c);
         feature = (c > FEATURE_ANGLE) ? EDGE : CORNER;
     }
-    for (int i = 0; i < 8; ++i) {
+    for (int i = 0; i < n; ++i) {
         t->normal[i] = normals[i];
         t->d[i] = (vertices[i] - com).dot(normals[i]);
     }
+    t->n = n;
     t->center_of_mass = com;
     t->feature = feature;
 }
@@ -740,14 +768,14 @@ void tangent_planes(const Vec3* vertices, const Vec3* normals, Planes* t) {
 // MinimiseQEF::place_feature_with_tangents (feature/qef.rs:36-68)
 Vec3 minimise_qef(const Planes& t) {
     if (t.feature == PLANAR) return t.center_of_mass;
-    double a[8][3];
-    for (int i = 0; i < 8; ++i) {
+    double a[12][3];
+    for (int i = 0; i < t.n; ++i) {
         a[i][0] = (double)t.normal[i].x;
         a[i][1] = (double)t.normal[i].y;
         a[i][2] = (double)t.normal[i].z;
     }
     svd::Svd s;
-    svd::compute(a, 8, &s);
+    svd::compute(a, t.n, &s);
     if (t.feature == EDGE) {
         double s_min = 1.7976931348623157e308;
         int id = 0;
@@ -758,8 +786,8 @@ Vec3 minimise_qef(const Planes& t) {
             }
         s.d[id] = 0.0;
     }
-    double b[8];
-    for (int i = 0; i < 8; ++i) b[i] = (double)t.d[i];
+    double b[12];
+    for (int i = 0; i < t.n; ++i) b[i] = (double)t.d[i];
     double x[3];
     svd::solve(&s, b, x);
     return t.center_of_mass + Vec3((float)x[0], (float)x[1], (float)x[2]);
@@ -780,7 +808,7 @@ Vec3 trilinear(const Vec3* corners, const Vec3* forces, const Vec3& p) {
 Vec3 particle_placement(const Vec3* corners, const Vec3* normals) {
     const float STEP_SIZE = 0.05f, THRESHOLD = 0.02f;
     Planes t;
-    tangent_planes(corners, normals, &t);
+    tangent_planes(corners, normals, 8, &t);
     float max_feature_size = corners[6].x - corners[0].x;
     Vec3 particle = t.center_of_mass;
     Vec3 forces[8];
@@ -820,7 +848,7 @@ void dual_contouring(const Source& src, uint32_t size, int placer, Mesh* mesh, s
             sample_normals_at_corners(src, pc, normals);
             if (placer == 0) {
                 Planes t;
-                tangent_planes(pc, normals, &t);
+                tangent_planes(pc, normals, 8, &t);
                 vertex = minimise_qef(t);
             } else {
                 vertex = particle_placement(pc, normals);
@@ -857,6 +885,176 @@ void dual_contouring(const Source& src, uint32_t size, int placer, Mesh* mesh, s
             mesh->cells++;
         }
     });
+    mb.finish();
+}
+
+// ===========================================================================
+// ExtendedMarchingCubes: src/extended_marching_cubes.rs over the Directed
+// metric (src/distance.rs:72-104)
+// ===========================================================================
+
+// Directed::is_positive (distance.rs:87-90): outside when any component is
+// positive; classify_corners (marching_cubes_impl.rs:26-37) sets bit i when
+// corner i is not outside
+inline int classify_directed(const Vec3* values) {
+    int cube = 0;
+    for (int i = 0; i < 8; ++i)
+        if (!(values[i].x > 0.0f || values[i].y > 0.0f || values[i].z > 0.0f)) cube |= 1 << i;
+    return cube;
+}
+
+// Vec3::max_component_index (vector.rs:255-263)
+inline int max_component_index(const Vec3& v) {
+    if (v.x > v.y && v.x > v.z) return 0;
+    if (v.y > v.z) return 1;
+    return 2;
+}
+inline float component(const Vec3& v, int axis) { return axis == 0 ? v.x : axis == 1 ? v.y : v.z; }
+
+// Directed::find_crossing_point (distance.rs:94-103): interpolate on the
+// component of the edge's own axis
+inline Vec3 find_crossing_directed(const Vec3& a, const Vec3& b, const Vec3& pa, const Vec3& pb) {
+    int axis = max_component_index((pa - pb).abs());
+    float delta = component(b, axis) - component(a, axis);
+    float t = (delta == 0.0f) ? 0.5f : -component(a, axis) / delta;
+    return pa * (1.0f - t) + pb * t;
+}
+
+struct EmcStats {
+    uint64_t features = 0;   // feature vertices spawned
+    uint64_t flips = 0;      // edges rotated
+    uint64_t conflicts = 0;  // flips that met a face an earlier flip rewrote
+};
+
+// Face::vertex_opposite (mesh.rs:190-199)
+inline uint32_t vertex_opposite(const uint32_t* f, uint32_t e0, uint32_t e1) {
+    for (int i = 0; i < 3; ++i)
+        if (f[i] != e0 && f[i] != e1) return f[i];
+    return f[0];  // unreachable for the faces extraction makes
+}
+
+// Face::matches_winding_direction (mesh.rs:201-213); false in *found when
+// the edge is not on the face (the reference panics there)
+inline bool matches_winding(const uint32_t* f, uint32_t e0, uint32_t e1, bool* found) {
+    for (int i = 0; i < 3; ++i) {
+        int j = (i + 1) % 3;
+        if (e0 == f[i] && e1 == f[j]) { *found = true; return true; }
+        if (e0 == f[j] && e1 == f[i]) { *found = true; return false; }
+    }
+    *found = false;
+    return false;
+}
+
+// flip_feature_edges (extended_marching_cubes.rs:157-186) with
+// MeshTopology::rotate_edge (mesh.rs:138-172).  The flips are chosen on the
+// finished mesh, then applied.  The reference applies them in the order of
+// its HashSet (random per run); when no face is rewritten by two flips the
+// result is the same in every order, which `conflicts` == 0 states.  Here
+// they are applied in ascending (start, end) order.
+void flip_feature_edges(MeshBuilder& mb, const std::vector<uint8_t>& feature, EmcStats* st) {
+    typedef std::pair<uint32_t, uint32_t> Edge;
+    std::vector<Edge> flips;
+    for (const Edge& e : mb.edges) {
+        if (feature[e.first] && feature[e.second]) continue;
+        auto it = mb.edge_to_face.find(e);
+        if (it == mb.edge_to_face.end() || it->second.size() != 2) continue;
+        const uint32_t* fa = &mb.faces[3 * (size_t)it->second[0]];
+        const uint32_t* fb = &mb.faces[3 * (size_t)it->second[1]];
+        if (feature[vertex_opposite(fa, e.first, e.second)] && feature[vertex_opposite(fb, e.first, e.second)])
+            flips.push_back(e);
+    }
+    std::sort(flips.begin(), flips.end());
+    std::vector<uint8_t> rewritten(mb.faces.size() / 3, 0);
+    for (const Edge& e : flips) {
+        auto it = mb.edge_to_face.find(e);
+        if (it == mb.edge_to_face.end() || it->second.size() != 2) continue;
+        uint32_t ha = it->second[0], hb = it->second[1];
+        if (rewritten[ha] || rewritten[hb]) st->conflicts++;
+        uint32_t fa[3], fb[3];
+        std::memcpy(fa, &mb.faces[3 * (size_t)ha], sizeof(fa));
+        std::memcpy(fb, &mb.faces[3 * (size_t)hb], sizeof(fb));
+        uint32_t c = vertex_opposite(fa, e.first, e.second);
+        uint32_t d = vertex_opposite(fb, e.first, e.second);
+        bool found;
+        bool m = matches_winding(fa, e.first, e.second, &found);
+        if (!found) continue;
+        uint32_t u = m ? e.second : e.first, v = m ? e.first : e.second;
+        uint32_t na[3] = {c, d, u}, nb[3] = {c, v, d};
+        std::memcpy(&mb.faces[3 * (size_t)ha], na, sizeof(na));
+        std::memcpy(&mb.faces[3 * (size_t)hb], nb, sizeof(nb));
+        rewritten[ha] = rewritten[hb] = 1;
+        Edge ne = c > d ? Edge(d, c) : Edge(c, d);
+        mb.edges.insert(ne);
+        mb.edge_to_face[ne] = std::vector<uint32_t>{ha, hb};
+        mb.edges.erase(e);
+        mb.edge_to_face.erase(e);
+        st->flips++;
+    }
+}
+
+// ExtendedMarchingCubes::extract (extended_marching_cubes.rs:64-93) and
+// march_cube_extended (:95-155): cells whose edge-crossing tangent planes
+// are planar take the marching-cubes triangles; the others spawn a feature
+// vertex placed by MinimiseQEF::place_feature_with_tangents and fan each of
+// the case's edge loops (EDGE_LOOPS) around it.
+void extended_marching_cubes(const Source& src, uint32_t size, Mesh* mesh, const Source* normal_source,
+                             EmcStats* st) {
+    MeshBuilder mb(mesh, normal_source, true);
+    LatticeKeys lk{size, size};
+    std::vector<uint8_t> feature;  // per vertex: 1 for a feature vertex
+    primal_grid<Vec3>(size, 0, size, [&](const Vec3& c) { return src.vec(c); },
+                      [&](uint32_t, uint32_t, uint32_t, const uint32_t (*keys)[3], const Vec3* corners,
+                          const Vec3* values) {
+        int cube = classify_directed(values);
+        Vec3 vertices[12], normals[12];
+        uint32_t edges = EDGE_CROSSING_MASK[cube];
+        for (int i = 0; i < 12; ++i)  // find_edge_crossings (marching_cubes_impl.rs:39-56)
+            if (edges & (1u << i)) {
+                int u = EDGE_CONNECTION[i][0], v = EDGE_CONNECTION[i][1];
+                vertices[i] = find_crossing_directed(values[u], values[v], corners[u], corners[v]);
+            }
+        for (int i = 0; i < 12; ++i)  // sample_normals_at_edge_crossings (:71-89)
+            if (edges & (1u << i)) normals[i] = src.normal(vertices[i]).normalised_or_zero();
+        // TangentPlanes::from_edge_crossings (feature/mod.rs:76-89)
+        Vec3 pv[12], pn[12];
+        int n = 0;
+        for (int i = 0; i < 12; ++i)
+            if (edges & (1u << i)) {
+                pv[n] = vertices[i];
+                pn[n] = normals[i];
+                ++n;
+            }
+        Planes t;
+        tangent_planes(pv, pn, n, &t);
+        if (t.feature == PLANAR) {
+            march_cube(cube, [&](int a, int b, int c) {
+                uint32_t ia = mb.add_vertex(grid_key(lk, keys, a), vertices[a]);
+                uint32_t ib = mb.add_vertex(grid_key(lk, keys, b), vertices[b]);
+                uint32_t ic = mb.add_vertex(grid_key(lk, keys, c), vertices[c]);
+                mb.add_face(ia, ib, ic);
+            });
+        } else {
+            uint32_t centre = mb.add_unkeyed(minimise_qef(t));
+            feature.resize((size_t)centre + 1, 0);
+            feature[centre] = 1;
+            st->features++;
+            int loops = EDGE_LOOPS[cube][0];
+            int at = 1 + loops;
+            for (int l = 0; l < loops; ++l) {
+                int k = EDGE_LOOPS[cube][1 + l];
+                for (int i = 0; i < k; ++i) {
+                    int e0 = EDGE_LOOPS[cube][at + i], e1 = EDGE_LOOPS[cube][at + (i + 1) % k];
+                    uint32_t a = mb.add_vertex(grid_key(lk, keys, e0), vertices[e0]);
+                    uint32_t b = mb.add_vertex(grid_key(lk, keys, e1), vertices[e1]);
+                    mb.add_face(a, b, centre);
+                }
+                at += k;
+            }
+        }
+        mesh->cells++;
+    });
+    feature.resize(mb.next_vertex, 0);
+    flip_feature_edges(mb, feature, st);
     mb.finish();
 }
 
@@ -1055,6 +1253,19 @@ void oracle_sample_normal(void* p, const float* pts, uint64_t n, float* out) {
     }
 }
 
+int oracle_program_has_vector(void* p) { return ((Program*)p)->src->has_vector() ? 1 : 0; }
+
+// VectorSource::sample_vector (the Directed metric), 3 floats per point
+void oracle_sample_vector(void* p, const float* pts, uint64_t n, float* out) {
+    const Source& s = *((Program*)p)->src;
+    for (uint64_t i = 0; i < n; ++i) {
+        Vec3 v = s.vec(Vec3(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]));
+        out[3 * i] = v.x;
+        out[3 * i + 1] = v.y;
+        out[3 * i + 2] = v.z;
+    }
+}
+
 // The sample grid of PrimalGrid: size x size x (size+1) values, x fastest.
 void oracle_sample_grid(void* p, uint32_t size, float* out) {
     const Source& s = *((Program*)p)->src;
@@ -1121,6 +1332,20 @@ uint64_t oracle_lhmc_nodes(void* p, uint32_t max_depth, uint64_t* out, uint64_t 
     return n;
 }
 
+// ExtendedMarchingCubes::new(size).extract; stats: features, flips, conflicts
+void* oracle_emc(void* p, uint32_t size, int normals, uint64_t* stats) {
+    const Source& s = *((Program*)p)->src;
+    Mesh* m = new Mesh();
+    EmcStats st;
+    extended_marching_cubes(s, size, m, normals ? &s : nullptr, &st);
+    if (stats) {
+        stats[0] = st.features;
+        stats[1] = st.flips;
+        stats[2] = st.conflicts;
+    }
+    return m;
+}
+
 uint64_t oracle_mesh_vertices(void* m) { return ((Mesh*)m)->vertices.size() / 3; }
 uint64_t oracle_mesh_indices(void* m) { return ((Mesh*)m)->indices.size(); }
 uint64_t oracle_mesh_cells(void* m) { return ((Mesh*)m)->cells; }
@@ -1153,7 +1378,7 @@ void oracle_place_feature(const float* corners, const float* normals, int placer
         n[i] = Vec3(normals[3 * i], normals[3 * i + 1], normals[3 * i + 2]);
     }
     Planes t;
-    tangent_planes(c, n, &t);
+    tangent_planes(c, n, 8, &t);
     if (topology) *topology = (int)t.feature;
     Vec3 v = placer == 0 ? minimise_qef(t) : particle_placement(c, n);
     out[0] = v.x;

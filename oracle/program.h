@@ -70,13 +70,20 @@ inline Vec3 operator*(float f, const Vec3& v) { return Vec3(f * v.x, f * v.y, f 
 
 // ---------------------------------------------------------------------------
 // Sources (src/source.rs:21-48). `scalar` is ScalarSource::sample_scalar,
-// `normal` HermiteSource::sample_normal (unnormalised).
+// `normal` HermiteSource::sample_normal (unnormalised), `vec`
+// VectorSource::sample_vector (the Directed metric: per axis, the signed
+// distance to the surface along that axis, f32::MAX where the axis line
+// misses it), defined where has_vector() holds.
 // ---------------------------------------------------------------------------
+const float F32_MAX = 3.40282347e+38f;
+
 struct Source {
     virtual ~Source() {}
     virtual float scalar(const Vec3& p) const = 0;
     virtual bool has_normal() const { return true; }
     virtual Vec3 normal(const Vec3& p) const = 0;
+    virtual bool has_vector() const { return false; }
+    virtual Vec3 vec(const Vec3&) const { return Vec3(); }
 };
 typedef std::unique_ptr<Source> SourcePtr;
 
@@ -86,6 +93,17 @@ struct Sphere : Source {
     explicit Sphere(float r) : radius(r) {}
     float scalar(const Vec3& p) const override { return p.len() - radius; }
     Vec3 normal(const Vec3& p) const override { return p; }
+    bool has_vector() const override { return true; }
+    // sphere.rs:41-57
+    Vec3 vec(const Vec3& p) const override {
+        Vec3 a = p.abs();
+        float r2 = radius * radius;
+        float l_yz = r2 - (a.y * a.y + a.z * a.z);
+        float l_xz = r2 - (a.x * a.x + a.z * a.z);
+        float l_xy = r2 - (a.x * a.x + a.y * a.y);
+        return Vec3(l_yz < 0.0f ? F32_MAX : a.x - std::sqrt(l_yz), l_xz < 0.0f ? F32_MAX : a.y - std::sqrt(l_xz),
+                    l_xy < 0.0f ? F32_MAX : a.z - std::sqrt(l_xy));
+    }
 };
 
 // src/implicit/rectangular_prism.rs:36-80
@@ -97,6 +115,18 @@ struct RectangularPrism : Source {
         return q.vmax(Vec3()).len() + std::fmin(q.max_component(), 0.0f);
     }
     Vec3 normal(const Vec3& p) const override { return p.clamp_to_cardinal_axis(); }
+    bool has_vector() const override { return true; }
+    // rectangular_prism.rs:43-70: outside the slab of the other two axes the
+    // axis line misses the box (+MAX); the mask is -MAX otherwise
+    Vec3 vec(const Vec3& p) const override {
+        Vec3 a = p.abs();
+        Vec3 mask = Vec3((a.y - half.y > 0.0f || a.z - half.z > 0.0f) ? 1.0f : -1.0f,
+                         (a.x - half.x > 0.0f || a.z - half.z > 0.0f) ? 1.0f : -1.0f,
+                         (a.x - half.x > 0.0f || a.y - half.y > 0.0f) ? 1.0f : -1.0f) *
+                    F32_MAX;
+        Vec3 closest = (a.x < half.x && a.y < half.y && a.z < half.z) ? a.vmax(half) : a.vmin(half);
+        return (a - closest).vmax(mask);
+    }
 };
 
 // src/implicit/cylinder.rs:41-85
@@ -116,6 +146,15 @@ struct Cylinder : Source {
         if (z > r) return Vec3(0.0f, 0.0f, p.z);
         return Vec3(p.x, p.y, 0.0f);
     }
+    bool has_vector() const override { return true; }
+    // cylinder.rs:50-71
+    Vec3 vec(const Vec3& p) const override {
+        Vec3 a = p.abs();
+        float r2 = radius * radius;
+        return Vec3((a.z > half_length || a.y > radius) ? F32_MAX : a.x - std::sqrt(r2 - a.y * a.y),
+                    (a.z > half_length || a.x > radius) ? F32_MAX : a.y - std::sqrt(r2 - a.x * a.x),
+                    (a.x * a.x + a.y * a.y > r2) ? F32_MAX : a.z - half_length);
+    }
 };
 
 // src/implicit/torus.rs:40-108
@@ -132,6 +171,31 @@ struct Torus : Source {
         if (!Vec3(p.x, p.y, 0.0f).normalised(&ring)) ring = Vec3(1.0f, 0.0f, 0.0f);
         return p - ring * radius;
     }
+    bool has_vector() const override { return true; }
+    // torus.rs:48-100.  Square roots of negative numbers give NaN, which
+    // f32::max (fmax) drops in favour of the other operand.
+    Vec3 vec(const Vec3& p) const override {
+        Vec3 a = p.abs();
+        float l = std::sqrt(a.x * a.x + a.y * a.y);
+        float l_xy = l - radius;
+        float trz = std::sqrt(tube * tube - a.z * a.z);
+        float rx = radius + trz, ry = radius - trz;
+        float x, y, z;
+        if (a.z > tube || a.y > radius + trz)
+            x = F32_MAX;
+        else if (a.x == 0.0f)
+            x = std::fabs(a.y - radius) - tube;
+        else
+            x = std::fmax(a.x - std::sqrt(rx * rx - a.y * a.y), std::sqrt(ry * ry - a.y * a.y) - a.x);
+        if (a.z > tube || a.x > radius + trz)
+            y = F32_MAX;
+        else if (a.y == 0.0f)
+            y = std::fabs(a.x - radius) - tube;
+        else
+            y = std::fmax(a.y - std::sqrt(rx * rx - a.x * a.x), std::sqrt(ry * ry - a.x * a.x) - a.y);
+        z = std::fabs(l_xy) > tube ? F32_MAX : a.z - std::sqrt(tube * tube - l_xy * l_xy);
+        return Vec3(x, y, z);
+    }
 };
 
 // src/implicit/csg.rs:22-51: min of values, component-wise min of normals
@@ -141,6 +205,8 @@ struct Union : Source {
     float scalar(const Vec3& p) const override { return std::fmin(a->scalar(p), b->scalar(p)); }
     bool has_normal() const override { return a->has_normal() && b->has_normal(); }
     Vec3 normal(const Vec3& p) const override { return a->normal(p).vmin(b->normal(p)); }
+    bool has_vector() const override { return a->has_vector() && b->has_vector(); }
+    Vec3 vec(const Vec3& p) const override { return a->vec(p).vmin(b->vec(p)); }  // csg.rs:41-45
 };
 
 // src/implicit/csg.rs:55-72 (values).  The reference defines no normal; the
@@ -153,6 +219,8 @@ struct Intersection : Source {
     Vec3 normal(const Vec3& p) const override {
         return (a->scalar(p) >= b->scalar(p)) ? a->normal(p) : b->normal(p);
     }
+    bool has_vector() const override { return a->has_vector() && b->has_vector(); }
+    Vec3 vec(const Vec3& p) const override { return a->vec(p).vmax(b->vec(p)); }  // csg.rs:74-78
 };
 
 // src/implicit/csg.rs:83-100: b minus a == max(b, -a).  Normal (new): normal of
@@ -165,6 +233,8 @@ struct Difference : Source {
     Vec3 normal(const Vec3& p) const override {
         return (b->scalar(p) >= -a->scalar(p)) ? b->normal(p) : -a->normal(p);
     }
+    bool has_vector() const override { return a->has_vector() && b->has_vector(); }
+    Vec3 vec(const Vec3& p) const override { return b->vec(p).vmax(-a->vec(p)); }  // csg.rs:102-106
 };
 
 // Polynomial smooth minimum (Inigo Quilez, "smooth minimum", 2013):
@@ -193,6 +263,8 @@ struct Translate : Source {
     float scalar(const Vec3& p) const override { return s->scalar(p - c); }
     bool has_normal() const override { return s->has_normal(); }
     Vec3 normal(const Vec3& p) const override { return s->normal(p - c); }
+    bool has_vector() const override { return s->has_vector(); }
+    Vec3 vec(const Vec3& p) const override { return s->vec(p - c); }
 };
 
 // q = M (p - t); normal rotated back with M^T
@@ -227,6 +299,8 @@ struct DomainMap : Source {
     float scalar(const Vec3& p) const override { return s->scalar(map(p)); }
     bool has_normal() const override { return s->has_normal(); }
     Vec3 normal(const Vec3& p) const override { return s->normal(map(p)); }
+    bool has_vector() const override { return s->has_vector(); }
+    Vec3 vec(const Vec3& p) const override { return s->vec(map(p)); }
 };
 
 // A left fold of Union (or SmoothUnion) over translated spheres.
@@ -269,6 +343,8 @@ struct CentralDifference : Source {
     float eps;
     CentralDifference(SourcePtr x, float e) : s(std::move(x)), eps(e) {}
     float scalar(const Vec3& p) const override { return s->scalar(p); }
+    bool has_vector() const override { return s->has_vector(); }
+    Vec3 vec(const Vec3& p) const override { return s->vec(p); }  // source.rs:76-80
     Vec3 normal(const Vec3& p) const override {
         Vec3 dx(eps, 0.0f, 0.0f), dy(0.0f, eps, 0.0f), dz(0.0f, 0.0f, eps);
         float vx = s->scalar(p + dx) - s->scalar(p - dx);

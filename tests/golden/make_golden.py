@@ -7,14 +7,15 @@ Run here (where the reference checkout exists) as
 It reads, as text only:
 
 * ``src/marching_cubes_tables.rs`` -> ``mc_tables.json`` (CORNERS, REMAP_CUBE,
-  EDGE_CONNECTION, EDGE_CROSSING_MASK, TRIANGLE_CONNECTION exactly as the
-  reference declares them, marching_cubes_tables.rs:16-331).
+  EDGE_CONNECTION, EDGE_CROSSING_MASK, TRIANGLE_CONNECTION and EDGE_LOOPS
+  exactly as the reference declares them, marching_cubes_tables.rs:16-594).
 * the inline ``#[cfg(test)]`` known-answer tests of the implicit primitives
   (sphere.rs:65-109, rectangular_prism.rs:82-130, cylinder.rs:87-140,
-  torus.rs:110-171, csg.rs:108-167) -> ``kats.json``.  Only the
-  ``sample_scalar`` and ``sample_normal(..).normalised()`` assertions are
-  kept: ``sample_vector`` belongs to the Directed metric that only
-  ExtendedMarchingCubes uses.
+  torus.rs:110-171, csg.rs:108-167) -> ``kats.json``: the ``sample_scalar``,
+  ``sample_normal(..).normalised()`` and ``sample_vector`` (the Directed
+  metric of ExtendedMarchingCubes) assertions.  Expected values written as
+  expressions (``Vec2::from_scalar(1.0 - (4.0f32 - 1.0f32).sqrt())
+  .extend(-3.0)``) are evaluated here in float32, as Rust evaluates them.
 
 The fixtures are committed so that nothing at test time reads the reference.
 """
@@ -52,11 +53,12 @@ def parse_tables(ref):
         "EDGE_CROSSING_MASK": t["EDGE_CROSSING_MASK"]["values"],
         "TRIANGLE_CONNECTION": [t["TRIANGLE_CONNECTION"]["values"][16 * i: 16 * i + 16]
                                 for i in range(256)],
+        "EDGE_LOOPS": [t["EDGE_LOOPS"]["values"][17 * i: 17 * i + 17] for i in range(256)],
         "source_lines": {k: v["line"] for k, v in t.items()},
     }
     assert len(out["EDGE_CROSSING_MASK"]) == 256
     assert len(t["TRIANGLE_CONNECTION"]["values"]) == 256 * 16
-    del out["source_lines"]["EDGE_LOOPS"]
+    assert len(t["EDGE_LOOPS"]["values"]) == 256 * 17
     return out
 
 
@@ -79,6 +81,60 @@ def _vec(expr):
     if m:
         return [_num(m.group(i)) for i in (1, 2, 3)]
     return None
+
+
+F32_MAX = 3.4028234663852886e38  # std::f32::MAX, exactly representable
+
+
+def _f32_eval(expr):
+    """A scalar Rust f32 expression (literals, MAX, + - * /, parentheses,
+    ``(..).sqrt()``) evaluated in float32, operation by operation."""
+    import numpy as np
+    e = re.sub(r"(\d+(?:\.\d*)?)(?:f32)?", r"F(\1)", expr)
+    e = e.replace("MAX", "F(%r)" % F32_MAX)
+    # innermost `( ... ).sqrt()` first
+    while ".sqrt()" in e:
+        e2 = re.sub(r"\(([^()]*(?:\([^()]*\)[^()]*)*)\)\.sqrt\(\)", r"np.sqrt(\1)", e, count=1)
+        assert e2 != e, expr
+        e = e2
+    v = eval(e, {"F": np.float32, "np": np})
+    assert isinstance(v, np.float32), (expr, type(v))
+    return float(v)
+
+
+def _split_args(s):
+    out, depth, cur = [], 0, ""
+    for ch in s:
+        if ch == "," and depth == 0:
+            out.append(cur)
+            cur = ""
+            continue
+        depth += (ch == "(") - (ch == ")")
+        cur += ch
+    out.append(cur)
+    return [a.strip() for a in out if a.strip()]
+
+
+def _vec_expr(expr):
+    """Expected Directed values: Vec3::zero / from_scalar / new, or
+    Vec2::from_scalar(x).extend(z), with f32 expressions as components."""
+    expr = expr.strip().rstrip(",").strip()
+    if expr == "Vec3::zero()":
+        return [0.0, 0.0, 0.0]
+    m = re.fullmatch(r"Vec3::from_scalar\((.*)\)", expr)
+    if m:
+        v = _f32_eval(m.group(1))
+        return [v, v, v]
+    m = re.fullmatch(r"Vec3::new\((.*)\)", expr)
+    if m:
+        args = _split_args(m.group(1))
+        assert len(args) == 3, expr
+        return [_f32_eval(a) for a in args]
+    m = re.fullmatch(r"Vec2::from_scalar\((.*)\)\.extend\((.*)\)", expr)
+    if m:
+        v = _f32_eval(m.group(1))
+        return [v, v, _f32_eval(m.group(2))]
+    raise ValueError("unparsed vector: " + expr)
 
 
 def _ctor(expr, env):
@@ -125,6 +181,12 @@ def parse_kats(ref):
                 kats.append({"file": "src/implicit/" + fname, "line": line,
                              "source": env[m.group(1)], "kind": "scalar",
                              "point": _vec(m.group(2)), "expected": _num(m.group(3))})
+                continue
+            m = re.match(r"assert_eq!\(\s*(\w+)\s*\.sample_vector\((.*?)\)\s*\.0,\s*(.*?)\s*\);$", flat)
+            if m:
+                kats.append({"file": "src/implicit/" + fname, "line": line,
+                             "source": env[m.group(1)], "kind": "vector",
+                             "point": _vec(m.group(2)), "expected": _vec_expr(m.group(3))})
                 continue
             m = re.match(r"assert_eq!\(\s*(\w+)\s*\.sample_normal\((.*?)\)\s*\.normalised\(\)\s*\.unwrap\(\),\s*(.*)\s*\);$", flat)
             if m:

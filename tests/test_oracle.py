@@ -29,11 +29,15 @@ def _normalised(n):
 
 @pytest.mark.parametrize("kat", _kats(), ids=lambda k: "%s:%d" % (os.path.basename(k["file"]), k["line"]))
 def test_reference_kats(kat):
-    """Every sample_scalar / sample_normal assertion of the reference's
-    primitive tests (src/implicit/*.rs) holds for the oracle, bit for bit."""
+    """Every sample_scalar / sample_normal / sample_vector assertion of the
+    reference's primitive tests (src/implicit/*.rs) holds for the oracle, bit
+    for bit."""
     p = oracle.Program(S.lower(S.from_spec(kat["source"])))
     if kat["kind"] == "scalar":
         assert p.sample_scalar(kat["point"])[0] == np.float32(kat["expected"])
+    elif kat["kind"] == "vector":
+        assert p.has_vector
+        assert np.array_equal(p.sample_vector(kat["point"])[0], np.asarray(kat["expected"], np.float32))
     else:
         got = _normalised(p.sample_normal(kat["point"])[0])
         assert np.array_equal(got, np.asarray(kat["expected"], np.float32))
