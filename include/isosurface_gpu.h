@@ -403,6 +403,23 @@ ISO_API iso_status iso_field_case_disagreement(iso_ctx* ctx, const float* fa, co
                                                uint32_t ny, uint32_t nz, uint64_t pitch, uint64_t* cells);
 
 /* ------------------------------------------------------------------------ */
+/* ExtendedMarchingCubes (src/extended_marching_cubes.rs:51-186)              */
+/* ------------------------------------------------------------------------ */
+/* ExtendedMarchingCubes::new(size).extract(&sampler, &mut e) over the
+ * Directed metric (src/distance.rs:72-104: per axis, the distance to the
+ * surface along that axis), so the program may hold only the primitives,
+ * Union, Intersection, Difference, the translate and domain-map point ops
+ * and CentralDifference (ISO_ERR_INVALID_ARG otherwise); size <= 513.  Cells
+ * whose edge-crossing normals span more than 30 degrees get a feature vertex
+ * (MinimiseQEF over their tangent planes) fanned to the case's edge loops;
+ * loop segments shared by two fans are then rotated to join the fan centres
+ * (flip_feature_edges).  Vertices and triangles come in the reference's
+ * order.  flags: ISO_FLAG_NORMALS for IndexedInterleavedNormals.  `flips`
+ * (nullable) receives the number of rotated edges. */
+ISO_API iso_status iso_emc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t flags,
+                                   iso_mesh_info* info, uint64_t* flips);
+
+/* ------------------------------------------------------------------------ */
 /* PointCloud (src/point_cloud.rs:50-63)                                      */
 /* ------------------------------------------------------------------------ */
 /* PointCloud::<Signed>::new(size).extract: the centre of every cell whose

@@ -84,6 +84,7 @@ SIGNATURES = {
     "iso_mc_extract_field_noalloc": (i32, [vp, u32, u32, u32, u64, vp, u64, vp, u64, vp, ctypes.POINTER(MeshInfo)]),
     "iso_mc_cases": (i32, [vp, vp, u32, u8p]),
     "iso_point_cloud_extract": (i32, [vp, vp, u32, u32, ctypes.POINTER(MeshInfo)]),
+    "iso_emc_extract": (i32, [vp, vp, u32, u32, ctypes.POINTER(MeshInfo), ctypes.POINTER(ctypes.c_uint64)]),
     "iso_dc_extract": (i32, [vp, vp, u32, u32, u32, ctypes.POINTER(MeshInfo)]),
     "iso_lhmc_extract": (i32, [vp, vp, u32, u32, ctypes.POINTER(MeshInfo)]),
     "iso_lhmc_stale_corners": (u64, [vp]),

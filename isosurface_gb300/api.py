@@ -183,6 +183,15 @@ class Context:
         check(lib().iso_point_cloud_extract(self.h, self.program(source).h, size, flags, ctypes.byref(info)), self.h)
         return info
 
+    def emc_extract(self, source, size, normals=False):
+        """ExtendedMarchingCubes::new(size).extract; returns (info, flips)."""
+        info = MeshInfo()
+        flips = ctypes.c_uint64()
+        flags = self._flags(False, normals)
+        check(lib().iso_emc_extract(self.h, self.program(source).h, size, flags, ctypes.byref(info),
+                                    ctypes.byref(flips)), self.h)
+        return info, flips.value
+
     def point_splat(self, width, height, voxel_half, view_proj=None, view_proj_inverse=None, clear=None):
         """Deferred point-splat image of the last PointCloud extraction with
         normals (examples/deferred_rasterisation.rs), (height, width, 4)
@@ -449,6 +458,21 @@ class LinearHashedMarchingCubes:
         ctx = self.context or default_context()
         info = ctx.lhmc_extract(_source_of(sampler), self.max_depth,
                                 normals=getattr(extractor, "with_normals", False))
+        _replay(extractor, ctx.download(info))
+
+
+class ExtendedMarchingCubes:
+    """ExtendedMarchingCubes::new(size) (src/extended_marching_cubes.rs:51-55)."""
+
+    def __init__(self, size, context=None):
+        if size < 1:
+            raise ValueError("size must be at least 1")
+        self.size = size
+        self.context = context
+
+    def extract(self, sampler, extractor):
+        ctx = self.context or default_context()
+        info, _ = ctx.emc_extract(_source_of(sampler), self.size, normals=getattr(extractor, "with_normals", False))
         _replay(extractor, ctx.download(info))
 
 

@@ -32,8 +32,9 @@ UNITS = {
     "mlp_infer.cu": [],
     "surrogate.cu": ["-fmad=false"],
     "splat.cu": ["-fmad=false"],
+    "emc.cu": ["-fmad=false"],
 }
-HEADERS = ["internal.h", "vm.cuh", "mc_tables.h", "mc_chunk.cuh", "qef.cuh", "mlp.h"]
+HEADERS = ["internal.h", "vm.cuh", "mc_tables.h", "mc_chunk.cuh", "qef.cuh", "mlp.h", "emc.cuh", "emc_tables.h"]
 
 
 def _deps():

@@ -223,6 +223,75 @@ def check_edge_loops(t):
     return stray
 
 
+def fan_order(t, case):
+    """The crossing edges of a feature cell in order of first use by its fans
+    (extended_marching_cubes.rs:136-153 adds e0, then e1, of each fan
+    triangle), and the number of fan triangles."""
+    row = t["EDGE_LOOPS"][case]
+    n = row[0]
+    at = 1 + n
+    order, tris = [], 0
+    for k in row[1:1 + n]:
+        loop = row[at:at + k]
+        for i in range(k):
+            for e in (loop[i], loop[(i + 1) % k]):
+                if e not in order:
+                    order.append(e)
+            tris += 1
+        at += k
+    return order, tris
+
+
+def edge_geometry(t):
+    """Per cube edge: its axis and the offsets of its lower end point in the
+    cell; and the edge at (axis, offsets) for each axis and offset pattern."""
+    axis, lo = [], []
+    for u, v in t["EDGE_CONNECTION"]:
+        a, b = t["CORNERS"][u], t["CORNERS"][v]
+        d = [i for i in range(3) if a[i] != b[i]]
+        assert len(d) == 1
+        axis.append(d[0])
+        lo.append([min(a[i], b[i]) for i in range(3)])
+    at = [[-1] * 8 for _ in range(3)]
+    for e in range(12):
+        at[axis[e]][lo[e][0] | lo[e][1] << 1 | lo[e][2] << 2] = e
+    return axis, lo, at
+
+
+def write_emc_header(t, path):
+    s = [LICENSE, "#pragma once", "#include <stdint.h>", "",
+         "// Storage class of the tables; a CUDA translation unit defines it as",
+         "// `static __device__ const` before including this header.",
+         "#ifndef ISO_TABLE", "#define ISO_TABLE static const", "#endif", "",
+         "// EDGE_LOOPS (marching_cubes_tables.rs:333-594): loop count, each loop's",
+         "// length, then the loops' edges",
+         "ISO_TABLE int8_t iso_emc_loops[256][17] = {"]
+    for row in t["EDGE_LOOPS"]:
+        s.append("    {" + ", ".join(str(v) for v in row) + "},")
+    s.append("};")
+    orders, counts = [], []
+    for case in range(256):
+        order, tris = fan_order(t, case)
+        assert sorted(order) == [e for e in range(12) if (t["EDGE_CROSSING_MASK"][case] >> e) & 1], case
+        w = 0
+        for k, e in enumerate(order):
+            w |= e << (4 * k)
+        orders.append(w)
+        counts.append(tris)
+    s += ["// fan triangles of a feature cell (the loops' total length)",
+          "ISO_TABLE uint8_t iso_emc_fan_count[256] = {", fmt_rows(counts, 16, str), "};",
+          "// crossing edges in order of first use by the fans, 4 bits each",
+          "ISO_TABLE uint64_t iso_emc_fan_order[256] = {", fmt_rows(orders, 4, lambda v: "0x%012xull" % v), "};"]
+    axis, lo, at = edge_geometry(t)
+    s += ["// per cube edge: axis, and the offsets of its lower end (x | y << 1 | z << 2)",
+          "ISO_TABLE uint8_t iso_emc_edge_axis[12] = {" + ", ".join(str(a) for a in axis) + "};",
+          "ISO_TABLE uint8_t iso_emc_edge_lo[12] = {" + ", ".join(str(l[0] | l[1] << 1 | l[2] << 2) for l in lo) + "};",
+          "// the edge along an axis whose lower end has the given offsets (-1: none)",
+          "ISO_TABLE int8_t iso_emc_edge_at[3][8] = {" + ", ".join("{" + ", ".join(str(v) for v in r) + "}" for r in at) + "};",
+          ""]
+    open(path, "w").write("\n".join(s))
+
+
 def write_oracle_header(t, path):
     s = [LICENSE, "#pragma once", "#include <stdint.h>", "",
          "namespace ref_tables {",
@@ -251,7 +320,8 @@ def main():
     assert check_edge_loops(t) == [167, 181, 229]
     write_device_header(t, os.path.join(HERE, "mc_tables.h"))
     write_oracle_header(t, os.path.join(ROOT, "oracle", "ref_tables.h"))
-    print("wrote mc_tables.h and oracle/ref_tables.h")
+    write_emc_header(t, os.path.join(HERE, "emc_tables.h"))
+    print("wrote mc_tables.h, emc_tables.h and oracle/ref_tables.h")
 
 
 if __name__ == "__main__":

@@ -1,4 +1,5 @@
-// Feature placement for DualContouring, on the device.
+// Feature placement for DualContouring (and, through the row-bounded SVD
+// steps, ExtendedMarchingCubes), on the device and on the host.
 //
 // * TangentPlanes::new over the 8 cell corners (src/feature/mod.rs:91-148)
 // * MinimiseQEF (src/feature/qef.rs:36-68) with the 3-column f64 SVD of
@@ -25,24 +26,24 @@ constexpr int QR_SWEEP_LIMIT = 10000;
 struct F3 {
     float x, y, z;
 };
-__device__ __forceinline__ F3 f3(float x, float y, float z) { return F3{x, y, z}; }
-__device__ __forceinline__ F3 add(F3 a, F3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
-__device__ __forceinline__ F3 sub(F3 a, F3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ F3 mul(F3 a, float f) { return f3(a.x * f, a.y * f, a.z * f); }
-__device__ __forceinline__ F3 mulf(float f, F3 a) { return f3(f * a.x, f * a.y, f * a.z); }
+__host__ __device__ __forceinline__ F3 f3(float x, float y, float z) { return F3{x, y, z}; }
+__host__ __device__ __forceinline__ F3 add(F3 a, F3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__host__ __device__ __forceinline__ F3 sub(F3 a, F3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__host__ __device__ __forceinline__ F3 mul(F3 a, float f) { return f3(a.x * f, a.y * f, a.z * f); }
+__host__ __device__ __forceinline__ F3 mulf(float f, F3 a) { return f3(f * a.x, f * a.y, f * a.z); }
 // dot == (a*b).component_sum() == (x + y) + z
-__device__ __forceinline__ float dot(F3 a, F3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
-__device__ __forceinline__ F3 cross(F3 a, F3 r) {
+__host__ __device__ __forceinline__ float dot(F3 a, F3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+__host__ __device__ __forceinline__ F3 cross(F3 a, F3 r) {
     return f3(a.y * r.z - a.z * r.y, a.z * r.x - a.x * r.z, a.x * r.y - a.y * r.x);
 }
-__device__ __forceinline__ F3 normalised_or_zero(F3 v) {
+__host__ __device__ __forceinline__ F3 normalised_or_zero(F3 v) {
     const float l = sqrtf((v.x * v.x + v.y * v.y) + v.z * v.z);
     if (fabsf(l) < 1.1920929e-07f) return f3(0.0f, 0.0f, 0.0f);
     return f3(v.x / l, v.y / l, v.z / l);
 }
 
 // factorize_hh
-__device__ inline double householder(double** x, int n) {
+__host__ __device__ inline double householder(double** x, int n) {
     double tau = 0.0;
     if (n > 1) {
         double xnorm;
@@ -76,9 +77,12 @@ __device__ inline double householder(double** x, int n) {
     return tau;
 }
 
-__device__ inline void bidiagonalise(double (*m)[3], double* tau_u, double* tau_v, int rows) {
+// R bounds `rows` (8 for DualContouring's corners, 12 for the edge crossings
+// of ExtendedMarchingCubes)
+template <int R = 8>
+__host__ __device__ inline void bidiagonalise(double (*m)[3], double* tau_u, double* tau_v, int rows) {
     for (int i = 0; i < 3; ++i) {
-        double* col[8];
+        double* col[R];
         const int n = rows - i;
         for (int q = 0; q < n; ++q) col[q] = &m[q + i][i];
         double tau = householder(col, n);
@@ -115,7 +119,7 @@ __device__ inline void bidiagonalise(double (*m)[3], double* tau_u, double* tau_
     }
 }
 
-__device__ inline void unpack(double (*u)[3], double (*v)[3], double* tau_u, double* tau_v, int rows) {
+__host__ __device__ inline void unpack(double (*u)[3], double (*v)[3], double* tau_u, double* tau_v, int rows) {
     v[0][0] = v[1][1] = v[2][2] = 1.0;
     v[0][1] = v[0][2] = v[1][0] = v[1][2] = v[2][0] = v[2][1] = 0.0;
     for (int i = 1; i >= 0; --i) {
@@ -155,7 +159,7 @@ __device__ inline void unpack(double (*u)[3], double (*v)[3], double* tau_u, dou
     }
 }
 
-__device__ inline void chop(double* a, double* b, int n) {
+__host__ __device__ inline void chop(double* a, double* b, int n) {
     double ai = a[0];
     for (int i = 0; i < n - 1; ++i) {
         const double bi = b[i];
@@ -165,7 +169,7 @@ __device__ inline void chop(double* a, double* b, int n) {
     }
 }
 
-__device__ inline void givens(double a, double b, double* c, double* s) {
+__host__ __device__ inline void givens(double a, double b, double* c, double* s) {
     if (b == 0.0) {
         *c = 1.0;
         *s = 0.0;
@@ -182,7 +186,7 @@ __device__ inline void givens(double a, double b, double* c, double* s) {
     }
 }
 
-__device__ inline void schur(double a1, double a2, double a3, double* c, double* s) {
+__host__ __device__ inline void schur(double a1, double a2, double a3, double* c, double* s) {
     const double apq = a1 * a2 * 2.0;
     if (apq == 0.0) {
         *c = 1.0;
@@ -197,7 +201,7 @@ __device__ inline void schur(double a1, double a2, double a3, double* c, double*
     }
 }
 
-__device__ __forceinline__ void rot_cols(double (*m)[3], int rows, int p, int q, double c, double s) {
+__host__ __device__ __forceinline__ void rot_cols(double (*m)[3], int rows, int p, int q, double c, double s) {
     for (int i = 0; i < rows; ++i) {
         const double mp = m[i][p], mq = m[i][q];
         m[i][p] = mp * c - mq * s;
@@ -205,7 +209,7 @@ __device__ __forceinline__ void rot_cols(double (*m)[3], int rows, int p, int q,
     }
 }
 
-__device__ inline void qr_middle(double (*u)[3], double* tau_u, double* tau_v, int rows, int cols, int col) {
+__host__ __device__ inline void qr_middle(double (*u)[3], double* tau_u, double* tau_v, int rows, int cols, int col) {
     double x = tau_v[col];
     double y = tau_u[col + 1];
     for (int j = col; j < cols - 1; ++j) {
@@ -227,7 +231,7 @@ __device__ inline void qr_middle(double (*u)[3], double* tau_u, double* tau_v, i
     }
 }
 
-__device__ inline void qr_end(double (*v)[3], double* tau_u, double* tau_v) {
+__host__ __device__ inline void qr_end(double (*v)[3], double* tau_u, double* tau_v) {
     double x = tau_u[1];
     double y = tau_v[1];
     for (int k = 1; k >= 0; --k) {
@@ -245,7 +249,7 @@ __device__ inline void qr_end(double (*v)[3], double* tau_u, double* tau_v) {
     }
 }
 
-__device__ inline double shift(const double* tau_u, const double* tau_v) {
+__host__ __device__ inline double shift(const double* tau_u, const double* tau_v) {
     const double ta = tau_u[1] * tau_u[1] + tau_v[0] * tau_v[0];
     const double tb = tau_u[2] * tau_u[2] + tau_v[1] * tau_v[1];
     const double tab = tau_u[1] * tau_v[1];
@@ -254,7 +258,7 @@ __device__ inline double shift(const double* tau_u, const double* tau_v) {
     return tb + tab * tab / (sqrt(dt * dt + tab * tab) - dt);
 }
 
-__device__ inline void qr_cols2(double (*u)[3], double (*v)[3], double* tau_u, double* tau_v, int rows) {
+__host__ __device__ inline void qr_cols2(double (*u)[3], double (*v)[3], double* tau_u, double* tau_v, int rows) {
     if (tau_u[0] == 0.0) {
         double c, s;
         givens(tau_v[0], tau_u[1], &c, &s);
@@ -302,7 +306,7 @@ __device__ inline void qr_cols2(double (*u)[3], double (*v)[3], double* tau_u, d
     }
 }
 
-__device__ inline void qr_step(double (*u)[3], double (*v)[3], double* tau_u, double* tau_v, int rows, int cols) {
+__host__ __device__ inline void qr_step(double (*u)[3], double (*v)[3], double* tau_u, double* tau_v, int rows, int cols) {
     if (cols == 2) {
         qr_cols2(u, v, tau_u, tau_v, rows);
         return;
@@ -361,7 +365,8 @@ __device__ inline void qr_step(double (*u)[3], double (*v)[3], double* tau_u, do
 }
 
 // returns false when the sweep bound was reached
-__device__ inline bool diagonalise(double (*u)[3], double (*v)[3], double* tau_u, double* tau_v, int rows) {
+template <int R = 8>
+__host__ __device__ inline bool diagonalise(double (*u)[3], double (*v)[3], double* tau_u, double* tau_v, int rows) {
     chop(tau_u, tau_v, 3);
     int b = 2;
     int guard = 0;
@@ -373,7 +378,7 @@ __device__ inline bool diagonalise(double (*u)[3], double (*v)[3], double* tau_u
             int a = b - 1;
             while (a > 0 && tau_v[a - 1] != 0.0) a -= 1;
             const int n = b - a + 1;
-            double u1[8][3], v1[3][3];
+            double u1[R][3], v1[3][3];
             for (int i = 0; i < rows; ++i) u1[i][0] = u1[i][1] = u1[i][2] = 0.0;
             for (int i = 0; i < 3; ++i) v1[i][0] = v1[i][1] = v1[i][2] = 0.0;
             for (int j = a; j <= b; ++j) {
@@ -391,7 +396,7 @@ __device__ inline bool diagonalise(double (*u)[3], double (*v)[3], double* tau_u
     return true;
 }
 
-__device__ inline void singularise(double (*u)[3], double (*v)[3], double* d, int rows) {
+__host__ __device__ inline void singularise(double (*u)[3], double (*v)[3], double* d, int rows) {
     for (int j = 0; j < 3; ++j) {
         if (d[j] < 0.0) {
             for (int i = 0; i < 3; ++i) v[i][j] = -v[i][j];
@@ -434,7 +439,7 @@ struct Planes {
     int feature;
 };
 
-__device__ inline void tangent_planes(const F3* vtx, const F3* nrm, Planes* t) {
+__host__ __device__ inline void tangent_planes(const F3* vtx, const F3* nrm, Planes* t) {
     F3 com = f3(0.0f, 0.0f, 0.0f), axis = f3(0.0f, 0.0f, 0.0f);
     float min_angle = 3.40282347e+38f;
     float count = 0.0f;
@@ -474,7 +479,7 @@ __device__ inline void tangent_planes(const F3* vtx, const F3* nrm, Planes* t) {
 }
 
 // MinimiseQEF::place_feature_with_tangents; *ok = false if the QR bound hit
-__device__ inline F3 minimise_qef(const Planes& t, bool* ok) {
+__host__ __device__ inline F3 minimise_qef(const Planes& t, bool* ok) {
     *ok = true;
     if (t.feature == PLANAR) return t.com;
     double u[8][3], v[3][3], d[3] = {0.0, 0.0, 0.0};
@@ -518,7 +523,7 @@ __device__ inline F3 minimise_qef(const Planes& t, bool* ok) {
     return add(t.com, f3((float)x[0], (float)x[1], (float)x[2]));
 }
 
-__device__ inline F3 trilinear(const F3* c, const F3* f, F3 p) {
+__host__ __device__ inline F3 trilinear(const F3* c, const F3* f, F3 p) {
     const F3 den = sub(f3(c[1].x, c[3].y, c[4].z), c[0]);
     const F3 num = sub(p, c[0]);
     const F3 g = f3(num.x / den.x, num.y / den.y, num.z / den.z);
@@ -531,7 +536,7 @@ __device__ inline F3 trilinear(const F3* c, const F3* f, F3 p) {
     return add(mulf(1.0f - g.z, c0), mulf(g.z, c1));
 }
 
-__device__ inline F3 particle_placement(const F3* corners, const F3* normals) {
+__host__ __device__ inline F3 particle_placement(const F3* corners, const F3* normals) {
     const float STEP_SIZE = 0.05f, THRESHOLD = 0.02f;
     Planes t;
     tangent_planes(corners, normals, &t);

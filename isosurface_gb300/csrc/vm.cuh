@@ -7,6 +7,7 @@
 // which keeps cube classification bit-exact.
 #pragma once
 #include <cuda_runtime.h>
+#include <string.h>
 
 #include "internal.h"
 
@@ -23,35 +24,55 @@ struct V3 {
     float x, y, z;
 };
 
+// Read-only loads: through the non-coherent cache on the device, plain on
+// the host (the evaluator also compiles for host code that checks it).
+template <class T>
+__host__ __device__ __forceinline__ T ld_ro(const T* p) {
+#ifdef __CUDA_ARCH__
+    return __ldg(p);
+#else
+    return *p;
+#endif
+}
+__host__ __device__ __forceinline__ uint32_t float_bits(float f) {
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(f);
+#else
+    uint32_t u;
+    memcpy(&u, &f, sizeof(u));
+    return u;
+#endif
+}
+
 __host__ __device__ __forceinline__ V3 v3(float x, float y, float z) { return V3{x, y, z}; }
-__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
-__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ V3 operator*(V3 a, float f) { return v3(a.x * f, a.y * f, a.z * f); }
-__device__ __forceinline__ float len_sq(V3 a) { return (a.x * a.x + a.y * a.y) + a.z * a.z; }
-__device__ __forceinline__ float vlen(V3 a) { return sqrtf(len_sq(a)); }
-__device__ __forceinline__ V3 vmin(V3 a, V3 b) { return v3(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z)); }
+__host__ __device__ __forceinline__ V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__host__ __device__ __forceinline__ V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__host__ __device__ __forceinline__ V3 operator*(V3 a, float f) { return v3(a.x * f, a.y * f, a.z * f); }
+__host__ __device__ __forceinline__ float len_sq(V3 a) { return (a.x * a.x + a.y * a.y) + a.z * a.z; }
+__host__ __device__ __forceinline__ float vlen(V3 a) { return sqrtf(len_sq(a)); }
+__host__ __device__ __forceinline__ V3 vmin(V3 a, V3 b) { return v3(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z)); }
 
 // primitives: sphere.rs:35-63, rectangular_prism.rs:36-80, cylinder.rs:41-85, torus.rs:40-108
-__device__ __forceinline__ float sd_sphere(V3 q, float r) { return vlen(q) - r; }
-__device__ __forceinline__ float sd_box(V3 q, float hx, float hy, float hz) {
+__host__ __device__ __forceinline__ float sd_sphere(V3 q, float r) { return vlen(q) - r; }
+__host__ __device__ __forceinline__ float sd_box(V3 q, float hx, float hy, float hz) {
     float ax = fabsf(q.x) - hx, ay = fabsf(q.y) - hy, az = fabsf(q.z) - hz;
     float l = vlen(v3(fmaxf(ax, 0.0f), fmaxf(ay, 0.0f), fmaxf(az, 0.0f)));
     return l + fminf(fmaxf(ax, fmaxf(ay, az)), 0.0f);
 }
-__device__ __forceinline__ float sd_cylinder(V3 q, float r, float hl) {
+__host__ __device__ __forceinline__ float sd_cylinder(V3 q, float r, float hl) {
     float qx = fabsf(sqrtf(q.x * q.x + q.y * q.y)) - r;
     float qz = fabsf(q.z) - hl;
     float dx = fmaxf(qx, 0.0f), dz = fmaxf(qz, 0.0f);
     float l = sqrtf((dx * dx + dz * dz) + 0.0f * 0.0f);
     return fminf(fmaxf(qx, qz), 0.0f) + l;
 }
-__device__ __forceinline__ float sd_torus(V3 q, float R, float r) {
+__host__ __device__ __forceinline__ float sd_torus(V3 q, float R, float r) {
     float qx = fabsf(sqrtf(q.x * q.x + q.y * q.y)) - R;
     float l = sqrtf(qx * qx + q.z * q.z);
     return l - r;
 }
 // Polynomial smooth minimum (Quilez 2013)
-__device__ __forceinline__ float smooth_min(float a, float b, float k) {
+__host__ __device__ __forceinline__ float smooth_min(float a, float b, float k) {
     const float gap = k - fabsf(a - b);
     // with k > 0 and no overlap, h is +0 and the formula gives min(a, b) - 0
     // exactly (also for -0 and NaN operands): skip the division
@@ -60,19 +81,19 @@ __device__ __forceinline__ float smooth_min(float a, float b, float k) {
     return fminf(a, b) - ((h * h) * k) * 0.25f;
 }
 
-__device__ __forceinline__ V3 n_box(V3 p) {  // vector.rs:612-621
+__host__ __device__ __forceinline__ V3 n_box(V3 p) {  // vector.rs:612-621
     float ax = fabsf(p.x), ay = fabsf(p.y), az = fabsf(p.z);
     if (ax > ay && ax > az) return v3(p.x, 0.0f, 0.0f);
     if (ay > az) return v3(0.0f, p.y, 0.0f);
     return v3(0.0f, 0.0f, p.z);
 }
-__device__ __forceinline__ V3 n_cylinder(V3 p, float r, float hl) {
+__host__ __device__ __forceinline__ V3 n_cylinder(V3 p, float r, float hl) {
     float z = fabsf(p.z) / hl;
     float rr = sqrtf(p.x * p.x + p.y * p.y) / r;
     if (z > rr) return v3(0.0f, 0.0f, p.z);
     return v3(p.x, p.y, 0.0f);
 }
-__device__ __forceinline__ V3 n_torus(V3 p, float R) {
+__host__ __device__ __forceinline__ V3 n_torus(V3 p, float R) {
     float l = sqrtf((p.x * p.x + p.y * p.y) + 0.0f * 0.0f);
     V3 ring;
     if (fabsf(l) < 1.1920929e-07f) ring = v3(1.0f, 0.0f, 0.0f);
@@ -80,7 +101,7 @@ __device__ __forceinline__ V3 n_torus(V3 p, float R) {
     return p - ring * R;
 }
 
-__device__ __forceinline__ V3 pt_apply(uint32_t op, const float* k, V3 p) {
+__host__ __device__ __forceinline__ V3 pt_apply(uint32_t op, const float* k, V3 p) {
     if (op == OP_PT_DOMAIN) return v3(p.x * k[0] + k[3], p.y * k[1] + k[4], p.z * k[2] + k[5]);
     if (op == OP_PT_TRANSLATE) return v3(p.x - k[0], p.y - k[1], p.z - k[2]);
     V3 d = v3(p.x - k[0], p.y - k[1], p.z - k[2]);
@@ -93,7 +114,7 @@ __device__ __forceinline__ V3 pt_apply(uint32_t op, const float* k, V3 p) {
 // The top value and the current point live in registers; only the entries
 // below them are kept in (local-memory) stacks, so a primitive, a binary
 // operator and a point op each touch memory at most once.
-static __device__ __noinline__ float eval_range(const ProgView& pv, uint32_t begin, uint32_t end, V3 p) {
+static __host__ __device__ __noinline__ float eval_range(const ProgView& pv, uint32_t begin, uint32_t end, V3 p) {
     float vs[VSTACK];  // values below the top: vs[0 .. vsp-2]
     V3 ps[PSTACK];     // points below the current one: ps[0 .. psp-1]
     float tos = 0.0f;  // top value (vsp > 0)
@@ -105,7 +126,7 @@ static __device__ __noinline__ float eval_range(const ProgView& pv, uint32_t beg
         ++vsp;
     };
     for (uint32_t pc = begin; pc < end; ++pc) {
-        const uint32_t w = __ldg(pv.ops + pc);
+        const uint32_t w = ld_ro(pv.ops + pc);
         const uint32_t op = w & 0xFFu;
         const float* k = pv.k + (w >> 8);
         switch (op) {
@@ -144,13 +165,13 @@ static __device__ __noinline__ float eval_range(const ProgView& pv, uint32_t beg
 
 // A hard union of translated primitives (ProgView::prims): the same
 // translate, primitive and fminf operations as the ops, in the same order.
-static __device__ __noinline__ float eval_prims(const ProgView& pv, V3 p) {
+static __host__ __device__ __noinline__ float eval_prims(const ProgView& pv, V3 p) {
     const V3 q = pv.dom_at >= 0 ? pt_apply(OP_PT_DOMAIN, pv.k + pv.dom_at, p) : p;
     float v = 0.0f;
     for (uint32_t i = 0; i < pv.nprims; ++i) {
-        const float4 c = __ldg(pv.prims + 2 * i), a = __ldg(pv.prims + 2 * i + 1);
+        const float4 c = ld_ro(pv.prims + 2 * i), a = ld_ro(pv.prims + 2 * i + 1);
         const V3 t = v3(q.x - c.x, q.y - c.y, q.z - c.z);
-        const uint32_t type = __float_as_uint(c.w);
+        const uint32_t type = float_bits(c.w);
         float d;
         if (type == OP_SPHERE) d = sd_sphere(t, a.x);
         else if (type == OP_BOX) d = sd_box(t, a.x, a.y, a.z);
@@ -161,12 +182,12 @@ static __device__ __noinline__ float eval_prims(const ProgView& pv, V3 p) {
     return v;
 }
 
-__device__ __forceinline__ float eval_scalar(const ProgView& pv, V3 p) {
+__host__ __device__ __forceinline__ float eval_scalar(const ProgView& pv, V3 p) {
     return pv.prims ? eval_prims(pv, p) : eval_range(pv, 0, pv.n_ops, p);
 }
 
 // Value and (unnormalised) normal: HermiteSource::sample_normal semantics.
-static __device__ __noinline__ float eval_hermite(const ProgView& pv, V3 p, V3* normal) {
+static __host__ __device__ __noinline__ float eval_hermite(const ProgView& pv, V3 p, V3* normal) {
     float vs[VSTACK];
     V3 ns[VSTACK];
     V3 ps[PSTACK];
