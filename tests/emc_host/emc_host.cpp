@@ -30,30 +30,62 @@
 
 using namespace iso;
 
+namespace {
+
+struct HostProgram {
+    std::vector<uint32_t> ops;
+    std::vector<float> consts;
+    std::vector<int32_t> jump;
+    ProgView view() const { return ProgView{ops.data(), consts.data(), jump.data(), (uint32_t)ops.size(), nullptr, 0, -1}; }
+};
+
+// the program's ops, constants (padded as the library pads them) and CD jump table
+bool parse(const uint8_t* bytes, size_t len, HostProgram* p) {
+    uint32_t h[4];
+    if (len < 16) return false;
+    std::memcpy(h, bytes, 16);
+    if (h[0] != 0x314F5349u || 16 + 4ull * h[1] + 4ull * h[2] != len) return false;
+    p->ops.assign(h[1], 0);
+    p->consts.assign(h[2] + 4, 0.0f);
+    std::memcpy(p->ops.data(), bytes + 16, 4ull * h[1]);
+    if (h[2]) std::memcpy(p->consts.data(), bytes + 16 + 4ull * h[1], 4ull * h[2]);
+    // CD_BEGIN -> its CD_END (scopes do not nest)
+    p->jump.assign(p->ops.size(), 0);
+    for (size_t pc = 0; pc < p->ops.size(); ++pc)
+        if ((p->ops[pc] & 0xFF) == OP_CD_BEGIN)
+            for (size_t e = pc + 1; e < p->ops.size(); ++e)
+                if ((p->ops[e] & 0xFF) == OP_CD_END) {
+                    p->jump[pc] = (int32_t)e;
+                    break;
+                }
+    return true;
+}
+
+}  // namespace
+
 extern "C" {
+
+// The device's Directed evaluator (emc::eval_vector) at n points, 3 floats each.
+int emc_host_sample_vector(const uint8_t* bytes, size_t len, const float* pts, uint64_t n, float* out) {
+    HostProgram p;
+    if (!parse(bytes, len, &p)) return 2;
+    const ProgView pv = p.view();
+    for (uint64_t i = 0; i < n; ++i) {
+        const V3 v = emc::eval_vector(pv, v3(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]));
+        out[3 * i] = v.x;
+        out[3 * i + 1] = v.y;
+        out[3 * i + 2] = v.z;
+    }
+    return 0;
+}
 
 // counts: vertices, triangles, flips, device error bits.  Returns 0, or 1
 // when the output capacities are too small (counts still filled), or 2 for
 // a malformed program.
 int emc_host_extract(const uint8_t* bytes, size_t len, uint32_t size, float* vout, uint64_t vcap, uint32_t* iout,
                      uint64_t icap, uint64_t* counts) {
-    uint32_t h[4];
-    if (len < 16) return 2;
-    std::memcpy(h, bytes, 16);
-    if (h[0] != 0x314F5349u || 16 + 4ull * h[1] + 4ull * h[2] != len) return 2;
-    std::vector<uint32_t> ops(h[1]);
-    std::vector<float> consts(h[2] + 4, 0.0f);
-    std::memcpy(ops.data(), bytes + 16, 4ull * h[1]);
-    if (h[2]) std::memcpy(consts.data(), bytes + 16 + 4ull * h[1], 4ull * h[2]);
-    // CD_BEGIN -> its CD_END (scopes do not nest)
-    std::vector<int32_t> jump(ops.size(), 0);
-    for (size_t pc = 0; pc < ops.size(); ++pc)
-        if ((ops[pc] & 0xFF) == OP_CD_BEGIN)
-            for (size_t e = pc + 1; e < ops.size(); ++e)
-                if ((ops[e] & 0xFF) == OP_CD_END) {
-                    jump[pc] = (int32_t)e;
-                    break;
-                }
+    HostProgram prog;
+    if (!parse(bytes, len, &prog)) return 2;
     counts[0] = counts[1] = counts[2] = counts[3] = 0;
     if (size < 2) return 0;
     const uint32_t n = size;
@@ -63,7 +95,7 @@ int emc_host_extract(const uint8_t* bytes, size_t len, uint32_t size, float* vou
     std::vector<uint32_t> voff(cells), toff(cells), edge_map(3 * points, 0xFFFFFFFFu);
     uint32_t err = 0;
     emc::Args A{};
-    A.prog = ProgView{ops.data(), consts.data(), jump.data(), (uint32_t)ops.size(), nullptr, 0, -1};
+    A.prog = prog.view();
     A.g = emc::Grid{n, 1.0f / (float)(n - 1)};
     A.field = field.data();
     A.cell = cell.data();

@@ -7,6 +7,7 @@ This checks on any machine the device code's arithmetic, vertex ownership,
 output order and flips; tests/test_emc_gpu.py checks the kernels themselves
 on a GPU."""
 import ctypes
+import json
 import os
 import sys
 
@@ -45,6 +46,20 @@ def host_emc(L, src, n):
     assert r == 0
     assert int(c[3]) == 0  # no QR sweep bound
     return v[:3 * int(c[0])].reshape(-1, 3), i[:3 * int(c[1])], int(c[2])
+
+
+def test_host_directed_evaluator_reference_kats(host_lib):
+    """The device's Directed evaluator (emc.cuh eval_vector), built for the
+    host, on every sample_vector assertion of the reference's primitive tests."""
+    kats = [k for k in json.load(open(os.path.join(HERE, "golden", "kats.json"))) if k["kind"] == "vector"]
+    assert len(kats) == 31
+    for k in kats:
+        b = S.lower(S.from_spec(k["source"]))
+        pt = np.asarray(k["point"], np.float32)
+        out = np.empty(3, np.float32)
+        assert host_lib.emc_host_sample_vector(b, len(b), pt.ctypes.data_as(ctypes.c_void_p), ctypes.c_uint64(1),
+                                               out.ctypes.data_as(ctypes.c_void_p)) == 0
+        assert np.array_equal(out, np.asarray(k["expected"], np.float32)), k
 
 
 def _check(L, src, n):
