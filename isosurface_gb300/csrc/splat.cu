@@ -160,6 +160,8 @@ iso_status iso_point_splat_render(iso_ctx* ctx, const float* view_proj, const fl
     iso_status s = set_device(ctx);
     if (s != ISO_OK) return s;
     const uint64_t npix = (uint64_t)width * height, n = ctx->last.num_vertices;
+    // the depth test's 64-bit key holds the point index in its low 32 bits
+    if (n > 0xFFFFFFFFull) return fail(ctx, ISO_ERR_TOO_LARGE, "point cloud above 2^32 points");
     // z-buffer | two position + normal buffer pairs | composited image
     const size_t zbytes = (8 * npix + 255) & ~(size_t)255, fbytes = 16 * npix;
     if ((s = ensure(ctx, ctx->aux, zbytes + 5 * fbytes)) != ISO_OK) return s;
