@@ -360,6 +360,18 @@ ISO_API iso_status iso_mlp_make_dataset(iso_mlp* net, const iso_program* exact, 
  * the loss of each step into history (nullable) */
 ISO_API iso_status iso_mlp_train(iso_mlp* net, uint32_t steps, uint32_t batch, float lr, float clamp_d,
                                  uint64_t seed, float* history);
+/* Training checkpoints: a 32-byte header ("ISOMLP01", u32 version 1, u32
+ * header size 32, u64 parameter count, u64 Adam steps taken) followed by the
+ * fp32 parameters and Adam's first and second moments (parameter count
+ * floats each, host byte order).  Loading restores the parameters, the
+ * moments and the step count (which Adam's bias correction and the batch
+ * sampling use), and rebuilds the bf16 inference copy; the dataset is not
+ * part of the checkpoint.  iso_mlp_checkpoint_info reads and checks a
+ * checkpoint's header and size without a device (ISO_ERR_INVALID_ARG for a
+ * missing, short or foreign file). */
+ISO_API iso_status iso_mlp_save(iso_mlp* net, const char* path);
+ISO_API iso_status iso_mlp_load(iso_mlp* net, const char* path);
+ISO_API iso_status iso_mlp_checkpoint_info(const char* path, uint64_t* nparams, uint64_t* step);
 
 /* Learned-surrogate marching cubes.  The field of MarchingCubes::new(size)
  * for `exact` is built as: the network (bf16 tensor cores) on every

@@ -105,6 +105,9 @@ SIGNATURES = {
     "iso_mlp_loss_grad": (i32, [vp, f32p, f32p, u32, ctypes.c_float, f32p, f32p]),
     "iso_mlp_make_dataset": (i32, [vp, vp, u32, ctypes.c_float, ctypes.c_float, u64]),
     "iso_mlp_train": (i32, [vp, u32, u32, ctypes.c_float, ctypes.c_float, u64, f32p]),
+    "iso_mlp_save": (i32, [vp, ctypes.c_char_p]),
+    "iso_mlp_load": (i32, [vp, ctypes.c_char_p]),
+    "iso_mlp_checkpoint_info": (i32, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
     "iso_surrogate_field": (i32, [vp, vp, vp, u32, u32, ctypes.c_float, vp, u64, ctypes.POINTER(SurrogateStats)]),
     "iso_surrogate_extract": (i32, [vp, vp, vp, u32, u32, ctypes.c_float, u32, ctypes.POINTER(SurrogateStats),
                                     ctypes.POINTER(MeshInfo)]),

@@ -21,6 +21,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -502,6 +503,88 @@ iso_status iso_mlp_train(iso_mlp* net, uint32_t steps, uint32_t batch, float lr,
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (d_hist) cudaFree(d_hist);
     return e == cudaSuccess ? check_launch(net->ctx, "mlp train") : cuda_fail(net->ctx, e, "mlp train");
+}
+
+// ------------------------------------------------------------- checkpoints ---
+// 32-byte header, then NPARAMS fp32 parameters, Adam's first and second
+// moments; host byte order (little-endian on both supported machines).
+namespace {
+constexpr char CKPT_MAGIC[8] = {'I', 'S', 'O', 'M', 'L', 'P', '0', '1'};
+struct CkptHeader {
+    char magic[8];
+    uint32_t version;       // 1
+    uint32_t header_bytes;  // 32
+    uint64_t nparams;
+    uint64_t step;          // Adam steps taken
+};
+static_assert(sizeof(CkptHeader) == 32, "checkpoint header layout");
+
+// 0 = ok, 1 = cannot open / short file, 2 = not a checkpoint of this network
+int read_header(FILE* f, CkptHeader* h) {
+    if (std::fread(h, sizeof(*h), 1, f) != 1) return 1;
+    if (std::memcmp(h->magic, CKPT_MAGIC, 8) != 0 || h->version != 1 || h->header_bytes != sizeof(*h) ||
+        h->nparams != NPARAMS)
+        return 2;
+    return 0;
+}
+}  // namespace
+
+iso_status iso_mlp_checkpoint_info(const char* path, uint64_t* nparams, uint64_t* step) {
+    if (!path) return ISO_ERR_INVALID_ARG;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return ISO_ERR_INVALID_ARG;
+    CkptHeader h;
+    const int r = read_header(f, &h);
+    std::fseek(f, 0, SEEK_END);
+    const long size = std::ftell(f);
+    std::fclose(f);
+    if (r != 0 || size != (long)(sizeof(h) + 12ull * NPARAMS)) return ISO_ERR_INVALID_ARG;
+    if (nparams) *nparams = h.nparams;
+    if (step) *step = h.step;
+    return ISO_OK;
+}
+
+iso_status iso_mlp_save(iso_mlp* net, const char* path) {
+    if (!net || !path) return ISO_ERR_INVALID_ARG;
+    iso_status s = set_device(net->ctx);
+    if (s != ISO_OK) return s;
+    std::vector<float> host(3 * NPARAMS);
+    cudaError_t e = cudaMemcpy(host.data(), net->params, 4ull * NPARAMS, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(host.data() + NPARAMS, net->m, 8ull * NPARAMS, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(net->ctx, e, "checkpoint read");
+    CkptHeader h{};
+    std::memcpy(h.magic, CKPT_MAGIC, 8);
+    h.version = 1;
+    h.header_bytes = sizeof(h);
+    h.nparams = NPARAMS;
+    h.step = net->step;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(net->ctx, ISO_ERR_INVALID_ARG, std::string("cannot write ") + path);
+    const bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 &&
+                    std::fwrite(host.data(), 4, host.size(), f) == host.size();
+    if (std::fclose(f) != 0 || !ok) return fail(net->ctx, ISO_ERR_INVALID_ARG, std::string("cannot write ") + path);
+    return ISO_OK;
+}
+
+iso_status iso_mlp_load(iso_mlp* net, const char* path) {
+    if (!net || !path) return ISO_ERR_INVALID_ARG;
+    iso_status s = iso_mlp_checkpoint_info(path, nullptr, nullptr);
+    if (s != ISO_OK) return fail(net->ctx, s, std::string("not a checkpoint of this network: ") + path);
+    if ((s = set_device(net->ctx)) != ISO_OK) return s;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(net->ctx, ISO_ERR_INVALID_ARG, std::string("cannot read ") + path);
+    CkptHeader h;
+    std::vector<float> host(3 * NPARAMS);
+    const bool ok = read_header(f, &h) == 0 && std::fread(host.data(), 4, host.size(), f) == host.size();
+    std::fclose(f);
+    if (!ok) return fail(net->ctx, ISO_ERR_INVALID_ARG, std::string("cannot read ") + path);
+    // parameters | gradients | first moments | second moments, one allocation
+    cudaError_t e = cudaMemcpy(net->params, host.data(), 4ull * NPARAMS, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(net->m, host.data() + NPARAMS, 8ull * NPARAMS, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(net->ctx, e, "checkpoint load");
+    net->step = h.step;
+    mlp_infer_invalidate(net);
+    return ISO_OK;
 }
 
 }  // extern "C"

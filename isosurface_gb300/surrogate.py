@@ -3,6 +3,7 @@ library's own kernels (csrc/mlp.cu), evaluated with BF16 tensor cores
 (csrc/mlp_infer.cu), and used to mesh an expensive source with exact
 re-sampling near the surface."""
 import ctypes
+import os
 
 import numpy as np
 
@@ -73,6 +74,14 @@ class Surrogate:
         check(lib().iso_mlp_train(self.h, steps, batch, lr, clamp_d, seed, hist.ctypes.data_as(f32p)), self.ctx.h)
         return hist
 
+    def save(self, path):
+        """Checkpoint of the training state: parameters, Adam moments and step."""
+        check(lib().iso_mlp_save(self.h, os.fsencode(path)), self.ctx.h)
+
+    def load(self, path):
+        """Restore a checkpoint written by save (the dataset stays as it is)."""
+        check(lib().iso_mlp_load(self.h, os.fsencode(path)), self.ctx.h)
+
     def field(self, exact_source, size, field_ptr, pitch, coarse_step=4, band_cells=2.0):
         """The surrogate field of MarchingCubes::new(size) into a device buffer
         laid out as Context.sample_grid writes it; returns the band statistics."""
@@ -95,6 +104,13 @@ class Surrogate:
 
 def _stats(st):
     return {"coarse_points": st.coarse_points, "band_points": st.band_points, "total_points": st.total_points}
+
+
+def checkpoint_info(path):
+    """(parameter count, Adam steps) of a checkpoint; needs no device."""
+    n, step = ctypes.c_uint64(), ctypes.c_uint64()
+    check(lib().iso_mlp_checkpoint_info(os.fsencode(path), ctypes.byref(n), ctypes.byref(step)))
+    return n.value, step.value
 
 
 def mesh_distance(ctx, a, b, bucket, max_rings=32):

@@ -3,7 +3,7 @@ through the C ABI: bit-exact vertices and indices, the same number of rotated
 edges, the normals sink, and the errors the entry point raises.
 
 The kernels' per-item code is checked on the host by test_emc_host.py.  These
-tests run the kernels themselves; they are skipped unless ISO_EMC_GPU=1 until
+tests run the kernels themselves; they are skipped unless ISO_PENDING_GPU_TESTS=1 until
 the kernels have run once on a GB300."""
 import os
 
@@ -17,8 +17,8 @@ from isosurface_gb300 import source as S
 from emc_scenes import FIXED, random_scenes
 
 pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(os.environ.get("ISO_EMC_GPU") != "1",
-                                 reason="ExtendedMarchingCubes kernels not yet run on a GB300 (set ISO_EMC_GPU=1)")]
+              pytest.mark.skipif(os.environ.get("ISO_PENDING_GPU_TESTS") != "1",
+                                 reason="ExtendedMarchingCubes kernels not yet run on a GB300 (set ISO_PENDING_GPU_TESTS=1)")]
 
 
 def _gpu(ctx, src, n, normals=False):
