@@ -62,7 +62,9 @@ def build(force=False, verbose=False):
             return LIB
     with cf.ThreadPoolExecutor(max_workers=min(8, len(UNITS))) as ex:
         objs = list(ex.map(lambda kv: _compile(*kv), UNITS.items()))
-    cmd = [NVCC, *ARCH, "-shared", "-cudart", "shared", "-o", LIB + ".tmp", *objs]
+    # -ldl: the NVTX ranges dlopen a profiler's injection library when one is
+    # attached (dlopen is in libc from glibc 2.34, in libdl before)
+    cmd = [NVCC, *ARCH, "-shared", "-cudart", "shared", "-o", LIB + ".tmp", *objs, "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))

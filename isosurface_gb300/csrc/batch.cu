@@ -322,6 +322,7 @@ iso_status iso_batch_set_slab(iso_batch* b, uint32_t size, uint32_t depth) {
 }
 
 iso_status iso_batch_run(iso_batch* b, uint32_t flags, iso_mesh_info* info) {
+    iso::NvtxRange nvtx_range("iso_batch_run");
     if (!b) return ISO_ERR_INVALID_ARG;
     iso_ctx* ctx = b->ctx;
     iso_status s = set_device(ctx);
@@ -390,6 +391,7 @@ iso_status iso_batch_run(iso_batch* b, uint32_t flags, iso_mesh_info* info) {
 }
 
 iso_status iso_batch_run_per_chunk(iso_batch* b, iso_mesh_info* info) {
+    iso::NvtxRange nvtx_range("iso_batch_run_per_chunk");
     if (!b) return ISO_ERR_INVALID_ARG;
     iso_ctx* ctx = b->ctx;
     iso_status s = set_device(ctx);

@@ -496,6 +496,7 @@ static iso_status check_size(iso_ctx* ctx, const iso_program* prog, uint32_t siz
 }
 
 iso_status iso_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t size, float* field, uint64_t pitch) {
+    iso::NvtxRange nvtx_range("iso_sample_grid");
     iso_status s = check_size(ctx, prog, size);
     if (s != ISO_OK) return s;
     if (!field || pitch < size) return fail(ctx, ISO_ERR_INVALID_ARG, "field null or pitch < size");
@@ -509,6 +510,7 @@ iso_status iso_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t size,
 }
 
 iso_status iso_mc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t flags, iso_mesh_info* info) {
+    iso::NvtxRange nvtx_range("iso_mc_extract");
     iso_status s = check_size(ctx, prog, size);
     if (s != ISO_OK) return s;
     if (flags & ~(uint32_t)(ISO_FLAG_KEYS | ISO_FLAG_NORMALS)) return fail(ctx, ISO_ERR_INVALID_ARG, "unknown flags");
@@ -554,6 +556,7 @@ iso_status iso_host_unregister(void* p) {
 
 iso_status iso_mc_extract_host(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t flags, float* vertices,
                                uint64_t vertex_floats, uint32_t* indices, uint64_t index_count, iso_mesh_info* info) {
+    iso::NvtxRange nvtx_range("iso_mc_extract_host");
     if (!ctx) return ISO_ERR_INVALID_ARG;
     if ((!vertices && vertex_floats) || (!indices && index_count))
         return fail(ctx, ISO_ERR_INVALID_ARG, "null host buffer with nonzero room");
@@ -587,6 +590,7 @@ iso_status iso_mc_extract_host(iso_ctx* ctx, const iso_program* prog, uint32_t s
 
 iso_status iso_mc_extract_field(iso_ctx* ctx, const float* field, uint32_t nx, uint32_t ny, uint32_t nz, uint64_t pitch,
                                 uint32_t flags, iso_mesh_info* info) {
+    iso::NvtxRange nvtx_range("iso_mc_extract_field");
     if (!ctx || !field) return ISO_ERR_INVALID_ARG;
     if (nx != ny || nx < 2 || nz < 2 || pitch < nx || nx > 65536 || nz > 65537)
         return fail(ctx, ISO_ERR_INVALID_ARG, "need nx == ny >= 2, nz >= 2, pitch >= nx");
@@ -636,6 +640,7 @@ iso_status iso_sample_points(iso_ctx* ctx, const iso_program* prog, const float*
 
 iso_status iso_point_cloud_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t flags,
                                    iso_mesh_info* info) {
+    iso::NvtxRange nvtx_range("iso_point_cloud_extract");
     iso_status s = check_size(ctx, prog, size);
     if (s != ISO_OK) return s;
     if (flags & ~(uint32_t)ISO_FLAG_NORMALS) return fail(ctx, ISO_ERR_INVALID_ARG, "unsupported flags");

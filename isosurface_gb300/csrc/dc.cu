@@ -191,6 +191,7 @@ static iso_status dc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint32_
 
 // ISO_FLAG_NORMALS: the *InterleavedNormals sinks, sample_normal at every vertex
 extern "C" iso_status iso_dc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t placer, uint32_t flags, iso_mesh_info* info) {
+    iso::NvtxRange nvtx_range("iso_dc_extract");
     if (!ctx || !prog) return ISO_ERR_INVALID_ARG;
     if (flags & ~(uint32_t)(ISO_FLAG_KEYS | ISO_FLAG_NORMALS)) return fail(ctx, ISO_ERR_INVALID_ARG, "unsupported flags");
     iso_status s = dc_extract_impl(ctx, prog, size, placer, flags & ~(uint32_t)ISO_FLAG_NORMALS, info);

@@ -180,6 +180,7 @@ static iso_status emc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint32
 // ISO_FLAG_NORMALS: IndexedInterleavedNormals, sample_normal at every vertex
 extern "C" iso_status iso_emc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t flags,
                                       iso_mesh_info* info, uint64_t* flips) {
+    iso::NvtxRange nvtx_range("iso_emc_extract");
     if (!ctx || !prog) return ISO_ERR_INVALID_ARG;
     if (flags & ~(uint32_t)ISO_FLAG_NORMALS) return fail(ctx, ISO_ERR_INVALID_ARG, "unsupported flags");
     iso_status s = emc_extract_impl(ctx, prog, size, info, flips);

@@ -6,9 +6,21 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/isosurface_gpu.h"
 
 namespace iso {
+
+// An NVTX range over one public call, named after it, for profilers that
+// record NVTX (ncu --nvtx, Nsight Systems); a pointer test when none is
+// attached.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // Device-side error bits (ctx->d_err), read back after each call.
 enum : uint32_t {

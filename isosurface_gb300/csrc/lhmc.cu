@@ -857,6 +857,7 @@ static iso_status lhmc_planned(iso_ctx* ctx, const iso_program* prog, uint32_t d
 
 // ISO_FLAG_NORMALS: the *InterleavedNormals sinks, sample_normal at every vertex
 extern "C" iso_status iso_lhmc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t max_depth, uint32_t flags, iso_mesh_info* info) {
+    iso::NvtxRange nvtx_range("iso_lhmc_extract");
     if (!ctx || !prog) return ISO_ERR_INVALID_ARG;
     if (flags & ~(uint32_t)(ISO_FLAG_KEYS | ISO_FLAG_NORMALS)) return fail(ctx, ISO_ERR_INVALID_ARG, "unsupported flags");
     iso_status s = lhmc_planned(ctx, prog, max_depth, flags & ~(uint32_t)ISO_FLAG_NORMALS, info);

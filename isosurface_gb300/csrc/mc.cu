@@ -1053,6 +1053,7 @@ extern "C" ISO_API iso_status iso_mc_extract_field_noalloc(const float* field, u
                                                             uint64_t pitch, float* vertices, uint64_t vertex_cap,
                                                             uint32_t* indices, uint64_t triangle_cap, void* stream,
                                                             iso_mesh_info* info) {
+    iso::NvtxRange nvtx_range("iso_mc_extract_field_noalloc");
     using namespace iso;
     if (!field || !info) return ISO_ERR_INVALID_ARG;
     *info = iso_mesh_info{};

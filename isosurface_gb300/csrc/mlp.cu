@@ -435,6 +435,7 @@ iso_status iso_mlp_loss_grad(iso_mlp* net, const float* pts, const float* target
 // draw n samples in [lo, hi]^3 labelled by `exact` (see file comment)
 iso_status iso_mlp_make_dataset(iso_mlp* net, const iso_program* exact, uint32_t n, float lo, float hi,
                                 uint64_t seed) {
+    iso::NvtxRange nvtx_range("iso_mlp_make_dataset");
     if (!net || !exact || n == 0) return ISO_ERR_INVALID_ARG;
     iso_status s = set_device(net->ctx);
     if (s != ISO_OK) return s;
@@ -468,6 +469,7 @@ iso_status iso_mlp_make_dataset(iso_mlp* net, const iso_program* exact, uint32_t
 // steps of Adam on random batches of the dataset; loss per step into history (nullable)
 iso_status iso_mlp_train(iso_mlp* net, uint32_t steps, uint32_t batch, float lr, float clampd, uint64_t seed,
                          float* history) {
+    iso::NvtxRange nvtx_range("iso_mlp_train");
     if (!net || batch == 0 || net->data_n == 0) return ISO_ERR_INVALID_ARG;
     iso_status s = set_device(net->ctx);
     if (s != ISO_OK || (s = ensure_work(net, batch)) != ISO_OK) return s;

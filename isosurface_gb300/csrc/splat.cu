@@ -150,6 +150,7 @@ extern "C" {
 iso_status iso_point_splat_render(iso_ctx* ctx, const float* view_proj, const float* view_proj_inverse,
                                   uint32_t width, uint32_t height, float voxel_half, const float* clear_rgb,
                                   float* rgba) {
+    iso::NvtxRange nvtx_range("iso_point_splat_render");
     if (!ctx) return ISO_ERR_INVALID_ARG;
     if (!view_proj || !view_proj_inverse || !clear_rgb || !rgba)
         return fail(ctx, ISO_ERR_INVALID_ARG, "null matrix, colour or image pointer");

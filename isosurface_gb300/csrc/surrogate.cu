@@ -319,6 +319,7 @@ extern "C" {
 iso_status iso_surrogate_field(iso_ctx* ctx, iso_mlp* net, const iso_program* exact, uint32_t size,
                                uint32_t coarse_step, float band_cells, float* field, uint64_t pitch,
                                iso_surrogate_stats* stats) {
+    iso::NvtxRange nvtx_range("iso_surrogate_field");
     iso_status s = check_args(ctx, net, exact, size, coarse_step, band_cells);
     if (s != ISO_OK) return s;
     if (!field || pitch < size) return fail(ctx, ISO_ERR_INVALID_ARG, "need a field with pitch >= size");
@@ -331,6 +332,7 @@ iso_status iso_surrogate_field(iso_ctx* ctx, iso_mlp* net, const iso_program* ex
 iso_status iso_surrogate_extract(iso_ctx* ctx, iso_mlp* net, const iso_program* exact, uint32_t size,
                                  uint32_t coarse_step, float band_cells, uint32_t flags, iso_surrogate_stats* stats,
                                  iso_mesh_info* info) {
+    iso::NvtxRange nvtx_range("iso_surrogate_extract");
     iso_status s = check_args(ctx, net, exact, size, coarse_step, band_cells);
     if (s != ISO_OK) return s;
     if (flags & ~(uint32_t)ISO_FLAG_KEYS) return fail(ctx, ISO_ERR_INVALID_ARG, "unknown flags");
@@ -348,6 +350,7 @@ iso_status iso_surrogate_extract(iso_ctx* ctx, iso_mlp* net, const iso_program* 
 
 iso_status iso_mesh_distance(iso_ctx* ctx, const float* a, uint64_t na, const float* b, uint64_t nb, float bucket,
                              uint32_t max_rings, iso_mesh_distance_result* out) {
+    iso::NvtxRange nvtx_range("iso_mesh_distance");
     if (!ctx || !out || (!a && na) || (!b && nb) || !(bucket > 0.0f) || max_rings == 0 || max_rings > 1024)
         return ISO_ERR_INVALID_ARG;
     if (na == 0 || nb == 0) return fail(ctx, ISO_ERR_INVALID_ARG, "both vertex sets must be non-empty");
@@ -445,6 +448,7 @@ iso_status iso_mesh_distance(iso_ctx* ctx, const float* a, uint64_t na, const fl
 
 iso_status iso_field_case_disagreement(iso_ctx* ctx, const float* fa, const float* fb, uint32_t nx, uint32_t ny,
                                        uint32_t nz, uint64_t pitch, uint64_t* cells) {
+    iso::NvtxRange nvtx_range("iso_field_case_disagreement");
     if (!ctx || !fa || !fb || !cells) return ISO_ERR_INVALID_ARG;
     if (nx < 2 || ny < 2 || nz < 2 || pitch < nx) return fail(ctx, ISO_ERR_INVALID_ARG, "need n >= 2, pitch >= nx");
     iso_status s = set_device(ctx);
