@@ -81,6 +81,13 @@ ISO_API iso_status iso_ctx_set_stream(iso_ctx* ctx, void* stream);
 /* Number of kernels this context has launched since creation. */
 ISO_API uint64_t iso_ctx_kernel_launches(const iso_ctx* ctx);
 
+/* Fault injection for tests: of this context's next device-buffer
+ * allocations, the one after `after` successful ones fails as a failed
+ * cudaMalloc does (the buffer it was to replace is already released; the
+ * call returns ISO_ERR_OUT_OF_MEMORY); the hook then switches itself off.
+ * A negative `after` switches it off.  Nothing happens on the device. */
+ISO_API iso_status iso_debug_fail_allocation(iso_ctx* ctx, int64_t after);
+
 /* Per-stage device timing: when enabled, every kernel the context launches is
  * bracketed by CUDA events on its stream.  iso_ctx_stage_times synchronises,
  * writes the accumulated milliseconds and launch counts of each stage

@@ -67,6 +67,7 @@ SIGNATURES = {
     "iso_ctx_get_stream": (i32, [vp, ctypes.POINTER(vp)]),
     "iso_ctx_set_stream": (i32, [vp, vp]),
     "iso_ctx_kernel_launches": (u64, [vp]),
+    "iso_debug_fail_allocation": (i32, [vp, ctypes.c_int64]),
     "iso_ctx_enable_stage_timing": (i32, [vp, i32]),
     "iso_ctx_stage_times": (i32, [vp, ctypes.POINTER(ctypes.c_double), u64p]),
     "iso_program_create": (i32, [vp, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(vp)]),

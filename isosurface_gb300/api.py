@@ -101,6 +101,11 @@ class Context:
     def kernel_launches(self):
         return lib().iso_ctx_kernel_launches(self.h)
 
+    def debug_fail_allocation(self, after):
+        """Test hook: the device-buffer allocation after `after` successful
+        ones fails as a failed cudaMalloc does (negative: off)."""
+        check(lib().iso_debug_fail_allocation(self.h, int(after)), self.h)
+
     def program(self, source):
         """Upload (once per distinct program) and return a Program (a Program
         of this context is returned as it is)."""

@@ -39,6 +39,11 @@ iso_status ensure(iso_ctx* ctx, DevBuf& b, size_t bytes) {
         b.p = nullptr;
         b.bytes = 0;
     }
+    if (ctx->fail_alloc_after == 0) {  // iso_debug_fail_allocation: fail here as cudaMalloc would
+        ctx->fail_alloc_after = -1;
+        return fail(ctx, ISO_ERR_OUT_OF_MEMORY, "injected allocation failure");
+    }
+    if (ctx->fail_alloc_after > 0) --ctx->fail_alloc_after;
     size_t want = bytes + bytes / 8 + 256;
     cudaError_t e = cudaMalloc(&b.p, want);
     if (e != cudaSuccess) {
@@ -351,6 +356,12 @@ iso_status iso_ctx_set_stream(iso_ctx* ctx, void* stream) {
 }
 
 uint64_t iso_ctx_kernel_launches(const iso_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+iso_status iso_debug_fail_allocation(iso_ctx* ctx, int64_t after) {
+    if (!ctx) return ISO_ERR_INVALID_ARG;
+    ctx->fail_alloc_after = after < 0 ? -1 : after;
+    return ISO_OK;
+}
 
 iso_status iso_ctx_enable_stage_timing(iso_ctx* ctx, int enable) {
     if (!ctx) return ISO_ERR_INVALID_ARG;

@@ -62,6 +62,7 @@ struct ProgView {
 struct iso_ctx {
     int device = 0;
     int sms = 1;  // streaming multiprocessors of the device
+    int64_t fail_alloc_after = -1;  // test hook: allocations to let through before one fails (-1: off)
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     // work buffers (grow-only, reused across calls)
