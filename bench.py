@@ -160,7 +160,30 @@ def secondary_workloads(ctx, torch, steps, only=None):
         out["lhmc_depth8"] = {"dual_cubes": int(info.num_cells), "ms": ms, "triangles": int(info.num_triangles)}
     if want("splat"):
         out["point_splat_1024x768"] = _point_splat_frame(ctx, steps)
+    if only is not None and "emc" in only:  # on request only
+        out["emc_128"] = _emc_workload(ctx, timed, steps)
     return out
+
+
+def _emc_workload(ctx, timed, steps):
+    """ExtendedMarchingCubes::new(128), the viewer's largest grid
+    (examples/sampler.rs:100-118), of a CSG scene with the Directed metric
+    (box minus sphere, union torus, centred in the sample frame); GPU time
+    with CUDA events beside the single-threaded oracle's."""
+    import oracle
+    from isosurface_gb300 import source as S
+    src = S.Translate(S.Union(S.Difference(S.Sphere(0.35), S.RectangularPrism((0.3, 0.3, 0.3))),
+                              S.Torus(0.25, 0.06)), (0.5, 0.5, 0.5))
+    for _ in range(3):
+        info, flips = ctx.emc_extract(src, 128)
+    gpu_ms = timed(lambda: ctx.emc_extract(src, 128), max(3, min(steps, 20)))
+    t0 = time.time()
+    m = oracle.Program(S.lower(src)).extended_marching_cubes(128)
+    cpu_ms = 1e3 * (time.time() - t0)
+    return {"cells": int(info.num_cells), "gpu_ms": gpu_ms, "cpu_baseline_ms": cpu_ms, "cpu_threads": 1,
+            "vertices": int(info.num_vertices), "triangles": int(info.num_triangles), "flips": int(flips),
+            "feature_vertices": int(m.features),
+            "matches_oracle": bool(info.num_vertices == len(m.vertices) and 3 * info.num_triangles == len(m.indices))}
 
 
 def _point_splat_frame(ctx, steps):
@@ -358,7 +381,8 @@ def main():
     ap.add_argument("--no-secondary", action="store_true", help="skip the batch / DC / LHMC timings")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-surrogate workload")
     ap.add_argument("--secondary-only", default=None,
-                    help="comma list among refshapes,batch,dc,lhmc,splat,surrogate: run only these secondary workloads")
+                    help="comma list among refshapes,batch,dc,lhmc,splat,surrogate,emc: run only these secondary "
+                         "workloads (emc runs only when named)")
     ap.add_argument("--surrogate-train-steps", type=int, default=4000)
     args = ap.parse_args()
     if args.warmup < 3:
