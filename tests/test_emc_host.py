@@ -86,3 +86,12 @@ def test_host_emc_random_csg(host_lib):
         features += m.features
         flips += m.flips
     assert features > 0 and flips > 0
+
+
+def test_host_emc_bench_scene(host_lib):
+    """The bench's ExtendedMarchingCubes workload: new(128) of box minus
+    sphere, union torus."""
+    src = S.Translate(S.Union(S.Difference(S.Sphere(0.35), S.RectangularPrism((0.3, 0.3, 0.3))),
+                              S.Torus(0.25, 0.06)), (0.5, 0.5, 0.5))
+    m = _check(host_lib, src, 128)
+    assert m.features > 1000 and m.conflicts == 0
