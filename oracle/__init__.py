@@ -28,7 +28,7 @@ def lib():
             "oracle_program_has_normal": (ctypes.c_int, [vp]),
             "oracle_program_has_vector": (ctypes.c_int, [vp]),
             "oracle_sample_vector": (None, [vp, f32p, ctypes.c_uint64, f32p]),
-            "oracle_emc": (vp, [vp, ctypes.c_uint32, ctypes.c_int, u64p]),
+            "oracle_emc": (vp, [vp, ctypes.c_uint32, ctypes.c_int, u64p, ctypes.c_uint64]),
             "oracle_sample_scalar": (None, [vp, f32p, ctypes.c_uint64, f32p]),
             "oracle_sample_normal": (None, [vp, f32p, ctypes.c_uint64, f32p]),
             "oracle_sample_grid": (None, [vp, ctypes.c_uint32, f32p]),
@@ -130,15 +130,17 @@ class Program:
         lib().oracle_sample_vector(self.h, _ptr(pts, ctypes.c_float), len(pts), _ptr(out, ctypes.c_float))
         return out
 
-    def extended_marching_cubes(self, size, normals=False):
+    def extended_marching_cubes(self, size, normals=False, flip_order_seed=0):
         """ExtendedMarchingCubes::new(size).extract; the mesh carries
         `features` (feature vertices), `flips` (edges rotated) and
-        `conflicts` (flips whose result would depend on their order)."""
+        `conflicts` (flips whose result would depend on their order).  The
+        reference applies its flips in HashSet order; flip_order_seed 0 uses
+        ascending order, other values a seeded random order."""
         if not self.has_vector:
             raise ValueError("ExtendedMarchingCubes needs a source with the Directed metric")
         stats = np.zeros(3, np.uint64)
-        m = Mesh(lib().oracle_emc(self.h, size, 1 if normals else 0, _ptr(stats, ctypes.c_uint64)),
-                 with_normals=normals)
+        m = Mesh(lib().oracle_emc(self.h, size, 1 if normals else 0, _ptr(stats, ctypes.c_uint64),
+                                  flip_order_seed), with_normals=normals)
         m.features, m.flips, m.conflicts = (int(v) for v in stats)
         return m
 

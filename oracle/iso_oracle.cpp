@@ -950,8 +950,9 @@ inline bool matches_winding(const uint32_t* f, uint32_t e0, uint32_t e1, bool* f
 // finished mesh, then applied.  The reference applies them in the order of
 // its HashSet (random per run); when no face is rewritten by two flips the
 // result is the same in every order, which `conflicts` == 0 states.  Here
-// they are applied in ascending (start, end) order.
-void flip_feature_edges(MeshBuilder& mb, const std::vector<uint8_t>& feature, EmcStats* st) {
+// they are applied in ascending (start, end) order, or, with a non-zero
+// `order_seed`, in a seeded random order (to check that claim).
+void flip_feature_edges(MeshBuilder& mb, const std::vector<uint8_t>& feature, EmcStats* st, uint64_t order_seed) {
     typedef std::pair<uint32_t, uint32_t> Edge;
     std::vector<Edge> flips;
     for (const Edge& e : mb.edges) {
@@ -964,6 +965,17 @@ void flip_feature_edges(MeshBuilder& mb, const std::vector<uint8_t>& feature, Em
             flips.push_back(e);
     }
     std::sort(flips.begin(), flips.end());
+    if (order_seed) {  // Fisher-Yates with SplitMix64
+        uint64_t x = order_seed;
+        for (size_t i = flips.size(); i > 1; --i) {
+            x += 0x9E3779B97F4A7C15ull;
+            uint64_t z = x;
+            z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+            z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+            z ^= z >> 31;
+            std::swap(flips[i - 1], flips[z % i]);
+        }
+    }
     std::vector<uint8_t> rewritten(mb.faces.size() / 3, 0);
     for (const Edge& e : flips) {
         auto it = mb.edge_to_face.find(e);
@@ -998,7 +1010,7 @@ void flip_feature_edges(MeshBuilder& mb, const std::vector<uint8_t>& feature, Em
 // vertex placed by MinimiseQEF::place_feature_with_tangents and fan each of
 // the case's edge loops (EDGE_LOOPS) around it.
 void extended_marching_cubes(const Source& src, uint32_t size, Mesh* mesh, const Source* normal_source,
-                             EmcStats* st) {
+                             EmcStats* st, uint64_t flip_order_seed = 0) {
     MeshBuilder mb(mesh, normal_source, true);
     LatticeKeys lk{size, size};
     std::vector<uint8_t> feature;  // per vertex: 1 for a feature vertex
@@ -1054,7 +1066,7 @@ void extended_marching_cubes(const Source& src, uint32_t size, Mesh* mesh, const
         mesh->cells++;
     });
     feature.resize(mb.next_vertex, 0);
-    flip_feature_edges(mb, feature, st);
+    flip_feature_edges(mb, feature, st, flip_order_seed);
     mb.finish();
 }
 
@@ -1332,12 +1344,14 @@ uint64_t oracle_lhmc_nodes(void* p, uint32_t max_depth, uint64_t* out, uint64_t 
     return n;
 }
 
-// ExtendedMarchingCubes::new(size).extract; stats: features, flips, conflicts
-void* oracle_emc(void* p, uint32_t size, int normals, uint64_t* stats) {
+// ExtendedMarchingCubes::new(size).extract; stats: features, flips, conflicts.
+// flip_order_seed 0 applies the flips in ascending order, others in a seeded
+// random order.
+void* oracle_emc(void* p, uint32_t size, int normals, uint64_t* stats, uint64_t flip_order_seed) {
     const Source& s = *((Program*)p)->src;
     Mesh* m = new Mesh();
     EmcStats st;
-    extended_marching_cubes(s, size, m, normals ? &s : nullptr, &st);
+    extended_marching_cubes(s, size, m, normals ? &s : nullptr, &st, flip_order_seed);
     if (stats) {
         stats[0] = st.features;
         stats[1] = st.flips;

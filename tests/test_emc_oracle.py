@@ -130,3 +130,16 @@ def test_emc_needs_directed_metric(src):
     assert not p.has_vector
     with pytest.raises(ValueError):
         p.extended_marching_cubes(8)
+
+
+def test_emc_result_does_not_depend_on_flip_order():
+    """The reference rotates its feature edges in HashSet order (random per
+    run); any order gives the same mesh."""
+    from emc_scenes import random_scenes
+    for n, src in random_scenes(5, 25):
+        p = oracle.Program(S.lower(src))
+        base = p.extended_marching_cubes(n)
+        for seed in (1, 2, 3):
+            m = p.extended_marching_cubes(n, flip_order_seed=seed)
+            assert m.flips == base.flips
+            assert np.array_equal(m.indices, base.indices) and np.array_equal(m.vertices, base.vertices)
