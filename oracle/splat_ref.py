@@ -14,7 +14,11 @@ Passes (examples/deferred_rasterisation.rs:95-127, 131-213, 342-421):
      keeps the nearest hit (ties: the later tap);
   3. a last gather along y that shades a hit with the hemisphere term and
      composites over the clear colour (alpha 1 for a hit, 0 otherwise).
-Row 0 of every buffer is the bottom row; texels outside the image are empty.
+Row 0 of every buffer is the bottom row.  Taps past the image edge read as
+empty (edge="empty", what the CUDA kernels do), or through mirrored-repeat
+addressing (edge="mirror": texel -1 reads texel 0, texel W reads W - 1, ...),
+the wrap of glium 0.26's default sampler through which the example reads its
+buffers.
 """
 import numpy as np
 
@@ -90,7 +94,13 @@ def eye_rays(vpinv, width, height):
     return eye, [dk / ln for dk in d]
 
 
-def gather(pos, nrm, eye, dirs, voxel, dx, dy, last, clear):
+def mirror_index(i, n):
+    """Mirrored-repeat addressing of texel i in a row of n texels."""
+    m = np.mod(i, 2 * n)
+    return np.where(m >= n, 2 * n - 1 - m, m)
+
+
+def gather(pos, nrm, eye, dirs, voxel, dx, dy, last, clear, edge="empty"):
     h, w = pos.shape[:2]
     with np.errstate(divide="ignore", invalid="ignore"):
         inv = [F(1.0) / d for d in dirs]
@@ -99,12 +109,18 @@ def gather(pos, nrm, eye, dirs, voxel, dx, dy, last, clear):
     rn = np.zeros((h, w, 3), F)
     vox = F(voxel)
     for t in range(-TAPS, TAPS + 1):
-        p = np.zeros((h, w, 3), F)
-        n = np.zeros((h, w, 3), F)
-        sy0, sy1 = max(0, t * dy), min(h, h + t * dy)
-        sx0, sx1 = max(0, t * dx), min(w, w + t * dx)
-        p[sy0 - t * dy:sy1 - t * dy, sx0 - t * dx:sx1 - t * dx] = pos[sy0:sy1, sx0:sx1, 0:3]
-        n[sy0 - t * dy:sy1 - t * dy, sx0 - t * dx:sx1 - t * dx] = nrm[sy0:sy1, sx0:sx1, 0:3]
+        if edge == "mirror":
+            ys = mirror_index(np.arange(h) + t * dy, h)
+            xs = mirror_index(np.arange(w) + t * dx, w)
+            p = pos[ys][:, xs, 0:3]
+            n = nrm[ys][:, xs, 0:3]
+        else:
+            p = np.zeros((h, w, 3), F)
+            n = np.zeros((h, w, 3), F)
+            sy0, sy1 = max(0, t * dy), min(h, h + t * dy)
+            sx0, sx1 = max(0, t * dx), min(w, w + t * dx)
+            p[sy0 - t * dy:sy1 - t * dy, sx0 - t * dx:sx1 - t * dx] = pos[sy0:sy1, sx0:sx1, 0:3]
+            n[sy0 - t * dy:sy1 - t * dy, sx0 - t * dx:sx1 - t * dx] = nrm[sy0:sy1, sx0:sx1, 0:3]
         full = (np.abs(p[..., 0]) + np.abs(p[..., 1])) + np.abs(p[..., 2]) > F(0.0)
         with np.errstate(invalid="ignore"):
             tmin, tmax = [], []
@@ -135,7 +151,7 @@ def gather(pos, nrm, eye, dirs, voxel, dx, dy, last, clear):
     return out
 
 
-def render(points, mvp, vpinv, width, height, voxel, clear):
+def render(points, mvp, vpinv, width, height, voxel, clear, edge="empty"):
     """The composited image, (height, width, 4) float32, row 0 at the bottom."""
     mvp = np.asarray(mvp, F)
     vpinv = np.asarray(vpinv, F)
@@ -143,5 +159,5 @@ def render(points, mvp, vpinv, width, height, voxel, clear):
     pos, nrm = gbuffer(points, owner)
     eye, dirs = eye_rays(vpinv, width, height)
     for i in range(3):
-        pos, nrm = gather(pos, nrm, eye, dirs, voxel, (i + 1) % 2, i % 2, False, clear)
-    return gather(pos, nrm, eye, dirs, voxel, 0, 1, True, clear)
+        pos, nrm = gather(pos, nrm, eye, dirs, voxel, (i + 1) % 2, i % 2, False, clear, edge)
+    return gather(pos, nrm, eye, dirs, voxel, 0, 1, True, clear, edge)
