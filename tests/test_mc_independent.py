@@ -1,5 +1,6 @@
-"""A second, independent restatement of MarchingCubes::extract in plain
-Python, for small grids, checked byte for byte against the oracle (which the
+"""Second, independent restatements of MarchingCubes::extract and of
+DualContouring's traversal in plain Python, for small grids, checked byte
+for byte against the oracle (which the
 GPU library is checked against).  It follows the reference's own structure
 rather than the oracle's: PrimalGrid::traverse (src/traversal/primal_grid.rs:
 39-89) over tuples, classify_corners / find_edge_crossings / march_cube
@@ -79,3 +80,81 @@ def test_independent_restatement_matches_oracle(name, size):
     assert np.array_equal(i, m.indices)
     if size == 12:
         assert len(i) > 30  # a real surface, not an empty mesh
+
+
+def _normalised_or_zero(n):
+    """Vec3::normalised (vector.rs:468-478) or zero, in f32."""
+    n = np.asarray(n, np.float32)
+    ln = np.sqrt(F(F(n[0] * n[0] + n[1] * n[1]) + n[2] * n[2]))
+    if abs(ln) < F(1.1920929e-07):
+        return np.zeros(3, np.float32)
+    return n / ln
+
+
+def dual_contouring(prog, size, placer):
+    """DualContouring::extract (src/dual_contouring.rs:65-105) over
+    DualGrid::traverse (src/traversal/dual_grid.rs:52-95): each primal cell's
+    dual vertex (placed when the cell is active, else the cell centre) and
+    value, then marching cubes on every dual cube once its far corner's cell
+    is reached.  Feature placement is the oracle's (place_feature)."""
+    one_over_size = F(1.0) / F(size - 1)
+    m = size - 1
+    pts = np.array([(x, y, z) for z in range(size + 1) for y in range(size) for x in range(size)], np.float32)
+    pos = pts * one_over_size
+    val = prog.sample_scalar(pos)
+    at = lambda x, y, z: (z * size + y) * size + x
+    duals = [[None] * (m * m), [None] * (m * m)]
+    vertices, indices, cache = [], [], {}
+    half = F(0.5)
+    for z in range(size):
+        for y in range(m):
+            for x in range(m):
+                keys = [(x + c[0], y + c[1], z + c[2]) for c in CORNERS]
+                corners = np.array([pos[at(*k)] for k in keys], np.float32)
+                values = [val[at(*k)] for k in keys]
+                cube = sum(1 << i for i in range(8) if not values[i] > F(0.0))
+                if cube in (0, 255):
+                    vertex = corners[0] * F(F(1.0) - half) + corners[6] * half  # Vec3::lerp
+                else:
+                    normals = np.array([_normalised_or_zero(prog.sample_normal(c)[0]) for c in corners], np.float32)
+                    vertex, _ = oracle.place_feature(corners, normals, placer)
+                value = F(F(F(1.0) - half) * values[0]) + F(half * values[6])  # Signed::lerp
+                duals[z % 2][y * m + x] = (np.asarray(vertex, np.float32), value)
+                if x > 0 and y > 0 and z > 0:
+                    bx, by, bz = x - 1, y - 1, z - 1
+                    dkeys = [(bx + c[0], by + c[1], bz + c[2]) for c in CORNERS]
+                    d = [duals[(bz + c[2]) % 2][(by + c[1]) * m + bx + c[0]] for c in CORNERS]
+                    dc = [e[0] for e in d]
+                    dv = [e[1] for e in d]
+                    c2 = sum(1 << i for i in range(8) if not dv[i] > F(0.0))
+                    verts = [None] * 12
+                    for i in range(12):
+                        if EDGE_CROSSING_MASK[c2] & (1 << i):
+                            u, v = EDGE_CONNECTION[i]
+                            delta = F(dv[v] - dv[u])
+                            t = F(0.5) if delta == F(0.0) else F(-dv[u] / delta)
+                            verts[i] = dc[u] * F(F(1.0) - t) + dc[v] * t
+                    row = TRIANGLE_CONNECTION[c2]
+                    for k in range(0, 15, 3):
+                        if row[k] < 0:
+                            break
+                        for e in row[k:k + 3]:
+                            u, v = EDGE_CONNECTION[e]
+                            key = tuple(sorted((dkeys[u], dkeys[v])))
+                            if key not in cache:
+                                cache[key] = len(cache)
+                                vertices.append(verts[e])
+                            indices.append(cache[key])
+    return np.array(vertices, np.float32).reshape(-1, 3), np.array(indices, np.uint32)
+
+
+@pytest.mark.parametrize("placer", [0, 1])
+@pytest.mark.parametrize("size", [3, 9, 14])
+def test_independent_dual_contouring_matches_oracle(placer, size):
+    prog = oracle.Program(S.lower(scenes.csg()))
+    v, i = dual_contouring(prog, size, placer)
+    m = prog.dual_contouring(size, placer)
+    assert np.array_equal(v, m.vertices)
+    assert np.array_equal(i, m.indices)
+    if size == 14:
+        assert len(i) > 30
