@@ -158,3 +158,25 @@ def test_independent_dual_contouring_matches_oracle(placer, size):
     assert np.array_equal(i, m.indices)
     if size == 14:
         assert len(i) > 30
+
+
+@pytest.mark.parametrize("size", [2, 7, 16])
+def test_independent_point_cloud_matches_oracle(size):
+    """PointCloud::extract (src/point_cloud.rs:50-63): the centre
+    corners[0].lerp(corners[6], 0.5) of every cell whose case is neither 0
+    nor 255, in traversal order."""
+    prog = oracle.Program(S.lower(scenes.csg()))
+    one_over_size = F(1.0) / F(size - 1)
+    half = F(0.5)
+    out = []
+    for z in range(size):
+        for y in range(size - 1):
+            for x in range(size - 1):
+                keys = [(x + c[0], y + c[1], z + c[2]) for c in CORNERS]
+                corners = np.array(keys, np.float32) * one_over_size
+                values = prog.sample_scalar(corners)
+                cube = sum(1 << i for i in range(8) if not values[i] > F(0.0))
+                if cube not in (0, 255):
+                    out.append(corners[0] * F(F(1.0) - half) + corners[6] * half)
+    m = prog.point_cloud(size)
+    assert np.array_equal(np.array(out, np.float32).reshape(-1, 3), m.vertices)
