@@ -1,6 +1,7 @@
-"""Second, independent restatements of MarchingCubes::extract and of
-DualContouring's traversal in plain Python, for small grids, checked byte
-for byte against the oracle (which the
+"""Second, independent restatements of MarchingCubes::extract, of
+DualContouring's traversal, of PointCloud and of LinearHashedMarchingCubes
+in plain Python, for small grids, checked against the oracle (byte for byte;
+LHMC as triangle sets, its reference output being in HashMap order) (which the
 GPU library is checked against).  It follows the reference's own structure
 rather than the oracle's: PrimalGrid::traverse (src/traversal/primal_grid.rs:
 39-89) over tuples, classify_corners / find_edge_crossings / march_cube
@@ -180,3 +181,134 @@ def test_independent_point_cloud_matches_oracle(size):
                     out.append(corners[0] * F(F(1.0) - half) + corners[6] * half)
     m = prog.point_cloud(size)
     assert np.array_equal(np.array(out, np.float32).reshape(-1, 3), m.vertices)
+
+
+# -- LinearHashedMarchingCubes ------------------------------------------------
+MASK64 = (1 << 64) - 1
+DILATE_TZ, DILATE_TY, DILATE_TX = 0x4924924924924924, 0x2492492492492492, 0x9249249249249249
+DILATE_T1, DILATE_T2, DILATE_T3 = 0xB6DB6DB6DB6DB6DB, 0xDB6DB6DB6DB6DB6D, 0x6DB6DB6DB6DB6DB6
+LG2_3 = 0.48089834696
+MAX_LEVEL = 21
+SQRT_OF_3 = F(1.7320508)
+
+
+def m_level(a):  # Morton::level: the reference's ln formula, floor((ln a) * LG2_3)
+    import math
+    return 0 if a == 0 else int(math.floor(math.log(float(a)) * LG2_3))
+
+
+def m_size(a):
+    return F(1.0) / F(2 << m_level(a))
+
+
+def m_center(a):
+    """Morton::center: de-interleave the bits below the level's top, then
+    (b as f32) * size2 + size per axis."""
+    lv = m_level(a)
+    b = [0, 0, 0]
+    for bit in range(lv):
+        for axis in range(3):
+            b[axis] |= ((a >> (3 * bit + axis)) & 1) << bit
+    size = m_size(a)
+    size2 = F(size * F(2.0))
+    return np.array([F(F(b[k]) * size2) + size for k in range(3)], np.float32)
+
+
+def m_add(a, b):
+    return ((((a | DILATE_T1) + (b & DILATE_TZ)) & DILATE_TZ) | (((a | DILATE_T2) + (b & DILATE_TY)) & DILATE_TY)
+            | (((a | DILATE_T3) + (b & DILATE_TX)) & DILATE_TX)) & MASK64
+
+
+def m_sub(a, b):
+    return ((((a & DILATE_TZ) - (b & DILATE_TZ)) & DILATE_TZ) | (((a & DILATE_TY) - (b & DILATE_TY)) & DILATE_TY)
+            | (((a & DILATE_TX) - (b & DILATE_TX)) & DILATE_TX)) & MASK64
+
+
+def m_primal_vertex(a, level, which):
+    k = 1 << (3 * level)
+    vk = m_add(a, which)
+    dk = m_sub(vk, k)
+    if vk >= (k << 1) or (dk & DILATE_TX) == 0 or (dk & DILATE_TY) == 0 or (dk & DILATE_TZ) == 0:
+        return 0
+    return (vk << (3 * (MAX_LEVEL - level))) & MASK64
+
+
+def m_dual_vertex(a, level, which):
+    return m_sub(a >> (3 * (MAX_LEVEL - level)), which)
+
+
+def lhmc(prog, max_depth):
+    """LinearHashedMarchingCubes::extract (src/linear_hashed_marching_cubes.rs:
+    62-84) over ImplicitOctree::traverse (src/traversal/implicit_octree.rs:
+    36-98) and LinearHashedOctree::build (src/linear_hashed_octree.rs:30-52).
+    Returns {MortonKey pair: vertex}, the triangles as MortonKey-pair triples,
+    and the number of dual-cube corners whose parent walk found no node."""
+    from collections import deque
+    nodes, leaves = {}, []
+    queue = deque([1])
+    while queue:
+        key = queue.popleft()
+        value = prog.sample_scalar(m_center(key))[0]
+        lv = m_level(key)
+        if lv < 2 or (lv < max_depth and abs(value) < F(m_size(key) * SQRT_OF_3)):
+            queue.extend((key << 3) | i for i in range(8))
+        else:
+            leaves.append(key)
+        nodes[key] = value
+    primal = {}
+    for key in leaves:
+        lv = m_level(key)
+        for i in range(8):
+            v = m_primal_vertex(key, lv, i)
+            if v != 0 and lv > primal.get(v, -1):
+                primal[v] = lv
+    verts, tris, missing = {}, [], 0
+    REMAP = T["REMAP_CUBE"]
+    for key, lv in sorted(primal.items()):
+        keys, corners, values = [None] * 8, [None] * 8, [None] * 8
+        for i in range(8):
+            m = m_dual_vertex(key, lv, REMAP[i])
+            while m > 1 and m not in nodes:
+                m = max(m >> 3, 1)
+            if m > 1:
+                keys[i], corners[i], values[i] = m, m_center(m), nodes[m]
+        if any(k is None for k in keys):
+            missing += sum(k is None for k in keys)
+            continue
+        cube = sum(1 << i for i in range(8) if not values[i] > F(0.0))
+        row = TRIANGLE_CONNECTION[cube]
+        for k in range(0, 15, 3):
+            if row[k] < 0:
+                break
+            tri = []
+            for e in row[k:k + 3]:
+                u, v = EDGE_CONNECTION[e]
+                pair = tuple(sorted((keys[u], keys[v])))
+                if pair not in verts:
+                    delta = F(values[v] - values[u])
+                    t = F(0.5) if delta == F(0.0) else F(-values[u] / delta)
+                    verts[pair] = corners[u] * F(F(1.0) - t) + corners[v] * t
+                tri.append(pair)
+            tris.append(tuple(tri))
+    return verts, tris, missing
+
+
+def _canonical(tri):
+    i = tri.index(min(tri))
+    return tri[i:] + tri[:i]
+
+
+@pytest.mark.parametrize("name,depth", [("sphere", 4), ("sphere", 5), ("torus", 5), ("csg", 5)])
+def test_independent_lhmc_matches_oracle(name, depth):
+    src = {"sphere": scenes.sphere(), "torus": S.Translate(S.Torus(0.25, 0.1), (0.5, 0.5, 0.5)),
+           "csg": scenes.csg()}[name]
+    prog = oracle.Program(S.lower(src))
+    verts, tris, missing = lhmc(prog, depth)
+    m = prog.lhmc(depth)
+    assert missing == 0 and m.stale_corners == 0  # no corner depends on the HashMap's order
+    keys = [tuple(int(x) for x in k) for k in m.keys]
+    got = {_canonical(tuple(keys[j] for j in t)) for t in m.triangles}
+    want = {_canonical(t) for t in tris}
+    assert got == want and len(tris) == len(m.triangles) > 20
+    for k, v in zip(keys, m.vertices):
+        np.testing.assert_allclose(v, verts[k], rtol=0, atol=1e-6)
