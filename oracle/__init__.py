@@ -29,6 +29,7 @@ def lib():
             "oracle_program_has_vector": (ctypes.c_int, [vp]),
             "oracle_sample_vector": (None, [vp, f32p, ctypes.c_uint64, f32p]),
             "oracle_emc": (vp, [vp, ctypes.c_uint32, ctypes.c_int, u64p, ctypes.c_uint64]),
+            "oracle_emc_place": (ctypes.c_int, [f32p, f32p, ctypes.c_int, f32p]),
             "oracle_sample_scalar": (None, [vp, f32p, ctypes.c_uint64, f32p]),
             "oracle_sample_normal": (None, [vp, f32p, ctypes.c_uint64, f32p]),
             "oracle_sample_grid": (None, [vp, ctypes.c_uint32, f32p]),
@@ -192,6 +193,16 @@ def svd_solve(mat, b):
     lib().oracle_svd_solve(_ptr(mat, ctypes.c_double), len(mat), _ptr(b, ctypes.c_double),
                            _ptr(d, ctypes.c_double), _ptr(x, ctypes.c_double))
     return d, x
+
+
+def emc_place(vertices, normals):
+    """Tangent planes over a cell's edge crossings and MinimiseQEF: (topology
+    0 planar / 1 edge / 2 corner, the placed point)."""
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+    n = np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
+    out = np.zeros(3, np.float32)
+    topo = lib().oracle_emc_place(_ptr(v, ctypes.c_float), _ptr(n, ctypes.c_float), len(v), _ptr(out, ctypes.c_float))
+    return topo, out
 
 
 def place_feature(corners, normals, placer=0):

@@ -1344,6 +1344,24 @@ uint64_t oracle_lhmc_nodes(void* p, uint32_t max_depth, uint64_t* out, uint64_t 
     return n;
 }
 
+// TangentPlanes::from_edge_crossings + MinimiseQEF::place_feature_with_tangents
+// over n (3..12) crossings with normalised normals: the topology (0 planar,
+// 1 edge, 2 corner) and, for a feature, the placed point in out.
+int oracle_emc_place(const float* vertices, const float* normals, int n, float* out) {
+    Vec3 v[12], nn[12];
+    for (int i = 0; i < n; ++i) {
+        v[i] = Vec3(vertices[3 * i], vertices[3 * i + 1], vertices[3 * i + 2]);
+        nn[i] = Vec3(normals[3 * i], normals[3 * i + 1], normals[3 * i + 2]);
+    }
+    Planes t;
+    tangent_planes(v, nn, n, &t);
+    Vec3 p = minimise_qef(t);
+    out[0] = p.x;
+    out[1] = p.y;
+    out[2] = p.z;
+    return (int)t.feature;
+}
+
 // ExtendedMarchingCubes::new(size).extract; stats: features, flips, conflicts.
 // flip_order_seed 0 applies the flips in ascending order, others in a seeded
 // random order.

@@ -1,6 +1,6 @@
 """Second, independent restatements of MarchingCubes::extract, of
-DualContouring's traversal, of PointCloud and of LinearHashedMarchingCubes
-in plain Python, for small grids, checked against the oracle (byte for byte;
+DualContouring's traversal, of PointCloud, of LinearHashedMarchingCubes and
+of ExtendedMarchingCubes in plain Python, for small grids, checked against the oracle (byte for byte;
 LHMC as triangle sets, its reference output being in HashMap order) (which the
 GPU library is checked against).  It follows the reference's own structure
 rather than the oracle's: PrimalGrid::traverse (src/traversal/primal_grid.rs:
@@ -312,3 +312,136 @@ def test_independent_lhmc_matches_oracle(name, depth):
     assert got == want and len(tris) == len(m.triangles) > 20
     for k, v in zip(keys, m.vertices):
         np.testing.assert_allclose(v, verts[k], rtol=0, atol=1e-6)
+
+
+# -- ExtendedMarchingCubes ----------------------------------------------------
+EDGE_LOOPS = T["EDGE_LOOPS"]
+
+
+def emc(prog, size, rng):
+    """ExtendedMarchingCubes::extract (src/extended_marching_cubes.rs:64-186)
+    with MeshTopology's edge bookkeeping and rotate_edge (src/mesh.rs:64-172);
+    the flips are chosen and applied in a shuffled order, as the reference's
+    HashSet yields them in a random one.  Tangent planes and MinimiseQEF over
+    a cell's crossings are the oracle's (emc_place)."""
+    one_over_size = F(1.0) / F(size - 1)
+    pts = np.array([(x, y, z) for z in range(size + 1) for y in range(size) for x in range(size)], np.float32)
+    pos = pts * one_over_size
+    vec = prog.sample_vector(pos)
+    at = lambda x, y, z: (z * size + y) * size + x
+    vertices, faces, cache, features = [], [], {}, set()
+    edges, edge_to_face = set(), {}
+
+    def add_vertex(key, v):
+        if key is not None and key in cache:
+            return cache[key]
+        h = len(vertices)
+        vertices.append(v)
+        if key is not None:
+            cache[key] = h
+        return h
+
+    def add_face(a, b, c):
+        f = len(faces)
+        faces.append([a, b, c])
+        for u, v in ((a, b), (b, c), (c, a)):
+            e = (min(u, v), max(u, v))
+            edges.add(e)
+            edge_to_face.setdefault(e, []).append(f)
+
+    for z in range(size):
+        for y in range(size - 1):
+            for x in range(size - 1):
+                keys = [(x + c[0], y + c[1], z + c[2]) for c in CORNERS]
+                corners = [pos[at(*k)] for k in keys]
+                values = [vec[at(*k)] for k in keys]
+                cube = sum(1 << i for i in range(8) if not np.any(values[i] > F(0.0)))
+                verts, norms, crossing = [None] * 12, [None] * 12, []
+                for i in range(12):
+                    if EDGE_CROSSING_MASK[cube] & (1 << i):
+                        u, v = EDGE_CONNECTION[i]
+                        d = np.abs(corners[u] - corners[v])
+                        axis = 0 if (d[0] > d[1] and d[0] > d[2]) else (1 if d[1] > d[2] else 2)
+                        delta = F(values[v][axis] - values[u][axis])
+                        t = F(0.5) if delta == F(0.0) else F(-values[u][axis] / delta)
+                        verts[i] = corners[u] * F(F(1.0) - t) + corners[v] * t
+                        norms[i] = _normalised_or_zero(prog.sample_normal(verts[i])[0])
+                        crossing.append(i)
+                key = lambda e: tuple(sorted((keys[EDGE_CONNECTION[e][0]], keys[EDGE_CONNECTION[e][1]])))
+                if not crossing:
+                    continue
+                topo, point = oracle.emc_place([verts[i] for i in crossing], [norms[i] for i in crossing])
+                if topo == 0:
+                    row = TRIANGLE_CONNECTION[cube]
+                    for k in range(0, 15, 3):
+                        if row[k] < 0:
+                            break
+                        a, b, c = (add_vertex(key(e), verts[e]) for e in row[k:k + 3])
+                        add_face(a, b, c)
+                else:
+                    centre = add_vertex(None, point)
+                    features.add(centre)
+                    row = EDGE_LOOPS[cube]
+                    at_ = 1 + row[0]
+                    for l in range(row[0]):
+                        n = row[1 + l]
+                        for i in range(n):
+                            e0, e1 = row[at_ + i], row[at_ + (i + 1) % n]
+                            a = add_vertex(key(e0), verts[e0])
+                            b = add_vertex(key(e1), verts[e1])
+                            add_face(a, b, centre)
+                        at_ += n
+
+    def opposite(f, e):
+        return next(v for v in f if v != e[0] and v != e[1])
+
+    flips = []
+    for e in rng.permutation(sorted(edges)).tolist():
+        e = tuple(e)
+        if e[0] in features and e[1] in features:
+            continue
+        adj = edge_to_face.get(e, [])
+        if len(adj) == 2 and opposite(faces[adj[0]], e) in features and opposite(faces[adj[1]], e) in features:
+            flips.append(e)
+    for e in flips:  # rotate_edge
+        adj = edge_to_face.get(e)
+        if not adj or len(adj) != 2:
+            continue
+        fa, fb = faces[adj[0]], faces[adj[1]]
+        c, d = opposite(fa, e), opposite(fb, e)
+        winding = any(fa[i] == e[0] and fa[(i + 1) % 3] == e[1] for i in range(3))
+        u, v = (e[1], e[0]) if winding else (e[0], e[1])
+        faces[adj[0]] = [c, d, u]
+        faces[adj[1]] = [c, v, d]
+        ne = (min(c, d), max(c, d))
+        edges.add(ne)
+        edge_to_face[ne] = [adj[0], adj[1]]
+        edges.discard(e)
+        del edge_to_face[e]
+    return np.array(vertices, np.float32).reshape(-1, 3), np.array(faces, np.uint32).reshape(-1)
+
+
+@pytest.mark.parametrize("size", [3, 9, 16])
+@pytest.mark.parametrize("seed", [0, 1])
+def test_independent_emc_matches_oracle(size, seed):
+    from emc_scenes import FIXED
+    for name in ("cube", "difference", "torus"):
+        prog = oracle.Program(S.lower(FIXED[name]))
+        v, i = emc(prog, size, np.random.default_rng(seed))
+        m = prog.extended_marching_cubes(size)
+        assert np.array_equal(v, m.vertices), name
+        assert np.array_equal(i, m.indices), name
+
+
+def test_independent_emc_random_csg():
+    from emc_scenes import random_scenes
+    rng = np.random.default_rng(7)
+    features = 0
+    for n, src in random_scenes(31, 12):
+        prog = oracle.Program(S.lower(src))
+        n = min(n, 14)
+        v, i = emc(prog, n, rng)
+        m = prog.extended_marching_cubes(n)
+        assert np.array_equal(v, m.vertices) and np.array_equal(i, m.indices)
+        features += m.features
+    assert features > 0
