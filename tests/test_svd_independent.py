@@ -5,7 +5,9 @@ rounded math.sqrt, no fused operations), of the reference's SVD
 qrstep_cols2 + computeGivens / computeSchur, singularize; SVD::solve =
 thresholds + solveSVD), operation for operation in the reference's order,
 checked bit for bit against the oracle's SVD, which DualContouring's and
-ExtendedMarchingCubes' feature placement (on the GPU too) follow."""
+ExtendedMarchingCubes' feature placement (on the GPU too) follow; and of the
+feature placers built on it (feature/mod.rs TangentPlanes, feature/qef.rs
+MinimiseQEF, feature/particle_minimisation.rs) in numpy float32."""
 import math
 
 import numpy as np
@@ -420,3 +422,139 @@ def test_independent_svd_matches_oracle(k):
     od, ox = oracle.svd_solve(a, b)
     assert np.array_equal(np.array(d), od), (d, od)
     assert np.array_equal(np.array(x), ox), (x, ox)
+
+
+# -- feature placement (DualContouring's corners) --------------------------------
+F = np.float32
+FEATURE_ANGLE = F(0.8660254037844387)
+
+
+def _dot(a, b):  # (a * b).component_sum() == (x + y) + z
+    p = a * b
+    return F(F(p[0] + p[1]) + p[2])
+
+
+def _cross(a, r):
+    return np.array([a[1] * r[2] - a[2] * r[1], a[2] * r[0] - a[0] * r[2], a[0] * r[1] - a[1] * r[0]], F)
+
+
+def _normalised_or_zero(v):
+    ln = np.sqrt(F(F(v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]))
+    return np.zeros(3, F) if abs(ln) < F(1.1920929e-07) else v / ln
+
+
+def tangent_planes(vertices, normals):
+    """TangentPlanes::new (feature/mod.rs:91-148): (normals, d, centre of mass, topology)."""
+    com = np.zeros(3, F)
+    axis = np.zeros(3, F)
+    min_angle = F(3.40282347e38)
+    count = F(0.0)
+    for i in range(len(vertices)):
+        for j in range(len(vertices)):
+            angle = _dot(normals[i], normals[j])
+            if angle < min_angle:
+                axis = _cross(normals[i], normals[j])
+                min_angle = angle
+        com = com + vertices[i]
+        count = F(count + F(1.0))
+    com = com / count
+    if min_angle > FEATURE_ANGLE:
+        topo = 0
+    else:
+        axis = _normalised_or_zero(axis)
+        min_c, max_c = F(1.0), F(-1.0)
+        for n in normals:
+            c = _dot(axis, n)
+            min_c, max_c = np.fmin(min_c, c), np.fmax(max_c, c)
+        c = np.fmax(abs(min_c), abs(max_c))
+        c = np.sqrt(F(F(1.0) - c * c))
+        topo = 1 if c > FEATURE_ANGLE else 2
+    d = [_dot(vertices[i] - com, normals[i]) for i in range(len(vertices))]
+    return normals, d, com, topo
+
+
+def minimise_qef(vertices, normals):
+    """MinimiseQEF::place_feature_with_tangents (feature/qef.rs:36-68)."""
+    nrm, d, com, topo = tangent_planes(vertices, normals)
+    if topo == 0:
+        return com
+    u, v, s = compute_svd([[float(x) for x in n] for n in nrm])
+    if topo == 1:  # an edge: zero the smallest singular value
+        s_min, idx = 1.7976931348623157e308, 0
+        for i in range(3):
+            if s[i] < s_min:
+                s_min, idx = s[i], i
+        s[idx] = 0.0
+    x = solve(u, v, s, [float(di) for di in d], len(nrm))
+    return com + np.array([F(x[0]), F(x[1]), F(x[2])], F)
+
+
+def particle_placement(corners, normals):
+    """ParticleBasedMinimisation::place_feature_in_cell (particle_minimisation.rs:27-72)."""
+    nrm, d, com, _ = tangent_planes(corners, normals)
+    mfs = F(corners[6][0] - corners[0][0])
+    particle = com
+    forces = [np.zeros(3, F) for _ in range(8)]
+    for i in range(8):
+        for j in range(8):
+            dist = F(_dot(nrm[j], corners[i]) - d[j])  # Plane::distance
+            closest = corners[i] - nrm[j] * dist  # point_closest_to
+            forces[i] = forces[i] + (corners[i] - closest)
+    span = np.array([corners[1][0], corners[3][1], corners[4][2]], F) - corners[0]
+    for _ in range(100):
+        f = (particle - corners[0]) / span
+        lx = lambda a, b: F(F(1.0) - f[0]) * a + f[0] * b
+        c00, c01 = lx(forces[0], forces[1]), lx(forces[4], forces[5])
+        c10, c11 = lx(forces[3], forces[2]), lx(forces[7], forces[6])
+        c0 = F(F(1.0) - f[1]) * c00 + f[1] * c10
+        c1 = F(F(1.0) - f[1]) * c01 + f[1] * c11
+        force = (F(F(1.0) - f[2]) * c0 + f[2] * c1) * F(0.05) * mfs
+        particle = particle + force
+        if F(F(force[0] * force[0] + force[1] * force[1]) + force[2] * force[2]) < F(F(0.02) * mfs):
+            break
+    return particle
+
+
+def _cells():
+    """Active cells of the CSG scene at new(9) (corners and normalised normals),
+    and synthetic cells whose normals form creases and corners."""
+    from isosurface_gb300 import scenes
+    from isosurface_gb300 import source as S
+    prog = oracle.Program(S.lower(scenes.csg()))
+    n = 9
+    inv = F(1.0) / F(n - 1)
+    out = []
+    offs = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+    for z in range(n):
+        for y in range(n - 1):
+            for x in range(n - 1):
+                corners = np.array([(x + a, y + b, z + c) for a, b, c in offs], F) * inv
+                vals = prog.sample_scalar(corners)
+                cube = sum(1 << i for i in range(8) if not vals[i] > F(0.0))
+                if cube in (0, 255):
+                    continue
+                normals = np.array([_normalised_or_zero(nm) for nm in prog.sample_normal(corners)], F)
+                out.append((corners, normals))
+    rng = np.random.default_rng(9)
+    axes = np.eye(3, dtype=F)
+    for k in range(40):
+        corners = (np.array(offs, F) * F(0.125) + F(rng.uniform(0, 0.8))).astype(F)
+        pick = [axes[0], axes[1]] if k % 2 else [axes[0], axes[1], axes[2]]
+        normals = np.array([pick[i % len(pick)] for i in range(8)], F)
+        normals = np.array([_normalised_or_zero(nm + F(0.01) * rng.normal(size=3).astype(F)) for nm in normals], F)
+        out.append((corners, normals))
+    return out
+
+
+CELLS = _cells()
+
+
+@pytest.mark.parametrize("placer", [0, 1])
+def test_independent_feature_placement_matches_oracle(placer):
+    topologies = set()
+    for corners, normals in CELLS:
+        want, topo = oracle.place_feature(corners, normals, placer)
+        got = minimise_qef(corners, normals) if placer == 0 else particle_placement(corners, normals)
+        assert np.array_equal(got, want), (placer, corners[0], got, want)
+        topologies.add(topo)
+    assert topologies == {0, 1, 2}
