@@ -12,9 +12,12 @@
 //
 // Parity pin: the Source layer is pinned against the reference's own
 // known-answer tests (tests/golden/kats.json, read from the reference's
-// src/implicit/*.rs tests).  The reference has no test of any extractor, so
-// the extraction stages (MC, DC, LHMC) are "parity unpinned" by reference
-// tests; they are cross-checked by mesh invariants in tests/.
+// src/implicit/*.rs tests: values, normals and Directed vectors).  The
+// reference has no test of any extractor, so the extraction stages (MC, DC,
+// LHMC, EMC) are "parity unpinned" by reference tests; tests/ cross-checks
+// them by mesh invariants and against independent plain-Python restatements
+// of the same reference code (tests/test_mc_independent.py,
+// tests/test_svd_independent.py).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
