@@ -1,4 +1,4 @@
-"""An independent float32 restatement of every source op's value, written
+"""An independent float32 restatement of every source op's value and normal, written
 from the program format's definitions in include/isosurface_gpu.h and the
 reference's primitives (src/implicit/{sphere,rectangular_prism,cylinder,
 torus,csg}.rs, src/math/vector.rs folds), checked bit for bit against the
@@ -113,3 +113,73 @@ def test_source_values_match_oracle(name):
     got = np.array([value(src, p) for p in pts], F)
     want = oracle.Program(S.lower(src)).sample_scalar(pts)
     assert np.array_equal(got, want), np.nonzero(got != want)[0][:5]
+
+
+def _v(x, y, z):
+    return np.array([x, y, z], F)
+
+
+def normal(src, p):
+    """HermiteSource::sample_normal (unnormalised): the primitives as in the
+    reference (sphere.rs, rectangular_prism.rs via Vec3::clamp_to_cardinal_axis,
+    cylinder.rs, torus.rs), Union's component-wise min (csg.rs:47-51), and the
+    header's definitions where the reference has none: Intersection,
+    Difference and SmoothUnion take the deciding operand's normal, Rigid
+    rotates it back by M^T, the other point ops pass it through,
+    CentralDifference differentiates the value (source.rs:82-95)."""
+    x, y, z = (F(c) for c in p)
+    if isinstance(src, S.Sphere):
+        return _v(x, y, z)
+    if isinstance(src, S.RectangularPrism):  # vector.rs:612-621
+        ax, ay, az = abs(x), abs(y), abs(z)
+        if ax > ay and ax > az:
+            return _v(x, 0.0, 0.0)
+        return _v(0.0, y, 0.0) if ay > az else _v(0.0, 0.0, z)
+    if isinstance(src, S.Cylinder):
+        zz = F(abs(z) / F(src.half_length))
+        r = F(np.sqrt(F(x * x + y * y)) / F(src.radius))
+        return _v(0.0, 0.0, z) if zz > r else _v(x, y, 0.0)
+    if isinstance(src, S.Torus):
+        ln = length(x, y, F(0.0))
+        ring = _v(1.0, 0.0, 0.0) if abs(ln) < F(1.1920929e-07) else _v(x / ln, y / ln, F(0.0) / ln)
+        return _v(x, y, z) - ring * F(src.radius)
+    if isinstance(src, S.Union):
+        return np.fmin(normal(src.a, p), normal(src.b, p))
+    if isinstance(src, S.Intersection):
+        return normal(src.a, p) if value(src.a, p) >= value(src.b, p) else normal(src.b, p)
+    if isinstance(src, S.Difference):
+        return normal(src.b, p) if value(src.b, p) >= -value(src.a, p) else -normal(src.a, p)
+    if isinstance(src, S.SmoothUnion):
+        return normal(src.a, p) if value(src.a, p) <= value(src.b, p) else normal(src.b, p)
+    if isinstance(src, S.Translate):
+        c = [F(v) for v in src.centre]
+        return normal(src.source, (F(x - c[0]), F(y - c[1]), F(z - c[2])))
+    if isinstance(src, S.Rigid):
+        t = [F(v) for v in src.t]
+        m = [F(v) for v in src.m]
+        d = (F(x - t[0]), F(y - t[1]), F(z - t[2]))
+        q = tuple(F(F(m[3 * r] * d[0] + m[3 * r + 1] * d[1]) + m[3 * r + 2] * d[2]) for r in range(3))
+        n = normal(src.source, q)
+        return np.array([F(F(m[c] * n[0] + m[3 + c] * n[1]) + m[6 + c] * n[2]) for c in range(3)], F)
+    if isinstance(src, S.DomainMap):
+        sc, of = [F(v) for v in src.scale], [F(v) for v in src.offset]
+        return normal(src.source, (F(x * sc[0] + of[0]), F(y * sc[1] + of[1]), F(z * sc[2] + of[2])))
+    if isinstance(src, S.CentralDifference):
+        e = F(src.epsilon)
+        f = lambda q: value(src.source, q)
+        vx = F(f((F(x + e), F(y + F(0.0)), F(z + F(0.0)))) - f((F(x - e), F(y - F(0.0)), F(z - F(0.0)))))
+        vy = F(f((F(x + F(0.0)), F(y + e), F(z + F(0.0)))) - f((F(x - F(0.0)), F(y - e), F(z - F(0.0)))))
+        vz = F(f((F(x + F(0.0)), F(y + F(0.0)), F(z + e))) - f((F(x - F(0.0)), F(y - F(0.0)), F(z - e))))
+        e2 = F(F(2.0) * e)
+        return _v(vx / e2, vy / e2, vz / e2)
+    raise TypeError(type(src))
+
+
+@pytest.mark.parametrize("name", sorted(n for n in SCENES if not n.startswith("sphere_set")))
+def test_source_normals_match_oracle(name):
+    src = SCENES[name]
+    pts = np.random.default_rng(8).uniform(-1.1, 1.1, (300, 3)).astype(F)
+    pts[:10] = 0.0
+    got = np.array([normal(src, p) for p in pts], F)
+    want = oracle.Program(S.lower(src)).sample_normal(pts)
+    assert np.array_equal(got, want), np.nonzero(np.any(got != want, axis=1))[0][:5]
