@@ -183,3 +183,77 @@ def test_source_normals_match_oracle(name):
     got = np.array([normal(src, p) for p in pts], F)
     want = oracle.Program(S.lower(src)).sample_normal(pts)
     assert np.array_equal(got, want), np.nonzero(np.any(got != want, axis=1))[0][:5]
+
+
+MAXF = F(3.40282347e38)
+
+
+def vector(src, p):
+    """VectorSource::sample_vector (the Directed metric of
+    ExtendedMarchingCubes): sphere.rs:41-57, rectangular_prism.rs:43-70,
+    cylinder.rs:50-71, torus.rs:48-100, csg.rs:41-45, 74-78, 102-106; a
+    translated source samples at p - centre, CentralDifference passes through."""
+    x, y, z = (F(c) for c in p)
+    a = np.array([abs(x), abs(y), abs(z)], F)
+    if isinstance(src, S.Sphere):
+        r2 = F(F(src.radius) * F(src.radius))
+        l_yz, l_xz, l_xy = (F(r2 - F(F(a[i] * a[i]) + F(a[j] * a[j]))) for i, j in ((1, 2), (0, 2), (0, 1)))
+        return np.array([MAXF if l < 0 else F(a[k] - np.sqrt(l)) for k, l in enumerate((l_yz, l_xz, l_xy))], F)
+    if isinstance(src, S.RectangularPrism):
+        h = np.array(src.half_extent, F)
+        outside = lambda i, j: F(a[i] - h[i]) > 0 or F(a[j] - h[j]) > 0
+        mask = np.array([(1.0 if outside(1, 2) else -1.0), (1.0 if outside(0, 2) else -1.0),
+                         (1.0 if outside(0, 1) else -1.0)], F) * MAXF
+        closest = np.fmax(a, h) if (a[0] < h[0] and a[1] < h[1] and a[2] < h[2]) else np.fmin(a, h)
+        return np.fmax(a - closest, mask)
+    if isinstance(src, S.Cylinder):
+        r, hl = F(src.radius), F(src.half_length)
+        r2 = F(r * r)
+        with np.errstate(invalid="ignore"):
+            vx = MAXF if (a[2] > hl or a[1] > r) else F(a[0] - np.sqrt(F(r2 - F(a[1] * a[1]))))
+            vy = MAXF if (a[2] > hl or a[0] > r) else F(a[1] - np.sqrt(F(r2 - F(a[0] * a[0]))))
+        vz = MAXF if F(F(a[0] * a[0]) + F(a[1] * a[1])) > r2 else F(a[2] - hl)
+        return np.array([vx, vy, vz], F)
+    if isinstance(src, S.Torus):
+        R, t = F(src.radius), F(src.tube_radius)
+        with np.errstate(invalid="ignore"):
+            l_xy = F(np.sqrt(F(F(a[0] * a[0]) + F(a[1] * a[1]))) - R)
+            trz = np.sqrt(F(F(t * t) - F(a[2] * a[2])))
+            rx, ry = F(R + trz), F(R - trz)
+
+            def along(u, w):  # the component along axis u, w the other planar axis
+                if a[2] > t or a[w] > F(R + trz):
+                    return MAXF
+                if a[u] == 0:
+                    return F(abs(F(a[w] - R)) - t)
+                return np.fmax(F(a[u] - np.sqrt(F(F(rx * rx) - F(a[w] * a[w])))),
+                               F(np.sqrt(F(F(ry * ry) - F(a[w] * a[w]))) - a[u]))
+            vz = MAXF if abs(l_xy) > t else F(a[2] - np.sqrt(F(F(t * t) - F(l_xy * l_xy))))
+            return np.array([along(0, 1), along(1, 0), vz], F)
+    if isinstance(src, S.Union):
+        return np.fmin(vector(src.a, p), vector(src.b, p))
+    if isinstance(src, S.Intersection):
+        return np.fmax(vector(src.a, p), vector(src.b, p))
+    if isinstance(src, S.Difference):
+        return np.fmax(vector(src.b, p), -vector(src.a, p))
+    if isinstance(src, S.Translate):
+        c = [F(v) for v in src.centre]
+        return vector(src.source, (F(x - c[0]), F(y - c[1]), F(z - c[2])))
+    if isinstance(src, S.DomainMap):
+        sc, of = [F(v) for v in src.scale], [F(v) for v in src.offset]
+        return vector(src.source, (F(x * sc[0] + of[0]), F(y * sc[1] + of[1]), F(z * sc[2] + of[2])))
+    if isinstance(src, S.CentralDifference):
+        return vector(src.source, p)
+    raise TypeError(type(src))
+
+
+@pytest.mark.parametrize("name", ["sphere", "box", "cylinder", "torus", "csg", "intersection", "domain",
+                                  "central_difference"])
+def test_source_directed_vectors_match_oracle(name):
+    src = SCENES[name]
+    pts = np.random.default_rng(12).uniform(-1.1, 1.1, (400, 3)).astype(F)
+    pts[:10] = 0.0
+    pts[10:30, 0] = 0.0  # the torus's a.x == 0 branch
+    got = np.array([vector(src, p) for p in pts], F)
+    want = oracle.Program(S.lower(src)).sample_vector(pts)
+    assert np.array_equal(got, want), np.nonzero(np.any(got != want, axis=1))[0][:5]
