@@ -464,6 +464,15 @@ ISO_API iso_status iso_point_splat_render(iso_ctx* ctx, const float* view_proj, 
                                           uint32_t width, uint32_t height, float voxel_half, const float* clear_rgb,
                                           float* rgba);
 
+/* The same with flags: ISO_SPLAT_MIRROR_EDGES reads gather taps past the
+ * image edge through mirrored-repeat addressing (texel -1 is texel 0, texel
+ * width is texel width - 1, ...), the wrap of the default sampler the example
+ * reads its buffers with; without it they read as empty. */
+#define ISO_SPLAT_MIRROR_EDGES 1u
+ISO_API iso_status iso_point_splat_render_ex(iso_ctx* ctx, const float* view_proj, const float* view_proj_inverse,
+                                             uint32_t width, uint32_t height, float voxel_half,
+                                             const float* clear_rgb, uint32_t flags, float* rgba);
+
 /* ------------------------------------------------------------------------ */
 /* Host-side sampling helpers                                                */
 /* ------------------------------------------------------------------------ */

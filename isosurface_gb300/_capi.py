@@ -79,6 +79,7 @@ SIGNATURES = {
     "iso_mc_extract": (i32, [vp, vp, u32, u32, ctypes.POINTER(MeshInfo)]),
     "iso_mc_extract_host": (i32, [vp, vp, u32, u32, vp, u64, vp, u64, ctypes.POINTER(MeshInfo)]),
     "iso_point_splat_render": (i32, [vp, vp, vp, u32, u32, ctypes.c_float, vp, vp]),
+    "iso_point_splat_render_ex": (i32, [vp, vp, vp, u32, u32, ctypes.c_float, vp, u32, vp]),
     "iso_host_register": (i32, [vp, u64]),
     "iso_host_unregister": (i32, [vp]),
     "iso_mc_extract_field": (i32, [vp, vp, u32, u32, u32, u64, u32, ctypes.POINTER(MeshInfo)]),

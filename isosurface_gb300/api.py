@@ -197,11 +197,15 @@ class Context:
                                     ctypes.byref(flips)), self.h)
         return info, flips.value
 
-    def point_splat(self, width, height, voxel_half, view_proj=None, view_proj_inverse=None, clear=None):
+    def point_splat(self, width, height, voxel_half, view_proj=None, view_proj_inverse=None, clear=None,
+                    edge="empty"):
         """Deferred point-splat image of the last PointCloud extraction with
         normals (examples/deferred_rasterisation.rs), (height, width, 4)
         float32, row 0 at the bottom.  Without matrices, the example's camera
-        (isosurface_gb300.render.splat_camera)."""
+        (isosurface_gb300.render.splat_camera).  edge: gather taps past the
+        image edge read as "empty", or through "mirror"ed-repeat addressing."""
+        if edge not in ("empty", "mirror"):
+            raise ValueError("edge must be 'empty' or 'mirror'")
         from . import render
         if view_proj is None or view_proj_inverse is None:
             view_proj, view_proj_inverse = render.splat_camera(width, height)
@@ -210,9 +214,15 @@ class Context:
         col = np.ascontiguousarray(render.CLEAR_RGB if clear is None else clear, np.float32).reshape(3)
         out = np.empty((height, width, 4), np.float32)
         f32p = ctypes.POINTER(ctypes.c_float)
-        check(lib().iso_point_splat_render(self.h, vp.ctypes.data_as(f32p), vpi.ctypes.data_as(f32p), width, height,
-                                           float(voxel_half), col.ctypes.data_as(f32p), out.ctypes.data_as(f32p)),
-              self.h)
+        if edge == "empty":
+            st = lib().iso_point_splat_render(self.h, vp.ctypes.data_as(f32p), vpi.ctypes.data_as(f32p), width,
+                                              height, float(voxel_half), col.ctypes.data_as(f32p),
+                                              out.ctypes.data_as(f32p))
+        else:
+            st = lib().iso_point_splat_render_ex(self.h, vp.ctypes.data_as(f32p), vpi.ctypes.data_as(f32p), width,
+                                                 height, float(voxel_half), col.ctypes.data_as(f32p), 1,
+                                                 out.ctypes.data_as(f32p))
+        check(st, self.h)
         return out
 
     def sample_grid(self, source, size, field_ptr, pitch):

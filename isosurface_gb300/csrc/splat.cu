@@ -16,7 +16,8 @@
 //                  shades hits with the hemisphere term and composites over
 //                  the clear colour.
 // Row 0 is the bottom row (GL's window convention); taps outside the image
-// read as empty.  Every expression has a fixed f32 operation order (this unit
+// read as empty, or, with ISO_SPLAT_MIRROR_EDGES, through mirrored-repeat
+// addressing (the wrap of the sampler the example reads its buffers with).  Every expression has a fixed f32 operation order (this unit
 // is compiled without FMA contraction), restated by the numpy oracle.
 #include <cuda_runtime.h>
 
@@ -87,8 +88,16 @@ struct GatherArgs {
     Mat4 vpinv;
     float voxel;
     int dx, dy, last;
+    int mirror;    // taps past the edge: 0 empty, 1 mirrored repeat
     float clear[3];
 };
+
+// mirrored-repeat addressing of texel i in a row of n: -1 -> 0, n -> n - 1, ...
+__device__ __forceinline__ int mirror_index(int i, int n) {
+    int m = i % (2 * n);
+    if (m < 0) m += 2 * n;
+    return m >= n ? 2 * n - 1 - m : m;
+}
 
 __global__ void splat_gather(GatherArgs A) {
     const uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -105,8 +114,13 @@ __global__ void splat_gather(GatherArgs A) {
     float best = NO_HIT;
     float3 res = make_float3(0.0f, 0.0f, 0.0f), rn = make_float3(0.0f, 0.0f, 0.0f);
     for (int t = -TAPS; t <= TAPS; ++t) {
-        const int tx = ix + t * A.dx, ty = iy + t * A.dy;
-        if (tx < 0 || tx >= (int)A.width || ty < 0 || ty >= (int)A.height) continue;
+        int tx = ix + t * A.dx, ty = iy + t * A.dy;
+        if (A.mirror) {
+            tx = mirror_index(tx, (int)A.width);
+            ty = mirror_index(ty, (int)A.height);
+        } else if (tx < 0 || tx >= (int)A.width || ty < 0 || ty >= (int)A.height) {
+            continue;
+        }
         const size_t at = (size_t)ty * A.width + tx;
         const float4 q = A.spos[at];
         if (!((fabsf(q.x) + fabsf(q.y)) + fabsf(q.z) > 0.0f)) continue;
@@ -147,11 +161,12 @@ using namespace iso;
 
 extern "C" {
 
-iso_status iso_point_splat_render(iso_ctx* ctx, const float* view_proj, const float* view_proj_inverse,
-                                  uint32_t width, uint32_t height, float voxel_half, const float* clear_rgb,
-                                  float* rgba) {
+iso_status iso_point_splat_render_ex(iso_ctx* ctx, const float* view_proj, const float* view_proj_inverse,
+                                     uint32_t width, uint32_t height, float voxel_half, const float* clear_rgb,
+                                     uint32_t flags, float* rgba) {
     iso::NvtxRange nvtx_range("iso_point_splat_render");
     if (!ctx) return ISO_ERR_INVALID_ARG;
+    if (flags & ~(uint32_t)ISO_SPLAT_MIRROR_EDGES) return fail(ctx, ISO_ERR_INVALID_ARG, "unsupported flags");
     if (!view_proj || !view_proj_inverse || !clear_rgb || !rgba)
         return fail(ctx, ISO_ERR_INVALID_ARG, "null matrix, colour or image pointer");
     if (width == 0 || height == 0 || width > 16384 || height > 16384)
@@ -190,6 +205,7 @@ iso_status iso_point_splat_render(iso_ctx* ctx, const float* view_proj, const fl
     g.height = height;
     g.vpinv = vpi;
     g.voxel = voxel_half;
+    g.mirror = (flags & ISO_SPLAT_MIRROR_EDGES) ? 1 : 0;
     for (int k = 0; k < 3; ++k) g.clear[k] = clear_rgb[k];
     for (int i = 0; i < 4; ++i) {
         const bool from_a = (i % 2) == 0;
@@ -208,6 +224,13 @@ iso_status iso_point_splat_render(iso_ctx* ctx, const float* view_proj, const fl
     e = cudaMemcpyAsync(rgba, out, fbytes, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     return e == cudaSuccess ? ISO_OK : cuda_fail(ctx, e, "image readback");
+}
+
+iso_status iso_point_splat_render(iso_ctx* ctx, const float* view_proj, const float* view_proj_inverse,
+                                  uint32_t width, uint32_t height, float voxel_half, const float* clear_rgb,
+                                  float* rgba) {
+    return iso_point_splat_render_ex(ctx, view_proj, view_proj_inverse, width, height, voxel_half, clear_rgb, 0,
+                                     rgba);
 }
 
 }  // extern "C"
