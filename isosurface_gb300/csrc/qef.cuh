@@ -11,6 +11,10 @@
 //   which leaves their projection in the solution unscaled).
 // * ParticleBasedMinimisation (src/feature/particle_minimisation.rs:25-72)
 //
+// The SVD steps are restated from swiftcoder/isosurface (src/math/svd.rs),
+// Copyright 2021 Tristam MacDonald, licensed under the Apache License, Version
+// 2.0 (http://www.apache.org/licenses/LICENSE-2.0).
+//
 // The steps and their operation order follow the reference so that vertex
 // positions match it bit for bit (the translation unit is built with
 // -fmad=false; f64 sqrt and division are IEEE).  The reference's QR loop has

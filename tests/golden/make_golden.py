@@ -198,7 +198,9 @@ def parse_kats(ref):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("ISO_REFERENCE_DIR")
+    if not ref:
+        sys.exit("usage: make_golden.py <reference checkout>  (or set ISO_REFERENCE_DIR)")
     tables = parse_tables(ref)
     with open(os.path.join(HERE, "mc_tables.json"), "w") as f:
         json.dump(tables, f, indent=0)

@@ -82,3 +82,29 @@ def test_batch_graph_survives_mesh_buffer_regrowth(ctx, chunk_set, want):
     info = b.run(graph=True)
     _check(b.meshes(info), want)
     b.close()
+
+
+def test_batch_4096_chunk_workload(ctx):
+    """The batch workload itself: the 4096 seeded chunks (50 % 16^3, 35 %
+    32^3, 15 % 64^3 cells, 1-16 random primitives each) extracted in one
+    CUDA graph replay; every chunk's mesh equals the oracle's MarchingCubes
+    of that chunk byte for byte.  The oracle runs on all host cores."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+    chunk_set = scenes.chunks(seed=7, count=4096)
+    b = Batch(ctx, chunk_set)
+    b.run(graph=True)               # eager run, sizes the graph
+    meshes = b.meshes(b.run(graph=True))
+    b.close()
+    assert len(meshes) == 4096
+
+    def check(i):
+        size, src = chunk_set[i]
+        w = oracle.Program(S.lower(src)).marching_cubes(size)
+        return np.array_equal(meshes[i].vertices, w.vertices) and np.array_equal(meshes[i].indices, w.indices)
+
+    with ThreadPoolExecutor(max(1, os.cpu_count() or 1)) as pool:
+        ok = list(pool.map(check, range(len(chunk_set))))
+    bad = [i for i, good in enumerate(ok) if not good]
+    assert not bad, "chunks differing from the oracle: %s" % bad[:20]
+    assert sum(len(m.indices) for m in meshes) // 3 > 20_000_000

@@ -2,11 +2,8 @@
 through the C ABI: bit-exact vertices and indices, the same number of rotated
 edges, the normals sink, and the errors the entry point raises.
 
-The kernels' per-item code is checked on the host by test_emc_host.py.  These
-tests run the kernels themselves; they are skipped unless ISO_PENDING_GPU_TESTS=1 until
-the kernels have run once on a GB300."""
-import os
-
+The kernels' per-item code is also checked on the host by test_emc_host.py;
+these tests run the kernels themselves."""
 import numpy as np
 import pytest
 
@@ -16,9 +13,7 @@ from isosurface_gb300 import source as S
 
 from emc_scenes import FIXED, random_scenes
 
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(os.environ.get("ISO_PENDING_GPU_TESTS") != "1",
-                                 reason="ExtendedMarchingCubes kernels not yet run on a GB300 (set ISO_PENDING_GPU_TESTS=1)")]
+pytestmark = pytest.mark.gpu
 
 
 def _gpu(ctx, src, n, normals=False):

@@ -3,9 +3,7 @@
 
 CPU: the header and size checks of the documented format.  GPU: a run
 resumed from a checkpoint follows the original loss trajectory (up to the
-rounding of the float atomics in the gradient and loss reductions); skipped
-unless ISO_PENDING_GPU_TESTS=1 until it has run once on a GB300."""
-import os
+rounding of the float atomics in the gradient and loss reductions)."""
 import struct
 
 import numpy as np
@@ -51,8 +49,6 @@ def test_checkpoint_info_missing_file(tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.skipif(os.environ.get("ISO_PENDING_GPU_TESTS") != "1",
-                    reason="checkpoint resume not yet run on a GB300 (set ISO_PENDING_GPU_TESTS=1)")
 def test_resume_follows_the_same_trajectory(ctx, tmp_path):
     from isosurface_gb300 import scenes
     net = SG.Surrogate(ctx, seed=3)

@@ -40,8 +40,6 @@ def test_point_splat_needs_a_point_cloud_with_normals(ctx):
         ctx.point_splat(64, 48, VOXEL)
 
 
-@pytest.mark.skipif(__import__("os").environ.get("ISO_PENDING_GPU_TESTS") != "1",
-                    reason="mirrored edge addressing not yet run on a GB300 (set ISO_PENDING_GPU_TESTS=1)")
 @pytest.mark.parametrize("width,height", [(96, 72), (256, 192)])
 def test_point_splat_mirrored_edges_match_oracle(ctx, width, height):
     pts = _point_cloud(ctx)
