@@ -4,8 +4,8 @@
  * The library replaces the extraction hot path of swiftcoder/isosurface
  * (a Rust crate).  Each extraction entry point below stands in for one
  * reference call; the reference's Rust wrapper would bind these functions
- * through `extern "C"` and replay the resulting mesh into
- * the caller's Extractor, so the reference API
+ * through `extern "C"` and replay the resulting mesh into the caller's
+ * Extractor, so the reference API
  *
  *     MarchingCubes::new(n).extract(&source, &mut extractor)
  *
@@ -87,6 +87,15 @@ ISO_API uint64_t iso_ctx_kernel_launches(const iso_ctx* ctx);
  * call returns ISO_ERR_OUT_OF_MEMORY); the hook then switches itself off.
  * A negative `after` switches it off.  Nothing happens on the device. */
 ISO_API iso_status iso_debug_fail_allocation(iso_ctx* ctx, int64_t after);
+
+/* Test hook for the bounded device-side waits: while enabled, the
+ * decoupled look-back scan of iso_mc_extract_field_noalloc runs with its
+ * first block never publishing its status and the other blocks giving up
+ * after 256 polls of a predecessor, so the call returns ISO_ERR_TIMEOUT
+ * instead of waiting; the next call after disabling it extracts normally.
+ * Process-wide (that entry point takes no context).  Nothing faults or
+ * hangs: every wait is bounded either way. */
+ISO_API iso_status iso_debug_scan_timeout(int enable);
 
 /* Per-stage device timing: when enabled, every kernel the context launches is
  * bracketed by CUDA events on its stream.  iso_ctx_stage_times synchronises,
@@ -243,7 +252,8 @@ ISO_API iso_status iso_mc_extract_field(iso_ctx* ctx, const float* field, uint32
  * device synchronisation and unbounded latency of those calls.  It needs no
  * iso_ctx (creating one allocates).
  *
- * Input and layout as iso_mc_extract_field.  The caller owns the outputs:
+ * Input and layout as iso_mc_extract_field, with nz <= 65536 (larger values
+ * are ISO_ERR_INVALID_ARG).  The caller owns the outputs:
  * `vertices` (3 floats per vertex, room for vertex_cap vertices) and
  * `indices` (3 u32 per triangle, room for triangle_cap triangles), both
  * device memory; work is queued on `stream` (a cudaStream_t, NULL for the
@@ -397,6 +407,26 @@ typedef struct iso_surrogate_stats {
 ISO_API iso_status iso_surrogate_field(iso_ctx* ctx, iso_mlp* net, const iso_program* exact, uint32_t size,
                                        uint32_t coarse_step, float band_cells, float* field, uint64_t pitch,
                                        iso_surrogate_stats* stats);
+/* iso_surrogate_field with options (no reference counterpart):
+ *   ISO_SURROGATE_EXACT_COARSE: the coarse grid from `exact` instead of the
+ *     network (`net` may be NULL): the same pipeline without the network, to
+ *     measure what the network gains;
+ *   ISO_SURROGATE_WITNESS: spot checks against `exact` at witness points of
+ *     each sphere of a sphere-set source (its centre and the six axis points
+ *     of its surface); a sphere whose interpolated surrogate value says
+ *     "outside" at its centre has every fine point inside it or within
+ *     band_cells + 1 cells (plus half the smooth-union k) of its surface
+ *     re-sampled exactly as well; a sphere whose surrogate value differs
+ *     from the exact one by more than band_cells - 1 cells (at least a
+ *     quarter cell) at a surface witness within two cells of the exact
+ *     surface has the points within that distance of its surface
+ *     re-sampled.  ISO_ERR_UNSUPPORTED for other sources.
+ *     *flagged_primitives (nullable) receives the flagged count. */
+#define ISO_SURROGATE_EXACT_COARSE 1u
+#define ISO_SURROGATE_WITNESS 2u
+ISO_API iso_status iso_surrogate_field_ex(iso_ctx* ctx, iso_mlp* net, const iso_program* exact, uint32_t size,
+                                          uint32_t coarse_step, float band_cells, uint32_t flags, float* field,
+                                          uint64_t pitch, iso_surrogate_stats* stats, uint64_t* flagged_primitives);
 /* the field, then marching cubes on it; the mesh stays in the context as
  * after iso_mc_extract (stats nullable) */
 ISO_API iso_status iso_surrogate_extract(iso_ctx* ctx, iso_mlp* net, const iso_program* exact, uint32_t size,

@@ -18,6 +18,8 @@ STATUS = {
 }
 ISO_FLAG_KEYS = 1
 ISO_FLAG_NORMALS = 2
+ISO_SURROGATE_EXACT_COARSE = 1
+ISO_SURROGATE_WITNESS = 2
 
 
 class IsoError(RuntimeError):
@@ -68,6 +70,7 @@ SIGNATURES = {
     "iso_ctx_set_stream": (i32, [vp, vp]),
     "iso_ctx_kernel_launches": (u64, [vp]),
     "iso_debug_fail_allocation": (i32, [vp, ctypes.c_int64]),
+    "iso_debug_scan_timeout": (i32, [ctypes.c_int]),
     "iso_ctx_enable_stage_timing": (i32, [vp, i32]),
     "iso_ctx_stage_times": (i32, [vp, ctypes.POINTER(ctypes.c_double), u64p]),
     "iso_program_create": (i32, [vp, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(vp)]),
@@ -111,6 +114,8 @@ SIGNATURES = {
     "iso_mlp_load": (i32, [vp, ctypes.c_char_p]),
     "iso_mlp_checkpoint_info": (i32, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
     "iso_surrogate_field": (i32, [vp, vp, vp, u32, u32, ctypes.c_float, vp, u64, ctypes.POINTER(SurrogateStats)]),
+    "iso_surrogate_field_ex": (i32, [vp, vp, vp, u32, u32, ctypes.c_float, u32, vp, u64,
+                                     ctypes.POINTER(SurrogateStats), ctypes.POINTER(u64)]),
     "iso_surrogate_extract": (i32, [vp, vp, vp, u32, u32, ctypes.c_float, u32, ctypes.POINTER(SurrogateStats),
                                     ctypes.POINTER(MeshInfo)]),
     "iso_mesh_distance": (i32, [vp, f32p, u64, f32p, u64, ctypes.c_float, u32, ctypes.POINTER(MeshDistance)]),

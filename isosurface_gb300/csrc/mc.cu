@@ -153,6 +153,8 @@ struct CountArgs {
     uint32_t* ticket;
     uint64_t* totals;       // [0] triangles [1] vertices
     uint32_t* err;
+    uint32_t spin_limit;    // polls of a predecessor's status before giving up
+    uint32_t withhold;      // test hook: the first block never publishes its status
 };
 
 // Pass 1: per-row counts + decoupled look-back exclusive scan (one warp per row).
@@ -197,7 +199,7 @@ __global__ void __launch_bounds__(WARPS * 32) mc_count_scan(CountArgs A) {
         uint32_t ti = warp_incl_scan(t, lane), vi = warp_incl_scan(v, lane);
         uint64_t agg_t = __shfl_sync(FULL, ti, WARPS - 1), agg_v = __shfl_sync(FULL, vi, WARPS - 1);
         volatile uint64_t* st = A.status;
-        if (lane == 0) {
+        if (lane == 0 && !(A.withhold && bid == 0)) {
             __threadfence();
             st[bid] = pack(bid == 0 ? FLAG_P : FLAG_A, agg_t, agg_v);
         }
@@ -210,7 +212,7 @@ __global__ void __launch_bounds__(WARPS * 32) mc_count_scan(CountArgs A) {
                 if (j >= 0) {
                     uint32_t it = 0;
                     s = st[j];
-                    while ((s & FLAG_MASK) == 0 && it < SPIN_LIMIT) {
+                    while ((s & FLAG_MASK) == 0 && it < A.spin_limit) {
                         __nanosleep(64);
                         s = st[j];
                         ++it;
@@ -1047,7 +1049,16 @@ iso_status noalloc_scratch(int device, unsigned char** out) {
 
 inline size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
+// iso_debug_scan_timeout: the look-back scan's first block withholds its
+// status and the others give up after a few polls
+std::atomic<int> g_debug_scan_timeout{0};
+
 }  // namespace
+
+extern "C" ISO_API iso_status iso_debug_scan_timeout(int enable) {
+    g_debug_scan_timeout.store(enable ? 1 : 0);
+    return ISO_OK;
+}
 
 extern "C" ISO_API iso_status iso_mc_extract_field_noalloc(const float* field, uint32_t nx, uint32_t ny, uint32_t nz,
                                                             uint64_t pitch, float* vertices, uint64_t vertex_cap,
@@ -1057,7 +1068,8 @@ extern "C" ISO_API iso_status iso_mc_extract_field_noalloc(const float* field, u
     using namespace iso;
     if (!field || !info) return ISO_ERR_INVALID_ARG;
     *info = iso_mesh_info{};
-    if (nx != ny || nx < 2 || nz < 2 || pitch < nx || nx > 65536 || nz > 65537) return ISO_ERR_INVALID_ARG;
+    // nz - 1 cell layers become the emit's grid.y, which CUDA caps at 65535
+    if (nx != ny || nx < 2 || nz < 2 || pitch < nx || nx > 65536 || nz > 65536) return ISO_ERR_INVALID_ARG;
     const uint32_t W = words_per_row(nx);
     const uint64_t rows = (uint64_t)(ny - 1) * (nz - 1);
     const uint64_t nblocks = (rows + WARPS - 1) / WARPS;
@@ -1089,7 +1101,9 @@ extern "C" ISO_API iso_status iso_mc_extract_field_noalloc(const float* field, u
     cudaError_t e = cudaMemsetAsync(s, 0, off_status + 8 * nblocks, cs);
     if (e == cudaSuccess) e = launch_sign_bits_on(cs, field, nx, ny, nz, pitch, bits);
     if (e != cudaSuccess) return ISO_ERR_CUDA;
-    CountArgs ca{bits, W, nx, ny, nz, (uint32_t)rows, rowtri, rowvert, status, ticket, totals, err};
+    const bool withhold = g_debug_scan_timeout.load() != 0;
+    CountArgs ca{bits,   W,      nx,  ny, nz, (uint32_t)rows, rowtri, rowvert, status, ticket, totals, err,
+                 withhold ? 256u : SPIN_LIMIT, withhold ? 1u : 0u};
     mc_count_scan<<<(unsigned)nblocks, WARPS * 32, 0, cs>>>(ca);
     uint64_t h[3] = {0, 0, 0};
     e = cudaGetLastError();

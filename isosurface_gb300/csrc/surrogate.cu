@@ -44,6 +44,7 @@ struct BandArgs {
     uint64_t pitch;
     uint32_t* list;       // fine point ids (z*ny + y)*nx + x of band points
     uint32_t* count;
+    const uint32_t* forced;  // null, or one bit per fine point id: re-sample it exactly
 };
 
 __device__ __forceinline__ float lerp1(float a, float b, float t) { return a + (b - a) * t; }
@@ -63,6 +64,10 @@ __global__ void __launch_bounds__(128) band_mark(BandArgs A) {
         const float v01 = lerp1(at(ix, iy, jz), at(jx, iy, jz), tx), v11 = lerp1(at(ix, jy, jz), at(jx, jy, jz), tx);
         const float v = lerp1(lerp1(v00, v10, ty), lerp1(v01, v11, ty), tz);
         band = fabsf(v) <= A.tau;
+        if (!band && A.forced) {
+            const uint32_t id = ((uint32_t)z * A.ny + y) * A.nx + x;
+            band = (__ldg(A.forced + (id >> 5)) >> (id & 31)) & 1u;
+        }
         if (!band) A.field[((size_t)z * A.ny + y) * A.pitch + x] = v;
     }
     const uint32_t m = __ballot_sync(FULL, band);
@@ -93,6 +98,123 @@ __global__ void __launch_bounds__(256) band_exact(ExactArgs A) {
         const uint32_t y = r % A.ny, z = r / A.ny;
         const float v = eval_scalar(A.pv, v3((float)x * A.inv, (float)y * A.inv, (float)z * A.inv));
         A.field[((size_t)z * A.ny + y) * A.pitch + x] = v;
+    }
+}
+
+// The coarse grid from the exact program instead of the network (the same
+// pipeline without the network, for comparison): coarse point (i, j, k) is
+// fine lattice point (i, j, k) * step, as the network sees it.
+__global__ void __launch_bounds__(256) coarse_exact(ProgView pv, uint32_t cx, uint32_t cy, uint32_t cz,
+                                                     uint32_t step, float inv, float* coarse) {
+    const uint64_t n = (uint64_t)cx * cy * cz;
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t i = (uint32_t)(t % cx), r = (uint32_t)(t / cx);
+        const uint32_t j = r % cy, k = r / cy;
+        coarse[t] = eval_scalar(pv, v3((float)(i * step) * inv, (float)(j * step) * inv, (float)(k * step) * inv));
+    }
+}
+
+// Spot checks of the surrogate against the exact source at witness points of
+// each sphere of a sphere-set source: its centre (inside the exact surface)
+// and the six points of its own surface on the axes.  A sphere is flagged
+// when the interpolated network value says "outside" at its centre, or when
+// at a surface witness that lies near the exact surface (|exact| within two
+// cells) the two differ by more than `tol`: there the band around the
+// network's surface may miss the exact one.
+struct WitnessArgs {
+    ProgView pv;
+    const float* spheres;   // n x (cx, cy, cz, r) in the source's frame
+    uint32_t n;
+    float scale[3], offset[3];  // sample frame -> source frame
+    float inv;              // 1 / (size - 1)
+    const float* coarse;
+    uint32_t cx, cy, cz, step;
+    float near, tol;        // field units
+    uint32_t* flags;        // per sphere: 1 shell, 2 ball (or both); flags[n] counts the flagged
+};
+
+__device__ __forceinline__ float coarse_at(const WitnessArgs& A, float u, float v, float w) {
+    // trilinear interpolation of the coarse grid at fine lattice coordinates
+    const float fu = fminf(fmaxf(u / (float)A.step, 0.0f), (float)(A.cx - 1));
+    const float fv = fminf(fmaxf(v / (float)A.step, 0.0f), (float)(A.cy - 1));
+    const float fw = fminf(fmaxf(w / (float)A.step, 0.0f), (float)(A.cz - 1));
+    const uint32_t i = min((uint32_t)fu, A.cx - 1), j = min((uint32_t)fv, A.cy - 1), k = min((uint32_t)fw, A.cz - 1);
+    const uint32_t i1 = min(i + 1, A.cx - 1), j1 = min(j + 1, A.cy - 1), k1 = min(k + 1, A.cz - 1);
+    const float tx = fu - (float)i, ty = fv - (float)j, tz = fw - (float)k;
+    auto at = [&](uint32_t a, uint32_t b, uint32_t c) { return __ldg(A.coarse + ((size_t)c * A.cy + b) * A.cx + a); };
+    const float v00 = lerp1(at(i, j, k), at(i1, j, k), tx), v10 = lerp1(at(i, j1, k), at(i1, j1, k), tx);
+    const float v01 = lerp1(at(i, j, k1), at(i1, j, k1), tx), v11 = lerp1(at(i, j1, k1), at(i1, j1, k1), tx);
+    return lerp1(lerp1(v00, v10, ty), lerp1(v01, v11, ty), tz);
+}
+
+__global__ void __launch_bounds__(256) witness_check(WitnessArgs A) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 7 * A.n) return;
+    const uint32_t s = t / 7, k = t % 7;
+    const float* q = A.spheres + 4 * (size_t)s;
+    const float4 sp = make_float4(q[0], q[1], q[2], q[3]);
+    float w[3] = {sp.x, sp.y, sp.z};
+    if (k > 0) w[(k - 1) >> 1] += (k & 1) ? sp.w : -sp.w;
+    float p[3], u[3];
+    for (int a = 0; a < 3; ++a) {
+        p[a] = (w[a] - A.offset[a]) / A.scale[a];  // sample frame
+        u[a] = p[a] / A.inv;                        // fine lattice coordinates
+    }
+    const float sv = coarse_at(A, u[0], u[1], u[2]);
+    uint32_t flag = 0;
+    if (k == 0) {
+        flag = sv > 0.0f ? 2u : 0u;  // missed at its centre: the whole ball
+    } else {
+        const float ev = eval_scalar(A.pv, v3(p[0], p[1], p[2]));
+        flag = fabsf(ev) <= A.near && fabsf(sv - ev) > A.tol ? 1u : 0u;  // off near its surface: the shell
+    }
+    if (flag && atomicOr(A.flags + s, flag) == 0u) atomicAdd(A.flags + A.n, 1u);  // count each sphere once
+}
+
+// Fine points within `shell` (field units) of a flagged sphere's surface are
+// forced into the band, and for a sphere missed at its centre every point
+// inside it as well (the network's signs there are wrong): one block per
+// sphere (unflagged ones return at once).
+struct ShellArgs {
+    const float* spheres;
+    const uint32_t* flags;
+    float scale[3], offset[3];
+    float inv, shell;
+    uint32_t nx, ny, nz;
+    uint32_t* forced;
+};
+
+__global__ void __launch_bounds__(256) witness_shells(ShellArgs A) {
+    const uint32_t flag = A.flags[blockIdx.x];
+    if (!flag) return;
+    const bool ball = flag & 2u;
+    const float* q4 = A.spheres + 4 * (size_t)blockIdx.x;
+    const float4 sp = make_float4(q4[0], q4[1], q4[2], q4[3]);
+    const float c[3] = {sp.x, sp.y, sp.z};
+    const float reach = sp.w + A.shell;
+    int32_t lo[3], hi[3];
+    const uint32_t dims[3] = {A.nx, A.ny, A.nz};
+    for (int a = 0; a < 3; ++a) {
+        // lattice coordinates of c -/+ reach (the scale may be negative)
+        const float e0 = (c[a] - reach - A.offset[a]) / A.scale[a] / A.inv;
+        const float e1 = (c[a] + reach - A.offset[a]) / A.scale[a] / A.inv;
+        lo[a] = max((int32_t)floorf(fminf(e0, e1)) - 1, 0);
+        hi[a] = min((int32_t)ceilf(fmaxf(e0, e1)) + 1, (int32_t)dims[a] - 1);
+        if (lo[a] > hi[a]) return;
+    }
+    const uint32_t ex = hi[0] - lo[0] + 1, ey = hi[1] - lo[1] + 1, ez = hi[2] - lo[2] + 1;
+    const uint64_t total = (uint64_t)ex * ey * ez;
+    for (uint64_t t = threadIdx.x; t < total; t += blockDim.x) {
+        const uint32_t x = lo[0] + (uint32_t)(t % ex), r = (uint32_t)(t / ex);
+        const uint32_t y = lo[1] + r % ey, z = lo[2] + r / ey;
+        const float qx = (float)x * A.inv * A.scale[0] + A.offset[0] - c[0];
+        const float qy = (float)y * A.inv * A.scale[1] + A.offset[1] - c[1];
+        const float qz = (float)z * A.inv * A.scale[2] + A.offset[2] - c[2];
+        const float d = sqrtf(qx * qx + qy * qy + qz * qz) - sp.w;
+        if (ball ? d <= A.shell : fabsf(d) <= A.shell) {
+            const uint32_t id = (z * A.ny + y) * A.nx + x;
+            atomicOr(A.forced + (id >> 5), 1u << (id & 31));
+        }
     }
 }
 
@@ -242,18 +364,37 @@ __global__ void case_diff(const uint32_t* ba, const uint32_t* bb, uint32_t nx, u
 inline unsigned blocks_for(uint64_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
 
 iso_status check_args(iso_ctx* ctx, iso_mlp* net, const iso_program* exact, uint32_t size, uint32_t step,
-                      float band) {
-    if (!ctx || !net || !exact) return ISO_ERR_INVALID_ARG;
-    if (net->ctx != ctx) return fail(ctx, ISO_ERR_INVALID_ARG, "network belongs to another context");
+                      float band, bool need_net = true) {
+    if (!ctx || !exact || (need_net && !net)) return ISO_ERR_INVALID_ARG;
+    if (net && net->ctx != ctx) return fail(ctx, ISO_ERR_INVALID_ARG, "network belongs to another context");
+    if (exact->ctx != ctx) return fail(ctx, ISO_ERR_INVALID_ARG, "program belongs to another context");
     if (size < 2 || size > 2048) return fail(ctx, ISO_ERR_INVALID_ARG, "size must be in [2, 2048]");
     if (step < 1 || step > 64) return fail(ctx, ISO_ERR_INVALID_ARG, "coarse step must be in [1, 64]");
     if (!(band >= 0.0f) || band > 1.0e6f) return fail(ctx, ISO_ERR_INVALID_ARG, "band must be >= 0");
     return set_device(ctx);
 }
 
-// field into `field`; uses ctx->aux (band list) and ctx->aux2 (coarse grid)
+// The sphere list of a sphere-set program ([domain map] SPHERE_SET, hard or
+// smooth) on the device, its size, smooth k (0 for a hard union) and frame.
+bool sphere_list(const iso_program* p, const float** d_spheres, uint32_t* n, float* k) {
+    const auto& o = p->ops;
+    size_t at = SIZE_MAX;
+    if (o.size() == 1 && (o[0] & 0xFF) == OP_SPHERE_SET) at = o[0] >> 8;
+    if (o.size() == 3 && (o[0] & 0xFF) == OP_PT_DOMAIN && (o[1] & 0xFF) == OP_SPHERE_SET &&
+        (o[2] & 0xFF) == OP_PT_POP)
+        at = o[1] >> 8;
+    if (at == SIZE_MAX) return false;
+    *n = (uint32_t)p->consts[at];
+    *k = p->consts[at + 1] != 0.0f ? p->consts[at + 2] : 0.0f;
+    *d_spheres = p->d_consts + at + 3;
+    return true;
+}
+
+// field into `field`; uses ctx->aux (band list), ctx->aux2 (coarse grid) and,
+// for the witness checks, ctx->aux3 (forced-point mask and sphere flags)
 iso_status surrogate_field(iso_ctx* ctx, iso_mlp* net, const iso_program* exact, uint32_t size, uint32_t step,
-                           float band, float* field, uint64_t pitch, iso_surrogate_stats* stats) {
+                           float band, uint32_t flags, float* field, uint64_t pitch, iso_surrogate_stats* stats,
+                           uint64_t* flagged) {
     const uint32_t nx = size, ny = size, nz = size + 1;
     const uint64_t npts = (uint64_t)nx * ny * nz;
     if (npts >= (1ull << 32)) return fail(ctx, ISO_ERR_TOO_LARGE, "more than 2^32 lattice points");
@@ -278,19 +419,53 @@ iso_status surrogate_field(iso_ctx* ctx, iso_mlp* net, const iso_program* exact,
     float* coarse = (float*)ctx->aux2.p;
     uint32_t* count = (uint32_t*)((char*)ctx->aux2.p + ((4 * ncoarse + 255) & ~255ull));
     uint32_t* list = (uint32_t*)ctx->aux.p;
-    if ((s = mlp_infer_launch(net, nullptr, 0, &g, coarse)) != ISO_OK) return s;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (flags & ISO_SURROGATE_EXACT_COARSE) {
+        StageTimer timer(ctx, ISO_STAGE_SAMPLE);
+        coarse_exact<<<(unsigned)sms * 8, 256, 0, ctx->stream>>>(exact->view(), g.nx, g.ny, g.nz, step, inv, coarse);
+        ctx->launches++;
+        if ((s = check_launch(ctx, "coarse exact")) != ISO_OK) return s;
+    } else if ((s = mlp_infer_launch(net, nullptr, 0, &g, coarse)) != ISO_OK) {
+        return s;
+    }
     cudaError_t e = cudaMemsetAsync(count, 0, 4, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "band count");
-    BandArgs b{coarse, g.nx, g.ny, g.nz, step, nx, ny, nz, 1.0f / (float)step, band * cell, field, pitch, list, count};
+    uint32_t* forced = nullptr;
+    uint32_t* sphere_flags = nullptr;
+    uint32_t nsph = 0;
+    if (flags & ISO_SURROGATE_WITNESS) {
+        const float* d_sph = nullptr;
+        float sk = 0.0f;
+        if (!sphere_list(exact, &d_sph, &nsph, &sk))
+            return fail(ctx, ISO_ERR_UNSUPPORTED, "witness checks need a sphere-set source");
+        const size_t mask_words = (npts + 31) / 32;
+        const size_t bytes = 4 * mask_words + 4 * ((size_t)nsph + 1) + 256;
+        if ((s = ensure(ctx, ctx->aux3, bytes)) != ISO_OK) return s;
+        forced = (uint32_t*)ctx->aux3.p;
+        sphere_flags = forced + ((mask_words + 63) & ~(size_t)63);
+        e = cudaMemsetAsync(ctx->aux3.p, 0, bytes, ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "witness scratch");
+        WitnessArgs w{exact->view(), d_sph, nsph, {g.scale[0], g.scale[1], g.scale[2]},
+                      {g.offset[0], g.offset[1], g.offset[2]}, inv, coarse, g.nx, g.ny, g.nz, step,
+                      2.0f * cell, std::max(band - 1.0f, 0.25f) * cell, sphere_flags};
+        ShellArgs sh{d_sph, sphere_flags, {g.scale[0], g.scale[1], g.scale[2]}, {g.offset[0], g.offset[1], g.offset[2]},
+                     inv, (band + 1.0f) * cell + 0.5f * sk, nx, ny, nz, forced};
+        StageTimer timer(ctx, ISO_STAGE_OTHER);
+        witness_check<<<blocks_for(7ull * nsph, 256), 256, 0, ctx->stream>>>(w);
+        witness_shells<<<nsph, 256, 0, ctx->stream>>>(sh);
+        ctx->launches += 2;
+        if ((s = check_launch(ctx, "witness checks")) != ISO_OK) return s;
+    }
+    BandArgs b{coarse, g.nx, g.ny, g.nz, step, nx, ny, nz, 1.0f / (float)step, band * cell, field, pitch, list, count,
+               forced};
     {
         StageTimer timer(ctx, ISO_STAGE_OTHER);
         band_mark<<<dim3(blocks_for(nx, 128), ny, nz), 128, 0, ctx->stream>>>(b);
     }
     ctx->launches++;
     if ((s = check_launch(ctx, "band mark")) != ISO_OK) return s;
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     ExactArgs x{exact->view(), list, count, nx, ny, inv, field, pitch};
     {
         StageTimer timer(ctx, ISO_STAGE_SAMPLE);
@@ -298,13 +473,19 @@ iso_status surrogate_field(iso_ctx* ctx, iso_mlp* net, const iso_program* exact,
     }
     ctx->launches++;
     if ((s = check_launch(ctx, "band exact")) != ISO_OK) return s;
-    if (stats) {
+    if (stats || flagged) {
         e = cudaMemcpyAsync(ctx->h_pinned, count, 4, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess && sphere_flags)
+            e = cudaMemcpyAsync((uint32_t*)ctx->h_pinned + 1, sphere_flags + nsph, 4, cudaMemcpyDeviceToHost,
+                                ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "band stats");
-        stats->coarse_points = ncoarse;
-        stats->band_points = *(uint32_t*)ctx->h_pinned;
-        stats->total_points = npts;
+        if (stats) {
+            stats->coarse_points = ncoarse;
+            stats->band_points = *(uint32_t*)ctx->h_pinned;
+            stats->total_points = npts;
+        }
+        if (flagged) *flagged = sphere_flags ? ((uint32_t*)ctx->h_pinned)[1] : 0;
     }
     return ISO_OK;
 }
@@ -323,7 +504,29 @@ iso_status iso_surrogate_field(iso_ctx* ctx, iso_mlp* net, const iso_program* ex
     iso_status s = check_args(ctx, net, exact, size, coarse_step, band_cells);
     if (s != ISO_OK) return s;
     if (!field || pitch < size) return fail(ctx, ISO_ERR_INVALID_ARG, "need a field with pitch >= size");
-    if ((s = surrogate_field(ctx, net, exact, size, coarse_step, band_cells, field, pitch, stats)) != ISO_OK) return s;
+    if ((s = surrogate_field(ctx, net, exact, size, coarse_step, band_cells, 0, field, pitch, stats, nullptr)) !=
+        ISO_OK)
+        return s;
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "surrogate field");
+    return read_device_errors(ctx);
+}
+
+iso_status iso_surrogate_field_ex(iso_ctx* ctx, iso_mlp* net, const iso_program* exact, uint32_t size,
+                                  uint32_t coarse_step, float band_cells, uint32_t flags, float* field, uint64_t pitch,
+                                  iso_surrogate_stats* stats, uint64_t* flagged_primitives) {
+    iso::NvtxRange nvtx_range("iso_surrogate_field_ex");
+    if (flags & ~(uint32_t)(ISO_SURROGATE_EXACT_COARSE | ISO_SURROGATE_WITNESS)) {
+        if (ctx) fail(ctx, ISO_ERR_INVALID_ARG, "unknown flags");
+        return ISO_ERR_INVALID_ARG;
+    }
+    iso_status s = check_args(ctx, net, exact, size, coarse_step, band_cells,
+                              !(flags & ISO_SURROGATE_EXACT_COARSE));
+    if (s != ISO_OK) return s;
+    if (!field || pitch < size) return fail(ctx, ISO_ERR_INVALID_ARG, "need a field with pitch >= size");
+    if ((s = surrogate_field(ctx, net, exact, size, coarse_step, band_cells, flags, field, pitch, stats,
+                             flagged_primitives)) != ISO_OK)
+        return s;
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "surrogate field");
     return read_device_errors(ctx);
@@ -342,7 +545,9 @@ iso_status iso_surrogate_extract(iso_ctx* ctx, iso_mlp* net, const iso_program* 
     if ((s = ensure(ctx, ctx->field, 4 * pitch * ny * nz)) != ISO_OK) return s;
     if ((s = ensure(ctx, ctx->bits, 4ull * W * ny * nz)) != ISO_OK) return s;
     float* field = (float*)ctx->field.p;
-    if ((s = surrogate_field(ctx, net, exact, size, coarse_step, band_cells, field, pitch, stats)) != ISO_OK) return s;
+    if ((s = surrogate_field(ctx, net, exact, size, coarse_step, band_cells, 0, field, pitch, stats, nullptr)) !=
+        ISO_OK)
+        return s;
     if ((s = launch_sign_bits(ctx, field, nx, ny, nz, pitch, (uint32_t*)ctx->bits.p)) != ISO_OK) return s;
     Lattice L{nx, ny, nz, pitch, field, (const uint32_t*)ctx->bits.p, W, 1.0f / (float)(nx - 1), nullptr};
     return mc_extract_lattice(ctx, L, flags, info);

@@ -7,7 +7,8 @@ import os
 
 import numpy as np
 
-from ._capi import ISO_FLAG_KEYS, MeshDistance, MeshInfo, SurrogateStats, check, lib
+from ._capi import (ISO_FLAG_KEYS, ISO_SURROGATE_EXACT_COARSE, ISO_SURROGATE_WITNESS, MeshDistance, MeshInfo,
+                    SurrogateStats, check, lib)
 
 f32p = ctypes.POINTER(ctypes.c_float)
 
@@ -90,6 +91,23 @@ class Surrogate:
                                         band_cells, ctypes.c_void_p(field_ptr), pitch, ctypes.byref(st)),
               self.ctx.h)
         return _stats(st)
+
+    def field_ex(self, exact_source, size, field_ptr, pitch, coarse_step=4, band_cells=2.0, exact_coarse=False,
+                 witness=False):
+        """iso_surrogate_field_ex: exact_coarse builds the coarse grid from the
+        exact source instead of the network (the pipeline without the
+        network); witness adds the spot checks at the sphere-set source's
+        witness points.  Returns the band statistics with the number of
+        flagged spheres."""
+        st, flagged = SurrogateStats(), ctypes.c_uint64()
+        flags = (ISO_SURROGATE_EXACT_COARSE if exact_coarse else 0) | (ISO_SURROGATE_WITNESS if witness else 0)
+        check(lib().iso_surrogate_field_ex(self.ctx.h, None if exact_coarse else self.h,
+                                           self.ctx.program(exact_source).h, size, coarse_step, band_cells, flags,
+                                           ctypes.c_void_p(field_ptr), pitch, ctypes.byref(st), ctypes.byref(flagged)),
+              self.ctx.h)
+        out = _stats(st)
+        out["flagged"] = int(flagged.value)
+        return out
 
     def extract(self, exact_source, size, coarse_step=4, band_cells=2.0, keys=False):
         """Marching cubes over the surrogate field; the mesh stays in the

@@ -184,3 +184,100 @@ def test_ablation_band_resampling(ctx):
     assert st2["band_points"] < 0.5 * st2["total_points"]
     assert d2["chamfer"] < d0["chamfer"]
     net.close()
+
+
+def test_exact_coarse_field_composition(ctx):
+    """ISO_SURROGATE_EXACT_COARSE: the same pipeline with the network replaced
+    by the exact source on the coarse grid -- exact inside the band, the
+    interpolated exact coarse values outside it."""
+    size, step, band = 33, 4, 1.5
+    src = scenes.smooth_spheres(count=64)
+    field, pitch = _device_field(size)
+    net = Surrogate(ctx, seed=2)
+    st = net.field_ex(src, size, field.data_ptr(), pitch, coarse_step=step, band_cells=band, exact_coarse=True)
+    got = field.cpu().numpy().reshape(size + 1, size, pitch)
+    exact_t, _ = _device_field(size)
+    ctx.sample_grid(src, size, exact_t.data_ptr(), pitch)
+    exact = exact_t.cpu().numpy().reshape(size + 1, size, pitch)
+    dims, _ = _coarse_points(size, step)
+    # coarse point (i, j, k) is lattice point (i, j, k) * step (the last ones
+    # may lie beyond the grid): the exact source there, in the sample frame
+    inv = np.float32(1.0) / np.float32(size - 1)
+    ax = [np.arange(d, dtype=np.float32) * np.float32(step) * inv for d in dims]
+    zz, yy, xx = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    coarse = ctx.sample_points(src, np.stack([xx.ravel(), yy.ravel(), zz.ravel()], 1))
+    interp = _interp(coarse, dims, size, step)
+    tau = np.float32(band) * (np.float32(1.0) / np.float32(size - 1)) * np.float32(2.0)
+    sure_band = np.abs(interp) <= tau * 0.999 - 1e-5
+    sure_out = np.abs(interp) > tau * 1.001 + 1e-5
+    assert sure_band.any() and sure_out.any()
+    assert np.array_equal(got[sure_band].view(np.uint32), exact[sure_band].view(np.uint32))
+    assert np.max(np.abs(got[sure_out] - interp[sure_out])) <= 1e-6
+    assert st["flagged"] == 0
+    net.close()
+
+
+def test_witness_checks_force_missed_spheres_into_the_band(ctx):
+    """ISO_SURROGATE_WITNESS with a network that says "outside" everywhere
+    (zero weights, output bias 1): without the checks the band is empty and
+    so is the mesh; with them every sphere is flagged at its centre, its ball
+    and shell are re-sampled exactly, and the mesh is the exact mesh.  A
+    source that is not a sphere set is refused."""
+    from isosurface_gb300 import IsoError
+    size = 65
+    src = scenes.smooth_spheres(count=64)
+    net = Surrogate(ctx, seed=5)
+    p = np.zeros(net.nparams, np.float32)
+    p[-1] = 1.0
+    net.params = p
+    cell = 1.0 / (size - 1)
+    exact = ctx.download(ctx.mc_extract(src, size))
+    out = {}
+    for witness in (False, True):
+        field, pitch = _device_field(size)
+        st = net.field_ex(src, size, field.data_ptr(), pitch, coarse_step=4, band_cells=2.0, witness=witness)
+        m = ctx.download(ctx.mc_extract_field(field.data_ptr(), size, size, size + 1, pitch))
+        d = mesh_distance(ctx, m.vertices, exact.vertices, 2 * cell, max_rings=64) if len(m.vertices) else None
+        out[witness] = (st, m, d)
+    st0, m0, d0 = out[False]
+    st1, m1, d1 = out[True]
+    assert st0["flagged"] == 0 and st0["band_points"] == 0 and len(m0.vertices) == 0
+    assert st1["flagged"] == 64
+    assert st1["band_points"] < st1["total_points"]
+    # every sphere the untrained network misses is re-sampled: the exact mesh
+    assert np.array_equal(m1.vertices, exact.vertices) and np.array_equal(m1.indices, exact.indices)
+    with pytest.raises(IsoError):
+        field, pitch = _device_field(size)
+        net.field_ex(scenes.csg(), size, field.data_ptr(), pitch, witness=True)
+    net.close()
+
+
+def test_what_the_network_gains(ctx):
+    """The comparison the surrogate exists for: network + band re-sampling
+    against the same pipeline with the network replaced by exact samples of
+    the coarse grid, at the same band.  With the network the exact source is
+    evaluated only in the band (the coarse grid costs no exact evaluation);
+    without it every coarse point is an exact evaluation too.  Both meshes
+    are scored against the exact mesh."""
+    size, step, band = 129, 2, 2.0
+    src = scenes.smooth_spheres(count=1024)
+    net = Surrogate(ctx, seed=3)
+    net.make_dataset(src.source, 1 << 21, -1.0, 1.0, seed=4)
+    net.train(800, batch=16384, lr=2e-3)
+    cell = 1.0 / (size - 1)
+    exact = ctx.download(ctx.mc_extract(src, size))
+    res = {}
+    for exact_coarse in (False, True):
+        field, pitch = _device_field(size)
+        st = net.field_ex(src, size, field.data_ptr(), pitch, coarse_step=step, band_cells=band,
+                          exact_coarse=exact_coarse, witness=True)
+        m = ctx.download(ctx.mc_extract_field(field.data_ptr(), size, size, size + 1, pitch))
+        d = mesh_distance(ctx, m.vertices, exact.vertices, 2 * cell, max_rings=64)
+        exact_evals = st["band_points"] + (st["coarse_points"] if exact_coarse else 0)
+        res[exact_coarse] = (st, d, exact_evals)
+    (stn, dn, en), (ste, de, ee) = res[False], res[True]
+    assert en < ee                          # the network saves the coarse grid's exact evaluations
+    assert stn["coarse_points"] == ste["coarse_points"]
+    assert dn["chamfer"] <= 0.05 * cell     # both close to the exact mesh
+    assert de["chamfer"] <= 0.05 * cell
+    net.close()
