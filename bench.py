@@ -105,6 +105,110 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# the kernels whose DRAM traffic profiles/traffic.json records; a capture
+# counts only for the sources it was taken from
+TRAFFIC_SOURCES = ["isosurface_gb300/csrc/" + f for f in
+                   ("mc.cu", "mc_chunk.cuh", "mc_tables.h", "sample.cu", "vm.cuh", "internal.h")]
+
+
+def kernel_sources_sha256():
+    import hashlib
+    h = hashlib.sha256()
+    for rel in TRAFFIC_SOURCES:
+        with open(os.path.join(ROOT, rel), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()
+
+
+def measured_traffic():
+    """DRAM bytes (read + write) per extraction of the extraction kernels,
+    from the ncu capture recorded in profiles/traffic.json, or None when that
+    capture was taken from other kernel sources than the ones built now."""
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(tpath):
+        return None, "no ncu capture recorded"
+    t = json.load(open(tpath))
+    if t.get("sources_sha256") != kernel_sources_sha256():
+        return None, "the recorded ncu capture predates the current kernel sources"
+    return t["classify_scan"] + t["emit"], "ncu capture of these kernel sources (profiles/traffic.json)"
+
+
+def fp32_peak():
+    """Measured FP32 rate (FMA chains on every SM, CUDA events): TFLOP/s."""
+    import ctypes
+    from isosurface_gb300 import build as gbuild
+    L = ctypes.CDLL(gbuild.PEAK_LIB)
+    L.iso_fp32_fma_peak.restype = ctypes.c_int
+    L.iso_fp32_fma_peak.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                    ctypes.POINTER(ctypes.c_double)]
+    tf, ms = ctypes.c_double(), ctypes.c_double()
+    rc = L.iso_fp32_fma_peak(0, 10, ctypes.byref(tf), ctypes.byref(ms))
+    if rc != 0:
+        raise RuntimeError("fp32 peak probe failed: CUDA error %d" % rc)
+    return tf.value
+
+
+# flops per sphere of a hard union as the reference evaluates it: p - c (3),
+# |p - c| (3 mul, 2 add, 1 sqrt), minus r (1), min with the running value (1)
+FLOPS_PER_SPHERE = 11
+
+
+def sampler_fp32_workload(ctx, torch, timed):
+    """The sampler against the FP32 rate: the same 64-sphere union written as
+    nested Union(Translate(Sphere)) nodes, which the library samples with its
+    general evaluator (every sphere at every sample, no culling), into the
+    full f32 field of MarchingCubes::new(513); flops per sample = the domain
+    map (3 mul + 3 add) + 64 x FLOPS_PER_SPHERE."""
+    from isosurface_gb300 import scenes
+    from isosurface_gb300 import source as S
+    sph = scenes.random_spheres(1234, 64, 0.8, (0.05, 0.25))
+    node = None
+    for cx, cy, cz, r in sph:
+        t = S.Translate(S.Sphere(float(r)), (float(cx), float(cy), float(cz)))
+        node = t if node is None else S.Union(node, t)
+    src = S.unit_to_cube(node)
+    field = torch.empty((SIZE + 1) * SIZE * SIZE, dtype=torch.float32, device="cuda")
+    prog = ctx.program(src)
+    for _ in range(2):
+        ctx.sample_grid(prog, SIZE, field.data_ptr(), SIZE)
+    ms = timed(lambda: ctx.sample_grid(prog, SIZE, field.data_ptr(), SIZE), 5)
+    samples = SIZE * SIZE * (SIZE + 1)
+    flops = samples * (6 + 64 * FLOPS_PER_SPHERE)
+    peak = fp32_peak()
+    achieved = flops / (ms / 1e3) / 1e12
+    del field
+    return {"bound": "fp32", "workload": "64-sphere union (seed 1234) as nested Union(Translate(Sphere)), general "
+                                         "evaluator, full f32 field of MarchingCubes::new(513)",
+            "ms": ms, "flops_per_sample": 6 + 64 * FLOPS_PER_SPHERE, "achieved_tflops": achieved,
+            "peak_tflops": peak, "peak_source": "measured (FMA chains, libiso_fp32_peak)", "frac": achieved / peak}
+
+
+def mc_csg_workload(ctx, timed, steps):
+    """A general program at the headline size: MarchingCubes::new(513) of the
+    rigid-transformed CSG scene (box minus sphere, union torus), sampled by
+    the general evaluator (full f32 field), device-resident, CUDA events."""
+    import ctypes
+    from isosurface_gb300 import scenes
+    from isosurface_gb300._capi import lib
+    src = scenes.csg()
+    prog = ctx.program(src)
+    for _ in range(3):
+        info = ctx.mc_extract(prog, SIZE)
+    ms = timed(lambda: ctx.mc_extract(prog, SIZE), max(5, min(steps, 30)))
+    ms_buf = (ctypes.c_double * 8)()
+    ln_buf = (ctypes.c_uint64 * 8)()
+    lib().iso_ctx_stage_times(ctx.h, ms_buf, ln_buf)
+    lib().iso_ctx_enable_stage_timing(ctx.h, 1)
+    for _ in range(5):
+        ctx.mc_extract(prog, SIZE)
+    lib().iso_ctx_stage_times(ctx.h, ms_buf, ln_buf)
+    lib().iso_ctx_enable_stage_timing(ctx.h, 0)
+    stages = {name: ms_buf[i] / max(int(ln_buf[i]), 1) for name, i in (("sample", 0), ("classify_scan", 1),
+                                                                          ("emit", 2))}
+    return {"cells": CELLS, "ms": ms, "cells_per_s": CELLS / (ms / 1e3), "triangles": int(info.num_triangles),
+            "vertices": int(info.num_vertices), "stage_ms": stages}
+
+
 def cpu_baseline_port(src_bytes, budget_s=12.0, threads=1):
     """The oracle's MarchingCubes over a bounded middle slab of the same grid."""
     import oracle
@@ -123,11 +227,13 @@ def cpu_baseline_port(src_bytes, budget_s=12.0, threads=1):
 
 def secondary_workloads(ctx, torch, steps, only=None):
     """The other workloads, timed with CUDA events on the library's stream:
-    the 4096-chunk batch (one CUDA graph vs one extraction per chunk),
+    the sampler against the measured FP32 rate, MarchingCubes::new(513) of a
+    general CSG program, the 4096-chunk batch (one CUDA graph vs one
+    extraction per chunk),
     DualContouring at 256^3, LinearHashedMarchingCubes at depth 8, the
     reference's own benchmark shapes and the deferred point-splat frame
     (`only`: a set of names among refshapes, batch, dc, lhmc, splat to run
-    just those)."""
+    just those; names: sampler, csg, refshapes, batch, dc, lhmc, splat, emc)."""
     from isosurface_gb300 import scenes
     stream = torch.cuda.ExternalStream(ctx.stream)
 
@@ -142,6 +248,10 @@ def secondary_workloads(ctx, torch, steps, only=None):
 
     out = {}
     want = (lambda name: only is None or name in only)
+    if want("sampler"):
+        out["sampler_fp32_512"] = sampler_fp32_workload(ctx, torch, timed)
+    if want("csg"):
+        out["mc_512_csg"] = mc_csg_workload(ctx, timed, steps)
     if want("refshapes"):
         out["reference_bench_shapes"] = _reference_bench_shapes(ctx, timed, steps)
     if want("batch"):
@@ -304,11 +414,22 @@ def surrogate_workload(ctx, torch, train_steps):
            "train": {"samples": 1 << 24, "steps": train_steps, "batch": 65536, "seconds": train_s,
                      "loss_first": float(hist[0]), "loss_last": float(np.mean(hist[-20:]))},
            "exact_ms": exact_ms, "exact_triangles": int(info.num_triangles), "bands": {}}
+    # the least an exact mesh can re-sample: every end of a crossing edge lies
+    # within one lattice step of the exact surface (the field is 1-Lipschitz),
+    # and such points are this fraction of the grid, which bounds any
+    # band-re-sampling surrogate's speed-up by its inverse
+    near = int((field.view(nz, size, pitch)[:, :, :size].abs() <= 2.0 * cell).sum().item())
+    out["exact_fraction_within_one_step"] = near / float(nz * size * size)
+    out["speedup_bound"] = float(nz * size * size) / max(near, 1)
     ms_buf = (ctypes.c_double * 8)()
     ln_buf = (ctypes.c_uint64 * 8)()
-    for band in (1.0, 2.0):
+    variants = [("%g" % b, b, False, False) for b in (1.0, 2.0)]
+    variants += [("%g+witness" % b, b, False, True) for b in (1.5, 2.0, 3.0)]
+    variants += [("%g+witness, exact coarse grid (no network)" % b, b, True, True) for b in (1.0, 2.0)]
+    for name, band, exact_coarse, witness in variants:
         def surrogate_path():
-            st = net.field(src, size, sfield.data_ptr(), pitch, coarse_step=4, band_cells=band)
+            st = net.field_ex(src, size, sfield.data_ptr(), pitch, coarse_step=4, band_cells=band,
+                              exact_coarse=exact_coarse, witness=witness)
             return st, ctx.mc_extract_field(sfield.data_ptr(), size, size, nz, pitch)
 
         surrogate_path()
@@ -322,10 +443,13 @@ def surrogate_workload(ctx, torch, train_steps):
         m = ctx.download(sinfo)
         d = mesh_distance(ctx, m.vertices, exact.vertices, 2 * cell, max_rings=64)
         dis = case_disagreement(ctx, field.data_ptr(), sfield.data_ptr(), size, size, nz, pitch)
-        out["bands"]["%g" % band] = {
+        out["bands"][name] = {
             "ms": ms, "speedup_vs_exact": exact_ms / ms, "band_fraction": st["band_points"] / st["total_points"],
-            "network_points": st["coarse_points"], "network_ms": mlp_ms, "exact_resample_ms": band_ms,
-            "network_tflops": MLP_FLOPS_PER_POINT * st["coarse_points"] / (mlp_ms / 1e3) / 1e12,
+            "flagged_spheres": st["flagged"], "coarse_points": st["coarse_points"],
+            "coarse_from": "exact source" if exact_coarse else "network", "network_ms": mlp_ms,
+            "exact_resample_ms": band_ms,
+            "network_tflops": (MLP_FLOPS_PER_POINT * st["coarse_points"] / (mlp_ms / 1e3) / 1e12
+                               if not exact_coarse and mlp_ms > 0 else None),
             "chamfer_cells": d["chamfer"] / cell, "hausdorff_cells": d["hausdorff"] / cell,
             "distance_search_capped": d["capped"],
             "case_disagreement": dis / float((size - 1) * (size - 1) * size), "triangles": int(sinfo.num_triangles)}
@@ -381,7 +505,8 @@ def main():
     ap.add_argument("--no-secondary", action="store_true", help="skip the batch / DC / LHMC timings")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-surrogate workload")
     ap.add_argument("--secondary-only", default=None,
-                    help="comma list among refshapes,batch,dc,lhmc,splat,surrogate,emc: run only these secondary "
+                    help="comma list among sampler,csg,refshapes,batch,dc,lhmc,splat,surrogate,emc: run only these "
+                         "secondary "
                          "workloads (emc runs only when named)")
     ap.add_argument("--surrogate-train-steps", type=int, default=4000)
     args = ap.parse_args()
@@ -471,15 +596,11 @@ def main():
     algo = 4 * samples + 12 * nv + 12 * nt
     peak, peak_kind = peaks()
     achieved = algo / (extract_ms / 1e3) / 1e9
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        t = json.load(open(tpath))
-        if "classify_scan" in t and "emit" in t:
-            traffic = t["classify_scan"] + t["emit"]
+    traffic, traffic_note = measured_traffic()
     roofline = {"bound": "hbm", "kernel": "extraction (mc_chunk_count, mc_range_scan, mc_cell_emit, mc_resolve_ids)",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                "traffic": traffic, "algorithmic_bytes": algo, "ms_per_launch": extract_ms,
+                "traffic": traffic, "traffic_source": traffic_note, "algorithmic_bytes": algo,
+                "ms_per_launch": extract_ms,
                 "sampler": {"ms_per_launch": per_stage["sample"]["ms_per_launch"],
                             "bytes_written": 4 * words * SIZE * (SIZE + 1) + 8 * nv,
                             "note": "sign bits of every sample and exact values only near the surface"}}

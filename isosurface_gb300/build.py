@@ -17,6 +17,10 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libisosurface_gpu.so")
+# the FP32 FMA-rate probe the benchmark reports the sampler against (not part
+# of the extraction library)
+PEAK_SRC = os.path.join(CSRC, "fp32_peak.cu")
+PEAK_LIB = os.path.join(OUT_DIR, "libiso_fp32_peak.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -55,8 +59,20 @@ def _compile(unit, flags):
     return obj
 
 
+def _build_peak(force):
+    if not force and os.path.exists(PEAK_LIB) and os.path.getmtime(PEAK_LIB) >= os.path.getmtime(PEAK_SRC):
+        return
+    cmd = [NVCC, *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "-cudart", "shared", PEAK_SRC,
+           "-o", PEAK_LIB + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed for fp32_peak.cu:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    os.replace(PEAK_LIB + ".tmp", PEAK_LIB)
+
+
 def build(force=False, verbose=False):
     os.makedirs(OUT_DIR, exist_ok=True)
+    _build_peak(force)
     if not force and os.path.exists(LIB):
         if os.path.getmtime(LIB) >= max(os.path.getmtime(p) for p in _deps()):
             return LIB
