@@ -127,6 +127,13 @@ __device__ __forceinline__ uint32_t cell_case(const uint32_t* a, const uint32_t*
            ((vc >> 1) & 1u) << 5 | ((vd >> 1) & 1u) << 6 | (vd & 1u) << 7;
 }
 
+// Programmatic dependent launch: a kernel launched with launch_pdl may start
+// while its predecessor on the stream still runs; pdl_wait blocks until that
+// predecessor has completed and its writes are visible, pdl_trigger lets the
+// next kernel start early.  Both are no-ops in a kernel launched without it.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ uint32_t warp_sum(uint32_t v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
     return v;
@@ -577,6 +584,21 @@ iso_status mc_cases_lattice(iso_ctx* ctx, const Lattice& L, uint8_t* d_cases) {
 namespace {
 __global__ void write_grid(Grid* dst, Grid g) { *dst = g; }
 
+template <typename... P, typename... A>
+cudaError_t launch_pdl(void (*kernel)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream, A... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 
 // cudaFuncSetAttribute only when the size grows (per device; it costs a host round trip)
 cudaError_t emit_smem_attribute(size_t smem) {
@@ -657,9 +679,13 @@ static iso_status mc_lattice_passes(iso_ctx* ctx, const Lattice& L, uint32_t fla
         ChunkCountArgs ca{d_grid, nullptr, (uint32_t)chunks, edge_map ? nullptr : local, rangeagg, segs, blockagg};
         if (edge_map) {
             // range prefixes inside blocks of 8 ranges; one scan over the block totals
-            mc_chunk_count<true><<<nblocks, 256, 0, ctx->stream>>>(ca);
-            mc_range_scan<<<1, 1024, 0, ctx->stream>>>(blockagg, nblocks, blockpre, totals, nullptr, (uint32_t)chunks,
-                                                       ctx->d_err);
+            // chained with programmatic dependent launch: each kernel starts
+            // while its predecessor finishes and waits for it on the device
+            e = launch_pdl(mc_chunk_count<true>, dim3(nblocks), dim3(256), 0, ctx->stream, ca);
+            if (e == cudaSuccess)
+                e = launch_pdl(mc_range_scan, dim3(1), dim3(1024), 0, ctx->stream, (const uint2*)blockagg, nblocks,
+                               blockpre, totals, (uint2*)nullptr, (uint32_t)chunks, ctx->d_err);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "count launch");
         } else {
             mc_chunk_count<false><<<nblocks, 256, 0, ctx->stream>>>(ca);
             mc_range_scan<<<1, 1024, 0, ctx->stream>>>(rangeagg, nranges, rangepre, totals, local, (uint32_t)chunks,
@@ -679,10 +705,13 @@ static iso_status mc_lattice_passes(iso_ctx* ctx, const Lattice& L, uint32_t fla
         {
             StageTimer timer(ctx, ISO_STAGE_EMIT);
             if (edge_map) {
-                mc_cell_emit<<<(nsegs + 8 * EMIT_SEGS - 1) / (8 * EMIT_SEGS), 256, 0, ctx->stream>>>(ea, segs, nsegs);
-                mc_resolve_ids<<<resolve_blocks(cap_t), 256, 0, ctx->stream>>>(
-                    (uint32_t*)ctx->mesh_i.p, totals, cap_t, (const uint32_t*)ctx->edges.p, (uint32_t)nedges, H.i,
-                    H.cap_v, H.cap_t, cap_v);
+                cudaError_t le = launch_pdl(mc_cell_emit, dim3((nsegs + 8 * EMIT_SEGS - 1) / (8 * EMIT_SEGS)),
+                                            dim3(256), 0, ctx->stream, ea, (const uint4*)segs, nsegs);
+                if (le == cudaSuccess)
+                    le = launch_pdl(mc_resolve_ids, dim3(resolve_blocks(cap_t)), dim3(256), 0, ctx->stream,
+                                    (uint32_t*)ctx->mesh_i.p, (const uint64_t*)totals, cap_t,
+                                    (const uint32_t*)ctx->edges.p, (uint32_t)nedges, H.i, H.cap_v, H.cap_t, cap_v);
+                if (le != cudaSuccess) return cuda_fail(ctx, le, "emit launch");
                 ctx->launches++;
             } else {
                 mc_block_emit<<<(unsigned)((chunks + 255) / 256), 256, smem, ctx->stream>>>(ea, CW);

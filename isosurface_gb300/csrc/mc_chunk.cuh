@@ -121,6 +121,8 @@ __global__ void __launch_bounds__(256) mc_chunk_count(ChunkCountArgs A) {
     __shared__ uint32_t s_tri[8][32];  // chunk mode, per warp: triangles of each of the round's chunks
     __shared__ ChunkStage<SEG ? 64 : 2> s_pair[8];  // segment mode, per warp: two rounds of chunks
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    pdl_wait();     // the grid record and the sign bits
+    pdl_trigger();
     s_ntri[threadIdx.x] = iso_tri_count[threadIdx.x];
     if (threadIdx.x < 8) s_owned[threadIdx.x] = iso_owned_mask[threadIdx.x];
     __syncthreads();
@@ -284,6 +286,8 @@ __global__ void __launch_bounds__(1024) mc_range_scan(const uint2* rangeagg, uin
                                                       uint64_t* totals, uint2* local, uint32_t chunks, uint32_t* err) {
     __shared__ uint64_t s_wv[32], s_wt[32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    pdl_wait();     // the counting pass's totals
+    pdl_trigger();
     uint64_t carry_t = 0, carry_v = 0;
     for (uint32_t base = 0; base < nr; base += 1024 * SCAN_ITEMS) {
         const uint32_t i0 = base + threadIdx.x * SCAN_ITEMS;
@@ -783,22 +787,11 @@ __device__ __forceinline__ void emit_cells(const ChunkEmitArgs& A, const Grid& g
 __global__ void __launch_bounds__(256, 5) mc_cell_emit(ChunkEmitArgs A, const uint4* segs, uint32_t nsegs) {
     __shared__ EmitChunks s_ch[8];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    pdl_trigger();
     const uint32_t seg0 = (blockIdx.x * 8 + warp) * EMIT_SEGS;  // the warp's first segment
     if (seg0 >= nsegs) return;
-    // records: (first vertex, first triangle) in the range, (vertices, triangles)
-    const uint4 sr = __ldg(&segs[seg0]);
-    uint32_t nv_w = sr.z, nt_w = sr.w;
-#pragma unroll
-    for (int h = 1; h < EMIT_SEGS; ++h)
-        if (seg0 + h < nsegs) {
-            const uint4 r = __ldg(&segs[seg0 + h]);
-            nv_w += r.z;
-            nt_w += r.w;
-        }
-    if (nt_w == 0) return;  // no triangle in the warp's segments
-    const uint32_t range = seg0 / (RANGE / 32);  // EMIT_SEGS divides the 8 segments of a range
-    const uint2 rin = __ldg(&A.rangepre[range]), rb = __ldg(&A.blockpre[range / 8]);
-    const uint32_t vbase = rb.x + rin.x + sr.x, tbase = rb.y + rin.y + sr.y;
+    // the staging below reads only the sign bits and the grid record, which
+    // the counting pass's predecessors wrote: it overlaps the counting pass
     const Grid g = A.grids[0];
     const uint32_t rc = seg0 * 32, c_end = min(rc + (uint32_t)EMIT_CH, g.nchunks);
     EmitChunks& S = s_ch[warp];
@@ -827,6 +820,17 @@ __global__ void __launch_bounds__(256, 5) mc_cell_emit(ChunkEmitArgs A, const ui
         S.excl[32 * h + lane] = total + incl - n;
         total += __shfl_sync(FULL, incl, 31);
     }
+    if (total == 0) return;  // no active cell: no vertex, no triangle
+    pdl_wait();              // the counts and their scan
+    // records: (first vertex, first triangle) in the range, (vertices, triangles)
+    const uint4 sr = __ldg(&segs[seg0]);
+    uint32_t nv_w = sr.z;
+#pragma unroll
+    for (int h = 1; h < EMIT_SEGS; ++h)
+        if (seg0 + h < nsegs) nv_w += __ldg(&segs[seg0 + h]).z;
+    const uint32_t range = seg0 / (RANGE / 32);  // EMIT_SEGS divides the 8 segments of a range
+    const uint2 rin = __ldg(&A.rangepre[range]), rb = __ldg(&A.blockpre[range / 8]);
+    const uint32_t vbase = rb.x + rin.x + sr.x, tbase = rb.y + rin.y + sr.y;
     __syncwarp();
     uint32_t koff = 0;
     if (lane < 12) {
@@ -864,6 +868,7 @@ __global__ void __launch_bounds__(256) mc_resolve_ids(uint32_t* __restrict__ idx
                                                       uint64_t cap_t, const uint32_t* __restrict__ edge_id,
                                                       uint32_t nedges, uint32_t* host_i, uint64_t host_cap_v,
                                                       uint64_t host_cap_t, uint64_t cap_v) {
+    pdl_wait();  // the emitted keys and the edge map
     const uint64_t n = 3 * min(totals[0], cap_t);
     const bool to_host = mesh_to_host(reinterpret_cast<const float*>(host_i), totals, host_cap_v, host_cap_t, cap_v,
                                       cap_t);
