@@ -22,8 +22,8 @@ kernels (profiles/traffic.json).
 single-threaded Rust CPU path; Rust does not build here) on all host cores,
 each step a bounded slab of the same grid.
 
-Multi-GPU: one process per GPU under torchrun runs an independent replica of
-the workload (the extraction has no cross-GPU exchange); value sums them.
+Multi-GPU (torchrun, N > 1): the grid is split into N z-slabs, one per GPU,
+with one all-gather of two counts per rank (run_sharded; strong scaling).
 """
 import argparse
 import json
@@ -270,7 +270,7 @@ def secondary_workloads(ctx, torch, steps, only=None):
         out["lhmc_depth8"] = {"dual_cubes": int(info.num_cells), "ms": ms, "triangles": int(info.num_triangles)}
     if want("splat"):
         out["point_splat_1024x768"] = _point_splat_frame(ctx, steps)
-    if only is not None and "emc" in only:  # on request only
+    if want("emc"):
         out["emc_128"] = _emc_workload(ctx, timed, steps)
     return out
 
@@ -353,9 +353,12 @@ def _batch_workload(ctx, timed, steps):
     graph_ms = timed(lambda: batch.run(graph=True), max(3, min(steps, 20)))
     info = batch.run(graph=True)
     per_ms = timed(batch.run_per_chunk, 2)
+    batch.run_per_chunk_async()
+    async_ms = timed(batch.run_per_chunk_async, 3)
     cells = info.num_cells
     out["batch_4096_chunks"] = {"cells": int(cells), "graph_ms": graph_ms, "per_chunk_ms": per_ms,
-                                "speedup": per_ms / graph_ms, "cells_per_s": cells / (graph_ms / 1e3),
+                                "per_chunk_no_sync_ms": async_ms, "speedup": per_ms / graph_ms,
+                                "speedup_vs_no_sync": async_ms / graph_ms, "cells_per_s": cells / (graph_ms / 1e3),
                                 "triangles": int(info.num_triangles), "slab_depth_by_size": chosen}
     batch.close()
     return out
@@ -493,6 +496,68 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def run_sharded(args, torch, dist, world, rank, ctx, stream, src):
+    """N > 1: the grid split into N z-slabs, one per GPU (isosurface_gb300/slabs.py):
+    each rank samples and meshes its cell layers plus one halo layer, the
+    ranks exchange their (vertices, triangles) counts with one NCCL
+    all-gather, and each renumbers its triangles into the whole mesh.  Strong
+    scaling: the whole 512^3 grid per step across the N GPUs.  `value` times
+    the device extraction and the exchange with CUDA events (max over
+    ranks); `e2e` adds the mesh's copy to host memory and the renumbering on
+    the host.  Not measured on hardware: this pool lends one GPU per run."""
+    from isosurface_gb300 import replicas, slabs
+    z0, z1 = slabs.slab_bounds(SIZE, world)[rank]
+    prog = ctx.program(src)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def step():
+        info, hv, ht = ctx.mc_extract_slab(prog, SIZE, z0, z1, keys=True)
+        slabs.all_gather_counts(info.num_vertices - hv, info.num_triangles - ht, dist)
+        return info, hv, ht
+
+    for _ in range(args.warmup):
+        step()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    dist.barrier()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    launches0 = ctx.kernel_launches
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xFF)
+            starts[k].record(stream)
+        step()
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    dist.barrier()
+    launches = ctx.kernel_launches - launches0
+    clk = clocks.stop()
+    ms = replicas.max_over_ranks(sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / args.steps, dist, "cuda")
+    e2e_times = []
+    for k in range(max(3, min(args.steps, 50))):
+        flush.fill_(k & 0xFF)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        v, i, base, tbase = slabs.extract_sharded(lambda a, b: slabs.extract_slab_device(ctx, prog, SIZE, a, b),
+                                                  SIZE, rank, world, dist)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = replicas.max_over_ranks(sum(e2e_times) / len(e2e_times), dist, "cuda")
+    if rank == 0:
+        out = {"metric": METRIC, "value": CELLS / (ms / 1e3), "unit": "cells/s", "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "strong",
+               "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+               "config": dict(WORKLOAD, parallelism="z-slabs x%d (one NCCL all-gather of 2 counts per rank)" % world),
+               "e2e": {"value": CELLS / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": 0,
+                       "d2h_bytes_per_step": 12 * len(v) + 4 * len(i), "ms_per_step": 1e3 * e2e_s,
+                       "note": "rank 0's slab bytes"},
+               "gpu_launches": int(launches), "clocks": clk, "roofline": None, "cpu_baseline": None}
+        print(json.dumps(out))
+    ctx.close()
+    dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -533,6 +598,9 @@ def main():
     ctx = Context(local)
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
+    if world > 1:
+        run_sharded(args, torch, dist, world, rank, ctx, stream, src)
+        return
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     def barrier():

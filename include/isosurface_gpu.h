@@ -275,6 +275,23 @@ ISO_API iso_status iso_mc_extract_field_noalloc(const float* field, uint32_t nx,
                                                 uint32_t* indices, uint64_t triangle_cap, void* stream,
                                                 iso_mesh_info* info);
 
+/* One slab of a z-partition of MarchingCubes::new(size) across GPUs (the
+ * reference is single-threaded and has no counterpart): the cell layers
+ * [z_begin, z_end), 0 <= z_begin < z_end <= size.  The slab samples and
+ * meshes one extra cell layer below it when z_begin > 0 (the halo layer
+ * z_begin - 1, sampled by this GPU, so no field data crosses GPUs) and
+ * leaves in the context the mesh of the layers [z_begin - halo, z_end) with
+ * vertex positions (and, with ISO_FLAG_KEYS, keys) in the whole grid's
+ * frame: its first *halo_vertices vertices and *halo_triangles triangles are
+ * the halo layer's (both 0 when z_begin == 0).  The mesh of the whole grid is
+ * the slabs' meshes in slab order with the halo parts dropped and the
+ * indices moved by the slab's first vertex (one exchange of the slabs'
+ * vertex counts): isosurface_gb300/slabs.py does that, byte-identical to
+ * iso_mc_extract.  Synchronous. */
+ISO_API iso_status iso_mc_extract_slab(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t z_begin,
+                                       uint32_t z_end, uint32_t flags, iso_mesh_info* info, uint64_t* halo_vertices,
+                                       uint64_t* halo_triangles);
+
 /* Case index of every cell of MarchingCubes::new(size) (the bits of
  * classify_corners, marching_cubes_impl.rs:26-37) into host memory:
  * size x (size-1) x (size-1) bytes, traversal order (z, y, x). */
@@ -336,6 +353,11 @@ ISO_API iso_status iso_batch_destroy(iso_batch* batch);
 ISO_API iso_status iso_batch_run(iso_batch* batch, uint32_t flags, iso_mesh_info* info);
 /* The same chunks one extraction at a time (the per-chunk-launch baseline). */
 ISO_API iso_status iso_batch_run_per_chunk(iso_batch* batch, iso_mesh_info* info);
+/* The same per-chunk comparison without a host synchronisation per chunk:
+ * each chunk's sampler, count, scan and emit launched back to back into the
+ * place and size the batch's previous run found for it (run the batch once
+ * first), one synchronisation at the start and one at the end. */
+ISO_API iso_status iso_batch_run_per_chunk_async(iso_batch* batch, iso_mesh_info* info);
 ISO_API iso_status iso_batch_extents(iso_batch* batch, uint32_t* extents /* 4 per chunk */);
 /* Sampler slab depth (z layers per work-queue tile) for chunks of `size`
  * (0: all sizes); depth 0 = whole chunk. */

@@ -87,6 +87,8 @@ SIGNATURES = {
     "iso_host_unregister": (i32, [vp]),
     "iso_mc_extract_field": (i32, [vp, vp, u32, u32, u32, u64, u32, ctypes.POINTER(MeshInfo)]),
     "iso_mc_extract_field_noalloc": (i32, [vp, u32, u32, u32, u64, vp, u64, vp, u64, vp, ctypes.POINTER(MeshInfo)]),
+    "iso_mc_extract_slab": (i32, [vp, vp, u32, u32, u32, u32, ctypes.POINTER(MeshInfo), ctypes.POINTER(u64),
+                                  ctypes.POINTER(u64)]),
     "iso_mc_cases": (i32, [vp, vp, u32, u8p]),
     "iso_point_cloud_extract": (i32, [vp, vp, u32, u32, ctypes.POINTER(MeshInfo)]),
     "iso_emc_extract": (i32, [vp, vp, u32, u32, ctypes.POINTER(MeshInfo), ctypes.POINTER(ctypes.c_uint64)]),
@@ -97,6 +99,7 @@ SIGNATURES = {
     "iso_batch_destroy": (i32, [vp]),
     "iso_batch_run": (i32, [vp, u32, ctypes.POINTER(MeshInfo)]),
     "iso_batch_run_per_chunk": (i32, [vp, ctypes.POINTER(MeshInfo)]),
+    "iso_batch_run_per_chunk_async": (i32, [vp, ctypes.POINTER(MeshInfo)]),
     "iso_batch_extents": (i32, [vp, u32p]),
     "iso_batch_set_slab": (i32, [vp, u32, u32]),
     "iso_batch_autotune": (i32, [vp, ctypes.c_char_p, u32p]),

@@ -160,6 +160,17 @@ class Context:
                                          ctypes.byref(info)), self.h)
         return info
 
+    def mc_extract_slab(self, source, size, z_begin, z_end, keys=False):
+        """One slab of a z-partition of MarchingCubes::new(size): cell layers
+        [z_begin, z_end) plus the halo layer below when z_begin > 0.  Returns
+        (MeshInfo, halo vertices, halo triangles); see slabs.py."""
+        info = MeshInfo()
+        hv, ht = ctypes.c_uint64(), ctypes.c_uint64()
+        flags = self._flags(keys, False)
+        check(lib().iso_mc_extract_slab(self.h, self.program(source).h, size, z_begin, z_end, flags,
+                                        ctypes.byref(info), ctypes.byref(hv), ctypes.byref(ht)), self.h)
+        return info, int(hv.value), int(ht.value)
+
     def mc_cases(self, source, size):
         out = np.empty((size, size - 1, size - 1), np.uint8)
         check(lib().iso_mc_cases(self.h, self.program(source).h, size,
@@ -312,6 +323,14 @@ class Batch:
         info = MeshInfo()
         self.ctx._vertex_floats = 3
         check(lib().iso_batch_run_per_chunk(self.h, ctypes.byref(info)), self.ctx.h)
+        return info
+
+    def run_per_chunk_async(self):
+        """One extraction per chunk with no host synchronisation per chunk
+        (the batch must have run once)."""
+        info = MeshInfo()
+        self.ctx._vertex_floats = 3
+        check(lib().iso_batch_run_per_chunk_async(self.h, ctypes.byref(info)), self.ctx.h)
         return info
 
     def set_slab(self, size, depth):

@@ -125,6 +125,9 @@ struct iso_batch {
     void* graph_v = nullptr;
     void* graph_i = nullptr;
     bool sized = false;
+    // iso_batch_run_per_chunk_async: each chunk as a grid of its own
+    void* d_solo_grids = nullptr;
+    std::vector<uint32_t> solo_chunks, solo_cw;
 };
 
 namespace {
@@ -310,6 +313,7 @@ iso_status iso_batch_destroy(iso_batch* b) {
     if (b->graph) cudaGraphDestroy(b->graph);
     if (b->d_tiles) cudaFree(b->d_tiles);
     if (b->arena) cudaFree(b->arena);
+    if (b->d_solo_grids) cudaFree(b->d_solo_grids);
     delete b;
     return ISO_OK;
 }
@@ -434,6 +438,65 @@ iso_status iso_batch_run_per_chunk(iso_batch* b, iso_mesh_info* info) {
     cudaMemcpyAsync(b->d_extents, ext.data(), 4 * ext.size(), cudaMemcpyHostToDevice, ctx->stream);
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "per-chunk run");
+    uint64_t cells = 0;
+    for (auto& c : b->chunks) cells += (uint64_t)(c.size - 1) * (c.size - 1) * c.size;
+    ctx->last = iso_mesh_info{nv, nt, cells};
+    ctx->last_flags = 0;
+    ctx->last_vertex_floats = 3;
+    if (info) *info = ctx->last;
+    return ISO_OK;
+}
+
+iso_status iso_batch_run_per_chunk_async(iso_batch* b, iso_mesh_info* info) {
+    iso::NvtxRange nvtx_range("iso_batch_run_per_chunk_async");
+    if (!b) return ISO_ERR_INVALID_ARG;
+    iso_ctx* ctx = b->ctx;
+    iso_status s = set_device(ctx);
+    if (s != ISO_OK) return s;
+    if (!b->sized) return fail(ctx, ISO_ERR_INVALID_ARG, "run the batch once first (it sizes every chunk's output)");
+    const uint32_t n_ch = (uint32_t)b->chunks.size();
+    if (!b->d_solo_grids) {
+        // every chunk as a grid of its own, chunk ids from 0
+        std::vector<char> grids(mc_grid_bytes() * n_ch);
+        b->solo_chunks.resize(n_ch);
+        b->solo_cw.resize(n_ch);
+        for (uint32_t i = 0; i < n_ch; ++i) {
+            const SampleGrid& g = b->sgrids[i];
+            Lattice L{g.n, g.n, g.n + 1, g.pitch, g.field, g.bits, g.W, g.inv, nullptr};
+            mc_fill_grid(grids.data() + mc_grid_bytes() * i, L, 0, &b->solo_chunks[i], &b->solo_cw[i]);
+        }
+        cudaError_t e = cudaMalloc(&b->d_solo_grids, grids.size());
+        if (e == cudaSuccess) e = cudaMemcpy(b->d_solo_grids, grids.data(), grids.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "per-chunk grids");
+    }
+    // each chunk's output place and size, from the last run of the batch
+    std::vector<uint32_t> ext(4ull * n_ch);
+    cudaError_t e = cudaMemcpyAsync(ext.data(), b->d_extents, 16ull * n_ch, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "chunk extents");
+    const uint64_t nv = (uint64_t)ext[4ull * (n_ch - 1)] + ext[4ull * (n_ch - 1) + 1];
+    const uint64_t nt = (uint64_t)ext[4ull * (n_ch - 1) + 2] + ext[4ull * (n_ch - 1) + 3];
+    if ((s = ensure(ctx, ctx->mesh_v, 12 * std::max<uint64_t>(nv, 1))) != ISO_OK) return s;
+    if ((s = ensure(ctx, ctx->mesh_i, 12 * std::max<uint64_t>(nt, 1))) != ISO_OK) return s;
+    float* out_v = (float*)ctx->mesh_v.p;
+    uint32_t* out_i = (uint32_t*)ctx->mesh_i.p;
+    uint32_t* dummy_extents = (uint32_t*)(b->d_totals + 4);  // [0, 16) of the totals block's unused half
+    uint64_t* totals = b->d_totals;
+    // per chunk: its sampler, count, scan and emit, queued back to back
+    for (uint32_t i = 0; i < n_ch; ++i) {
+        const SampleGrid& g = b->sgrids[i];
+        if ((s = launch_sample_grid(ctx, b->programs[b->chunks[i].prog], g.n, g.n, g.n + 1, g.inv, g.field, g.pitch,
+                                    g.bits)) != ISO_OK)
+            return s;
+        if ((s = mc_extract_grids(ctx, (const char*)b->d_solo_grids + mc_grid_bytes() * i, 1, nullptr,
+                                  b->solo_chunks[i], b->solo_cw[i], b->d_scratch, ext[4ull * i + 1],
+                                  ext[4ull * i + 3], out_v + 3ull * ext[4ull * i], out_i + 3ull * ext[4ull * i + 2],
+                                  dummy_extents, totals, false)) != ISO_OK)
+            return s;
+    }
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "per-chunk run");
+    if ((s = read_device_errors(ctx)) != ISO_OK) return s;
     uint64_t cells = 0;
     for (auto& c : b->chunks) cells += (uint64_t)(c.size - 1) * (c.size - 1) * c.size;
     ctx->last = iso_mesh_info{nv, nt, cells};

@@ -269,6 +269,22 @@ iso_status sample_lattice(iso_ctx* ctx, const iso_program* prog, uint32_t size, 
     return ISO_OK;
 }
 
+iso_status sample_lattice_slab(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t zlo, uint32_t nz,
+                               Lattice* L) {
+    const uint32_t nx = size, ny = size;
+    const uint64_t pitch = default_pitch(nx);
+    const uint32_t W = words_per_row(nx);
+    iso_status s;
+    if ((s = ensure(ctx, ctx->field, 4ull * pitch * ny * nz)) != ISO_OK) return s;
+    if ((s = ensure(ctx, ctx->bits, 4ull * W * ny * nz)) != ISO_OK) return s;
+    const float inv = 1.0f / (float)(size - 1);
+    if ((s = launch_sample_grid(ctx, prog, nx, ny, nz, inv, (float*)ctx->field.p, pitch, (uint32_t*)ctx->bits.p,
+                                true, zlo)) != ISO_OK)
+        return s;
+    *L = Lattice{nx, ny, nz, pitch, (const float*)ctx->field.p, (const uint32_t*)ctx->bits.p, W, inv, nullptr, zlo};
+    return ISO_OK;
+}
+
 }  // namespace iso
 
 extern "C" {
@@ -613,6 +629,18 @@ iso_status iso_mc_extract_field(iso_ctx* ctx, const float* field, uint32_t nx, u
     if ((s = launch_sign_bits(ctx, field, nx, ny, nz, pitch, (uint32_t*)ctx->bits.p)) != ISO_OK) return s;
     Lattice L{nx, ny, nz, pitch, field, (const uint32_t*)ctx->bits.p, W, 1.0f / (float)(nx - 1), nullptr};
     return mc_extract_lattice(ctx, L, flags, info);
+}
+
+iso_status iso_mc_extract_slab(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t z_begin,
+                               uint32_t z_end, uint32_t flags, iso_mesh_info* info, uint64_t* halo_vertices,
+                               uint64_t* halo_triangles) {
+    iso::NvtxRange nvtx_range("iso_mc_extract_slab");
+    iso_status s = check_size(ctx, prog, size);
+    if (s != ISO_OK) return s;
+    if (size < 2 || !(z_begin < z_end) || z_end > size)
+        return fail(ctx, ISO_ERR_INVALID_ARG, "need size >= 2 and 0 <= z_begin < z_end <= size");
+    if (flags & ~(uint32_t)ISO_FLAG_KEYS) return fail(ctx, ISO_ERR_INVALID_ARG, "unknown flags");
+    return mc_extract_slab(ctx, prog, size, z_begin, z_end, flags, info, halo_vertices, halo_triangles);
 }
 
 iso_status iso_mc_cases(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint8_t* cases_host) {

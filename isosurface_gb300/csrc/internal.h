@@ -176,7 +176,8 @@ iso_status set_device(iso_ctx* ctx);
 
 // sample.cu
 iso_status launch_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t nx, uint32_t ny, uint32_t nz,
-                              float inv, float* field, uint64_t pitch, uint32_t* bits, bool near_only = false);
+                              float inv, float* field, uint64_t pitch, uint32_t* bits, bool near_only = false,
+                              uint32_t zoff = 0);
 iso_status launch_sign_bits(iso_ctx* ctx, const float* field, uint32_t nx, uint32_t ny, uint32_t nz,
                             uint64_t pitch, uint32_t* bits);
 iso_status launch_sample_points(iso_ctx* ctx, const iso_program* prog, const float* d_pts, uint64_t n,
@@ -194,8 +195,11 @@ struct Lattice {
     uint32_t words_per_row;
     float inv;               // point position = (x*inv, y*inv, z*inv)
     const float4* positions; // DC: explicit xyz per point (w unused); null = regular grid
+    uint32_t zoff = 0;       // regular grid: lattice z of layer 0 (a slab of a larger grid)
 };
 iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, iso_mesh_info* info);
+iso_status mc_extract_slab(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t z_begin, uint32_t z_end,
+                           uint32_t flags, iso_mesh_info* info, uint64_t* halo_vertices, uint64_t* halo_triangles);
 // iso_mc_extract without the normals sink: sampler + MarchingCubes, replaying
 // the context's recorded graph when it applies
 iso_status mc_extract_program(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t flags,
@@ -203,6 +207,9 @@ iso_status mc_extract_program(iso_ctx* ctx, const iso_program* prog, uint32_t si
 // the sampler half (signs everywhere, values near the surface) into the
 // context's field and sign buffers
 iso_status sample_lattice(iso_ctx* ctx, const iso_program* prog, uint32_t size, Lattice* L);
+// sample layers [zlo, zlo + nz) of MarchingCubes::new(size)'s lattice (a slab, L->zoff = zlo)
+iso_status sample_lattice_slab(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t zlo, uint32_t nz,
+                               Lattice* L);
 void mc_plan_release(iso_ctx* ctx);
 void lhmc_plan_release(iso_ctx* ctx);
 iso_status mc_cases_lattice(iso_ctx* ctx, const Lattice& L, uint8_t* d_cases);

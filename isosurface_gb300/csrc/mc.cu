@@ -757,6 +757,71 @@ iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, is
     return mc_lattice_passes(ctx, L, flags, info, false);
 }
 
+namespace {
+// Triangles and owned vertices of the cells of a lattice's first cell layer,
+// which the lattice treats as its z == 0 face: one warp per cell row.
+__global__ void __launch_bounds__(WARPS * 32) mc_layer_counts(const uint32_t* bits, uint32_t W, uint32_t nx,
+                                                              uint32_t ny, unsigned long long* totals) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t y = blockIdx.x * WARPS + (threadIdx.x >> 5);
+    if (y + 1 >= ny) return;
+    const uint32_t* a = bits + (uint64_t)y * W;
+    const uint32_t* b = a + W;
+    const uint32_t* cz = a + (uint64_t)ny * W;
+    const uint32_t* d = cz + W;
+    uint32_t tri = 0, vert = 0;
+    for (uint32_t c = 0; c < W; ++c) {
+        const uint32_t x = 32 * c + lane;
+        const uint32_t cs = cell_case(a, b, cz, d, c, W, lane);
+        if (x + 1 < nx) {
+            const int cls = (x == 0 ? 1 : 0) | (y == 0 ? 2 : 0) | 4;
+            tri += iso_tri_count[cs];
+            vert += __popc((uint32_t)iso_edge_mask[cs] & iso_owned_mask[cls]);
+        }
+    }
+    tri = warp_sum(tri);
+    vert = warp_sum(vert);
+    if (lane == 0) {
+        atomicAdd(totals, (unsigned long long)tri);
+        atomicAdd(totals + 1, (unsigned long long)vert);
+    }
+}
+}  // namespace
+
+// MarchingCubes::new(size) restricted to the cell layers [z_begin, z_end),
+// for one slab of a z-partition across GPUs: see iso_mc_extract_slab.
+iso_status mc_extract_slab(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t z_begin, uint32_t z_end,
+                           uint32_t flags, iso_mesh_info* info, uint64_t* halo_vertices, uint64_t* halo_triangles) {
+    const uint32_t halo = z_begin > 0 ? 1u : 0u, zlo = z_begin - halo;
+    Lattice L;
+    iso_status s = sample_lattice_slab(ctx, prog, size, zlo, z_end - zlo + 1, &L);
+    if (s != ISO_OK) return s;
+    uint64_t hv = 0, ht = 0;
+    if (halo) {
+        if ((s = ensure(ctx, ctx->aux, 64)) != ISO_OK) return s;
+        unsigned long long* t = (unsigned long long*)ctx->aux.p;
+        cudaError_t e = cudaMemsetAsync(t, 0, 16, ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "halo counts");
+        {
+            StageTimer timer(ctx, ISO_STAGE_CLASSIFY);
+            mc_layer_counts<<<(L.ny - 1 + WARPS - 1) / WARPS, WARPS * 32, 0, ctx->stream>>>(L.bits, L.words_per_row,
+                                                                                          L.nx, L.ny, t);
+        }
+        ctx->launches++;
+        uint64_t h[2] = {0, 0};
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h, t, 16, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "halo counts");
+        ht = h[0];
+        hv = h[1];
+    }
+    if ((s = mc_lattice_passes(ctx, L, flags, info, false)) != ISO_OK) return s;
+    if (halo_vertices) *halo_vertices = hv;
+    if (halo_triangles) *halo_triangles = ht;
+    return ISO_OK;
+}
+
 void mc_plan_release(iso_ctx* ctx) {
     if (ctx->mc_plan.exec) cudaGraphExecDestroy(ctx->mc_plan.exec);
     ctx->mc_plan = iso_ctx::McPlan{};

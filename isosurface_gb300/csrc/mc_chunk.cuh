@@ -45,6 +45,7 @@ struct Grid {
     uint32_t W, CW, nx, ny, nz;
     FastDiv div_cw, div_ncy;
     float inv;
+    uint32_t zoff;     // lattice z of layer 0 (a slab of a larger grid): positions and keys use z + zoff
     uint32_t chunk0;   // first global chunk id (a multiple of RANGE)
     uint32_t nchunks;  // CW * (ny-1) * (nz-1)
 };
@@ -63,6 +64,7 @@ inline Grid make_grid(const Lattice& L, uint32_t chunk0) {
     g.div_cw = make_fastdiv(g.CW);
     g.div_ncy = make_fastdiv(L.ny - 1);
     g.inv = L.inv;
+    g.zoff = L.zoff;
     g.chunk0 = chunk0;
     g.nchunks = g.CW * (L.ny - 1) * (L.nz - 1);
     return g;
@@ -114,8 +116,11 @@ using EmitChunks = ChunkStage<EMIT_CH>;
 // counts and in-range prefixes.  One warp per range of 256 chunks, 32 per
 // round (no barrier); the next round's corner words are loaded while this
 // round is counted, so the loads' latency overlaps the counting.
+#ifndef ISO_COUNT_BLOCKS
+#define ISO_COUNT_BLOCKS 4  // resident blocks per SM the register budget is sized for (64 registers)
+#endif
 template <bool SEG>
-__global__ void __launch_bounds__(256) mc_chunk_count(ChunkCountArgs A) {
+__global__ void __launch_bounds__(256, ISO_COUNT_BLOCKS) mc_chunk_count(ChunkCountArgs A) {
     __shared__ uint8_t s_ntri[256];
     __shared__ uint16_t s_owned[8];
     __shared__ uint32_t s_tri[8][32];  // chunk mode, per warp: triangles of each of the round's chunks
@@ -549,8 +554,8 @@ __global__ void __launch_bounds__(256) mc_block_emit(ChunkEmitArgs A, uint32_t m
                         const float4 qb = __ldg(g.positions + ((size_t)vz * g.ny + vy) * g.nx + vx);
                         pax = qa.x; pay = qa.y; paz = qa.z; pbx = qb.x; pby = qb.y; pbz = qb.z;
                     } else {
-                        pax = (float)ux * g.inv; pay = (float)uy * g.inv; paz = (float)uz * g.inv;
-                        pbx = (float)vx * g.inv; pby = (float)vy * g.inv; pbz = (float)vz * g.inv;
+                        pax = (float)ux * g.inv; pay = (float)uy * g.inv; paz = (float)(uz + g.zoff) * g.inv;
+                        pbx = (float)vx * g.inv; pby = (float)vy * g.inv; pbz = (float)(vz + g.zoff) * g.inv;
                     }
                     // Signed::find_crossing_point (distance.rs:64-69)
                     const float delta = fb - fa;
@@ -563,7 +568,7 @@ __global__ void __launch_bounds__(256) mc_block_emit(ChunkEmitArgs A, uint32_t m
                         A.out_v[3 * (size_t)vid + 2] = paz * omt + pbz * tt;
                         if (A.out_k) {
                             const uint32_t lx = x + c_edge_lo[e][0], ly = y + c_edge_lo[e][1], lz = z + c_edge_lo[e][2];
-                            A.out_k[2 * (size_t)vid] = (((uint64_t)lz * g.ny + ly) * g.nx + lx) * 3 + c_edge_axis[e];
+                            A.out_k[2 * (size_t)vid] = (((uint64_t)(lz + g.zoff) * g.ny + ly) * g.nx + lx) * 3 + c_edge_axis[e];
                             A.out_k[2 * (size_t)vid + 1] = 0;
                         }
                     } else {
@@ -647,7 +652,7 @@ __device__ __forceinline__ void put_vertex(const ChunkEmitArgs& A, const Grid& g
         A.out_v[3 * (size_t)vid + 1] = pay * omt + pby * tt;
         A.out_v[3 * (size_t)vid + 2] = paz * omt + pbz * tt;
         if (A.out_k) {
-            A.out_k[2 * (size_t)vid] = (((uint64_t)lz * g.ny + ly) * g.nx + lx) * 3 + ax;
+            A.out_k[2 * (size_t)vid] = (((uint64_t)(lz + g.zoff) * g.ny + ly) * g.nx + lx) * 3 + ax;
             A.out_k[2 * (size_t)vid + 1] = 0;
         }
     } else {
@@ -724,7 +729,7 @@ __device__ __forceinline__ void emit_cells(const ChunkEmitArgs& A, const Grid& g
             const float f2 = e10 ? __ldg(v6 - (size_t)g.ny * g.pitch) : 0.0f;    // corner 2
             const float X0 = (float)c.x * g.inv, X1 = (float)(c.x + 1) * g.inv;
             const float Y0 = (float)c.y * g.inv, Y1 = (float)(c.y + 1) * g.inv;
-            const float Z0 = (float)c.z * g.inv, Z1 = (float)(c.z + 1) * g.inv;
+            const float Z0 = (float)(c.z + g.zoff) * g.inv, Z1 = (float)(c.z + 1 + g.zoff) * g.inv;
             const uint32_t k6 = 3 * (cell + g.nx * (g.ny + 1) + 1);  // corner 6's key base
             if (e5)  // corners 5 -> 6, y axis
                 put_vertex(A, g, f5, f6, X1, Y0, Z1, X1, Y1, Z1, vstart + (c.pk.z >> 16 & 15u), k6 + 1, grid_v0,
@@ -750,8 +755,8 @@ __device__ __forceinline__ void emit_cells(const ChunkEmitArgs& A, const Grid& g
                                vz = c.z + __ldg(&iso_corners[v][2]);
                 const float fa = __ldg(g.values + ((size_t)uz * g.ny + uy) * g.pitch + ux);
                 const float fb = __ldg(g.values + ((size_t)vz * g.ny + vy) * g.pitch + vx);
-                put_vertex(A, g, fa, fb, (float)ux * g.inv, (float)uy * g.inv, (float)uz * g.inv,
-                           (float)vx * g.inv, (float)vy * g.inv, (float)vz * g.inv,
+                put_vertex(A, g, fa, fb, (float)ux * g.inv, (float)uy * g.inv, (float)(uz + g.zoff) * g.inv,
+                           (float)vx * g.inv, (float)vy * g.inv, (float)(vz + g.zoff) * g.inv,
                            vstart + (uint32_t)(rk >> (4 * e) & 15u), ((hz * g.ny + hy) * g.nx + hx) * 3 + ax,
                            grid_v0, lx, ly, lz, ax);
             }

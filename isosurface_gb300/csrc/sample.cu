@@ -21,7 +21,8 @@ constexpr uint32_t FULL = 0xFFFFFFFFu;
 
 // One warp per (32-point chunk, row): generic program evaluator.
 __global__ void __launch_bounds__(256) sample_generic(ProgView pv, uint32_t nx, uint32_t ny, uint32_t nz, float inv,
-                                                      float* field, uint64_t pitch, uint32_t* bits, uint32_t W) {
+                                                      float* field, uint64_t pitch, uint32_t* bits, uint32_t W,
+                                                      uint32_t zoff) {
     const int lane = threadIdx.x & 31;
     const uint64_t gw = (uint64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
     if (gw >= (uint64_t)W * ny * nz) return;
@@ -31,7 +32,7 @@ __global__ void __launch_bounds__(256) sample_generic(ProgView pv, uint32_t nx, 
     const uint32_t x = 32 * w + lane;
     bool inside = false;
     if (x < nx) {
-        float v = eval_scalar(pv, v3((float)x * inv, (float)y * inv, (float)z * inv));
+        float v = eval_scalar(pv, v3((float)x * inv, (float)y * inv, (float)(z + zoff) * inv));
         field[row * pitch + x] = v;
         inside = !(v > 0.0f);
     }
@@ -65,6 +66,7 @@ struct SetArgs {
     // distance at least one lattice step plus rounding slack); signs everywhere
     bool near_only;
     float reach;
+    uint32_t zoff;  // global lattice z of layer 0 (a slab of a larger grid)
 };
 
 __device__ __forceinline__ float world(float g, float s, float o, bool dom) { return dom ? g * s + o : g; }
@@ -117,7 +119,7 @@ __device__ __forceinline__ void near_column(const SetArgs& A, const float* dxy, 
                                             const float* T, const float* U, const float* L, uint32_t x, uint32_t y,
                                             uint32_t z0, uint32_t z1, bool valid, int lane, uint32_t wx) {
     const uint32_t nzt = z1 - z0 + 1;
-    const float pzl = world((float)(z0 + lane) * A.inv, A.sz, A.oz, A.domain);  // lane k: layer z0 + k
+    const float pzl = world((float)((z0 + lane) + A.zoff) * A.inv, A.sz, A.oz, A.domain);  // lane k: layer z0 + k
     uint32_t nearmask = 0, word = 0;
     auto layer = [&](uint32_t k) {
         const float pz = __shfl_sync(FULL, pzl, k);
@@ -155,7 +157,7 @@ __device__ __forceinline__ void near_column(const SetArgs& A, const float* dxy, 
         for (int i = 0; i < N; ++i) sdxy[i] = __shfl_sync(FULL, dxy[i], src);
         if (kk < total) {
             const uint32_t z = z0 + __fns(smask, 0, (int)(kk - sexcl) + 1);
-            const float pz = world((float)z * A.inv, A.sz, A.oz, A.domain);
+            const float pz = world((float)(z + A.zoff) * A.inv, A.sz, A.oz, A.domain);
             float dz = pz - cz[0];
             float v = sqrtf(sdxy[0] + dz * dz) - cr[0];
 #pragma unroll
@@ -196,7 +198,7 @@ __device__ __forceinline__ void sphere_column(const SetArgs& A, const float4* ke
     }
 #pragma unroll 2
     for (uint32_t z = z0; z <= z1; ++z) {
-        const float pz = world((float)z * A.inv, A.sz, A.oz, A.domain);
+        const float pz = world((float)(z + A.zoff) * A.inv, A.sz, A.oz, A.domain);
         const size_t row = (size_t)z * A.ny + y;
         float dz = pz - cz[0];
         float v = sqrtf(dxy[0] + dz * dz) - cr[0];
@@ -224,7 +226,7 @@ __device__ __forceinline__ void sample_column(const SetArgs& A, const float4* ke
     default: break;
     }
     for (uint32_t z = z0; z <= z1; ++z) {
-        const float pz = world((float)z * A.inv, A.sz, A.oz, A.domain);
+        const float pz = world((float)(z + A.zoff) * A.inv, A.sz, A.oz, A.domain);
         float v = 0.0f;
         for (uint32_t i = 0; i < nk; ++i) {
             float4 c = keep[i];
@@ -249,7 +251,7 @@ __global__ void __launch_bounds__(256) sample_sphere_set(SetArgs A) {
     // tile box in world coordinates (the map is affine, so the box's images are the extremes)
     float ax = world((float)x0 * A.inv, A.sx, A.ox, A.domain), bx = world((float)x1 * A.inv, A.sx, A.ox, A.domain);
     float ay = world((float)y0 * A.inv, A.sy, A.oy, A.domain), by = world((float)y1 * A.inv, A.sy, A.oy, A.domain);
-    float az = world((float)z0 * A.inv, A.sz, A.oz, A.domain), bz = world((float)z1 * A.inv, A.sz, A.oz, A.domain);
+    float az = world((float)(z0 + A.zoff) * A.inv, A.sz, A.oz, A.domain), bz = world((float)(z1 + A.zoff) * A.inv, A.sz, A.oz, A.domain);
     const float lox = fminf(ax, bx), hix = fmaxf(ax, bx), loy = fminf(ay, by), hiy = fmaxf(ay, by);
     const float loz = fminf(az, bz), hiz = fmaxf(az, bz);
     const float4* sp = reinterpret_cast<const float4*>(A.spheres);
@@ -403,7 +405,7 @@ __global__ void __launch_bounds__(32 * TILE_WARPS) set_tiles(SetArgs A, uint32_t
     const TileBox tb = tile_box(A, wx, rt % tiles_y, rt / tiles_y);
     float ax = world((float)tb.x0 * A.inv, A.sx, A.ox, A.domain), bx = world((float)tb.x1 * A.inv, A.sx, A.ox, A.domain);
     float ay = world((float)tb.y0 * A.inv, A.sy, A.oy, A.domain), by = world((float)tb.y1 * A.inv, A.sy, A.oy, A.domain);
-    float az = world((float)tb.z0 * A.inv, A.sz, A.oz, A.domain), bz = world((float)tb.z1 * A.inv, A.sz, A.oz, A.domain);
+    float az = world((float)(tb.z0 + A.zoff) * A.inv, A.sz, A.oz, A.domain), bz = world((float)(tb.z1 + A.zoff) * A.inv, A.sz, A.oz, A.domain);
     const float lox = fminf(ax, bx), hix = fmaxf(ax, bx), loy = fminf(ay, by), hiy = fmaxf(ay, by);
     const float loz = fminf(az, bz), hiz = fmaxf(az, bz);
     const float4* sp = reinterpret_cast<const float4*>(A.spheres);
@@ -503,8 +505,8 @@ __global__ void __launch_bounds__(256, SET_ROWS_BLOCKS) set_rows(SetArgs A, uint
                 // bounds of this sphere's value over the row box
                 const float ax = world((float)tb.x0 * A.inv, A.sx, A.ox, A.domain);
                 const float bx = world((float)tb.x1 * A.inv, A.sx, A.ox, A.domain);
-                const float az = world((float)tb.z0 * A.inv, A.sz, A.oz, A.domain);
-                const float bz = world((float)tb.z1 * A.inv, A.sz, A.oz, A.domain);
+                const float az = world((float)(tb.z0 + A.zoff) * A.inv, A.sz, A.oz, A.domain);
+                const float bz = world((float)(tb.z1 + A.zoff) * A.inv, A.sz, A.oz, A.domain);
                 const float lox = fminf(ax, bx), hix = fmaxf(ax, bx), loz = fminf(az, bz), hiz = fmaxf(az, bz);
                 const float fx = fmaxf(fabsf(c.x - lox), fabsf(c.x - hix)), fy = fabsf(c.y - py);
                 const float fz = fmaxf(fabsf(c.z - loz), fabsf(c.z - hiz));
@@ -579,7 +581,7 @@ iso_status attach_normals(iso_ctx* ctx, const iso_program* prog) {
 }
 
 iso_status launch_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t nx, uint32_t ny, uint32_t nz, float inv,
-                              float* field, uint64_t pitch, uint32_t* bits, bool near_only) {
+                              float* field, uint64_t pitch, uint32_t* bits, bool near_only, uint32_t zoff) {
     const uint32_t W = words_per_row(nx);
     if (prog->kind == PK_SPHERE_SET_HARD && prog->set_n <= 8192) {
         near_only = near_only && prog->set_n <= 4096 && nx > 1;
@@ -592,6 +594,7 @@ iso_status launch_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t nx
         a.nx = nx; a.ny = ny; a.nz = nz; a.inv = inv;
         a.field = field; a.pitch = pitch; a.bits = bits; a.W = W;
         a.near_only = near_only;
+        a.zoff = zoff;
         // a crossing edge joins samples one lattice step apart, and the field
         // is 1-Lipschitz in world units: both ends lie within one step (the
         // largest axis step after the domain map) of zero, plus rounding slack
@@ -633,7 +636,7 @@ iso_status launch_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t nx
         uint64_t warps = (uint64_t)W * ny * nz;
         StageTimer timer(ctx, ISO_STAGE_SAMPLE);
         sample_generic<<<(unsigned)((warps + 7) / 8), 256, 0, ctx->stream>>>(prog->view(), nx, ny, nz, inv, field, pitch,
-                                                                          bits, W);
+                                                                          bits, W, zoff);
     }
     ctx->launches++;
     return check_launch(ctx, "sample_grid");

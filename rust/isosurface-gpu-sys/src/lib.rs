@@ -175,6 +175,17 @@ extern "C" {
         stream: *mut c_void,
         info: *mut IsoMeshInfo,
     ) -> IsoStatus;
+    pub fn iso_mc_extract_slab(
+        ctx: *mut IsoCtx,
+        prog: *const IsoProgram,
+        size: u32,
+        z_begin: u32,
+        z_end: u32,
+        flags: u32,
+        info: *mut IsoMeshInfo,
+        halo_vertices: *mut u64,
+        halo_triangles: *mut u64,
+    ) -> IsoStatus;
     pub fn iso_mc_cases(
         ctx: *mut IsoCtx,
         prog: *const IsoProgram,
@@ -208,6 +219,7 @@ extern "C" {
     pub fn iso_batch_destroy(batch: *mut IsoBatch) -> IsoStatus;
     pub fn iso_batch_run(batch: *mut IsoBatch, flags: u32, info: *mut IsoMeshInfo) -> IsoStatus;
     pub fn iso_batch_run_per_chunk(batch: *mut IsoBatch, info: *mut IsoMeshInfo) -> IsoStatus;
+    pub fn iso_batch_run_per_chunk_async(batch: *mut IsoBatch, info: *mut IsoMeshInfo) -> IsoStatus;
     pub fn iso_batch_extents(batch: *mut IsoBatch, extents: *mut u32) -> IsoStatus;
     pub fn iso_batch_set_slab(batch: *mut IsoBatch, size: u32, depth: u32) -> IsoStatus;
     pub fn iso_batch_autotune(batch: *mut IsoBatch, cache_path: *const c_char, chosen: *mut u32) -> IsoStatus;

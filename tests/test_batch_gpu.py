@@ -39,6 +39,9 @@ def test_batch_eager_graph_and_per_chunk(ctx, chunk_set, want):
         _check(b.meshes(info), want)
     info = b.run_per_chunk()
     _check(b.meshes(info), want)
+    for _ in range(2):
+        info = b.run_per_chunk_async()
+        _check(b.meshes(info), want)
     b.close()
 
 
