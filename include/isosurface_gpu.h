@@ -202,6 +202,22 @@ ISO_API iso_status iso_mesh_device(iso_ctx* ctx, const float** vertices, const u
  * y, then z: size+1 layers of size rows). */
 ISO_API iso_status iso_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t size,
                            float* field, uint64_t pitch);
+/* The same points sampled the way the extractors sample them: every sign
+ * bit, but values only where marching cubes can read them.  `bits` (device
+ * memory, ceil(size/32) words per row, rows as in `field`) receives bit x%32
+ * of word x/32 set iff !(value > 0); `field` receives the value of at least
+ * every sample within one lattice step's worth of value change of zero (the
+ * ends of every edge whose signs differ), bit-identical to iso_sample_grid's;
+ * other entries may be left unwritten.  Unions of spheres and programs with a
+ * known Lipschitz bound (iso_program_lipschitz) skip the work far from the
+ * surface. */
+ISO_API iso_status iso_sample_grid_near(iso_ctx* ctx, const iso_program* prog, uint32_t size,
+                                float* field, uint64_t pitch, uint32_t* bits);
+/* A bound on the program value's Lipschitz constant with respect to the
+ * sample point (how much the value can change per unit of distance), from
+ * its primitives (exact distances) and point maps; 0 when the program has
+ * none (culled sampling is then off). */
+ISO_API iso_status iso_program_lipschitz(const iso_program* prog, float* lip);
 
 /* ------------------------------------------------------------------------ */
 /* MarchingCubes (src/marching_cubes.rs:59-82)                               */

@@ -239,6 +239,18 @@ class Context:
     def sample_grid(self, source, size, field_ptr, pitch):
         check(lib().iso_sample_grid(self.h, self.program(source).h, size, ctypes.c_void_p(field_ptr), pitch), self.h)
 
+    def sample_grid_near(self, source, size, field_ptr, pitch, bits_ptr):
+        """Sign bits everywhere and values where marching cubes reads them
+        (iso_sample_grid_near); other field entries may be left unwritten."""
+        check(lib().iso_sample_grid_near(self.h, self.program(source).h, size, ctypes.c_void_p(field_ptr), pitch,
+                                         ctypes.c_void_p(bits_ptr)), self.h)
+
+    def lipschitz(self, source):
+        """The program's Lipschitz bound used for culled sampling (0: none)."""
+        out = ctypes.c_float()
+        check(lib().iso_program_lipschitz(self.program(source).h, ctypes.byref(out)), self.h)
+        return out.value
+
     def sample_points(self, source, points, normals=False):
         pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
         vals = np.empty(len(pts), np.float32)

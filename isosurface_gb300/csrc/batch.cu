@@ -1,10 +1,11 @@
 // Batched MarchingCubes: thousands of independent chunks, each a
 // MarchingCubes::new(size_i).extract over its own source, in one pass.
 //
-// * Sampling: one persistent kernel drains a work queue of (chunk, z-slab)
-//   tiles (largest cost first); each block evaluates its tile's points with
-//   the chunk's program and writes the chunk's field and sign bits.  The slab
-//   depth per chunk-size class comes from iso_batch_autotune.
+// * Sampling: one persistent kernel drains a work queue of (chunk, z-slab,
+//   y-range) tiles (largest cost first); each block samples its tile with the
+//   culled sampler of bricks.cuh (sign bits everywhere, values where marching
+//   cubes can read them, primitives pruned per sub-brick).  The slab depth
+//   per chunk-size class comes from iso_batch_autotune.
 // * Classification, scan and emission: the chunked marching-cubes passes of
 //   mc.cu over a table of grids whose 32-cell chunks are laid out
 //   range-aligned in one global index space (mc_chunk.cuh).
@@ -29,6 +30,7 @@
 #include <string>
 #include <vector>
 
+#include "bricks.cuh"
 #include "internal.h"
 #include "vm.cuh"
 
@@ -57,37 +59,50 @@ struct SampleGrid {
 };
 
 struct Tile {
-    uint32_t grid, z0, z1;
+    uint32_t grid, z0, z1, y0, y1;  // layers [z0, z1), rows [y0, y1), all x
 };
 
-__global__ void __launch_bounds__(256) batch_sample(const Tile* tiles, uint32_t ntiles, const SampleGrid* grids,
-                                                    uint32_t* next) {
-    __shared__ uint32_t s_tile;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// The batch's tiles for the culled sampler (bricks.cuh).
+struct BatchTiles {
+    const Tile* tiles;
+    const SampleGrid* grids;
+    __device__ __forceinline__ BrickTile tile(uint32_t t) const {
+        const Tile tl = tiles[t];
+        const SampleGrid sg = grids[tl.grid];
+        return BrickTile{BrickLattice{sg.pv, sg.n, sg.n, sg.n + 1, sg.inv, sg.field, sg.pitch, sg.bits, sg.W, 0},
+                         tl.y0, tl.y1, tl.z0, tl.z1};
+    }
+};
+
+// A persistent grid: each block takes tiles from the work queue (largest
+// first) and samples them whole.
+__global__ void __launch_bounds__(256) batch_sample(BatchTiles bt, uint32_t ntiles, uint32_t* next) {
+    __shared__ uint32_t s_tile, s_n;
+    __shared__ uint8_t s_cls[BRICK_MAX];
+    __shared__ uint32_t s_keep[BRICK_MAX];
+    __shared__ uint32_t s_list[BRICK_MAX];
     while (true) {
-        __syncthreads();
+        __syncthreads();  // the previous tile is done with the shared arrays
         if (threadIdx.x == 0) s_tile = atomicAdd(next, 1u);
         __syncthreads();
         const uint32_t t = s_tile;
         if (t >= ntiles) return;
-        const Tile tl = tiles[t];
-        const SampleGrid g = grids[tl.grid];
-        const uint32_t tasks = (tl.z1 - tl.z0) * g.n * g.W;
-        for (uint32_t task = warp; task < tasks; task += 8) {
-            const uint32_t w = task % g.W, r = task / g.W;
-            const uint32_t y = r % g.n, z = tl.z0 + r / g.n;
-            const uint32_t x = 32 * w + lane;
-            bool inside = false;
-            const size_t row = (size_t)z * g.n + y;
-            if (x < g.n) {
-                const float v = eval_scalar(g.pv, v3((float)x * g.inv, (float)y * g.inv, (float)z * g.inv));
-                g.field[row * g.pitch + x] = v;
-                inside = !(v > 0.0f);
-            }
-            const uint32_t b = __ballot_sync(0xFFFFFFFFu, inside);
-            if (lane == 0) g.bits[row * g.W + w] = b;
-        }
+        brick_tile(bt.tile(t), s_cls, s_keep, s_list, &s_n);
     }
+}
+
+// The tiles of one chunk of `n` (n x n x (n + 1) samples) for slab depth
+// `depth` (0: the whole chunk), rounded up to whole sub-bricks (4 layers)
+// and cut in y so that a tile holds at most BRICK_MAX sub-bricks.
+template <class F>
+void chunk_tiles(uint32_t grid, uint32_t n, uint32_t depth, F&& add) {
+    const uint32_t nz = n + 1, SX = 4 * words_per_row(n);
+    uint32_t zg = ((depth ? depth : nz) + 3) / 4;
+    zg = std::max(1u, std::min(zg, BRICK_MAX / SX));
+    const uint32_t ty = std::max(1u, std::min((n + 3) / 4, BRICK_MAX / (SX * zg)));
+    for (uint32_t z0 = 0; z0 < nz; z0 += 4 * zg)
+        for (uint32_t y0 = 0; y0 < n; y0 += 4 * ty)
+            add(Tile{grid, z0, std::min(nz, z0 + 4 * zg), y0, std::min(n, y0 + 4 * ty)});
 }
 
 struct Chunk {
@@ -109,7 +124,7 @@ struct iso_batch {
     uint32_t* d_range_grid = nullptr;
     Tile* d_tiles = nullptr;
     uint32_t ntiles = 0;
-    uint32_t* d_next = nullptr;
+    uint32_t* d_next = nullptr;  // the sampler's work-queue counter
     uint32_t* d_extents = nullptr;   // 4 per chunk
     uint64_t* d_totals = nullptr;    // [0] triangles [1] vertices
     void* d_scratch = nullptr;       // chunk-pass scratch
@@ -132,16 +147,22 @@ struct iso_batch {
 
 namespace {
 
+// Device copy of `tiles`.
+cudaError_t upload_tiles(const std::vector<Tile>& tiles, Tile** d_tiles) {
+    cudaError_t e = cudaMalloc((void**)d_tiles, sizeof(Tile) * std::max<size_t>(tiles.size(), 1));
+    if (e == cudaSuccess && !tiles.empty())
+        e = cudaMemcpy(*d_tiles, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice);
+    return e;
+}
+
 iso_status build_tiles(iso_batch* b) {
     std::vector<std::pair<double, Tile>> t;
     for (uint32_t i = 0; i < b->chunks.size(); ++i) {
-        const uint32_t n = b->chunks[i].size, nz = n + 1;
-        const uint32_t depth = b->slab[i] ? b->slab[i] : nz;
-        const double cost_per_layer = (double)n * ((n + 31) / 32 * 32) * (double)b->programs[b->chunks[i].prog]->ops.size();
-        for (uint32_t z0 = 0; z0 < nz; z0 += depth) {
-            const uint32_t z1 = std::min(nz, z0 + depth);
-            t.push_back({cost_per_layer * (z1 - z0), Tile{i, z0, z1}});
-        }
+        const uint32_t n = b->chunks[i].size;
+        const double cost_per_point = (double)b->programs[b->chunks[i].prog]->ops.size();
+        chunk_tiles(i, n, b->slab[i], [&](const Tile& tl) {
+            t.push_back({cost_per_point * ((n + 31) / 32 * 32) * (tl.y1 - tl.y0) * (tl.z1 - tl.z0), tl});
+        });
     }
     std::stable_sort(t.begin(), t.end(), [](const auto& a, const auto& c) { return a.first > c.first; });
     std::vector<Tile> tiles(t.size());
@@ -149,9 +170,7 @@ iso_status build_tiles(iso_batch* b) {
     if (b->d_tiles) cudaFree(b->d_tiles);
     b->d_tiles = nullptr;
     b->ntiles = (uint32_t)tiles.size();
-    cudaError_t e = cudaMalloc(&b->d_tiles, sizeof(Tile) * std::max<size_t>(tiles.size(), 1));
-    if (e == cudaSuccess && !tiles.empty())
-        e = cudaMemcpy(b->d_tiles, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice);
+    cudaError_t e = upload_tiles(tiles, &b->d_tiles);
     if (b->exec) {
         cudaGraphExecDestroy(b->exec);
         b->exec = nullptr;
@@ -163,25 +182,38 @@ iso_status build_tiles(iso_batch* b) {
     return e == cudaSuccess ? ISO_OK : cuda_fail(b->ctx, e, "tiles");
 }
 
-int sample_blocks() {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return std::max(1, sms) * 8;
+// blocks of batch_sample that fill every SM (looked up once per process)
+unsigned sample_blocks(int sms) {
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batch_sample, 256, 0) != cudaSuccess || b < 1) {
+            cudaGetLastError();
+            b = 4;
+        }
+        per_sm = b;
+    }
+    return (unsigned)(per_sm * std::max(sms, 1));
+}
+
+// the culled sampler over `ntiles` tiles (the queue counter zeroed first)
+cudaError_t launch_sampler(iso_ctx* ctx, const Tile* d_tiles, uint32_t ntiles, const SampleGrid* d_sgrids,
+                           uint32_t* next) {
+    cudaError_t e = cudaMemsetAsync(next, 0, 4, ctx->stream);
+    if (e != cudaSuccess) return e;
+    batch_sample<<<sample_blocks(ctx->sms), 256, 0, ctx->stream>>>(BatchTiles{d_tiles, d_sgrids}, ntiles, next);
+    return cudaGetLastError();
 }
 
 // enqueue the whole batch on the context's stream (no host sync)
 iso_status enqueue(iso_batch* b, bool sync_sizes) {
     iso_ctx* ctx = b->ctx;
-    cudaError_t e = cudaMemsetAsync(b->d_next, 0, 4, ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "memset queue");
     {
         StageTimer timer(ctx, ISO_STAGE_SAMPLE);
-        batch_sample<<<sample_blocks(), 256, 0, ctx->stream>>>(b->d_tiles, b->ntiles, b->d_sgrids, b->d_next);
+        cudaError_t e = launch_sampler(ctx, b->d_tiles, b->ntiles, b->d_sgrids, b->d_next);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "batch sampler");
     }
     ctx->launches++;
-    iso_status s = check_launch(ctx, "batch_sample");
-    if (s != ISO_OK) return s;
     return mc_extract_grids(ctx, b->d_grids, (uint32_t)b->chunks.size(), b->d_range_grid, b->total_chunks, b->max_cw,
                             b->d_scratch, b->cap_v, b->cap_t, (float*)ctx->mesh_v.p, (uint32_t*)ctx->mesh_i.p,
                             b->d_extents, b->d_totals, sync_sizes);
@@ -414,7 +446,7 @@ iso_status iso_batch_run_per_chunk(iso_batch* b, iso_mesh_info* info) {
         const SampleGrid& g = b->sgrids[i];
         const uint32_t n = g.n;
         if ((s = launch_sample_grid(ctx, b->programs[b->chunks[i].prog], n, n, n + 1, g.inv, g.field, g.pitch,
-                                    g.bits)) != ISO_OK)
+                                    g.bits, true)) != ISO_OK)
             return s;
         Lattice L{n, n, n + 1, g.pitch, g.field, g.bits, g.W, g.inv, nullptr};
         iso_mesh_info mi;
@@ -486,7 +518,7 @@ iso_status iso_batch_run_per_chunk_async(iso_batch* b, iso_mesh_info* info) {
     for (uint32_t i = 0; i < n_ch; ++i) {
         const SampleGrid& g = b->sgrids[i];
         if ((s = launch_sample_grid(ctx, b->programs[b->chunks[i].prog], g.n, g.n, g.n + 1, g.inv, g.field, g.pitch,
-                                    g.bits)) != ISO_OK)
+                                    g.bits, true)) != ISO_OK)
             return s;
         if ((s = mc_extract_grids(ctx, (const char*)b->d_solo_grids + mc_grid_bytes() * i, 1, nullptr,
                                   b->solo_chunks[i], b->solo_cw[i], b->d_scratch, ext[4ull * i + 1],
@@ -521,7 +553,8 @@ iso_status iso_batch_autotune(iso_batch* b, const char* cache_path, uint32_t* ch
     if (s != ISO_OK) return s;
     cudaDeviceProp prop;
     cudaGetDeviceProperties(&prop, ctx->device);
-    const std::string gpu = prop.name;
+    // cached depths are for this sampler design on this GPU model
+    const std::string gpu = std::string(prop.name) + " bricks";
     std::map<uint32_t, uint32_t> classes;  // size -> chunk count
     for (auto& c : b->chunks) classes[c.size]++;
     std::map<uint32_t, uint32_t> best;
@@ -539,7 +572,7 @@ iso_status iso_batch_autotune(iso_batch* b, const char* cache_path, uint32_t* ch
             std::fclose(f);
         }
     }
-    const uint32_t candidates[] = {1, 2, 4, 8, 16, 0};
+    const uint32_t candidates[] = {4, 8, 16, 0};
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -554,20 +587,20 @@ iso_status iso_batch_autotune(iso_batch* b, const char* cache_path, uint32_t* ch
             std::vector<std::pair<double, Tile>> t;
             for (uint32_t i = 0; i < b->chunks.size(); ++i) {
                 if (b->chunks[i].size != cl.first) continue;
-                const uint32_t nz = cl.first + 1, depth = d ? d : nz;
-                for (uint32_t z0 = 0; z0 < nz; z0 += depth) t.push_back({0.0, Tile{i, z0, std::min(nz, z0 + depth)}});
+                chunk_tiles(i, cl.first, d, [&](const Tile& tl) { t.push_back({0.0, tl}); });
             }
             std::vector<Tile> tiles(t.size());
             for (size_t i = 0; i < t.size(); ++i) tiles[i] = t[i].second;
             Tile* d_t = nullptr;
-            if (cudaMalloc(&d_t, sizeof(Tile) * tiles.size()) != cudaSuccess) return ISO_ERR_OUT_OF_MEMORY;
-            cudaMemcpy(d_t, tiles.data(), sizeof(Tile) * tiles.size(), cudaMemcpyHostToDevice);
+            if (upload_tiles(tiles, &d_t) != cudaSuccess) {
+                if (d_t) cudaFree(d_t);
+                cudaGetLastError();
+                return fail(ctx, ISO_ERR_OUT_OF_MEMORY, "autotune tiles");
+            }
             float ms = 1e30f;
             for (int rep = 0; rep < 4; ++rep) {
-                cudaMemsetAsync(b->d_next, 0, 4, ctx->stream);
                 cudaEventRecord(e0, ctx->stream);
-                batch_sample<<<sample_blocks(), 256, 0, ctx->stream>>>(d_t, (uint32_t)tiles.size(), b->d_sgrids,
-                                                                       b->d_next);
+                launch_sampler(ctx, d_t, (uint32_t)tiles.size(), b->d_sgrids, b->d_next);
                 cudaEventRecord(e1, ctx->stream);
                 cudaEventSynchronize(e1);
                 float t_ms = 0.0f;

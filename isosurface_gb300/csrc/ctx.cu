@@ -248,6 +248,95 @@ void classify(iso_program* p) {
     }
 }
 
+// Bounds for culled sampling.  Every primitive (sphere.rs, rectangular_prism.rs,
+// cylinder.rs, torus.rs) and sphere set is an exact signed distance, so
+// 1-Lipschitz in its own coordinates; a translation keeps distances, a domain
+// map scales them by at most its largest |scale|, a rigid map by its matrix's
+// spectral norm (bounded by Gershgorin's theorem on M^T M); min, max,
+// negation and the polynomial smooth minimum (partial derivatives
+// non-negative and summing to 1) keep the larger bound of their operands.
+// So the value's bound is the largest product of point-map norms above any
+// primitive.  The magnitude of every point coordinate and value the
+// evaluator meets is tracked alongside, for points in [0, 2]^3; the f32
+// rounding error of a value is a few tens of units in the last place of that
+// magnitude, and the slack allows 2^10 of them for each of two values.
+void cull_bounds(iso_program* p) {
+    p->lip = 0.0f;
+    p->slack = 0.0f;
+    const auto& o = p->ops;
+    const float* K = p->consts.data();
+    for (float c : p->consts)
+        if (!std::isfinite(c)) return;
+    double scale = 1.0, mag = 2.0 * std::sqrt(3.0), lip = 0.0, vmag = 0.0;
+    std::vector<std::pair<double, double>> saved;
+    auto norm3 = [](const float* v) { return std::sqrt((double)v[0] * v[0] + (double)v[1] * v[1] + (double)v[2] * v[2]); };
+    for (size_t pc = 0; pc < o.size(); ++pc) {
+        const uint32_t op = o[pc] & 0xFFu;
+        const float* k = K + (o[pc] >> 8);
+        switch (op) {
+        case OP_PT_DOMAIN: {
+            const double s = std::max({std::fabs((double)k[0]), std::fabs((double)k[1]), std::fabs((double)k[2])});
+            saved.push_back({scale, mag});
+            scale *= s;
+            mag = s * mag + norm3(k + 3);
+            break;
+        }
+        case OP_PT_TRANSLATE:
+            saved.push_back({scale, mag});
+            mag += norm3(k);
+            break;
+        case OP_PT_RIGID: {
+            double g = 0.0;  // Gershgorin bound on the largest eigenvalue of M^T M
+            for (int i = 0; i < 3; ++i) {
+                double row = 0.0;
+                for (int j = 0; j < 3; ++j) {
+                    double a = 0.0;
+                    for (int r = 0; r < 3; ++r) a += (double)k[3 + 3 * r + i] * (double)k[3 + 3 * r + j];
+                    row += std::fabs(a);
+                }
+                g = std::max(g, row);
+            }
+            const double n = std::sqrt(g) * (1.0 + 1e-6);
+            saved.push_back({scale, mag});
+            scale *= n;
+            mag = n * (mag + norm3(k));
+            break;
+        }
+        case OP_PT_POP:
+            if (saved.empty()) return;
+            scale = saved.back().first;
+            mag = saved.back().second;
+            saved.pop_back();
+            break;
+        case OP_SPHERE: case OP_BOX: case OP_CYLINDER: case OP_TORUS: {
+            const int na = op == OP_SPHERE ? 1 : (op == OP_BOX ? 3 : 2);
+            double a = 0.0;
+            for (int j = 0; j < na; ++j) a += std::fabs((double)k[j]);
+            lip = std::max(lip, scale);
+            vmag = std::max(vmag, mag + a);
+            break;
+        }
+        case OP_SPHERE_SET: {
+            const uint32_t n = (uint32_t)k[0];
+            double cmax = 0.0;
+            for (uint32_t i = 0; i < n; ++i) cmax = std::max(cmax, norm3(k + 3 + 4 * i) + std::fabs((double)k[6 + 4 * i]));
+            lip = std::max(lip, scale);
+            vmag = std::max(vmag, mag + cmax + std::fabs((double)k[2]));
+            break;
+        }
+        case OP_SMOOTH_UNION:
+            vmag += std::fabs((double)k[0]);
+            break;
+        default:
+            break;  // min, max, negation and the CD markers
+        }
+    }
+    const double m = std::max(vmag, mag);
+    if (!(lip > 0.0) || !(lip < 1e30) || !(m < 1e30)) return;
+    p->lip = (float)(lip * (1.0 + 1e-6));
+    p->slack = (float)(m * std::ldexp(1.0, -13));
+}
+
 }  // namespace
 
 namespace iso {
@@ -432,6 +521,7 @@ iso_status iso_program_create(iso_ctx* ctx, const uint8_t* bytes, size_t len, is
         return fail(ctx, ISO_ERR_BAD_PROGRAM, err);
     }
     classify(p);
+    cull_bounds(p);
     iso_status s = set_device(ctx);
     if (s != ISO_OK) {
         delete p;
@@ -534,6 +624,24 @@ iso_status iso_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t size,
         return s;
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     return e == cudaSuccess ? ISO_OK : cuda_fail(ctx, e, "sample grid");
+}
+
+iso_status iso_sample_grid_near(iso_ctx* ctx, const iso_program* prog, uint32_t size, float* field, uint64_t pitch,
+                                uint32_t* bits) {
+    iso::NvtxRange nvtx_range("iso_sample_grid_near");
+    iso_status s = check_size(ctx, prog, size);
+    if (s != ISO_OK) return s;
+    if (!field || !bits || pitch < size) return fail(ctx, ISO_ERR_INVALID_ARG, "field or bits null or pitch < size");
+    const float inv = size > 1 ? 1.0f / (float)(size - 1) : 0.0f;
+    if ((s = launch_sample_grid(ctx, prog, size, size, size + 1, inv, field, pitch, bits, true)) != ISO_OK) return s;
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    return e == cudaSuccess ? ISO_OK : cuda_fail(ctx, e, "sample grid near");
+}
+
+iso_status iso_program_lipschitz(const iso_program* prog, float* lip) {
+    if (!prog || !lip) return ISO_ERR_INVALID_ARG;
+    *lip = prog->lip;
+    return ISO_OK;
 }
 
 iso_status iso_mc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t flags, iso_mesh_info* info) {

@@ -5,7 +5,9 @@
 // to size the mesh.
 //
 //   emc_sample     Directed value of every lattice point (float4 per point)
-//   emc_count      case, feature decision, vertex and triangle counts per cell
+//   emc_active     case of every cell; the cells with corners on both sides
+//                  go to a list, which the later passes walk instead of the grid
+//   emc_count      feature decision, vertex and triangle counts per active cell
 //   scan_u32 x 2   first vertex and first triangle of every cell
 //   emc_vertices   feature points and owned edge vertices; the edge map
 //   emc_triangles  marching-cubes triangles and fans, in traversal order
@@ -35,25 +37,63 @@ __global__ void __launch_bounds__(256) emc_sample(emc::Args A, uint64_t points) 
         emc::sample_item(A, i);
 }
 
-__global__ void __launch_bounds__(128) emc_count(emc::Args A, uint64_t cells) {
-    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += (uint64_t)gridDim.x * blockDim.x)
-        emc::count_item(A, c);
+// Every cell's case; the cells with corners on both sides (the only ones
+// with work in the later passes) are appended to `list` in any order, the
+// others get their case and zero counts here.
+__global__ void __launch_bounds__(256) emc_active(emc::Args A, uint64_t cells, uint32_t* list, uint32_t* count) {
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint64_t c0 = (uint64_t)blockIdx.x * blockDim.x; c0 < cells; c0 += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t c = c0 + threadIdx.x;
+        bool active = false;
+        if (c < cells) {
+            uint32_t x, y, z;
+            emc::cell_xyz(A.g.n, c, &x, &y, &z);
+            V3 corners[8], values[8];
+            emc::load_cell(A.field, A.g, x, y, z, corners, values);
+            const int cube = emc::classify_directed(values);
+            active = cube != 0 && cube != 255;
+            if (!active) {
+                A.cell[c] = (uint16_t)cube;
+                A.voff[c] = 0;
+                A.toff[c] = 0;
+            }
+        }
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, active);
+        if (m) {
+            const uint32_t leader = (uint32_t)__ffs(m) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+            base = __shfl_sync(0xFFFFFFFFu, base, leader);
+            if (active) list[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)c;
+        }
+    }
 }
 
-__global__ void __launch_bounds__(128) emc_vertices(emc::Args A, uint64_t cells) {
-    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += (uint64_t)gridDim.x * blockDim.x)
-        emc::vertex_item(A, c);
+// The per-cell passes over the active cells only (one thread per cell, grid-stride).
+__global__ void __launch_bounds__(128) emc_count(emc::Args A, const uint32_t* list, const uint32_t* count) {
+    const uint32_t n = *count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        emc::count_item(A, list[i]);
 }
 
-__global__ void __launch_bounds__(256) emc_triangles(emc::Args A, uint64_t cells) {
-    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += (uint64_t)gridDim.x * blockDim.x)
-        emc::triangle_item(A, c);
+__global__ void __launch_bounds__(128) emc_vertices(emc::Args A, const uint32_t* list, const uint32_t* count) {
+    const uint32_t n = *count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        emc::vertex_item(A, list[i]);
 }
 
-__global__ void __launch_bounds__(256) emc_flips(emc::Args A, uint64_t cells, unsigned long long* flips) {
+__global__ void __launch_bounds__(256) emc_triangles(emc::Args A, const uint32_t* list, const uint32_t* count) {
+    const uint32_t n = *count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        emc::triangle_item(A, list[i]);
+}
+
+__global__ void __launch_bounds__(256) emc_flips(emc::Args A, const uint32_t* list, const uint32_t* count,
+                                                 unsigned long long* flips) {
+    const uint32_t n = *count;
     uint32_t mine = 0;
-    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += (uint64_t)gridDim.x * blockDim.x)
-        mine += emc::flip_item(A, c);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        mine += emc::flip_item(A, list[i]);
     if (mine) atomicAdd(flips, (unsigned long long)mine);
 }
 
@@ -118,6 +158,10 @@ static iso_status emc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint32
     const uint64_t off_words = 2 * cells, sum_words = 2ull * nsums;
     if ((s = ensure(ctx, ctx->scan, 4 * (off_words + sum_words) + 64)) != ISO_OK) return s;
     if ((s = ensure(ctx, ctx->edges, 12 * points)) != ISO_OK) return s;
+    // the active cells and their count
+    if ((s = ensure(ctx, ctx->aux2, 4 * cells + 256)) != ISO_OK) return s;
+    uint32_t* active = (uint32_t*)ctx->aux2.p;
+    uint32_t* nactive = active + ((cells + 63) & ~(uint64_t)63);
     uint32_t* scan_base = (uint32_t*)ctx->scan.p;
     uint32_t* sums = scan_base + off_words;
     uint32_t* totals = sums + sum_words;  // vertices, triangles, then the flip counter (8-byte aligned)
@@ -138,8 +182,11 @@ static iso_status emc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint32
     }
     {
         StageTimer timer(ctx, ISO_STAGE_CLASSIFY);
-        emc_count<<<grid_for(ctx, cells, 128, 32), 128, 0, ctx->stream>>>(A, cells);
-        ctx->launches += 2;
+        cudaError_t me = cudaMemsetAsync(nactive, 0, 4, ctx->stream);
+        if (me != cudaSuccess) return cuda_fail(ctx, me, "emc active count");
+        emc_active<<<grid_for(ctx, cells, 256, 16), 256, 0, ctx->stream>>>(A, cells, active, nactive);
+        emc_count<<<grid_for(ctx, cells, 128, 32), 128, 0, ctx->stream>>>(A, active, nactive);
+        ctx->launches += 3;
         if ((s = check_launch(ctx, "emc count")) != ISO_OK) return s;
         if ((s = scan_u32(ctx, A.voff, A.voff, (uint32_t)cells, sums, totals)) != ISO_OK) return s;
         if ((s = scan_u32(ctx, A.toff, A.toff, (uint32_t)cells, sums + nsums, totals + 1)) != ISO_OK) return s;
@@ -158,9 +205,9 @@ static iso_status emc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint32
     A.cap_t = nt;
     {
         StageTimer timer(ctx, ISO_STAGE_EMIT);
-        emc_vertices<<<grid_for(ctx, cells, 128, 32), 128, 0, ctx->stream>>>(A, cells);
-        emc_triangles<<<grid_for(ctx, cells, 256, 16), 256, 0, ctx->stream>>>(A, cells);
-        emc_flips<<<grid_for(ctx, cells, 256, 16), 256, 0, ctx->stream>>>(A, cells, flips);
+        emc_vertices<<<grid_for(ctx, cells, 128, 32), 128, 0, ctx->stream>>>(A, active, nactive);
+        emc_triangles<<<grid_for(ctx, cells, 256, 16), 256, 0, ctx->stream>>>(A, active, nactive);
+        emc_flips<<<grid_for(ctx, cells, 256, 16), 256, 0, ctx->stream>>>(A, active, nactive, flips);
     }
     ctx->launches += 3;
     if ((s = check_launch(ctx, "emc emit")) != ISO_OK) return s;

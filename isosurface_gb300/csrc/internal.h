@@ -55,6 +55,11 @@ struct ProgView {
     const float4* prims = nullptr;
     uint32_t nprims = 0;
     int32_t dom_at = -1;  // constants of a leading domain map, or -1
+    // a bound on the value's Lipschitz constant with respect to the sample
+    // point (0: none known), and a generous bound on the f32 rounding error
+    // of two values the evaluator computes at points in [0, 2]^3
+    float lip = 0.0f;
+    float slack = 0.0f;
 };
 
 }  // namespace iso
@@ -158,10 +163,11 @@ struct iso_program {
     std::vector<float> prims;  // 8 floats per primitive
     float4* d_prims = nullptr;
     int32_t prim_dom_at = -1;
+    float lip = 0.0f, slack = 0.0f;  // see ProgView
     uint64_t uid = 0;  // unique per program created in this process
     iso::ProgView view() const {
         return iso::ProgView{d_ops, d_consts, d_jump, (uint32_t)ops.size(), d_prims, (uint32_t)(prims.size() / 8),
-                             prim_dom_at};
+                             prim_dom_at, lip, slack};
     }
 };
 

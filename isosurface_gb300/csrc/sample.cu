@@ -9,8 +9,10 @@
 // the reference's f32 evaluation.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <utility>
 
+#include "bricks.cuh"
 #include "internal.h"
 #include "vm.cuh"
 
@@ -580,6 +582,17 @@ iso_status attach_normals(iso_ctx* ctx, const iso_program* prog) {
     return ISO_OK;
 }
 
+// Tiles of the culled sampler over one lattice: 4 layers x 4 * ty rows, ty
+// = brick_tile_groups (at most 8 groups of 4 rows, at most BRICK_MAX
+// sub-bricks).
+uint32_t brick_tile_groups(uint32_t W, uint32_t ny) {
+    return std::max(1u, std::min(std::min(8u, (ny + 3) / 4), BRICK_MAX / (4 * W)));
+}
+uint64_t brick_tiles(uint32_t W, uint32_t ny, uint32_t nz) {
+    const uint32_t rows = 4 * brick_tile_groups(W, ny);
+    return (uint64_t)((ny + rows - 1) / rows) * ((nz + 3) / 4);
+}
+
 iso_status launch_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t nx, uint32_t ny, uint32_t nz, float inv,
                               float* field, uint64_t pitch, uint32_t* bits, bool near_only, uint32_t zoff) {
     const uint32_t W = words_per_row(nx);
@@ -632,6 +645,29 @@ iso_status launch_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t nx
             StageTimer timer(ctx, ISO_STAGE_SAMPLE);
             sample_sphere_set<<<grid, 256, smem, ctx->stream>>>(a);
         }
+    } else if (near_only && prog->lip > 0.0f && 4 * W <= BRICK_MAX &&
+               brick_tiles(W, ny, nz) >= (uint64_t)ctx->sms && brick_tiles(W, ny, nz) < (1ull << 22)) {
+        // values only where marching cubes can read them (bricks.cuh): tiles
+        // of 4 layers x up to 32 rows, one block each, then the mixed
+        // sub-bricks over a persistent grid.  A grid with fewer tiles than
+        // SMs takes the plain sampler, whose one launch has less latency.
+        const uint32_t ty = brick_tile_groups(W, ny);
+        const uint32_t rows = 4 * ty, ytiles = (ny + rows - 1) / rows;
+        const uint64_t ntiles = brick_tiles(W, ny, nz);
+        const uint64_t cap = ntiles * 4 * W * ty;  // every sub-brick of every tile
+        iso_status s = ensure(ctx, ctx->tiles, sizeof(BrickTask) * cap + 256);
+        if (s != ISO_OK) return s;
+        BrickTask* list = (BrickTask*)ctx->tiles.p;
+        uint32_t* count = (uint32_t*)((char*)ctx->tiles.p + sizeof(BrickTask) * cap);
+        cudaError_t e = cudaMemsetAsync(count, 0, 4, ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "brick list count");
+        const GridTiles gt{BrickLattice{prog->view(), nx, ny, nz, inv, field, pitch, bits, W, zoff}, rows, ytiles};
+        StageTimer timer(ctx, ISO_STAGE_SAMPLE);
+        brick_classify<GridTiles><<<(unsigned)ntiles, 256, 0, ctx->stream>>>(gt, list, count, (uint32_t)cap,
+                                                                              ctx->d_err);
+        brick_rows<GridTiles><<<brick_rows_blocks<GridTiles>(ctx->sms), 256, 0, ctx->stream>>>(gt, list, count,
+                                                                                               (uint32_t)cap);
+        ctx->launches++;
     } else {
         uint64_t warps = (uint64_t)W * ny * nz;
         StageTimer timer(ctx, ISO_STAGE_SAMPLE);

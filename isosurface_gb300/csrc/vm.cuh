@@ -163,22 +163,50 @@ static __host__ __device__ __noinline__ float eval_range(const ProgView& pv, uin
     return tos;
 }
 
+// Primitive i of ProgView::prims at q (a point after the leading domain map):
+// the translate and primitive operations of its ops.
+__host__ __device__ __forceinline__ float prim_at(const ProgView& pv, uint32_t i, V3 q) {
+    const float4 c = ld_ro(pv.prims + 2 * i), a = ld_ro(pv.prims + 2 * i + 1);
+    const V3 t = v3(q.x - c.x, q.y - c.y, q.z - c.z);
+    const uint32_t type = float_bits(c.w);
+    if (type == OP_SPHERE) return sd_sphere(t, a.x);
+    if (type == OP_BOX) return sd_box(t, a.x, a.y, a.z);
+    if (type == OP_CYLINDER) return sd_cylinder(t, a.x, a.y);
+    return sd_torus(t, a.x, a.y);
+}
+
+__host__ __device__ __forceinline__ V3 prims_point(const ProgView& pv, V3 p) {
+    return pv.dom_at >= 0 ? pt_apply(OP_PT_DOMAIN, pv.k + pv.dom_at, p) : p;
+}
+
 // A hard union of translated primitives (ProgView::prims): the same
 // translate, primitive and fminf operations as the ops, in the same order.
 static __host__ __device__ __noinline__ float eval_prims(const ProgView& pv, V3 p) {
-    const V3 q = pv.dom_at >= 0 ? pt_apply(OP_PT_DOMAIN, pv.k + pv.dom_at, p) : p;
+    const V3 q = prims_point(pv, p);
     float v = 0.0f;
     for (uint32_t i = 0; i < pv.nprims; ++i) {
-        const float4 c = ld_ro(pv.prims + 2 * i), a = ld_ro(pv.prims + 2 * i + 1);
-        const V3 t = v3(q.x - c.x, q.y - c.y, q.z - c.z);
-        const uint32_t type = float_bits(c.w);
-        float d;
-        if (type == OP_SPHERE) d = sd_sphere(t, a.x);
-        else if (type == OP_BOX) d = sd_box(t, a.x, a.y, a.z);
-        else if (type == OP_CYLINDER) d = sd_cylinder(t, a.x, a.y);
-        else d = sd_torus(t, a.x, a.y);
+        const float d = prim_at(pv, i, q);
         v = (i == 0) ? d : fminf(v, d);
     }
+    return v;
+}
+
+// The same union over the primitives whose bits are set in `keep` (nonzero;
+// at most 32 primitives), in the same order.  Equal to eval_prims wherever
+// every dropped primitive's value exceeds some kept one's: fminf returns one
+// of its operands, so the minimum over a subset that holds the minimiser is
+// the minimum over all.
+__host__ __device__ __forceinline__ uint32_t lowest_bit(uint32_t m) {
+#ifdef __CUDA_ARCH__
+    return (uint32_t)(__ffs((int)m) - 1);
+#else
+    return (uint32_t)__builtin_ctz(m);
+#endif
+}
+static __host__ __device__ __noinline__ float eval_prims_kept(const ProgView& pv, uint32_t keep, V3 p) {
+    const V3 q = prims_point(pv, p);
+    float v = prim_at(pv, lowest_bit(keep), q);
+    for (keep &= keep - 1; keep; keep &= keep - 1) v = fminf(v, prim_at(pv, lowest_bit(keep), q));
     return v;
 }
 

@@ -132,6 +132,15 @@ extern "C" {
         field: *mut f32,
         pitch: u64,
     ) -> IsoStatus;
+    pub fn iso_sample_grid_near(
+        ctx: *mut IsoCtx,
+        prog: *const IsoProgram,
+        size: u32,
+        field: *mut f32,
+        pitch: u64,
+        bits: *mut u32,
+    ) -> IsoStatus;
+    pub fn iso_program_lipschitz(prog: *const IsoProgram, lip: *mut f32) -> IsoStatus;
     pub fn iso_mc_extract(
         ctx: *mut IsoCtx,
         prog: *const IsoProgram,

@@ -1,0 +1,135 @@
+"""Culled sampling for the extractors (iso_sample_grid_near, the batch
+sampler): sign bits everywhere, values wherever marching cubes can read them.
+
+Against the full sampler (iso_sample_grid, itself pinned to the oracle in
+test_mc_gpu.py) on the same program and size:
+  * every sign bit is equal (bits past the last sample of a row clear);
+  * every value written is bit-identical, and every end of an edge whose
+    signs differ (the only values marching cubes reads) is written;
+  * the culling is real: far from the surface values are left unwritten;
+and the meshes extracted through the culled sampler equal the meshes of the
+full field byte for byte.  Programs: the MarchingCubes test sources, random
+chunk scenes (unions of translated primitives, which also prune primitives
+per sub-brick) and a domain map with a large scale."""
+import numpy as np
+import pytest
+
+from isosurface_gb300 import scenes
+from isosurface_gb300 import source as S
+from isosurface_gb300.scenes import SplitMix64
+
+from test_mc_gpu import _sources
+
+pytestmark = pytest.mark.gpu
+
+
+def _programs():
+    out = dict(_sources())
+    rng = SplitMix64(2024)
+    for i in range(4):
+        out["chunk%d" % i] = scenes.chunk_scene(rng)
+    out["scaled_domain"] = S.DomainMap(S.Union(S.Translate(S.Sphere(300.0), (100.0, 0.0, 0.0)),
+                                               S.Translate(S.Torus(250.0, 60.0), (-120.0, 50.0, 0.0))),
+                                       scale=(1000.0, 1000.0, 1000.0), offset=(-500.0, -500.0, -500.0))
+    out["csg_rigid"] = scenes.csg(seed=7)
+    return out
+
+
+# programs on the culled general path whose surface is small against the grid
+CULLED = {"box", "csg", "csg_rigid", "cylinder", "intersection", "prim_union", "scaled_domain", "smooth", "sphere",
+          "torus", "central_difference"}
+
+
+def _pack(inside, W):
+    import torch
+    nz, ny, nx = inside.shape
+    pad = torch.zeros((nz, ny, 32 * W), dtype=torch.int64, device=inside.device)
+    pad[:, :, :nx] = inside.to(torch.int64)
+    weights = torch.bitwise_left_shift(torch.ones(32, dtype=torch.int64, device=inside.device),
+                                       torch.arange(32, device=inside.device))
+    return (pad.view(nz, ny, W, 32) * weights).sum(-1)
+
+
+def _crossing_ends(inside):
+    import torch
+    need = torch.zeros_like(inside)
+    for axis in (0, 1, 2):
+        n = inside.shape[axis]
+        a = inside.narrow(axis, 0, n - 1)
+        b = inside.narrow(axis, 1, n - 1)
+        d = a != b
+        need.narrow(axis, 0, n - 1).logical_or_(d)
+        need.narrow(axis, 1, n - 1).logical_or_(d)
+    return need
+
+
+# below about one tile of 4 layers x 32 rows per SM (here 17 and 65) the
+# library takes the plain sampler; 161 and 200 take the culled one
+@pytest.mark.parametrize("name", sorted(_programs()))
+@pytest.mark.parametrize("size", [17, 65, 161, 200])
+def test_near_sampling_matches_full(ctx, name, size):
+    import torch
+    src = _programs()[name]
+    pitch = size + 3
+    W = (size + 31) // 32
+    full = torch.empty(((size + 1) * size * pitch,), dtype=torch.float32, device="cuda")
+    ctx.sample_grid(src, size, full.data_ptr(), pitch)
+    near = torch.full_like(full, float("nan"))
+    bits = torch.full(((size + 1) * size * W,), -1, dtype=torch.int32, device="cuda")
+    ctx.sample_grid_near(src, size, near.data_ptr(), pitch, bits.data_ptr())
+    f = full.view(size + 1, size, pitch)[:, :, :size]
+    g = near.view(size + 1, size, pitch)[:, :, :size]
+    assert not torch.isnan(f).any()
+    inside = ~(f > 0)
+    want_bits = _pack(inside, W)
+    got_bits = bits.view(size + 1, size, W).to(torch.int64) & 0xFFFFFFFF
+    assert torch.equal(got_bits, want_bits)
+    written = ~torch.isnan(g)
+    assert torch.equal(f.view(torch.int32)[written], g.view(torch.int32)[written])
+    need = _crossing_ends(inside)
+    assert bool(written[need].all()), int((need & ~written).sum())
+    if size == 200 and name in CULLED:
+        # far from the surface nothing is evaluated
+        assert float(written.float().mean()) < 0.5
+
+
+@pytest.mark.parametrize("name", ["csg", "prim_union", "smooth", "central_difference", "chunk1", "scaled_domain"])
+def test_culled_mesh_equals_full_field_mesh(ctx, name):
+    import torch
+    src = _programs()[name]
+    size = 161
+    pitch = size
+    full = torch.empty(((size + 1) * size * pitch,), dtype=torch.float32, device="cuda")
+    ctx.sample_grid(src, size, full.data_ptr(), pitch)
+    want = ctx.download(ctx.mc_extract_field(full.data_ptr(), size, size, size + 1, pitch))
+    got = ctx.download(ctx.mc_extract(src, size))
+    assert np.array_equal(got.vertices, want.vertices)
+    assert np.array_equal(got.indices, want.indices)
+
+
+@pytest.mark.parametrize("name", ["csg", "prim_union", "chunk2"])
+def test_culled_mesh_equals_oracle(ctx, name):
+    import oracle
+    src = _programs()[name]
+    want = oracle.Program(S.lower(src)).marching_cubes(161)
+    got = ctx.download(ctx.mc_extract(src, 161, keys=True), keys=True)
+    assert np.array_equal(got.keys, want.keys)
+    assert np.array_equal(got.indices, want.indices)
+    assert np.array_equal(got.vertices, want.vertices)
+
+
+@pytest.mark.parametrize("name", sorted(_programs()))
+def test_lipschitz_bound_holds(ctx, name):
+    """The bound the culling relies on, checked on random pairs of nearby
+    points: |f(a) - f(b)| <= lip |a - b| (up to f32 rounding)."""
+    src = _programs()[name]
+    lip = ctx.lipschitz(src)
+    assert lip > 0
+    rng = np.random.default_rng(3)
+    a = rng.uniform(0.0, 1.0, size=(20000, 3)).astype(np.float32)
+    b = (a + rng.normal(0.0, 0.01, size=a.shape)).astype(np.float32)
+    fa = ctx.sample_points(src, a).astype(np.float64)
+    fb = ctx.sample_points(src, b).astype(np.float64)
+    dist = np.linalg.norm(a.astype(np.float64) - b.astype(np.float64), axis=1)
+    slack = 1e-5 * (1.0 + np.maximum(np.abs(fa), np.abs(fb)))
+    assert np.all(np.abs(fa - fb) <= lip * dist * (1 + 1e-4) + slack)
