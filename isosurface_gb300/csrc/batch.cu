@@ -69,7 +69,7 @@ struct BatchTiles {
     __device__ __forceinline__ BrickTile tile(uint32_t t) const {
         const Tile tl = tiles[t];
         const SampleGrid sg = grids[tl.grid];
-        return BrickTile{BrickLattice{sg.pv, sg.n, sg.n, sg.n + 1, sg.inv, sg.field, sg.pitch, sg.bits, sg.W, 0},
+        return BrickTile{BrickLattice{sg.pv, sg.n, sg.n, sg.n + 1, sg.inv, sg.field, sg.pitch, sg.bits, sg.W, 0, 1.0f},
                          tl.y0, tl.y1, tl.z0, tl.z1};
     }
 };
@@ -79,7 +79,7 @@ struct BatchTiles {
 __global__ void __launch_bounds__(256) batch_sample(BatchTiles bt, uint32_t ntiles, uint32_t* next) {
     __shared__ uint32_t s_tile, s_n;
     __shared__ uint8_t s_cls[BRICK_MAX];
-    __shared__ uint32_t s_keep[BRICK_MAX];
+    __shared__ uint64_t s_keep[BRICK_MAX];
     __shared__ uint32_t s_list[BRICK_MAX];
     while (true) {
         __syncthreads();  // the previous tile is done with the shared arrays
@@ -184,16 +184,16 @@ iso_status build_tiles(iso_batch* b) {
 
 // blocks of batch_sample that fill every SM (looked up once per process)
 unsigned sample_blocks(int sms) {
-    static int per_sm = 0;
-    if (per_sm == 0) {
-        int b = 0;
+    static std::atomic<int> per_sm{0};
+    int b = per_sm.load(std::memory_order_relaxed);
+    if (b == 0) {
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batch_sample, 256, 0) != cudaSuccess || b < 1) {
             cudaGetLastError();
             b = 4;
         }
-        per_sm = b;
+        per_sm.store(b, std::memory_order_relaxed);
     }
-    return (unsigned)(per_sm * std::max(sms, 1));
+    return (unsigned)(b * std::max(sms, 1));
 }
 
 // the culled sampler over `ntiles` tiles (the queue counter zeroed first)

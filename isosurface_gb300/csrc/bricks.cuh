@@ -11,7 +11,7 @@
 // evaluated with the ordinary evaluator, so every value written is
 // bit-identical to sample_generic's, and so is every sign bit.
 //
-// For a hard union of translated primitives (ProgView::prims, at most 32)
+// For a hard union of translated primitives (ProgView::prims, at most 64)
 // each sub-brick also keeps only the primitives that can attain the minimum
 // in it: primitive i's values over the sub-brick lie within lip * h of
 // d_i(centre), so i is dropped when d_i - lip * h exceeds min_j (d_j + lip *
@@ -35,6 +35,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "internal.h"
 #include "vm.cuh"
 
@@ -52,6 +54,7 @@ struct BrickLattice {
     uint32_t* bits;
     uint32_t W;     // sign words per row
     uint32_t zoff;  // lattice z of layer 0 (a slab of a larger lattice)
+    float reach_steps;  // values are needed within this many lattice steps' worth of change of zero
 };
 
 // One tile: the lattice and its rows / layers.
@@ -62,8 +65,18 @@ struct BrickTile {
 
 // A mixed sub-brick: tile * BRICK_MAX + sub-brick, and the primitives it keeps.
 struct BrickTask {
-    uint32_t tile_sb, keep;
+    uint32_t tile_sb, unused;
+    uint64_t keep;
 };
+
+constexpr uint32_t PRUNE_MAX = 64;  // primitives a keep mask covers
+
+// OR of a 64-bit mask over the warp (every lane calls it).
+__device__ __forceinline__ uint64_t warp_or64(uint64_t m) {
+    const uint32_t lo = __reduce_or_sync(0xFFFFFFFFu, (uint32_t)m);
+    const uint32_t hi = __reduce_or_sync(0xFFFFFFFFu, (uint32_t)(m >> 32));
+    return ((uint64_t)hi << 32) | lo;
+}
 
 // The tiles of one lattice: 4 layers x `rows` rows each.
 struct GridTiles {
@@ -82,17 +95,19 @@ __host__ __device__ __forceinline__ uint32_t brick_count(uint32_t W, uint32_t ro
 
 // Class and kept primitives of every sub-brick of a tile, into shared memory
 // (every thread of the block calls it; no barrier at the end).
-__device__ __forceinline__ void brick_classes(const BrickTile& T, uint8_t* s_cls, uint32_t* s_keep) {
+__device__ __forceinline__ void brick_classes(const BrickTile& T, uint8_t* s_cls, uint64_t* s_keep) {
     const BrickLattice& g = T.g;
     const ProgView& pv = g.pv;
     const uint32_t SX = 4 * g.W, SY = (T.y1 - T.y0 + 3) / 4, SZ = (T.z1 - T.z0 + 3) / 4;
     const uint32_t nsb = SX * SY * SZ;
     const bool cull = pv.lip > 0.0f;
-    const bool prune = cull && pv.prims != nullptr && pv.nprims <= 32;
-    // both ends of a crossing edge lie within lip * inv of zero (rounded up)
-    const float reach = pv.lip * g.inv * (1.0f + 1.0f / 1024.0f) + pv.slack;
+    const bool prune = cull && pv.prims != nullptr && pv.nprims <= PRUNE_MAX;
+    // both ends of a crossing edge lie within lip * inv of zero (rounded up);
+    // a caller may need values further out (reach_steps > 1)
+    const float reach = pv.lip * g.inv * g.reach_steps * (1.0f + 1.0f / 1024.0f) + pv.slack;
     for (uint32_t s = threadIdx.x; s < nsb; s += blockDim.x) {
-        uint32_t cls = BRICK_MIXED, keep = 0xFFFFFFFFu;
+        uint32_t cls = BRICK_MIXED;
+        uint64_t keep = ~0ull;
         if (cull) {
             const uint32_t sx = s % SX, sy = (s / SX) % SY, sz = s / (SX * SY);
             const uint32_t xa = 8 * sx, ya = T.y0 + 4 * sy, za = T.z0 + 4 * sz;
@@ -117,7 +132,7 @@ __device__ __forceinline__ void brick_classes(const BrickTile& T, uint8_t* s_cls
                     }
                     keep = 0;
                     for (uint32_t i = 0; i < pv.nprims; ++i)
-                        if (!(prim_at(pv, i, q) - spread > upper)) keep |= 1u << i;
+                        if (!(prim_at(pv, i, q) - spread > upper)) keep |= 1ull << i;
                 } else {
                     v = eval_scalar(pv, c);
                 }
@@ -183,7 +198,7 @@ __device__ __forceinline__ uint32_t brick_group_bits(const BrickTile& T, uint32_
 // = ~0u: none) and the eight lanes' signs go out as one byte of the row's
 // sign word.  `keep` (the same in every lane) holds every primitive any of
 // the sub-bricks keeps.  Every lane of the warp calls it.
-__device__ __forceinline__ void brick_quad(const BrickTile& T, uint32_t sb, uint32_t keep) {
+__device__ __forceinline__ void brick_quad(const BrickTile& T, uint32_t sb, uint64_t keep) {
     const BrickLattice& g = T.g;
     const ProgView& pv = g.pv;
     const uint32_t lane = threadIdx.x & 31;
@@ -196,7 +211,7 @@ __device__ __forceinline__ void brick_quad(const BrickTile& T, uint32_t sb, uint
         za = T.z0 + 4 * (sb / (SX * SY));
     }
     const uint32_t x = 8 * sx + (lane & 7);
-    const bool prune = pv.lip > 0.0f && pv.prims != nullptr && pv.nprims <= 32;
+    const bool prune = pv.lip > 0.0f && pv.prims != nullptr && pv.nprims <= PRUNE_MAX;
     for (uint32_t r = 0; r < 16; ++r) {
         const uint32_t y = ya + (r & 3), z = za + (r >> 2);
         const bool row_ok = have && y < T.y1 && z < T.z1;
@@ -217,7 +232,7 @@ __device__ __forceinline__ void brick_quad(const BrickTile& T, uint32_t sb, uint
 // Classify one tile, write its decided sign bits and list its mixed
 // sub-bricks (every thread of the block calls it).
 __device__ __forceinline__ void brick_classify_tile(const BrickTile& T, uint32_t tile, uint8_t* s_cls,
-                                                    uint32_t* s_keep, BrickTask* list, uint32_t* count,
+                                                    uint64_t* s_keep, BrickTask* list, uint32_t* count,
                                                     uint32_t cap, uint32_t* err) {
     brick_classes(T, s_cls, s_keep);
     __syncthreads();
@@ -239,7 +254,7 @@ __device__ __forceinline__ void brick_classify_tile(const BrickTile& T, uint32_t
             base = __shfl_sync(0xFFFFFFFFu, base, 31) + incl - n;
             for (uint32_t m = mixed; m; m &= m - 1, ++base) {
                 const uint32_t sb = 4 * gi + (uint32_t)(__ffs(m) - 1);
-                if (base < cap) list[base] = BrickTask{tile * BRICK_MAX + sb, s_keep[sb]};
+                if (base < cap) list[base] = BrickTask{tile * BRICK_MAX + sb, 0, s_keep[sb]};
                 else atomicOr(err, DERR_CAPACITY);
             }
         }
@@ -249,7 +264,7 @@ __device__ __forceinline__ void brick_classify_tile(const BrickTile& T, uint32_t
 // Sample a whole tile in the block: classes, decided sign bits, then the
 // mixed sub-bricks four to a warp from a list in shared memory (every thread
 // of the block calls it).
-__device__ __forceinline__ void brick_tile(const BrickTile& T, uint8_t* s_cls, uint32_t* s_keep, uint32_t* s_list,
+__device__ __forceinline__ void brick_tile(const BrickTile& T, uint8_t* s_cls, uint64_t* s_keep, uint32_t* s_list,
                                            uint32_t* s_n) {
     if (threadIdx.x == 0) *s_n = 0;
     brick_classes(T, s_cls, s_keep);
@@ -267,7 +282,7 @@ __device__ __forceinline__ void brick_tile(const BrickTile& T, uint8_t* s_cls, u
     for (uint32_t q = 4 * (threadIdx.x >> 5); q < n; q += 4 * (blockDim.x >> 5)) {
         const uint32_t e = q + (lane >> 3);
         const uint32_t sb = e < n ? s_list[e] : 0xFFFFFFFFu;
-        const uint32_t keep = __reduce_or_sync(0xFFFFFFFFu, e < n ? s_keep[sb] : 0u);
+        const uint64_t keep = warp_or64(e < n ? s_keep[sb] : 0ull);
         brick_quad(T, sb, keep);
     }
 }
@@ -277,7 +292,7 @@ template <class Tiles>
 __global__ void __launch_bounds__(256) brick_classify(Tiles tiles, BrickTask* list, uint32_t* count, uint32_t cap,
                                                       uint32_t* err) {
     __shared__ uint8_t s_cls[BRICK_MAX];
-    __shared__ uint32_t s_keep[BRICK_MAX];
+    __shared__ uint64_t s_keep[BRICK_MAX];
     brick_classify_tile(tiles.tile(blockIdx.x), blockIdx.x, s_cls, s_keep, list, count, cap, err);
 }
 
@@ -289,9 +304,9 @@ __global__ void __launch_bounds__(256) brick_rows(Tiles tiles, const BrickTask* 
     const uint32_t warps = gridDim.x * (blockDim.x >> 5);
     for (uint32_t q = 4 * (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)); q < n; q += 4 * warps) {
         const uint32_t e = q + (lane >> 3);
-        BrickTask k{0, 0};
+        BrickTask k{0, 0, 0};
         if (e < n) k = list[e];
-        const uint32_t keep = __reduce_or_sync(0xFFFFFFFFu, k.keep);
+        const uint64_t keep = warp_or64(k.keep);
         brick_quad(tiles.tile(k.tile_sb / BRICK_MAX), e < n ? k.tile_sb % BRICK_MAX : 0xFFFFFFFFu, keep);
     }
 }
@@ -300,16 +315,16 @@ __global__ void __launch_bounds__(256) brick_rows(Tiles tiles, const BrickTask* 
 // for these tiles, looked up once per process).
 template <class Tiles>
 inline unsigned brick_rows_blocks(int sms) {
-    static int per_sm = 0;
-    if (per_sm == 0) {
-        int b = 0;
+    static std::atomic<int> per_sm{0};
+    int b = per_sm.load(std::memory_order_relaxed);
+    if (b == 0) {
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, brick_rows<Tiles>, 256, 0) != cudaSuccess || b < 1) {
             cudaGetLastError();
             b = 4;
         }
-        per_sm = b;
+        per_sm.store(b, std::memory_order_relaxed);
     }
-    return (unsigned)(per_sm * (sms > 0 ? sms : 1));
+    return (unsigned)(b * (sms > 0 ? sms : 1));
 }
 
 }  // namespace iso

@@ -2,6 +2,8 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <mutex>
+#include <unordered_set>
 #include <utility>
 
 #include <algorithm>
@@ -376,6 +378,39 @@ iso_status sample_lattice_slab(iso_ctx* ctx, const iso_program* prog, uint32_t s
 
 }  // namespace iso
 
+namespace {
+
+// Contexts alive in this process: a program destroyed after its context
+// (a caller's order, or a garbage collector's) frees its block directly.
+std::mutex g_ctx_mutex;
+std::unordered_set<const iso_ctx*> g_live_ctx;
+
+constexpr size_t POOL_BLOCKS = 32;  // free program blocks a context keeps
+
+// A device block of at least `bytes` for a program: the smallest free one
+// of the context that is not more than twice too large, else a new one.
+cudaError_t program_block(iso_ctx* ctx, size_t bytes, void** block, size_t* cap) {
+    {
+        std::lock_guard<std::mutex> lock(g_ctx_mutex);
+        auto& fb = ctx->free_blocks;
+        size_t best = fb.size();
+        for (size_t i = 0; i < fb.size(); ++i)
+            if (fb[i].first >= bytes && fb[i].first <= 2 * bytes + 4096 &&
+                (best == fb.size() || fb[i].first < fb[best].first))
+                best = i;
+        if (best < fb.size()) {
+            *cap = fb[best].first;
+            *block = fb[best].second;
+            fb.erase(fb.begin() + (ptrdiff_t)best);
+            return cudaSuccess;
+        }
+    }
+    *cap = (bytes + 255) & ~(size_t)255;
+    return cudaMalloc(block, *cap);
+}
+
+}  // namespace
+
 extern "C" {
 
 const char* iso_status_str(iso_status s) {
@@ -422,6 +457,10 @@ iso_status iso_ctx_create(int device, iso_ctx** out) {
         return r;
     }
     ctx->stream = ctx->own_stream;
+    {
+        std::lock_guard<std::mutex> lock(g_ctx_mutex);
+        g_live_ctx.insert(ctx);
+    }
     *out = ctx;
     return ISO_OK;
 }
@@ -430,6 +469,12 @@ iso_status iso_ctx_destroy(iso_ctx* ctx) {
     if (!ctx) return ISO_ERR_INVALID_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    {
+        std::lock_guard<std::mutex> lock(g_ctx_mutex);
+        g_live_ctx.erase(ctx);
+        for (auto& b : ctx->free_blocks) cudaFree(b.second);
+        ctx->free_blocks.clear();
+    }
     DevBuf* bufs[] = {&ctx->field, &ctx->bits, &ctx->rowtri, &ctx->rowvert, &ctx->scan, &ctx->aux,
                       &ctx->aux2, &ctx->aux3, &ctx->tiles, &ctx->edges, &ctx->mesh_v, &ctx->mesh_i, &ctx->mesh_k};
     for (DevBuf* b : bufs)
@@ -456,6 +501,9 @@ iso_status iso_ctx_get_stream(iso_ctx* ctx, void** stream) {
 
 iso_status iso_ctx_set_stream(iso_ctx* ctx, void* stream) {
     if (!ctx) return ISO_ERR_INVALID_ARG;
+    // program uploads are ordered on the context's stream: let them land
+    // before work moves to another one
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
     return ISO_OK;
 }
@@ -509,6 +557,7 @@ iso_status iso_program_create(iso_ctx* ctx, const uint8_t* bytes, size_t len, is
     iso_program* p = new (std::nothrow) iso_program();
     if (!p) return ISO_ERR_OUT_OF_MEMORY;
     p->ctx = ctx;
+    p->device = ctx->device;
     static std::atomic<uint64_t> next_uid{1};
     p->uid = next_uid.fetch_add(1);
     p->ops.resize(h[1]);
@@ -528,8 +577,10 @@ iso_status iso_program_create(iso_ctx* ctx, const uint8_t* bytes, size_t len, is
         return s;
     }
     // one device block holds every array (16-byte aligned pieces, so the
-    // sphere data of the fast path takes float4 loads): one allocation, one
-    // copy, one free per program
+    // sphere data of the fast path takes float4 loads), from the context's
+    // pool of blocks that destroyed programs left (else a new allocation),
+    // filled by one copy ordered on the context's stream: after the work
+    // that used the block before, before the work that uses it now
     const size_t nk = p->consts.size() + 4;
     auto at16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
     const size_t o_ops = 0, o_consts = at16(o_ops + 4 * p->ops.size()), o_jump = at16(o_consts + 4 * nk);
@@ -542,8 +593,11 @@ iso_status iso_program_create(iso_ctx* ctx, const uint8_t* bytes, size_t len, is
     if (!p->jump.empty()) std::memcpy(staged.data() + o_jump, p->jump.data(), 4 * p->jump.size());
     if (set_bytes) std::memcpy(staged.data() + o_set, p->consts.data() + p->set_at + 3, set_bytes);
     if (!p->prims.empty()) std::memcpy(staged.data() + o_prims, p->prims.data(), 4 * p->prims.size());
+    uint64_t hash = 0xCBF29CE484222325ull;  // FNV-1a 64
+    for (size_t i = 0; i < len; ++i) hash = (hash ^ bytes[i]) * 0x100000001B3ull;
+    p->content_hash = hash;
     unsigned char* block = nullptr;
-    cudaError_t e = cudaMalloc(&block, total);
+    cudaError_t e = program_block(ctx, total, (void**)&block, &p->block_bytes);
     if (e == cudaSuccess) {
         p->d_block = block;
         p->d_ops = (uint32_t*)(block + o_ops);
@@ -551,7 +605,8 @@ iso_status iso_program_create(iso_ctx* ctx, const uint8_t* bytes, size_t len, is
         p->d_jump = (int32_t*)(block + o_jump);
         if (set_bytes) p->d_set = (float*)(block + o_set);
         if (!p->prims.empty()) p->d_prims = (float4*)(block + o_prims);
-        e = cudaMemcpy(block, staged.data(), total, cudaMemcpyHostToDevice);
+        // from pageable memory: returns once the bytes are staged
+        e = cudaMemcpyAsync(block, staged.data(), total, cudaMemcpyHostToDevice, ctx->stream);
     }
     if (e != cudaSuccess) {
         iso_status r = cuda_fail(ctx, e, "program upload");
@@ -564,8 +619,27 @@ iso_status iso_program_create(iso_ctx* ctx, const uint8_t* bytes, size_t len, is
 
 iso_status iso_program_destroy(iso_program* p) {
     if (!p) return ISO_ERR_INVALID_ARG;
-    if (p->ctx) cudaSetDevice(p->ctx->device);
-    if (p->d_block) cudaFree(p->d_block);
+    if (p->d_block) {
+        bool pooled = false;
+        {
+            std::lock_guard<std::mutex> lock(g_ctx_mutex);
+            if (p->ctx && g_live_ctx.count(p->ctx) && p->ctx->free_blocks.size() < POOL_BLOCKS) {
+                // kept for the context's next upload, which its stream orders
+                // after every kernel queued so far that reads this block
+                p->ctx->free_blocks.push_back({p->block_bytes, p->d_block});
+                pooled = true;
+            }
+        }
+        if (!pooled) {
+            // the context may be gone: the program keeps its own device
+            int cur = 0;
+            const bool moved = cudaGetDevice(&cur) == cudaSuccess && cur != p->device &&
+                               cudaSetDevice(p->device) == cudaSuccess;
+            cudaFree(p->d_block);
+            if (moved) cudaSetDevice(cur);
+            cudaGetLastError();
+        }
+    }
     delete p;
     return ISO_OK;
 }

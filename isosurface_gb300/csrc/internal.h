@@ -107,8 +107,13 @@ struct iso_ctx {
     } host_out;
     struct McPlan {
         cudaGraphExec_t exec = nullptr;
-        const iso_program* prog = nullptr;
         uint64_t prog_uid = 0;
+        // the recorded program's device block and contents: a program
+        // uploaded again with the same contents into the same block (the
+        // block pool hands it back) replays the recording too
+        const void* prog_block = nullptr;
+        std::vector<uint32_t> prog_ops;
+        std::vector<float> prog_consts;
         uint32_t size = 0, flags = 0;
         void* bufs[12] = {};
         float* host_v = nullptr;  // host buffers baked into the recorded kernels
@@ -117,7 +122,11 @@ struct iso_ctx {
         bool host_armed = false;  // the recorded kernels deliver to the host buffers
         uint64_t launches = 0;
     } mc_plan;
-    uint64_t mc_last_key[3] = {};  // (program uid, size, flags) of the last eager extraction
+    uint64_t mc_last_key[3] = {};  // (program identity, size, flags) of the last eager extraction
+    // device blocks of destroyed programs, reused by the next uploads
+    // (capacity, block): no allocation or free, and so no device-wide
+    // synchronisation, while programs come and go at a steady size
+    std::vector<std::pair<size_t, void*>> free_blocks;
     // the same for LinearHashedMarchingCubes (lhmc.cu), with the counts found
     struct LhmcPlan {
         cudaGraphExec_t exec = nullptr;
@@ -145,6 +154,7 @@ struct StageTimer {
 
 struct iso_program {
     iso_ctx* ctx = nullptr;
+    int device = 0;  // the context's device (the program may outlive the context)
     std::vector<uint32_t> ops;
     std::vector<float> consts;
     std::vector<int32_t> jump;
@@ -164,6 +174,8 @@ struct iso_program {
     float4* d_prims = nullptr;
     int32_t prim_dom_at = -1;
     float lip = 0.0f, slack = 0.0f;  // see ProgView
+    size_t block_bytes = 0;          // capacity of d_block
+    uint64_t content_hash = 0;       // FNV-1a of the program bytes
     uint64_t uid = 0;  // unique per program created in this process
     iso::ProgView view() const {
         return iso::ProgView{d_ops, d_consts, d_jump, (uint32_t)ops.size(), d_prims, (uint32_t)(prims.size() / 8),
@@ -181,9 +193,12 @@ iso_status read_device_errors(iso_ctx* ctx);
 iso_status set_device(iso_ctx* ctx);
 
 // sample.cu
+// near_only: sign bits everywhere, values at least within reach_steps
+// lattice steps' worth of value change of zero (1: the ends of crossing
+// edges, which marching cubes reads); other values may be left unwritten
 iso_status launch_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t nx, uint32_t ny, uint32_t nz,
                               float inv, float* field, uint64_t pitch, uint32_t* bits, bool near_only = false,
-                              uint32_t zoff = 0);
+                              uint32_t zoff = 0, float reach_steps = 1.0f);
 iso_status launch_sign_bits(iso_ctx* ctx, const float* field, uint32_t nx, uint32_t ny, uint32_t nz,
                             uint64_t pitch, uint32_t* bits);
 iso_status launch_sample_points(iso_ctx* ctx, const iso_program* prog, const float* d_pts, uint64_t n,

@@ -594,9 +594,38 @@ uint64_t brick_tiles(uint32_t W, uint32_t ny, uint32_t nz) {
 }
 
 iso_status launch_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t nx, uint32_t ny, uint32_t nz, float inv,
-                              float* field, uint64_t pitch, uint32_t* bits, bool near_only, uint32_t zoff) {
+                              float* field, uint64_t pitch, uint32_t* bits, bool near_only, uint32_t zoff,
+                              float reach_steps) {
     const uint32_t W = words_per_row(nx);
-    if (prog->kind == PK_SPHERE_SET_HARD && prog->set_n <= 8192) {
+    // the culled sampler (bricks.cuh) for the extractors on general
+    // programs; hard sphere unions have their own culling below
+    const bool bricks = near_only && prog->lip > 0.0f && 4 * W <= BRICK_MAX &&
+                        brick_tiles(W, ny, nz) >= (uint64_t)ctx->sms && brick_tiles(W, ny, nz) < (1ull << 22) &&
+                        !(prog->kind == PK_SPHERE_SET_HARD && prog->set_n <= 8192);
+    if (bricks) {
+        // values only where marching cubes can read them (bricks.cuh): tiles
+        // of 4 layers x up to 32 rows, one block each, then the mixed
+        // sub-bricks over a persistent grid.  A grid with fewer tiles than
+        // SMs takes the plain sampler, whose one launch has less latency.
+        const uint32_t ty = brick_tile_groups(W, ny);
+        const uint32_t rows = 4 * ty, ytiles = (ny + rows - 1) / rows;
+        const uint64_t ntiles = brick_tiles(W, ny, nz);
+        const uint64_t cap = ntiles * 4 * W * ty;  // every sub-brick of every tile
+        iso_status s = ensure(ctx, ctx->tiles, sizeof(BrickTask) * cap + 256);
+        if (s != ISO_OK) return s;
+        BrickTask* list = (BrickTask*)ctx->tiles.p;
+        uint32_t* count = (uint32_t*)((char*)ctx->tiles.p + sizeof(BrickTask) * cap);
+        cudaError_t e = cudaMemsetAsync(count, 0, 4, ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "brick list count");
+        const GridTiles gt{BrickLattice{prog->view(), nx, ny, nz, inv, field, pitch, bits, W, zoff, reach_steps}, rows,
+                           ytiles};
+        StageTimer timer(ctx, ISO_STAGE_SAMPLE);
+        brick_classify<GridTiles><<<(unsigned)ntiles, 256, 0, ctx->stream>>>(gt, list, count, (uint32_t)cap,
+                                                                              ctx->d_err);
+        brick_rows<GridTiles><<<brick_rows_blocks<GridTiles>(ctx->sms), 256, 0, ctx->stream>>>(gt, list, count,
+                                                                                               (uint32_t)cap);
+        ctx->launches++;
+    } else if (prog->kind == PK_SPHERE_SET_HARD && prog->set_n <= 8192) {
         near_only = near_only && prog->set_n <= 4096 && nx > 1;
         SetArgs a;
         a.spheres = prog->d_set;
@@ -612,7 +641,7 @@ iso_status launch_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t nx
         // is 1-Lipschitz in world units: both ends lie within one step (the
         // largest axis step after the domain map) of zero, plus rounding slack
         const float step = inv * (prog->has_domain ? fmaxf(fabsf(a.sx), fmaxf(fabsf(a.sy), fabsf(a.sz))) : 1.0f);
-        a.reach = step * 1.001f + 1e-4f;
+        a.reach = step * reach_steps * 1.001f + 1e-4f;
         size_t smem = (near_only ? 32 : 16) * (size_t)prog->set_n;
         if (smem > 48 * 1024) {
             cudaError_t e = cudaFuncSetAttribute(sample_sphere_set, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -645,29 +674,6 @@ iso_status launch_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t nx
             StageTimer timer(ctx, ISO_STAGE_SAMPLE);
             sample_sphere_set<<<grid, 256, smem, ctx->stream>>>(a);
         }
-    } else if (near_only && prog->lip > 0.0f && 4 * W <= BRICK_MAX &&
-               brick_tiles(W, ny, nz) >= (uint64_t)ctx->sms && brick_tiles(W, ny, nz) < (1ull << 22)) {
-        // values only where marching cubes can read them (bricks.cuh): tiles
-        // of 4 layers x up to 32 rows, one block each, then the mixed
-        // sub-bricks over a persistent grid.  A grid with fewer tiles than
-        // SMs takes the plain sampler, whose one launch has less latency.
-        const uint32_t ty = brick_tile_groups(W, ny);
-        const uint32_t rows = 4 * ty, ytiles = (ny + rows - 1) / rows;
-        const uint64_t ntiles = brick_tiles(W, ny, nz);
-        const uint64_t cap = ntiles * 4 * W * ty;  // every sub-brick of every tile
-        iso_status s = ensure(ctx, ctx->tiles, sizeof(BrickTask) * cap + 256);
-        if (s != ISO_OK) return s;
-        BrickTask* list = (BrickTask*)ctx->tiles.p;
-        uint32_t* count = (uint32_t*)((char*)ctx->tiles.p + sizeof(BrickTask) * cap);
-        cudaError_t e = cudaMemsetAsync(count, 0, 4, ctx->stream);
-        if (e != cudaSuccess) return cuda_fail(ctx, e, "brick list count");
-        const GridTiles gt{BrickLattice{prog->view(), nx, ny, nz, inv, field, pitch, bits, W, zoff}, rows, ytiles};
-        StageTimer timer(ctx, ISO_STAGE_SAMPLE);
-        brick_classify<GridTiles><<<(unsigned)ntiles, 256, 0, ctx->stream>>>(gt, list, count, (uint32_t)cap,
-                                                                              ctx->d_err);
-        brick_rows<GridTiles><<<brick_rows_blocks<GridTiles>(ctx->sms), 256, 0, ctx->stream>>>(gt, list, count,
-                                                                                               (uint32_t)cap);
-        ctx->launches++;
     } else {
         uint64_t warps = (uint64_t)W * ny * nz;
         StageTimer timer(ctx, ISO_STAGE_SAMPLE);
