@@ -10,7 +10,8 @@
 // (dual_contouring.rs:88-101 is the same cell kernel with GridKey dedup), so
 // the last two passes are mc_extract_lattice.
 //
-// Passes: (1) grid sampler (field + sign bits), (2) dc_dual: value and centre
+// Passes: (1) grid sampler (sign bits everywhere; for a program with a
+// Lipschitz bound, values only near the surface, NaN elsewhere), (2) dc_dual: value and centre
 // of every dual vertex, active primal cells appended to a list, (3) dc_place:
 // one thread per active cell -- eight normals from the program
 // (sample_normals_at_corners, marching_cubes_impl.rs:58-69), tangent planes,
@@ -26,7 +27,9 @@ namespace iso {
 namespace {
 
 struct DualArgs {
-    const float* field;
+    const float* field;   // primal values; NaN where the sampler left them unwritten
+    const uint32_t* bits; // primal sign bits (bit set iff !(v > 0)), W words per row
+    uint32_t W;
     uint64_t pitch;       // primal row pitch
     uint32_t n;           // primal size: n x n x (n+1) samples
     float inv;
@@ -49,25 +52,27 @@ __global__ void __launch_bounds__(256) dc_dual(DualArgs A) {
         const uint64_t r = id / m;
         const uint32_t y = (uint32_t)(r % m), z = (uint32_t)(r / m);
         // corners in CORNERS order (marching_cubes_tables.rs:16-25)
+        // corner signs from the sign bits, in CORNERS order
+        auto sign_bit = [&](uint32_t xx, uint32_t yy, uint32_t zz) {
+            return (__ldg(A.bits + ((size_t)zz * A.n + yy) * A.W + (xx >> 5)) >> (xx & 31)) & 1u;
+        };
+        uint32_t cs = sign_bit(x, y, z) | sign_bit(x + 1, y, z) << 1 | sign_bit(x + 1, y + 1, z) << 2 |
+                      sign_bit(x, y + 1, z) << 3 | sign_bit(x, y, z + 1) << 4 | sign_bit(x + 1, y, z + 1) << 5 |
+                      sign_bit(x + 1, y + 1, z + 1) << 6 | sign_bit(x, y + 1, z + 1) << 7;
         const float* f0 = A.field + ((size_t)z * A.n + y) * A.pitch + x;
-        const float* f1 = f0 + (size_t)A.n * A.pitch;
-        const float v0 = __ldg(f0), v1 = __ldg(f0 + 1), v2 = __ldg(f0 + A.pitch + 1), v3 = __ldg(f0 + A.pitch);
-        const float v4 = __ldg(f1), v5 = __ldg(f1 + 1), v6 = __ldg(f1 + A.pitch + 1), v7 = __ldg(f1 + A.pitch);
-        uint32_t cs = 0;
-        cs |= !(v0 > 0.0f) ? 1u : 0u;
-        cs |= !(v1 > 0.0f) ? 2u : 0u;
-        cs |= !(v2 > 0.0f) ? 4u : 0u;
-        cs |= !(v3 > 0.0f) ? 8u : 0u;
-        cs |= !(v4 > 0.0f) ? 16u : 0u;
-        cs |= !(v5 > 0.0f) ? 32u : 0u;
-        cs |= !(v6 > 0.0f) ? 64u : 0u;
-        cs |= !(v7 > 0.0f) ? 128u : 0u;
+        const float v0 = __ldg(f0), v6 = __ldg(f0 + (size_t)A.n * A.pitch + A.pitch + 1);
         // Vec3::lerp / Signed::lerp with f = 0.5: (1 - f) * a + f * b
         const float c0x = (float)x * A.inv, c0y = (float)y * A.inv, c0z = (float)z * A.inv;
         const float c6x = (float)(x + 1) * A.inv, c6y = (float)(y + 1) * A.inv, c6z = (float)(z + 1) * A.inv;
         const float of = 1.0f - 0.5f;
         A.dpos[id] = make_float4(of * c0x + 0.5f * c6x, of * c0y + 0.5f * c6y, of * c0z + 0.5f * c6z, 0.0f);
-        A.dval[((size_t)z * m + y) * A.dpitch + x] = of * v0 + 0.5f * v6;
+        // a corner the sampler skipped lies more than 2.5 lattice steps' worth
+        // of value change from zero, so (by the Lipschitz bound) v0 and v6
+        // share its sign and the dual value is more than 1.6 steps' worth
+        // from zero: never the end of a crossing dual edge, whose ends lie
+        // within one step's worth.  Only its sign is ever read.
+        const float dv = (v0 == v0 && v6 == v6) ? of * v0 + 0.5f * v6 : ((cs & 1u) ? -3.0e38f : 3.0e38f);
+        A.dval[((size_t)z * m + y) * A.dpitch + x] = dv;
         active = cs != 0 && cs != 255;
     }
     // warp-aggregated append of the active cells (their order does not matter)
@@ -171,12 +176,21 @@ static iso_status dc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint32_
     uint32_t* count = dbits + dW * m * n;
     uint32_t* list = count + 64;
     const float inv = 1.0f / (float)(n - 1);
-    if ((s = launch_sample_grid(ctx, prog, n, n, n + 1, inv, field, pitch, bits)) != ISO_OK) return s;
-    cudaError_t e = cudaMemsetAsync(count, 0, 4, ctx->stream);
+    // values only near the surface (programs with a Lipschitz bound): the
+    // dual values read the primal ones up to 1 + sqrt(3)/2 lattice steps'
+    // worth of change from zero (a dual crossing end within one step's
+    // worth, and half the cell diagonal between its two corners); the
+    // sampler keeps 2.5, and the others stay NaN for dc_dual to recognise
+    const bool near = prog->lip > 0.0f;
+    cudaError_t e = cudaSuccess;
+    if (near) e = cudaMemsetAsync(field, 0xFF, 4ull * pitch * n * (n + 1), ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "clear field");
+    if ((s = launch_sample_grid(ctx, prog, n, n, n + 1, inv, field, pitch, bits, near, 0, 2.5f)) != ISO_OK) return s;
+    e = cudaMemsetAsync(count, 0, 4, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "memset");
     {
         StageTimer timer(ctx, ISO_STAGE_PLACE);
-        DualArgs da{field, pitch, n, inv, dval, dpitch, dpos, list, count, (uint32_t)ndual, ctx->d_err};
+        DualArgs da{field, bits, (uint32_t)W, pitch, n, inv, dval, dpitch, dpos, list, count, (uint32_t)ndual, ctx->d_err};
         dc_dual<<<(unsigned)((ndual + 255) / 256), 256, 0, ctx->stream>>>(da);
         PlaceArgs pa{prog->view(), n, inv, list, count, dpos, (int)placer, ctx->d_err};
         const uint64_t place_blocks = std::min<uint64_t>((ndual + 127) / 128, 152 * 64);

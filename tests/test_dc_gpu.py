@@ -47,6 +47,16 @@ def test_dc_bytes_identical(ctx, name, size, placer):
     _compare(got, want, size)
 
 
+@pytest.mark.parametrize("name", ["sphere", "torus", "central_difference", "box"])
+def test_dc_culled_sampling_161(ctx, name):
+    """A grid large enough for the culled sampler (values only near the
+    surface): the dual values of skipped corners are never read as values."""
+    src = _sources()[name]
+    want = oracle.Program(S.lower(src)).dual_contouring(161, placer=0)
+    got = ctx.download(ctx.dc_extract(src, 161, keys=True), keys=True)
+    _compare(got, want, 161)
+
+
 def test_dc_csg_257(ctx):
     """The DualContouring workload: 256^3 cells, rigid-transformed CSG scene,
     analytic-gradient normals, MinimiseQEF."""
