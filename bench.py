@@ -9,8 +9,11 @@ classification + scan, vertex/index emission.  `value` is timed with CUDA
 events on the library's stream with the program already resident and the
 mesh left on the device; `e2e` times the public C ABI with host buffers
 (program upload H2D from host bytes, iso_mc_extract_host into page-locked
-host buffers) on the host clock.  L2 is flushed (a 256 MiB write) before
-every timed step.
+host buffers) on the host clock, from two host threads with a context each
+(steps back to back; the mesh delivered by DMA, ISO_FLAG_HOST_COPY), and
+`e2e.serial` the same from one thread.  L2 is flushed (a 256 MiB write)
+before every timed step of `value` and `e2e.serial`; a step's working set
+(540 MB) exceeds L2 in the two-thread run.
 
 `roofline` covers the extraction pass (counting, scan, emission, resolve):
 achieved = (4 B per sample for the field read once + 12 B per vertex + 12 B
@@ -679,13 +682,13 @@ def main():
     ibuf = torch.empty((nt * 3 + 1024,), dtype=torch.int32, pin_memory=True)
     f32p, u32p = ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_uint32)
 
-    def e2e_step(c=ctx, vb=vbuf, ib=ibuf):
+    def e2e_step(c=ctx, vb=vbuf, ib=ibuf, flags=0):
         # a program uploaded from host bytes and the mesh delivered into the
         # caller's page-locked buffers, as a binding's extract() would do
         ph = ctypes.c_void_p()
         check(lib().iso_program_create(c.h, src_bytes, len(src_bytes), ctypes.byref(ph)), c.h)
         mi = MeshInfo()
-        check(lib().iso_mc_extract_host(c.h, ph, SIZE, 0, ctypes.cast(vb.data_ptr(), f32p), vb.numel(),
+        check(lib().iso_mc_extract_host(c.h, ph, SIZE, flags, ctypes.cast(vb.data_ptr(), f32p), vb.numel(),
                                         ctypes.cast(ib.data_ptr(), u32p), ib.numel(), ctypes.byref(mi)), c.h)
         lib().iso_program_destroy(ph)
         return mi
@@ -704,25 +707,28 @@ def main():
     e2e_s = replicas.max_over_ranks(sum(e2e_times) / len(e2e_times), dist, "cuda")
     serial_mesh = (vbuf[:3 * mi.num_vertices].clone(), ibuf[:3 * mi.num_triangles].clone())
     # the same calls from two host threads, each with its own context (and
-    # stream) and page-locked buffers, steps back to back: one extraction's
-    # mesh crosses the CPU-GPU link while the other samples and counts.  The
-    # working set of a step (540 MB of sign bits and values, the 53 MB mesh)
-    # is larger than L2, so nothing carries over between steps.
+    # stream) and page-locked buffers, steps back to back, with the mesh
+    # delivered by the DMA engines after each extraction (ISO_FLAG_HOST_COPY):
+    # one extraction's mesh crosses the CPU-GPU link while the other samples,
+    # counts and emits on the SMs.  The working set of a step (540 MB of sign
+    # bits and values, the 53 MB mesh) is larger than L2, so nothing carries
+    # over between steps.
     ctx2 = Context(local)
     stream2 = torch.cuda.Stream()
     ctx2.set_stream(stream2.cuda_stream)
     lanes = [(ctx, vbuf, ibuf),
              (ctx2, torch.empty_like(vbuf).pin_memory(), torch.empty_like(ibuf).pin_memory())]
+    HOST_COPY = 4  # ISO_FLAG_HOST_COPY
     for c, vb, ib in lanes:
         for _ in range(max(args.warmup, 2)):
-            e2e_step(c, vb, ib)
+            e2e_step(c, vb, ib, HOST_COPY)
     barrier()
     errors = []
 
     def lane(c, vb, ib):
         try:
             for _ in range(args.steps):
-                e2e_step(c, vb, ib)
+                e2e_step(c, vb, ib, HOST_COPY)
         except Exception as exc:  # reported after the join
             errors.append(exc)
 
@@ -742,10 +748,12 @@ def main():
     e2e = {"value": replicas.whole_job_rate(CELLS, world, pipe_s), "unit": "cells/s",
            "h2d_bytes_per_step": len(src_bytes), "d2h_bytes_per_step": 12 * mi.num_vertices + 12 * mi.num_triangles,
            "ms_per_step": 1e3 * pipe_s,
-           "schedule": "two host threads, one context and stream each, steps back to back",
+           "schedule": "two host threads, one context and stream each, steps back to back, "
+                       "mesh delivered by DMA after each extraction (ISO_FLAG_HOST_COPY)",
            "meshes_equal_serial": bool(same),
            "serial": {"value": replicas.whole_job_rate(CELLS, world, e2e_s), "ms_per_step": 1e3 * e2e_s,
-                      "l2": "flushed before each step"}}
+                      "l2": "flushed before each step",
+                      "schedule": "one thread, mesh written to the host buffers by the extraction kernels"}}
 
     secondary = None
     if not args.no_secondary:

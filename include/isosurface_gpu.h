@@ -191,6 +191,7 @@ ISO_API iso_status iso_mesh_device(iso_ctx* ctx, const float** vertices, const u
 /* Extraction flags */
 #define ISO_FLAG_KEYS 1u      /* also produce per-vertex dedup keys          */
 #define ISO_FLAG_NORMALS 2u   /* IndexedInterleavedNormals: per-vertex source normal */
+#define ISO_FLAG_HOST_COPY 4u /* iso_mc_extract_host: deliver by copy after the extraction */
 
 /* ------------------------------------------------------------------------ */
 /* Grid sampling (PrimalGrid, src/traversal/primal_grid.rs:39-89)            */
@@ -234,7 +235,10 @@ ISO_API iso_status iso_mc_extract(iso_ctx* ctx, const iso_program* prog, uint32_
  * triangle).  When both are page-locked (cudaHostAlloc, cudaHostRegister)
  * and `indices` is 16-byte aligned, the extraction kernels write the mesh into
  * them as they produce it, so the transfer overlaps the extraction; any other
- * host memory receives an ordinary copy afterwards.  The mesh also stays on
+ * host memory receives an ordinary copy afterwards.  ISO_FLAG_HOST_COPY asks
+ * for that copy (the DMA engines, no SM time) with page-locked buffers too:
+ * a lone call finishes later, but calls on other contexts then overlap the
+ * transfer with their own extraction in full.  The mesh also stays on
  * the device (iso_mesh_download, iso_mesh_device) and `info` receives its
  * size.  If either buffer is too small, neither is written and the call
  * returns ISO_ERR_CAPACITY (a caller can grow its buffers and call

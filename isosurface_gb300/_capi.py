@@ -18,6 +18,7 @@ STATUS = {
 }
 ISO_FLAG_KEYS = 1
 ISO_FLAG_NORMALS = 2
+ISO_FLAG_HOST_COPY = 4
 ISO_SURROGATE_EXACT_COARSE = 1
 ISO_SURROGATE_WITNESS = 2
 

@@ -771,7 +771,8 @@ iso_status iso_mc_extract_host(iso_ctx* ctx, const iso_program* prog, uint32_t s
         return fail(ctx, ISO_ERR_INVALID_ARG, "null host buffer with nonzero room");
     iso_status s = check_size(ctx, prog, size);
     if (s != ISO_OK) return s;
-    if (flags & ~(uint32_t)(ISO_FLAG_KEYS | ISO_FLAG_NORMALS)) return fail(ctx, ISO_ERR_INVALID_ARG, "unknown flags");
+    if (flags & ~(uint32_t)(ISO_FLAG_KEYS | ISO_FLAG_NORMALS | ISO_FLAG_HOST_COPY))
+        return fail(ctx, ISO_ERR_INVALID_ARG, "unknown flags");
     void* dv = flags == 0 && size > 1 ? pinned_device_view(vertices) : nullptr;
     void* di = dv ? pinned_device_view(indices) : nullptr;
     const bool direct = dv && di && ((uintptr_t)di & 15) == 0;
@@ -789,6 +790,7 @@ iso_status iso_mc_extract_host(iso_ctx* ctx, const iso_program* prog, uint32_t s
         // the lattice went through the block emit, which writes only the device mesh
         return iso_mesh_download(ctx, vertices, vertex_floats, indices, index_count, nullptr, 0);
     }
+    flags &= ~(uint32_t)ISO_FLAG_HOST_COPY;
     if ((s = iso_mc_extract(ctx, prog, size, flags, &mi)) != ISO_OK) return s;
     if (info) *info = mi;
     const uint64_t vf = (flags & ISO_FLAG_NORMALS) ? 6 : 3;

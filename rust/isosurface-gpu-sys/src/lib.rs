@@ -32,6 +32,7 @@ pub const ISO_STAGE_COUNT: usize = 8;
 
 pub const ISO_FLAG_KEYS: u32 = 1;
 pub const ISO_FLAG_NORMALS: u32 = 2;
+pub const ISO_FLAG_HOST_COPY: u32 = 4;
 pub const ISO_PLACER_MINIMISE_QEF: u32 = 0;
 pub const ISO_PLACER_PARTICLES: u32 = 1;
 pub const ISO_BATCH_GRAPH: u32 = 1;

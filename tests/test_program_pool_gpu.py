@@ -40,7 +40,8 @@ def test_alternating_reuploads_extract_their_own_meshes():
     c.close()
 
 
-def test_reuploaded_program_delivers_to_host_buffers():
+@pytest.mark.parametrize("flags", [0, 4])  # ISO_FLAG_HOST_COPY: delivery by copy after the extraction
+def test_reuploaded_program_delivers_to_host_buffers(flags):
     c = Context(0)
     src = scenes.csg()
     want = _want(src)
@@ -48,6 +49,9 @@ def test_reuploaded_program_delivers_to_host_buffers():
     nv, nt = len(want.vertices), len(want.indices) // 3
     v = np.zeros(3 * nv + 64, np.float32)
     i = np.zeros(3 * nt + 64, np.uint32)
+    # page-locked, so that without ISO_FLAG_HOST_COPY the kernels write them
+    check(lib().iso_host_register(v.ctypes.data_as(ctypes.c_void_p), v.nbytes))
+    check(lib().iso_host_register(i.ctypes.data_as(ctypes.c_void_p), i.nbytes))
     f32p, u32p = ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_uint32)
     for _ in range(5):
         ph = ctypes.c_void_p()
@@ -55,12 +59,14 @@ def test_reuploaded_program_delivers_to_host_buffers():
         mi = MeshInfo()
         v[:] = 0
         i[:] = 0
-        check(lib().iso_mc_extract_host(c.h, ph, SIZE, 0, v.ctypes.data_as(f32p), v.size, i.ctypes.data_as(u32p),
+        check(lib().iso_mc_extract_host(c.h, ph, SIZE, flags, v.ctypes.data_as(f32p), v.size, i.ctypes.data_as(u32p),
                                         i.size, ctypes.byref(mi)), c.h)
         lib().iso_program_destroy(ph)
         assert (mi.num_vertices, mi.num_triangles) == (nv, nt)
         assert np.array_equal(v[:3 * nv], want.vertices.reshape(-1))
         assert np.array_equal(i[:3 * nt], want.indices)
+    lib().iso_host_unregister(v.ctypes.data_as(ctypes.c_void_p))
+    lib().iso_host_unregister(i.ctypes.data_as(ctypes.c_void_p))
     c.close()
 
 
