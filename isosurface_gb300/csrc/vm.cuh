@@ -192,18 +192,18 @@ static __host__ __device__ __noinline__ float eval_prims(const ProgView& pv, V3 
 }
 
 // The same union over the primitives whose bits are set in `keep` (nonzero;
-// at most 32 primitives), in the same order.  Equal to eval_prims wherever
+// at most 64 primitives), in the same order.  Equal to eval_prims wherever
 // every dropped primitive's value exceeds some kept one's: fminf returns one
 // of its operands, so the minimum over a subset that holds the minimiser is
 // the minimum over all.
-__host__ __device__ __forceinline__ uint32_t lowest_bit(uint32_t m) {
+__host__ __device__ __forceinline__ uint32_t lowest_bit(uint64_t m) {
 #ifdef __CUDA_ARCH__
-    return (uint32_t)(__ffs((int)m) - 1);
+    return (uint32_t)(__ffsll((long long)m) - 1);
 #else
-    return (uint32_t)__builtin_ctz(m);
+    return (uint32_t)__builtin_ctzll(m);
 #endif
 }
-static __host__ __device__ __noinline__ float eval_prims_kept(const ProgView& pv, uint32_t keep, V3 p) {
+static __host__ __device__ __noinline__ float eval_prims_kept(const ProgView& pv, uint64_t keep, V3 p) {
     const V3 q = prims_point(pv, p);
     float v = prim_at(pv, lowest_bit(keep), q);
     for (keep &= keep - 1; keep; keep &= keep - 1) v = fminf(v, prim_at(pv, lowest_bit(keep), q));
