@@ -219,6 +219,15 @@ ISO_API iso_status iso_sample_grid_near(iso_ctx* ctx, const iso_program* prog, u
  * its primitives (exact distances) and point maps; 0 when the program has
  * none (culled sampling is then off). */
 ISO_API iso_status iso_program_lipschitz(const iso_program* prog, float* lip);
+/* Whether the extractors' sampling of this program runs a kernel compiled
+ * for it (written out as straight-line code and compiled with NVRTC on first
+ * use, cached per program contents; values bit-identical to the
+ * interpreter's) rather than the interpreter: 1 or 0.  General programs
+ * (no sphere set; not a flat union of translated primitives, which the
+ * interpreter prunes per sub-brick) are compiled while NVRTC is available
+ * and compilation is enabled (iso_jit_enable, process-wide, default on). */
+ISO_API iso_status iso_program_compiled(const iso_program* prog, int* compiled);
+ISO_API iso_status iso_jit_enable(int enable);
 
 /* ------------------------------------------------------------------------ */
 /* MarchingCubes (src/marching_cubes.rs:59-82)                               */

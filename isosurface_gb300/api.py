@@ -245,6 +245,12 @@ class Context:
         check(lib().iso_sample_grid_near(self.h, self.program(source).h, size, ctypes.c_void_p(field_ptr), pitch,
                                          ctypes.c_void_p(bits_ptr)), self.h)
 
+    def compiled(self, source):
+        """Whether the program's culled sampling runs a kernel compiled for it (iso_program_compiled)."""
+        out = ctypes.c_int()
+        check(lib().iso_program_compiled(self.program(source).h, ctypes.byref(out)), self.h)
+        return bool(out.value)
+
     def lipschitz(self, source):
         """The program's Lipschitz bound used for culled sampling (0: none)."""
         out = ctypes.c_float()

@@ -37,8 +37,27 @@ UNITS = {
     "surrogate.cu": ["-fmad=false"],
     "splat.cu": ["-fmad=false"],
     "emc.cu": ["-fmad=false"],
+    "jit.cu": ["-fmad=false"],
 }
-HEADERS = ["internal.h", "vm.cuh", "mc_tables.h", "mc_chunk.cuh", "qef.cuh", "mlp.h", "emc.cuh", "emc_tables.h"]
+HEADERS = ["internal.h", "vm.cuh", "vm_math.cuh", "bricks.cuh", "bricks_core.cuh", "mc_tables.h", "mc_chunk.cuh",
+           "qef.cuh", "mlp.h", "emc.cuh", "emc_tables.h"]
+# sources the library compiles again at run time, for one program at a time
+# (jit.cu): embedded as string literals in _build/jit_sources.inc
+JIT_SOURCES = (("kJitVmMath", "vm_math.cuh"), ("kJitBricksCore", "bricks_core.cuh"))
+JIT_INC = os.path.join(OUT_DIR, "jit_sources.inc")
+
+
+def _write_jit_sources():
+    parts = ["// written by isosurface_gb300/build.py from csrc/vm_math.cuh and csrc/bricks_core.cuh\n"]
+    for name, fname in JIT_SOURCES:
+        text = open(os.path.join(CSRC, fname)).read()
+        text = "".join(l for l in text.splitlines(True) if l.strip() != "#pragma once")
+        assert ")ISOJIT\"" not in text
+        parts.append("static const char %s[] = R\"ISOJIT(%s)ISOJIT\";\n" % (name, text))
+    data = "".join(parts)
+    if not os.path.exists(JIT_INC) or open(JIT_INC).read() != data:
+        with open(JIT_INC, "w") as f:
+            f.write(data)
 
 
 def _deps():
@@ -52,7 +71,7 @@ def _compile(unit, flags):
     src = os.path.join(CSRC, unit)
     obj = os.path.join(OUT_DIR, unit + ".o")
     cmd = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
-           "-I", os.path.join(ROOT, "include"), "-c", src, "-o", obj, *flags]
+           "-I", os.path.join(ROOT, "include"), "-I", OUT_DIR, "-c", src, "-o", obj, *flags]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (unit, " ".join(cmd), r.stderr))
@@ -72,6 +91,7 @@ def _build_peak(force):
 
 def build(force=False, verbose=False):
     os.makedirs(OUT_DIR, exist_ok=True)
+    _write_jit_sources()
     _build_peak(force)
     if not force and os.path.exists(LIB):
         if os.path.getmtime(LIB) >= max(os.path.getmtime(p) for p in _deps()):

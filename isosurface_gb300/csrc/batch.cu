@@ -62,21 +62,10 @@ struct Tile {
     uint32_t grid, z0, z1, y0, y1;  // layers [z0, z1), rows [y0, y1), all x
 };
 
-// The batch's tiles for the culled sampler (bricks.cuh).
-struct BatchTiles {
-    const Tile* tiles;
-    const SampleGrid* grids;
-    __device__ __forceinline__ BrickTile tile(uint32_t t) const {
-        const Tile tl = tiles[t];
-        const SampleGrid sg = grids[tl.grid];
-        return BrickTile{BrickLattice{sg.pv, sg.n, sg.n, sg.n + 1, sg.inv, sg.field, sg.pitch, sg.bits, sg.W, 0, 1.0f},
-                         tl.y0, tl.y1, tl.z0, tl.z1};
-    }
-};
-
 // A persistent grid: each block takes tiles from the work queue (largest
-// first) and samples them whole.
-__global__ void __launch_bounds__(256) batch_sample(BatchTiles bt, uint32_t ntiles, uint32_t* next) {
+// first) and samples them whole with the culled sampler (bricks.cuh).
+__global__ void __launch_bounds__(256) batch_sample(const Tile* tiles, const SampleGrid* grids, uint32_t ntiles,
+                                                    uint32_t* next) {
     __shared__ uint32_t s_tile, s_n;
     __shared__ uint8_t s_cls[BRICK_MAX];
     __shared__ uint64_t s_keep[BRICK_MAX];
@@ -87,7 +76,12 @@ __global__ void __launch_bounds__(256) batch_sample(BatchTiles bt, uint32_t ntil
         __syncthreads();
         const uint32_t t = s_tile;
         if (t >= ntiles) return;
-        brick_tile(bt.tile(t), s_cls, s_keep, s_list, &s_n);
+        const Tile tl = tiles[t];
+        const SampleGrid sg = grids[tl.grid];
+        const BrickTile T{BrickLattice{sg.pv.lip, sg.pv.slack, sg.n, sg.n, sg.n + 1, sg.inv, sg.field, sg.pitch,
+                                       sg.bits, sg.W, 0, 1.0f},
+                          tl.y0, tl.y1, tl.z0, tl.z1};
+        brick_tile(VmEval{sg.pv}, T, s_cls, s_keep, s_list, &s_n);
     }
 }
 
@@ -185,15 +179,7 @@ iso_status build_tiles(iso_batch* b) {
 // blocks of batch_sample that fill every SM (looked up once per process)
 unsigned sample_blocks(int sms) {
     static std::atomic<int> per_sm{0};
-    int b = per_sm.load(std::memory_order_relaxed);
-    if (b == 0) {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batch_sample, 256, 0) != cudaSuccess || b < 1) {
-            cudaGetLastError();
-            b = 4;
-        }
-        per_sm.store(b, std::memory_order_relaxed);
-    }
-    return (unsigned)(b * std::max(sms, 1));
+    return persistent_blocks((const void*)batch_sample, per_sm, sms);
 }
 
 // the culled sampler over `ntiles` tiles (the queue counter zeroed first)
@@ -201,7 +187,7 @@ cudaError_t launch_sampler(iso_ctx* ctx, const Tile* d_tiles, uint32_t ntiles, c
                            uint32_t* next) {
     cudaError_t e = cudaMemsetAsync(next, 0, 4, ctx->stream);
     if (e != cudaSuccess) return e;
-    batch_sample<<<sample_blocks(ctx->sms), 256, 0, ctx->stream>>>(BatchTiles{d_tiles, d_sgrids}, ntiles, next);
+    batch_sample<<<sample_blocks(ctx->sms), 256, 0, ctx->stream>>>(d_tiles, d_sgrids, ntiles, next);
     return cudaGetLastError();
 }
 

@@ -617,13 +617,19 @@ iso_status launch_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t nx
         uint32_t* count = (uint32_t*)((char*)ctx->tiles.p + sizeof(BrickTask) * cap);
         cudaError_t e = cudaMemsetAsync(count, 0, 4, ctx->stream);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "brick list count");
-        const GridTiles gt{BrickLattice{prog->view(), nx, ny, nz, inv, field, pitch, bits, W, zoff, reach_steps}, rows,
-                           ytiles};
+        const GridTiles gt{brick_lattice(prog, nx, ny, nz, inv, field, pitch, bits, W, zoff, reach_steps), rows, ytiles};
         StageTimer timer(ctx, ISO_STAGE_SAMPLE);
-        brick_classify<GridTiles><<<(unsigned)ntiles, 256, 0, ctx->stream>>>(gt, list, count, (uint32_t)cap,
-                                                                              ctx->d_err);
-        brick_rows<GridTiles><<<brick_rows_blocks<GridTiles>(ctx->sms), 256, 0, ctx->stream>>>(gt, list, count,
-                                                                                               (uint32_t)cap);
+        cudaError_t je = cudaSuccess;
+        if (jit_sample_bricks(ctx, prog, gt, (uint32_t)ntiles, list, count, (uint32_t)cap, &je)) {
+            // the program's compiled evaluator (jit.cu)
+            if (je != cudaSuccess) return cuda_fail(ctx, je, "compiled sampler launch");
+        } else {
+            const VmEval ev{prog->view()};
+            brick_classify<GridTiles><<<(unsigned)ntiles, 256, 0, ctx->stream>>>(ev, gt, list, count,
+                                                                                  (uint32_t)cap, ctx->d_err);
+            brick_rows<GridTiles><<<brick_rows_blocks<GridTiles>(ctx->sms), 256, 0, ctx->stream>>>(
+                ev, gt, list, count, (uint32_t)cap);
+        }
         ctx->launches++;
     } else if (prog->kind == PK_SPHERE_SET_HARD && prog->set_n <= 8192) {
         near_only = near_only && prog->set_n <= 4096 && nx > 1;

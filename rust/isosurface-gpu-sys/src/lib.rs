@@ -142,6 +142,8 @@ extern "C" {
         bits: *mut u32,
     ) -> IsoStatus;
     pub fn iso_program_lipschitz(prog: *const IsoProgram, lip: *mut f32) -> IsoStatus;
+    pub fn iso_program_compiled(prog: *const IsoProgram, compiled: *mut c_int) -> IsoStatus;
+    pub fn iso_jit_enable(enable: c_int) -> IsoStatus;
     pub fn iso_mc_extract(
         ctx: *mut IsoCtx,
         prog: *const IsoProgram,

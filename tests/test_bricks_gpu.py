@@ -32,6 +32,17 @@ def _programs():
                                                S.Translate(S.Torus(250.0, 60.0), (-120.0, 50.0, 0.0))),
                                        scale=(1000.0, 1000.0, 1000.0), offset=(-500.0, -500.0, -500.0))
     out["csg_rigid"] = scenes.csg(seed=7)
+    # unions of translated primitives past 32 (64-bit keep masks) and past 64
+    # (no pruning, classification only)
+    for n in (40, 70):
+        r = np.random.default_rng(n)
+        prims = [S.Translate(S.Sphere(float(r.uniform(0.05, 0.2))) if i % 2 else
+                             S.RectangularPrism(tuple(float(x) for x in r.uniform(0.03, 0.15, 3))),
+                             tuple(float(x) for x in r.uniform(-0.8, 0.8, 3))) for i in range(n)]
+        u = prims[0]
+        for q in prims[1:]:
+            u = S.Union(u, q)
+        out["prims%d" % n] = S.unit_to_cube(u)
     return out
 
 
@@ -107,7 +118,7 @@ def test_culled_mesh_equals_full_field_mesh(ctx, name):
     assert np.array_equal(got.indices, want.indices)
 
 
-@pytest.mark.parametrize("name", ["csg", "prim_union", "chunk2"])
+@pytest.mark.parametrize("name", ["csg", "prim_union", "chunk2", "prims40", "prims70"])
 def test_culled_mesh_equals_oracle(ctx, name):
     import oracle
     src = _programs()[name]
@@ -133,3 +144,32 @@ def test_lipschitz_bound_holds(ctx, name):
     dist = np.linalg.norm(a.astype(np.float64) - b.astype(np.float64), axis=1)
     slack = 1e-5 * (1.0 + np.maximum(np.abs(fa), np.abs(fb)))
     assert np.all(np.abs(fa - fb) <= lip * dist * (1 + 1e-4) + slack)
+
+
+def test_compiled_evaluator_matches_interpreter(ctx):
+    """General programs are sampled by a kernel compiled for them (NVRTC);
+    with compilation switched off the interpreter runs instead, and the
+    sign bits and every value both write are identical."""
+    import torch
+    from isosurface_gb300._capi import lib
+    progs = _programs()
+    for name in ("csg", "csg_rigid", "smooth", "central_difference", "intersection", "cylinder", "box"):
+        assert ctx.compiled(progs[name]), name
+    # sphere sets, and flat unions of translated primitives (pruned per sub-brick by the interpreter)
+    for name in ("sphere_set", "smooth_set", "prim_union", "chunk0", "prims40", "scaled_domain"):
+        assert not ctx.compiled(progs[name]), name
+    size, pitch = 200, 203
+    W = (size + 31) // 32
+    for name in ("csg", "smooth", "central_difference"):
+        out = []
+        for enable in (1, 0):
+            lib().iso_jit_enable(enable)
+            try:
+                f = torch.full(((size + 1) * size * pitch,), float("nan"), dtype=torch.float32, device="cuda")
+                b = torch.zeros(((size + 1) * size * W,), dtype=torch.int32, device="cuda")
+                ctx.sample_grid_near(progs[name], size, f.data_ptr(), pitch, b.data_ptr())
+                out.append((f.view(torch.int32).clone(), b.clone()))
+            finally:
+                lib().iso_jit_enable(1)
+        assert torch.equal(out[0][1], out[1][1]), name
+        assert torch.equal(out[0][0], out[1][0]), name  # the same samples written, the same bits
