@@ -189,15 +189,30 @@ def sampler_fp32_workload(ctx, torch, timed):
 def mc_csg_workload(ctx, timed, steps):
     """A general program at the headline size: MarchingCubes::new(513) of the
     rigid-transformed CSG scene (box minus sphere, union torus), sampled by
-    the general evaluator (full f32 field), device-resident, CUDA events."""
+    the culled sampler with the program's compiled evaluator (the first
+    extraction compiles it: `first_ms`, host clock), device-resident, CUDA
+    events; `interpreted_ms` is the same with compilation switched off."""
     import ctypes
     from isosurface_gb300 import scenes
     from isosurface_gb300._capi import lib
     src = scenes.csg()
     prog = ctx.program(src)
-    for _ in range(3):
+    t0 = time.perf_counter()
+    info = ctx.mc_extract(prog, SIZE)
+    first_ms = 1e3 * (time.perf_counter() - t0)
+    for _ in range(2):
         info = ctx.mc_extract(prog, SIZE)
     ms = timed(lambda: ctx.mc_extract(prog, SIZE), max(5, min(steps, 30)))
+    compiled = ctx.compiled(prog)
+    lib().iso_jit_enable(0)
+    try:
+        for _ in range(2):
+            ctx.mc_extract(prog, SIZE)
+        interpreted_ms = timed(lambda: ctx.mc_extract(prog, SIZE), max(5, min(steps, 30)))
+    finally:
+        lib().iso_jit_enable(1)
+    for _ in range(2):
+        ctx.mc_extract(prog, SIZE)
     ms_buf = (ctypes.c_double * 8)()
     ln_buf = (ctypes.c_uint64 * 8)()
     lib().iso_ctx_stage_times(ctx.h, ms_buf, ln_buf)
@@ -209,7 +224,8 @@ def mc_csg_workload(ctx, timed, steps):
     stages = {name: ms_buf[i] / max(int(ln_buf[i]), 1) for name, i in (("sample", 0), ("classify_scan", 1),
                                                                           ("emit", 2))}
     return {"cells": CELLS, "ms": ms, "cells_per_s": CELLS / (ms / 1e3), "triangles": int(info.num_triangles),
-            "vertices": int(info.num_vertices), "stage_ms": stages}
+            "vertices": int(info.num_vertices), "stage_ms": stages, "compiled": bool(compiled),
+            "first_ms": first_ms, "interpreted_ms": interpreted_ms}
 
 
 def cpu_baseline_port(src_bytes, budget_s=12.0, threads=1):

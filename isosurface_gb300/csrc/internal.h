@@ -115,6 +115,7 @@ struct iso_ctx {
         std::vector<uint32_t> prog_ops;
         std::vector<float> prog_consts;
         uint32_t size = 0, flags = 0;
+        uint64_t jit_gen = 0;  // jit_generation() when recorded
         void* bufs[12] = {};
         float* host_v = nullptr;  // host buffers baked into the recorded kernels
         uint32_t* host_i = nullptr;
@@ -191,6 +192,9 @@ iso_status ensure(iso_ctx* ctx, DevBuf& b, size_t bytes);
 iso_status check_launch(iso_ctx* ctx, const char* what);
 iso_status read_device_errors(iso_ctx* ctx);
 iso_status set_device(iso_ctx* ctx);
+
+// jit.cu: changes whenever per-program compilation is switched on or off
+uint64_t jit_generation();
 
 // sample.cu
 // near_only: sign bits everywhere, values at least within reach_steps

@@ -302,8 +302,15 @@ bool jit_sample_bricks(iso_ctx* ctx, const iso_program* prog, const GridTiles& t
 
 }  // namespace iso
 
+namespace iso {
+// bumped whenever compilation is switched on or off: recorded extractions
+// hold the kernels of the setting they were recorded with
+std::atomic<uint64_t> g_jit_generation{0};
+uint64_t jit_generation() { return g_jit_generation.load(); }
+}  // namespace iso
+
 extern "C" iso_status iso_jit_enable(int enable) {
-    iso::g_jit_enabled.store(enable ? 1 : 0);
+    if (iso::g_jit_enabled.exchange(enable ? 1 : 0) != (enable ? 1 : 0)) iso::g_jit_generation.fetch_add(1);
     return ISO_OK;
 }
 

@@ -200,6 +200,38 @@ __global__ void scan_add(uint32_t* out, uint32_t n, const uint32_t* sums) {
     if (i < n) out[i] += sums[blockIdx.x];
 }
 
+// The whole scan in one block for n <= SCAN_SMALL: 16 consecutive entries
+// per thread (read before any is written, so in == out is fine).
+constexpr uint32_t SCAN_SMALL = 16 * 1024;
+__global__ void __launch_bounds__(1024) scan_small(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* total) {
+    __shared__ uint32_t s_w[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t i0 = 16 * threadIdx.x;
+    uint32_t v[16], sum = 0;
+    for (int k = 0; k < 16; ++k) {
+        v[k] = i0 + k < n ? in[i0 + k] : 0u;
+        sum += v[k];
+    }
+    uint32_t x = sum;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(FULL, x, o);
+        if (lane >= o) x += t;
+    }
+    if (lane == 31) s_w[warp] = x;
+    __syncthreads();
+    uint32_t before = 0, all = 0;
+    for (int w = 0; w < 32; ++w) {
+        if (w < warp) before += s_w[w];
+        all += s_w[w];
+    }
+    uint32_t run = before + x - sum;
+    for (int k = 0; k < 16; ++k) {
+        if (i0 + k < n) out[i0 + k] = run;
+        run += v[k];
+    }
+    if (threadIdx.x == 0) *total = all;
+}
+
 // ------------------------------------------------------------ octree build ---
 struct GenArgs {
     ProgView pv;
@@ -303,9 +335,9 @@ __global__ void leaf_write(LeafArgs A, const uint32_t* offsets, unsigned long lo
 
 // ---------------------------------------------------------------- dual cubes ---
 struct CubeArgs {
-    const unsigned long long* nkeys;  // sorted node keys
+    const unsigned long long* ntable;  // node key -> index (node_insert)
+    uint32_t nmask;
     const float* nvals;
-    uint32_t nodes;
     const unsigned long long* pv_key;
     const uint8_t* pv_level;
     uint32_t ncubes;
@@ -315,14 +347,31 @@ struct CubeArgs {
     unsigned long long* stale;
 };
 
-__device__ __forceinline__ uint32_t find_node(const unsigned long long* keys, uint32_t n, uint64_t key) {
-    uint32_t lo = 0, hi = n;
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (keys[mid] < key) lo = mid + 1;
-        else hi = mid;
+// Node key -> index for the parent walks: open addressing over
+// (key << 32 | index) words, 0 empty (keys lie in [1, 2^31)), at most half
+// full, so a lookup takes one or two probes where a binary search over the
+// sorted keys took twenty dependent loads.
+__global__ void node_insert(const unsigned long long* keys, uint32_t n, unsigned long long* table, uint32_t mask) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint64_t key = keys[i];
+    const unsigned long long word = (key << 32) | i;
+    uint32_t slot = (uint32_t)mix64(key) & mask;
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        if (atomicCAS(table + slot, 0ull, word) == 0ull) return;
+        slot = (slot + 1) & mask;
     }
-    return (lo < n && keys[lo] == key) ? lo : 0xFFFFFFFFu;
+}
+
+__device__ __forceinline__ uint32_t find_node(const unsigned long long* table, uint32_t mask, uint64_t key) {
+    uint32_t slot = (uint32_t)mix64(key) & mask;
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+        const unsigned long long w = __ldg(table + slot);
+        if (w == 0ull) return 0xFFFFFFFFu;
+        if ((w >> 32) == key) return (uint32_t)w;
+        slot = (slot + 1) & mask;
+    }
+    return 0xFFFFFFFFu;
 }
 
 __global__ void cube_gather(CubeArgs A) {
@@ -336,7 +385,7 @@ __global__ void cube_gather(CubeArgs A) {
         uint64_t m = morton::dual_vertex(v, lv, iso_remap_cube[i]);
         uint32_t found = 0xFFFFFFFFu;
         while (m > 1) {
-            found = find_node(A.nkeys, A.nodes, m);
+            found = find_node(A.ntable, A.nmask, m);
             if (found != 0xFFFFFFFFu) break;
             m = morton::parent(m);
         }
@@ -483,6 +532,11 @@ iso_status scan_u32(iso_ctx* ctx, const uint32_t* in, uint32_t* out, uint32_t n,
     if (n == 0) {
         cudaMemsetAsync(total, 0, 4, ctx->stream);
         return ISO_OK;
+    }
+    if (n <= SCAN_SMALL) {
+        scan_small<<<1, 1024, 0, ctx->stream>>>(in, out, n, total);
+        ctx->launches++;
+        return check_launch(ctx, "scan");
     }
     scan_blocks<<<nb, 1024, 0, ctx->stream>>>(in, out, n, sums);
     scan_sums<<<1, 1024, 0, ctx->stream>>>(sums, nb, total);
@@ -674,7 +728,14 @@ static iso_status lhmc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint3
     ctx->launches += 2;
     if ((s = scan_u32(ctx, counts, offsets, nodes, sums2, total2)) != ISO_OK) return s;
     leaf_write<<<(nodes + 255) / 256, 256, 0, ctx->stream>>>(la, offsets, pv_key, pv_level);
-    ctx->launches++;
+    // the node table for the parent walks, in the primal-vertex table's
+    // memory (2 slots per node against its 16, and done with it now)
+    const uint32_t ncap = pow2_at_least(2ull * nodes);
+    unsigned long long* ntable = hk1;
+    e = cudaMemsetAsync(ntable, 0, 8ull * ncap, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "memset node table");
+    node_insert<<<(nodes + 255) / 256, 256, 0, ctx->stream>>>(nkeys, nodes, ntable, ncap - 1);
+    ctx->launches += 2;
     uint32_t ncubes = 0;
     if (rec) {
         ncubes = replay->ncubes;
@@ -710,7 +771,7 @@ static iso_status lhmc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint3
     if (e == cudaSuccess) e = cudaMemsetAsync(stale, 0, 8, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "memset");
     if (ncubes) {
-        CubeArgs ca{nkeys, nvals, nodes, pv_key, pv_level, ncubes, corner, cases, tcount, stale};
+        CubeArgs ca{ntable, ncap - 1, nvals, pv_key, pv_level, ncubes, corner, cases, tcount, stale};
         cube_gather<<<(ncubes + 127) / 128, 128, 0, ctx->stream>>>(ca);
         EdgeArgs ea{nkeys, corner, cases, ncubes, hk2, hv2, hcap2 - 1, vcount, owned, ctx->d_err};
         edge_visit<<<(ncubes + 127) / 128, 128, 0, ctx->stream>>>(ea);

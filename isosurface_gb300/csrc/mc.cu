@@ -852,6 +852,7 @@ iso_status mc_extract_program(iso_ctx* ctx, const iso_program* prog, uint32_t si
         (P.prog_block == prog->d_block && P.prog_ops == prog->ops && P.prog_consts.size() == prog->consts.size() &&
          std::memcmp(P.prog_consts.data(), prog->consts.data(), 4 * prog->consts.size()) == 0);
     const bool match = P.exec && !ctx->timing && same_program && P.size == size && P.flags == flags &&
+                       P.jit_gen == jit_generation() &&
                        std::memcmp(P.bufs, bufs, sizeof(bufs)) == 0 && P.host_v == H.v && P.host_i == H.i &&
                        P.host_cap_v == H.cap_v && P.host_cap_t == H.cap_t;
     if (match) {
@@ -918,6 +919,7 @@ iso_status mc_extract_program(iso_ctx* ctx, const iso_program* prog, uint32_t si
             P.prog_block = prog->d_block;
             P.prog_ops = prog->ops;
             P.prog_consts = prog->consts;
+            P.jit_gen = jit_generation();
             P.size = size;
             P.flags = flags;
             plan_buffers(ctx, P.bufs);
