@@ -296,8 +296,7 @@ ISO_API iso_status iso_mc_extract_field(iso_ctx* ctx, const float* field, uint32
  * needs about nx*ny*nz/8 + 9*ny*nz bytes of it; the largest cubic grid that
  * fits is 613 x 613 x 614 samples (MarchingCubes::new(613)), and grids whose
  * scratch would not fit are rejected with ISO_ERR_TOO_LARGE.  The first call on each device looks up that
- * array's device address; make that first call before any stream capture.
- * All calls share the one array, so calls whose GPU work overlaps (other
+ * array's device address.  All calls share the one array, so calls whose GPU work overlaps (other
  * streams or host threads) race and must be serialised by the caller. */
 ISO_API iso_status iso_mc_extract_field_noalloc(const float* field, uint32_t nx, uint32_t ny, uint32_t nz,
                                                 uint64_t pitch, float* vertices, uint64_t vertex_cap,
