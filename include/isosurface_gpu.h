@@ -228,6 +228,12 @@ ISO_API iso_status iso_program_lipschitz(const iso_program* prog, float* lip);
  * and compilation is enabled (iso_jit_enable, process-wide, default on). */
 ISO_API iso_status iso_program_compiled(const iso_program* prog, int* compiled);
 ISO_API iso_status iso_jit_enable(int enable);
+/* The CUDA C the library compiles for the program in `bytes` (host only: no
+ * device or context needed), NUL-terminated into `out` (room for `cap`
+ * bytes); `needed` receives its size.  `out` null: size only.
+ * ISO_ERR_UNSUPPORTED for a program the library does not compile (sphere
+ * sets, flat unions of translated primitives). */
+ISO_API iso_status iso_program_source(const uint8_t* bytes, size_t len, char* out, size_t cap, size_t* needed);
 
 /* ------------------------------------------------------------------------ */
 /* MarchingCubes (src/marching_cubes.rs:59-82)                               */

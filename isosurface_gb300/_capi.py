@@ -84,6 +84,8 @@ SIGNATURES = {
     "iso_program_lipschitz": (i32, [vp, ctypes.POINTER(ctypes.c_float)]),
     "iso_program_compiled": (i32, [vp, ctypes.POINTER(ctypes.c_int)]),
     "iso_jit_enable": (i32, [ctypes.c_int]),
+    "iso_program_source": (i32, [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t,
+                                 ctypes.POINTER(ctypes.c_size_t)]),
     "iso_mc_extract": (i32, [vp, vp, u32, u32, ctypes.POINTER(MeshInfo)]),
     "iso_mc_extract_host": (i32, [vp, vp, u32, u32, vp, u64, vp, u64, ctypes.POINTER(MeshInfo)]),
     "iso_point_splat_render": (i32, [vp, vp, vp, u32, u32, ctypes.c_float, vp, vp]),

@@ -545,33 +545,51 @@ iso_status iso_ctx_stage_times(iso_ctx* ctx, double* ms, uint64_t* launches) {
     return ISO_OK;
 }
 
+}  // extern "C"
+
+namespace iso {
+// The host side of a program from its bytes: header checks, ops and
+// constants, validation, fast-path forms and culling bounds (no device work).
+iso_status parse_program(const uint8_t* bytes, size_t len, iso_program* p, std::string* err) {
+    if (len < 16) return *err = "program shorter than its header", ISO_ERR_BAD_PROGRAM;
+    uint32_t h[4];
+    std::memcpy(h, bytes, 16);
+    if (h[0] != 0x314F5349u) return *err = "bad magic", ISO_ERR_BAD_PROGRAM;
+    if ((uint64_t)16 + 4ull * h[1] + 4ull * h[2] != len)
+        return *err = "length does not match header", ISO_ERR_BAD_PROGRAM;
+    if (h[1] == 0) return *err = "empty program", ISO_ERR_BAD_PROGRAM;
+    p->ops.resize(h[1]);
+    p->consts.resize(h[2]);
+    std::memcpy(p->ops.data(), bytes + 16, 4ull * h[1]);
+    if (h[2]) std::memcpy(p->consts.data(), bytes + 16 + 4ull * h[1], 4ull * h[2]);
+    if (!validate(p, err)) return ISO_ERR_BAD_PROGRAM;
+    classify(p);
+    cull_bounds(p);
+    uint64_t hash = 0xCBF29CE484222325ull;  // FNV-1a 64
+    for (size_t i = 0; i < len; ++i) hash = (hash ^ bytes[i]) * 0x100000001B3ull;
+    p->content_hash = hash;
+    return ISO_OK;
+}
+}  // namespace iso
+
+extern "C" {
+
 iso_status iso_program_create(iso_ctx* ctx, const uint8_t* bytes, size_t len, iso_program** out) {
     if (!ctx || !bytes || !out) return ISO_ERR_INVALID_ARG;
     *out = nullptr;
-    if (len < 16) return fail(ctx, ISO_ERR_BAD_PROGRAM, "program shorter than its header");
-    uint32_t h[4];
-    std::memcpy(h, bytes, 16);
-    if (h[0] != 0x314F5349u) return fail(ctx, ISO_ERR_BAD_PROGRAM, "bad magic");
-    if ((uint64_t)16 + 4ull * h[1] + 4ull * h[2] != len) return fail(ctx, ISO_ERR_BAD_PROGRAM, "length does not match header");
-    if (h[1] == 0) return fail(ctx, ISO_ERR_BAD_PROGRAM, "empty program");
     iso_program* p = new (std::nothrow) iso_program();
     if (!p) return ISO_ERR_OUT_OF_MEMORY;
     p->ctx = ctx;
     p->device = ctx->device;
     static std::atomic<uint64_t> next_uid{1};
     p->uid = next_uid.fetch_add(1);
-    p->ops.resize(h[1]);
-    p->consts.resize(h[2]);
-    std::memcpy(p->ops.data(), bytes + 16, 4ull * h[1]);
-    if (h[2]) std::memcpy(p->consts.data(), bytes + 16 + 4ull * h[1], 4ull * h[2]);
     std::string err;
-    if (!validate(p, &err)) {
+    iso_status s = parse_program(bytes, len, p, &err);
+    if (s != ISO_OK) {
         delete p;
-        return fail(ctx, ISO_ERR_BAD_PROGRAM, err);
+        return fail(ctx, s, err);
     }
-    classify(p);
-    cull_bounds(p);
-    iso_status s = set_device(ctx);
+    s = set_device(ctx);
     if (s != ISO_OK) {
         delete p;
         return s;
@@ -593,9 +611,6 @@ iso_status iso_program_create(iso_ctx* ctx, const uint8_t* bytes, size_t len, is
     if (!p->jump.empty()) std::memcpy(staged.data() + o_jump, p->jump.data(), 4 * p->jump.size());
     if (set_bytes) std::memcpy(staged.data() + o_set, p->consts.data() + p->set_at + 3, set_bytes);
     if (!p->prims.empty()) std::memcpy(staged.data() + o_prims, p->prims.data(), 4 * p->prims.size());
-    uint64_t hash = 0xCBF29CE484222325ull;  // FNV-1a 64
-    for (size_t i = 0; i < len; ++i) hash = (hash ^ bytes[i]) * 0x100000001B3ull;
-    p->content_hash = hash;
     unsigned char* block = nullptr;
     cudaError_t e = program_block(ctx, total, (void**)&block, &p->block_bytes);
     if (e == cudaSuccess) {

@@ -193,6 +193,9 @@ iso_status check_launch(iso_ctx* ctx, const char* what);
 iso_status read_device_errors(iso_ctx* ctx);
 iso_status set_device(iso_ctx* ctx);
 
+// ctx.cu: the host side of a program from its bytes (no device work)
+iso_status parse_program(const uint8_t* bytes, size_t len, iso_program* p, std::string* err);
+
 // jit.cu: changes whenever per-program compilation is switched on or off
 uint64_t jit_generation();
 

@@ -314,6 +314,23 @@ extern "C" iso_status iso_jit_enable(int enable) {
     return ISO_OK;
 }
 
+extern "C" iso_status iso_program_source(const uint8_t* bytes, size_t len, char* out, size_t cap, size_t* needed) {
+    if (!bytes || !needed) return ISO_ERR_INVALID_ARG;
+    *needed = 0;
+    iso_program p;
+    std::string err;
+    iso_status s = iso::parse_program(bytes, len, &p, &err);
+    if (s != ISO_OK) return s;
+    std::string body;
+    if (!p.prims.empty() || p.kind != iso::PK_GENERIC || !iso::emit_value(&p, &body)) return ISO_ERR_UNSUPPORTED;
+    const std::string src = iso::module_source(body);
+    *needed = src.size() + 1;
+    if (!out) return ISO_OK;
+    if (cap < src.size() + 1) return ISO_ERR_CAPACITY;
+    std::memcpy(out, src.c_str(), src.size() + 1);
+    return ISO_OK;
+}
+
 extern "C" iso_status iso_program_compiled(const iso_program* prog, int* compiled) {
     if (!prog || !compiled) return ISO_ERR_INVALID_ARG;
     *compiled = iso::module_for(prog) != nullptr ? 1 : 0;

@@ -144,6 +144,13 @@ extern "C" {
     pub fn iso_program_lipschitz(prog: *const IsoProgram, lip: *mut f32) -> IsoStatus;
     pub fn iso_program_compiled(prog: *const IsoProgram, compiled: *mut c_int) -> IsoStatus;
     pub fn iso_jit_enable(enable: c_int) -> IsoStatus;
+    pub fn iso_program_source(
+        bytes: *const u8,
+        len: usize,
+        out: *mut c_char,
+        cap: usize,
+        needed: *mut usize,
+    ) -> IsoStatus;
     pub fn iso_mc_extract(
         ctx: *mut IsoCtx,
         prog: *const IsoProgram,
