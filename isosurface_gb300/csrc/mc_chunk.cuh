@@ -185,14 +185,23 @@ __global__ void __launch_bounds__(256, ISO_COUNT_BLOCKS) mc_chunk_count(ChunkCou
                 // lane in chunk order, their triangles summed per segment
                 const uint32_t h = r & 1;
                 ChunkStage<64>& P = s_pair[warp];
+                uint32_t vr = 0;
+                if (__any_sync(FULL, act != 0)) {
 #pragma unroll
-                for (int k = 0; k < 8; ++k) P.q[32 * h + lane][k] = q.k[k];
-                P.act[32 * h + lane] = act;
-                const uint32_t n = __popc(act);
-                const uint32_t incl = warp_incl_scan(n, lane);
-                P.excl[32 * h + lane] = pair_total + incl - n;
-                pair_total += __shfl_sync(FULL, incl, 31);
-                const uint32_t vr = __reduce_add_sync(FULL, v);
+                    for (int k = 0; k < 8; ++k) P.q[32 * h + lane][k] = q.k[k];
+                    P.act[32 * h + lane] = act;
+                    const uint32_t n = __popc(act);
+                    const uint32_t incl = warp_incl_scan(n, lane);
+                    P.excl[32 * h + lane] = pair_total + incl - n;
+                    pair_total += __shfl_sync(FULL, incl, 31);
+                    vr = __reduce_add_sync(FULL, v);
+                } else {
+                    // no active cell in the round (most rounds): no corners to
+                    // stage, no counts to scan (v is 0 without active cells);
+                    // the chunk lookup never lands on a chunk without any
+                    P.act[32 * h + lane] = 0;
+                    P.excl[32 * h + lane] = pair_total;
+                }
                 if (h == 0) {
                     vr_first = vr;
                     continue;
@@ -817,13 +826,20 @@ __global__ void __launch_bounds__(256, 5) mc_cell_emit(ChunkEmitArgs A, const ui
 #pragma unroll
             for (int k = 0; k < 8; ++k) q.k[k] = 0;
         }
+        if (__any_sync(FULL, act != 0)) {
 #pragma unroll
-        for (int k = 0; k < 8; ++k) S.q[32 * h + lane][k] = q.k[k];
-        S.act[32 * h + lane] = act;
-        const uint32_t n = __popc(act);
-        const uint32_t incl = warp_incl_scan(n, lane);
-        S.excl[32 * h + lane] = total + incl - n;
-        total += __shfl_sync(FULL, incl, 31);
+            for (int k = 0; k < 8; ++k) S.q[32 * h + lane][k] = q.k[k];
+            S.act[32 * h + lane] = act;
+            const uint32_t n = __popc(act);
+            const uint32_t incl = warp_incl_scan(n, lane);
+            S.excl[32 * h + lane] = total + incl - n;
+            total += __shfl_sync(FULL, incl, 31);
+        } else {
+            // no active cell in the segment: nothing to stage (the chunk
+            // lookup never lands on a chunk without active cells)
+            S.act[32 * h + lane] = 0;
+            S.excl[32 * h + lane] = total;
+        }
     }
     if (total == 0) return;  // no active cell: no vertex, no triangle
     pdl_wait();              // the counts and their scan
