@@ -244,7 +244,7 @@ def cpu_baseline_port(src_bytes, budget_s=12.0, threads=1):
                       % (z0, z0 + layers, cells, secs)}
 
 
-def secondary_workloads(ctx, torch, steps, only=None):
+def secondary_workloads(ctx, torch, steps, only=None, per_chunk=True):
     """The other workloads, timed with CUDA events on the library's stream:
     the sampler against the measured FP32 rate, MarchingCubes::new(513) of a
     general CSG program, the 4096-chunk batch (one CUDA graph vs one
@@ -274,7 +274,7 @@ def secondary_workloads(ctx, torch, steps, only=None):
     if want("refshapes"):
         out["reference_bench_shapes"] = _reference_bench_shapes(ctx, timed, steps)
     if want("batch"):
-        out.update(_batch_workload(ctx, timed, steps))
+        out.update(_batch_workload(ctx, timed, steps, per_chunk))
     src = scenes.csg()
     if want("dc"):
         for _ in range(2):
@@ -359,7 +359,7 @@ def _reference_bench_shapes(ctx, timed, steps):
     return out
 
 
-def _batch_workload(ctx, timed, steps):
+def _batch_workload(ctx, timed, steps, per_chunk=True):
     from isosurface_gb300 import scenes
     from isosurface_gb300.api import Batch
     out = {}
@@ -371,14 +371,15 @@ def _batch_workload(ctx, timed, steps):
     batch.run(graph=True)
     graph_ms = timed(lambda: batch.run(graph=True), max(3, min(steps, 20)))
     info = batch.run(graph=True)
-    per_ms = timed(batch.run_per_chunk, 2)
-    batch.run_per_chunk_async()
-    async_ms = timed(batch.run_per_chunk_async, 3)
     cells = info.num_cells
-    out["batch_4096_chunks"] = {"cells": int(cells), "graph_ms": graph_ms, "per_chunk_ms": per_ms,
-                                "per_chunk_no_sync_ms": async_ms, "speedup": per_ms / graph_ms,
-                                "speedup_vs_no_sync": async_ms / graph_ms, "cells_per_s": cells / (graph_ms / 1e3),
+    out["batch_4096_chunks"] = {"cells": int(cells), "graph_ms": graph_ms, "cells_per_s": cells / (graph_ms / 1e3),
                                 "triangles": int(info.num_triangles), "slab_depth_by_size": chosen}
+    if per_chunk:
+        per_ms = timed(batch.run_per_chunk, 2)
+        batch.run_per_chunk_async()
+        async_ms = timed(batch.run_per_chunk_async, 3)
+        out["batch_4096_chunks"].update({"per_chunk_ms": per_ms, "per_chunk_no_sync_ms": async_ms,
+                                         "speedup": per_ms / graph_ms, "speedup_vs_no_sync": async_ms / graph_ms})
     batch.close()
     return out
 
@@ -593,6 +594,9 @@ def main():
                          "secondary "
                          "workloads (emc runs only when named)")
     ap.add_argument("--surrogate-train-steps", type=int, default=4000)
+    ap.add_argument("--no-per-chunk", action="store_true",
+                    help="batch workload: time the batch graph only, not the one-extraction-per-chunk comparisons "
+                         "(for profiling, where their 65 K launches are slow)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -774,7 +778,7 @@ def main():
     secondary = None
     if not args.no_secondary:
         only = set(args.secondary_only.split(",")) if args.secondary_only else None
-        secondary = secondary_workloads(ctx, torch, args.steps, only)
+        secondary = secondary_workloads(ctx, torch, args.steps, only, per_chunk=not args.no_per_chunk)
         if not args.no_surrogate and (only is None or "surrogate" in only):
             secondary["surrogate_512"] = surrogate_workload(ctx, torch, args.surrogate_train_steps)
 
