@@ -1,8 +1,13 @@
 // Grid sampling: the sample loops of PrimalGrid::traverse
-// (src/traversal/primal_grid.rs:44-70) as one kernel that writes the f32 field
+// (src/traversal/primal_grid.rs:44-70) as kernels that write the f32 field
 // and, with warp ballots, the packed sign bits (bit set iff !(v > 0),
 // classify_corners, marching_cubes_impl.rs:26-37) that the marching-cubes
-// passes classify from.
+// passes classify from.  launch_sample_grid picks one of three samplers:
+// for the extractors (near_only) on a hard union of spheres, the per-tile
+// sphere culling below; on another program with a Lipschitz bound and a
+// lattice of at least one tile per SM, the culled sampler of bricks_core.cuh
+// (compiled for the program by jit.cu when it can be, else interpreted);
+// otherwise, and for a full field, sample_generic.
 //
 // Point (x, y, z) sits at (x*inv, y*inv, z*inv), inv = 1/(size-1) in f32, as
 // in the reference.  Built with -fmad=false: the values are bit-identical to
