@@ -115,11 +115,18 @@ TRAFFIC_SOURCES = ["isosurface_gb300/csrc/" + f for f in
 
 
 def kernel_sources_sha256():
+    """Hash of the extraction kernels' sources with comments and blank lines
+    removed (a comment edit leaves the captured kernels as they were)."""
     import hashlib
+    import re
     h = hashlib.sha256()
     for rel in TRAFFIC_SOURCES:
-        with open(os.path.join(ROOT, rel), "rb") as f:
-            h.update(f.read())
+        with open(os.path.join(ROOT, rel)) as f:
+            text = f.read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        lines = [l.rstrip() for l in text.splitlines() if l.strip()]
+        h.update("\n".join(lines).encode())
     return h.hexdigest()
 
 
