@@ -173,3 +173,25 @@ def test_compiled_evaluator_matches_interpreter(ctx):
                 lib().iso_jit_enable(1)
         assert torch.equal(out[0][1], out[1][1]), name
         assert torch.equal(out[0][0], out[1][0]), name  # the same samples written, the same bits
+
+
+def test_toggling_compilation_reruns_recorded_extractions(ctx):
+    """A recorded extraction holds the sampler kernels of the setting it was
+    recorded with: switching compilation off and on again must not replay
+    the other setting's recording, and every mesh is the same."""
+    from isosurface_gb300._capi import lib
+    src = _programs()["csg"]
+    size = 161
+    want = None
+    try:
+        for enable in (1, 1, 1, 0, 0, 0, 1, 1):  # repeats record and replay each setting
+            lib().iso_jit_enable(enable)
+            launches0 = ctx.kernel_launches
+            got = ctx.download(ctx.mc_extract(src, size))
+            assert ctx.kernel_launches > launches0
+            if want is None:
+                want = got
+            assert np.array_equal(got.vertices, want.vertices)
+            assert np.array_equal(got.indices, want.indices)
+    finally:
+        lib().iso_jit_enable(1)
