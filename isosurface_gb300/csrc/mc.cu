@@ -41,7 +41,6 @@
 
 #include <algorithm>
 #include <cstring>
-#include <mutex>
 
 #include "internal.h"
 #define ISO_TABLE static __device__ const
@@ -1132,24 +1131,17 @@ namespace {
 constexpr size_t NOALLOC_SCRATCH_BYTES = 32ull << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 
-// Host handle of the array per device: the array's name is only a host-side
-// stand-in, so its device address is looked up once per device.
-std::mutex g_noalloc_mutex;
-void* g_noalloc_addr[256] = {};
-
-iso_status noalloc_scratch(int device, unsigned char** out) {
-    if (device < 0 || device >= 256) return ISO_ERR_NO_DEVICE;
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_addr[device]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || p == nullptr) {
-            cudaGetLastError();
-            return ISO_ERR_CUDA;
-        }
-        g_noalloc_addr[device] = p;
+// The array's device address in the current context, looked up on every
+// call (a cached address would dangle after a device reset or under another
+// context), which costs little next to the call's two synchronisations.
+iso_status noalloc_scratch(unsigned char** out) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+        cudaGetLastError();
+        return ISO_ERR_CUDA;
     }
-    *out = (unsigned char*)g_noalloc_addr[device];
+    *out = (unsigned char*)p;
     return ISO_OK;
 }
 
@@ -1193,7 +1185,7 @@ extern "C" ISO_API iso_status iso_mc_extract_field_noalloc(const float* field, u
         return ISO_ERR_NO_DEVICE;
     }
     unsigned char* s = nullptr;
-    iso_status st = noalloc_scratch(device, &s);
+    iso_status st = noalloc_scratch(&s);
     if (st != ISO_OK) return st;
     cudaStream_t cs = (cudaStream_t)stream;
     uint32_t* err = (uint32_t*)(s + off_head);
