@@ -223,16 +223,18 @@ ISO_API iso_status iso_program_lipschitz(const iso_program* prog, float* lip);
  * for it (written out as straight-line code and compiled with NVRTC on first
  * use, cached per program contents; values bit-identical to the
  * interpreter's) rather than the interpreter: 1 or 0.  General programs
- * (no sphere set; not a flat union of translated primitives, which the
- * interpreter prunes per sub-brick) are compiled while NVRTC is available
- * and compilation is enabled (iso_jit_enable, process-wide, default on). */
+ * (no sphere set) are compiled while NVRTC is available and compilation is
+ * enabled (iso_jit_enable, process-wide, default on); iso_sample_grid runs
+ * every compiled program's full-field kernel, while the extractors sample a
+ * flat union of translated primitives with the interpreter, which prunes
+ * the primitives per sub-brick (0 here). */
 ISO_API iso_status iso_program_compiled(const iso_program* prog, int* compiled);
 ISO_API iso_status iso_jit_enable(int enable);
 /* The CUDA C the library compiles for the program in `bytes` (host only: no
  * device or context needed), NUL-terminated into `out` (room for `cap`
  * bytes); `needed` receives its size.  `out` null: size only.
  * ISO_ERR_UNSUPPORTED for a program the library does not compile (sphere
- * sets, flat unions of translated primitives). */
+ * sets). */
 ISO_API iso_status iso_program_source(const uint8_t* bytes, size_t len, char* out, size_t cap, size_t* needed);
 
 /* ------------------------------------------------------------------------ */

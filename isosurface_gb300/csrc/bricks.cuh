@@ -64,6 +64,12 @@ inline unsigned persistent_blocks(const void* kernel, std::atomic<int>& per_sm, 
 bool jit_sample_bricks(iso_ctx* ctx, const iso_program* prog, const GridTiles& tiles, uint32_t ntiles,
                        BrickTask* list, uint32_t* count, uint32_t cap, cudaError_t* err);
 
+// jit.cu: the full field of one lattice (blocks of eight field_warp warps)
+// with the program's compiled evaluator; false (nothing launched) when the
+// program has none
+bool jit_sample_field(iso_ctx* ctx, const iso_program* prog, const BrickLattice& g, uint64_t blocks,
+                      cudaError_t* err);
+
 template <class Tiles>
 inline unsigned brick_rows_blocks(int sms) {
     static std::atomic<int> per_sm{0};

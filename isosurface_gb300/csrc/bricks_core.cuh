@@ -1,5 +1,6 @@
-// Culled sampling of a general program for marching cubes: the device code,
-// written so that it also compiles on its own under NVRTC (no includes: the
+// Culled sampling of a general program for marching cubes (and, at the end,
+// the plain sampler of every point): the device code, written so that it
+// also compiles on its own under NVRTC (no includes: the
 // library includes it after its own headers, the run-time compiler after a
 // prelude of fixed-width integer types and vm_math.cuh).
 //
@@ -315,6 +316,27 @@ __device__ __forceinline__ void brick_rows_body(const Ev& ev, const Tiles& tiles
         const uint64_t keep = warp_or64(k.keep);
         brick_quad(ev, tiles.tile(k.tile_sb / BRICK_MAX), e < n ? k.tile_sb % BRICK_MAX : 0xFFFFFFFFu, keep);
     }
+}
+
+// The plain sampler (every point, nothing culled; the lattice's culling
+// fields unused): warp gw of the lattice's W * ny * nz takes 32 consecutive
+// points of one row, writes their values and, by ballot, the row's sign word.
+template <class Ev>
+__device__ __forceinline__ void field_warp(const Ev& ev, const BrickLattice& g, uint64_t gw) {
+    if (gw >= (uint64_t)g.W * g.ny * g.nz) return;  // warp-uniform
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t w = (uint32_t)(gw % g.W);
+    const uint64_t row = gw / g.W;
+    const uint32_t y = (uint32_t)(row % g.ny), z = (uint32_t)(row / g.ny);
+    const uint32_t x = 32 * w + lane;
+    bool inside = false;
+    if (x < g.nx) {
+        const float v = ev.value(v3((float)x * g.inv, (float)y * g.inv, (float)(z + g.zoff) * g.inv));
+        g.field[row * g.pitch + x] = v;
+        inside = !(v > 0.0f);
+    }
+    const uint32_t b = __ballot_sync(0xFFFFFFFFu, inside);
+    if (lane == 0) g.bits[row * g.W + w] = b;
 }
 
 }  // namespace iso

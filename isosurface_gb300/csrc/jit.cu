@@ -1,14 +1,16 @@
-// Per-program compiled evaluators for the culled sampler.
+// Per-program compiled evaluators for the culled sampler and the full field.
 //
 // The interpreter (vm.cuh) spends most of its instructions on dispatch and
 // on its value and point stacks in local memory.  For a general program (no
-// flat primitive list, no sphere set) the library instead writes the
-// program out as straight-line CUDA C -- the same primitive functions
-// (vm_math.cuh) and the same f32 operations in the same order, constants as
-// exact bit patterns -- around the culled sampler's device code
-// (bricks_core.cuh), compiles it with NVRTC at run time (--fmad=false, so
-// nothing is contracted: values stay bit-identical to the interpreter's),
-// and launches the two kernels from the loaded module.  Modules are cached
+// sphere set) the library instead writes the program out as straight-line
+// CUDA C -- the same primitive functions (vm_math.cuh) and the same f32
+// operations in the same order, constants as exact bit patterns -- around
+// the samplers' device code (bricks_core.cuh), compiles it with NVRTC at run
+// time (--fmad=false, so nothing is contracted: values stay bit-identical to
+// the interpreter's), and launches the kernels from the loaded module: the
+// culled sampler's two (not for a flat union of translated primitives,
+// whose interpreted form prunes the primitives per sub-brick) and the full
+// field's one.  Modules are cached
 // per program contents for the life of the process.  NVRTC is loaded with
 // dlopen on first use; without it, or when a compilation fails, the
 // interpreter runs instead.
@@ -178,7 +180,9 @@ std::string module_source(const std::string& value_body) {
          "    iso::brick_classify_body(iso::JitEval{}, tiles, list, count, cap, err);\n}\n"
          "extern \"C\" __global__ void __launch_bounds__(256) iso_jit_rows(iso::GridTiles tiles, "
          "const iso::BrickTask* list, const uint32_t* count, uint32_t cap) {\n"
-         "    iso::brick_rows_body(iso::JitEval{}, tiles, list, count, cap);\n}\n";
+         "    iso::brick_rows_body(iso::JitEval{}, tiles, list, count, cap);\n}\n"
+         "extern \"C\" __global__ void __launch_bounds__(256) iso_jit_field(iso::BrickLattice g) {\n"
+         "    iso::field_warp(iso::JitEval{}, g, (uint64_t)blockIdx.x * 8 + (threadIdx.x >> 5));\n}\n";
     return s;
 }
 
@@ -188,7 +192,7 @@ struct Module {
     std::vector<float> consts;
     bool ok = false;
     cudaLibrary_t lib = nullptr;
-    cudaKernel_t classify = nullptr, rows = nullptr;
+    cudaKernel_t classify = nullptr, rows = nullptr, field = nullptr;
     std::atomic<int> rows_per_sm{0};
 };
 
@@ -244,6 +248,7 @@ Module* compile_module(const iso_program* p, std::string* why) {
     cudaError_t e = cudaLibraryLoadData(&m->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
     if (e == cudaSuccess) e = cudaLibraryGetKernel(&m->classify, m->lib, "iso_jit_classify");
     if (e == cudaSuccess) e = cudaLibraryGetKernel(&m->rows, m->lib, "iso_jit_rows");
+    if (e == cudaSuccess) e = cudaLibraryGetKernel(&m->field, m->lib, "iso_jit_field");
     if (e != cudaSuccess) {
         cudaGetLastError();
         if (m->lib) cudaLibraryUnload(m->lib);
@@ -257,7 +262,7 @@ Module* compile_module(const iso_program* p, std::string* why) {
 
 // The compiled module of a program (compiled on first use), or null.
 Module* module_for(const iso_program* p) {
-    if (!g_jit_enabled.load() || !p->prims.empty() || p->kind != PK_GENERIC) return nullptr;
+    if (!g_jit_enabled.load() || p->kind != PK_GENERIC) return nullptr;
     std::lock_guard<std::mutex> lock(g_jit_mutex);
     auto range = g_modules.equal_range(p->content_hash);
     for (auto it = range.first; it != range.second; ++it) {
@@ -281,6 +286,9 @@ Module* module_for(const iso_program* p) {
 // launched) when the program has none, so the caller runs the interpreter.
 bool jit_sample_bricks(iso_ctx* ctx, const iso_program* prog, const GridTiles& tiles, uint32_t ntiles,
                        BrickTask* list, uint32_t* count, uint32_t cap, cudaError_t* err) {
+    // a flat union of translated primitives stays with the interpreter,
+    // which prunes the primitives per sub-brick
+    if (!prog->prims.empty()) return false;
     Module* m = module_for(prog);
     if (!m) return false;
     static_assert(sizeof(GridTiles) % 8 == 0, "kernel argument layout");
@@ -297,6 +305,17 @@ bool jit_sample_bricks(iso_ctx* ctx, const iso_program* prog, const GridTiles& t
         e = cudaLaunchKernel((const void*)m->rows, dim3(blocks), dim3(256), a2, 0, ctx->stream);
     }
     *err = e;
+    return true;
+}
+
+bool jit_sample_field(iso_ctx* ctx, const iso_program* prog, const BrickLattice& g, uint64_t blocks,
+                      cudaError_t* err) {
+    Module* m = module_for(prog);
+    if (!m) return false;
+    static_assert(sizeof(BrickLattice) % 8 == 0, "kernel argument layout");
+    BrickLattice a = g;
+    void* args[] = {&a};
+    *err = cudaLaunchKernel((const void*)m->field, dim3((unsigned)blocks), dim3(256), args, 0, ctx->stream);
     return true;
 }
 
@@ -322,7 +341,7 @@ extern "C" iso_status iso_program_source(const uint8_t* bytes, size_t len, char*
     iso_status s = iso::parse_program(bytes, len, &p, &err);
     if (s != ISO_OK) return s;
     std::string body;
-    if (!p.prims.empty() || p.kind != iso::PK_GENERIC || !iso::emit_value(&p, &body)) return ISO_ERR_UNSUPPORTED;
+    if (p.kind != iso::PK_GENERIC || !iso::emit_value(&p, &body)) return ISO_ERR_UNSUPPORTED;
     const std::string src = iso::module_source(body);
     *needed = src.size() + 1;
     if (!out) return ISO_OK;
@@ -333,6 +352,8 @@ extern "C" iso_status iso_program_source(const uint8_t* bytes, size_t len, char*
 
 extern "C" iso_status iso_program_compiled(const iso_program* prog, int* compiled) {
     if (!prog || !compiled) return ISO_ERR_INVALID_ARG;
-    *compiled = iso::module_for(prog) != nullptr ? 1 : 0;
+    // the extractors' sampler of a flat union of primitives is the
+    // interpreter's pruned one, compiled module or not
+    *compiled = prog->prims.empty() && iso::module_for(prog) != nullptr ? 1 : 0;
     return ISO_OK;
 }

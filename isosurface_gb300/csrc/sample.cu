@@ -7,7 +7,9 @@
 // sphere culling below; on another program with a Lipschitz bound and a
 // lattice of at least one tile per SM, the culled sampler of bricks_core.cuh
 // (compiled for the program by jit.cu when it can be, else interpreted);
-// otherwise, and for a full field, sample_generic.
+// otherwise every point (field_warp): for a full field with the program's
+// compiled evaluator when it has one (jit.cu), else interpreted
+// (sample_generic).
 //
 // Point (x, y, z) sits at (x*inv, y*inv, z*inv), inv = 1/(size-1) in f32, as
 // in the reference.  Built with -fmad=false: the values are bit-identical to
@@ -26,25 +28,10 @@ namespace {
 
 constexpr uint32_t FULL = 0xFFFFFFFFu;
 
-// One warp per (32-point chunk, row): generic program evaluator.
-__global__ void __launch_bounds__(256) sample_generic(ProgView pv, uint32_t nx, uint32_t ny, uint32_t nz, float inv,
-                                                      float* field, uint64_t pitch, uint32_t* bits, uint32_t W,
-                                                      uint32_t zoff) {
-    const int lane = threadIdx.x & 31;
-    const uint64_t gw = (uint64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (gw >= (uint64_t)W * ny * nz) return;
-    const uint32_t w = (uint32_t)(gw % W);
-    const uint64_t row = gw / W;
-    const uint32_t y = (uint32_t)(row % ny), z = (uint32_t)(row / ny);
-    const uint32_t x = 32 * w + lane;
-    bool inside = false;
-    if (x < nx) {
-        float v = eval_scalar(pv, v3((float)x * inv, (float)y * inv, (float)(z + zoff) * inv));
-        field[row * pitch + x] = v;
-        inside = !(v > 0.0f);
-    }
-    uint32_t b = __ballot_sync(FULL, inside);
-    if (lane == 0) bits[row * W + w] = b;
+// One warp per (32-point chunk, row): the interpreter at every point
+// (field_warp, bricks_core.cuh).
+__global__ void __launch_bounds__(256) sample_generic(VmEval ev, BrickLattice g) {
+    field_warp(ev, g, (uint64_t)blockIdx.x * 8 + (threadIdx.x >> 5));
 }
 
 // Union of spheres, hard min, optionally behind a domain map.  Each block
@@ -686,10 +673,18 @@ iso_status launch_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t nx
             sample_sphere_set<<<grid, 256, smem, ctx->stream>>>(a);
         }
     } else {
-        uint64_t warps = (uint64_t)W * ny * nz;
+        const uint64_t warps = (uint64_t)W * ny * nz;
+        const BrickLattice g = brick_lattice(prog, nx, ny, nz, inv, field, pitch, bits, W, zoff, reach_steps);
         StageTimer timer(ctx, ISO_STAGE_SAMPLE);
-        sample_generic<<<(unsigned)((warps + 7) / 8), 256, 0, ctx->stream>>>(prog->view(), nx, ny, nz, inv, field, pitch,
-                                                                          bits, W, zoff);
+        cudaError_t je = cudaSuccess;
+        // a full field: the program's compiled evaluator when it has one
+        // (jit.cu; the extractors' small lattices stay interpreted, as a
+        // compilation would cost more than it saves there)
+        if (!near_only && jit_sample_field(ctx, prog, g, (warps + 7) / 8, &je)) {
+            if (je != cudaSuccess) return cuda_fail(ctx, je, "compiled field sampler launch");
+        } else {
+            sample_generic<<<(unsigned)((warps + 7) / 8), 256, 0, ctx->stream>>>(VmEval{prog->view()}, g);
+        }
     }
     ctx->launches++;
     return check_launch(ctx, "sample_grid");

@@ -175,6 +175,31 @@ def test_compiled_evaluator_matches_interpreter(ctx):
         assert torch.equal(out[0][0], out[1][0]), name  # the same samples written, the same bits
 
 
+@pytest.mark.parametrize("name", ["csg", "csg_rigid", "smooth", "central_difference", "prim_union", "prims40",
+                                  "prims70", "scaled_domain", "chunk0", "sphere_set"])
+def test_compiled_full_field_matches_interpreter_and_oracle(ctx, name):
+    """iso_sample_grid runs the program's compiled full-field kernel (every
+    general program, flat unions of translated primitives included; sphere
+    sets stay interpreted): the field is bit-identical to the interpreter's
+    and to the oracle's at every sample."""
+    import torch
+    import oracle
+    from isosurface_gb300._capi import lib
+    src = _programs()[name]
+    size, pitch = 97, 101
+    out = []
+    for enable in (1, 0):
+        lib().iso_jit_enable(enable)
+        try:
+            f = torch.full(((size + 1) * size * pitch,), float("nan"), dtype=torch.float32, device="cuda")
+            ctx.sample_grid(src, size, f.data_ptr(), pitch)
+            out.append(f.view(size + 1, size, pitch)[:, :, :size].cpu().numpy())
+        finally:
+            lib().iso_jit_enable(1)
+    assert np.array_equal(out[0].view(np.uint32), out[1].view(np.uint32)), name
+    assert np.array_equal(out[0], oracle.Program(S.lower(src)).sample_grid(size)), name
+
+
 def test_toggling_compilation_reruns_recorded_extractions(ctx):
     """A recorded extraction holds the sampler kernels of the setting it was
     recorded with: switching compilation off and on again must not replay

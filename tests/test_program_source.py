@@ -1,8 +1,10 @@
 """The CUDA C the library compiles per general program (csrc/jit.cu), on
 the CPU: iso_program_source needs no device, and NVRTC compiles for sm_103a
-without one.  Every general test program's module must compile, and the
-generated evaluator must walk the program's ops as the interpreter does
-(one statement per primitive, operator and point map)."""
+without one.  Every general test program's module must compile (its three
+kernels: the culled sampler's two and the full field's), and the generated
+evaluator must walk the program's ops as the interpreter does (one
+statement per primitive, operator and point map); sphere sets are not
+compiled."""
 import ctypes
 
 import numpy as np
@@ -82,6 +84,9 @@ def _general():
         "nested": S.unit_to_cube(S.Difference(S.Union(rigid(S.Torus(0.5, 0.1)), rigid(S.Sphere(0.4))),
                                               S.Intersection(rigid(S.RectangularPrism((0.3, 0.2, 0.6))),
                                                              S.Cylinder(0.2, 0.9)))),
+        # a flat union of translated primitives (compiled for the full field)
+        "flat": S.unit_to_cube(S.Union(S.Translate(S.Sphere(0.3), (0.1, 0, 0)),
+                                       S.Translate(S.RectangularPrism((0.2, 0.2, 0.2)), (-0.3, 0, 0)))),
     }
 
 
@@ -99,6 +104,8 @@ def test_generated_module_compiles(name):
     maps = int(np.isin(ops, [0x01, 0x02, 0x03]).sum())
     assert body.count("const float val") == prims + binary
     assert body.count("const V3 pt") == maps
+    for kernel in ("iso_jit_classify", "iso_jit_rows", "iso_jit_field"):
+        assert 'extern "C" __global__ void __launch_bounds__(256) %s(' % kernel in text
     rc, cubin, log = _compile(text)
     assert rc == 0 and cubin > 0, log
 
@@ -107,8 +114,6 @@ def test_uncompiled_forms_are_reported():
     rng = np.random.default_rng(1)
     sph = rng.uniform(-0.8, 0.8, size=(12, 4)).astype(np.float32)
     sph[:, 3] = np.abs(sph[:, 3]) * 0.3 + 0.05
-    flat = S.unit_to_cube(S.Union(S.Translate(S.Sphere(0.3), (0.1, 0, 0)),
-                                  S.Translate(S.RectangularPrism((0.2, 0.2, 0.2)), (-0.3, 0, 0))))
-    for src in (S.unit_to_cube(S.SphereSet(sph)), S.unit_to_cube(S.SphereSet(sph, smooth_k=0.05)), flat):
+    for src in (S.unit_to_cube(S.SphereSet(sph)), S.unit_to_cube(S.SphereSet(sph, smooth_k=0.05))):
         assert _source(bytes(S.lower(src)))[0] == ISO_ERR_UNSUPPORTED
     assert _source(b"\x00" * 8)[0] == 5  # ISO_ERR_BAD_PROGRAM
