@@ -361,7 +361,10 @@ ISO_API iso_status iso_lhmc_extract(iso_ctx* ctx, const iso_program* prog, uint3
 /* Dual-cube corners of the last iso_lhmc_extract call on `ctx` whose parent
  * walk found no node.  The reference keeps the previous primal vertex's
  * corner data there (traversal/implicit_octree.rs:84-95), which depends on its
- * HashMap order; 0 means the extraction involved no such corner. */
+ * HashMap order; 0 means the extraction involved no such corner.  No input
+ * reaches that case (every level-2 node exists and every primal vertex lies
+ * strictly inside the domain, so each walk ends at a node of level >= 2):
+ * the count is a check and reads 0. */
 ISO_API uint64_t iso_lhmc_stale_corners(const iso_ctx* ctx);
 
 /* ------------------------------------------------------------------------ */

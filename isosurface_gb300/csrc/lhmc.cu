@@ -19,7 +19,9 @@
 //    REMAP_CUBE[i]) walks parent() until a node exists; the corner is that
 //    node's centre and value.  A corner with no ancestor keeps the previous
 //    corner's data in the reference (an order-dependent case); it is counted
-//    and reported through iso_lhmc_stale_corners.
+//    and reported through iso_lhmc_stale_corners.  No input reaches it: all
+//    64 level-2 nodes always exist and primal vertices lie strictly inside,
+//    so every walk meets a node at level 2 or deeper.
 // 4. Marching cubes on the dual cubes with MortonKey dedup: each vertex is
 //    owned by the first (cube, first-use rank) that references its key, found
 //    with a 64-bit atomicMin in a second hash table.
