@@ -30,6 +30,27 @@ iso_status set_device(iso_ctx* ctx) {
     return e == cudaSuccess ? ISO_OK : cuda_fail(ctx, e, "cudaSetDevice");
 }
 
+iso_status fork_side(iso_ctx* ctx, cudaStream_t* side) {
+    cudaError_t e = cudaSuccess;
+    if (!ctx->side) {
+        e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->side_fork, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->side_join, cudaEventDisableTiming);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "side stream");
+    }
+    e = cudaEventRecord(ctx->side_fork, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->side, ctx->side_fork, 0);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "fork side stream");
+    *side = ctx->side;
+    return ISO_OK;
+}
+
+iso_status join_side(iso_ctx* ctx) {
+    cudaError_t e = cudaEventRecord(ctx->side_join, ctx->side);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, ctx->side_join, 0);
+    return e == cudaSuccess ? ISO_OK : cuda_fail(ctx, e, "join side stream");
+}
+
 iso_status ensure(iso_ctx* ctx, DevBuf& b, size_t bytes) {
     if (bytes <= b.bytes) return ISO_OK;
     if (ctx->capturing) return fail(ctx, ISO_ERR_INVALID_ARG, "allocation while recording a graph");
@@ -488,6 +509,12 @@ iso_status iso_ctx_destroy(iso_ctx* ctx) {
     for (cudaEvent_t ev : ctx->event_pool) cudaEventDestroy(ev);
     mc_plan_release(ctx);
     lhmc_plan_release(ctx);
+    if (ctx->side) {
+        cudaStreamSynchronize(ctx->side);
+        cudaStreamDestroy(ctx->side);
+    }
+    if (ctx->side_fork) cudaEventDestroy(ctx->side_fork);
+    if (ctx->side_join) cudaEventDestroy(ctx->side_join);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
     return ISO_OK;

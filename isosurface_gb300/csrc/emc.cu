@@ -7,9 +7,11 @@
 //   emc_sample     Directed value of every lattice point (float4 per point)
 //   emc_active     case of every cell; the cells with corners on both sides
 //                  go to a list, which the later passes walk instead of the grid
-//   emc_count      feature decision, vertex and triangle counts per active cell
+//   emc_count      feature decision, vertex and triangle counts per active
+//                  cell; the feature cells go to a second list
 //   scan_u32 x 2   first vertex and first triangle of every cell
-//   emc_vertices   feature points and owned edge vertices; the edge map
+//   emc_vertices   owned edge vertices; the edge map
+//   emc_features   the feature points (MinimiseQEF), a few cells per warp
 //   emc_triangles  marching-cubes triangles and fans, in traversal order
 //   emc_flips      feature-edge rotations
 #include <cuda_runtime.h>
@@ -69,17 +71,36 @@ __global__ void __launch_bounds__(256) emc_active(emc::Args A, uint64_t cells, u
     }
 }
 
-// The per-cell passes over the active cells only (one thread per cell, grid-stride).
-__global__ void __launch_bounds__(128) emc_count(emc::Args A, const uint32_t* list, const uint32_t* count) {
+// The per-cell passes over the active cells only (one thread per cell,
+// grid-stride).  The counting pass also lists the feature cells.
+__global__ void __launch_bounds__(128) emc_count(emc::Args A, const uint32_t* list, const uint32_t* count,
+                                                 uint32_t* features, uint32_t* nfeatures) {
     const uint32_t n = *count;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        emc::count_item(A, list[i]);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t c = list[i];
+        emc::count_item(A, c);
+        if ((A.cell[c] >> 8) & 1) features[atomicAdd(nfeatures, 1u)] = c;
+    }
 }
 
+// every vertex but the feature points
 __global__ void __launch_bounds__(128) emc_vertices(emc::Args A, const uint32_t* list, const uint32_t* count) {
     const uint32_t n = *count;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        emc::vertex_item(A, list[i]);
+        emc::vertex_item(A, list[i], false);
+}
+
+// The feature points: `per` listed feature cells to a one-warp block.  Each
+// is one serial chain of f64 operations (the SVD, in the reference's order),
+// and a warp's f64 instruction holds its sub-partition's f64 unit for many
+// cycles whatever its active lanes, so the chains go to as many warps as the
+// SMs' sub-partitions can take, each warp with a few, rather than scattered
+// over every warp of the vertex pass.
+__global__ void __launch_bounds__(32) emc_features(emc::Args A, const uint32_t* features, const uint32_t* nfeatures,
+                                                   uint32_t per) {
+    const uint32_t lane = threadIdx.x;
+    const uint64_t i = (uint64_t)blockIdx.x * per + lane;
+    if (lane < per && i < *nfeatures) emc::feature_item(A, features[i]);
 }
 
 __global__ void __launch_bounds__(256) emc_triangles(emc::Args A, const uint32_t* list, const uint32_t* count) {
@@ -158,10 +179,13 @@ static iso_status emc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint32
     const uint64_t off_words = 2 * cells, sum_words = 2ull * nsums;
     if ((s = ensure(ctx, ctx->scan, 4 * (off_words + sum_words) + 64)) != ISO_OK) return s;
     if ((s = ensure(ctx, ctx->edges, 12 * points)) != ISO_OK) return s;
-    // the active cells and their count
-    if ((s = ensure(ctx, ctx->aux2, 4 * cells + 256)) != ISO_OK) return s;
+    // the active cells, their count, the feature cells' count, the feature cells
+    const uint64_t list_words = (cells + 63) & ~(uint64_t)63;
+    if ((s = ensure(ctx, ctx->aux2, 4 * (2 * list_words + 64))) != ISO_OK) return s;
     uint32_t* active = (uint32_t*)ctx->aux2.p;
-    uint32_t* nactive = active + ((cells + 63) & ~(uint64_t)63);
+    uint32_t* nactive = active + list_words;
+    uint32_t* nfeatures = nactive + 1;
+    uint32_t* features = nactive + 64;
     uint32_t* scan_base = (uint32_t*)ctx->scan.p;
     uint32_t* sums = scan_base + off_words;
     uint32_t* totals = sums + sum_words;  // vertices, triangles, then the flip counter (8-byte aligned)
@@ -182,18 +206,19 @@ static iso_status emc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint32
     }
     {
         StageTimer timer(ctx, ISO_STAGE_CLASSIFY);
-        cudaError_t me = cudaMemsetAsync(nactive, 0, 4, ctx->stream);
+        cudaError_t me = cudaMemsetAsync(nactive, 0, 8, ctx->stream);  // and nfeatures
         if (me != cudaSuccess) return cuda_fail(ctx, me, "emc active count");
         emc_active<<<grid_for(ctx, cells, 256, 16), 256, 0, ctx->stream>>>(A, cells, active, nactive);
-        emc_count<<<grid_for(ctx, cells, 128, 32), 128, 0, ctx->stream>>>(A, active, nactive);
+        emc_count<<<grid_for(ctx, cells, 128, 32), 128, 0, ctx->stream>>>(A, active, nactive, features, nfeatures);
         ctx->launches += 3;
         if ((s = check_launch(ctx, "emc count")) != ISO_OK) return s;
         if ((s = scan_u32(ctx, A.voff, A.voff, (uint32_t)cells, sums, totals)) != ISO_OK) return s;
         if ((s = scan_u32(ctx, A.toff, A.toff, (uint32_t)cells, sums + nsums, totals + 1)) != ISO_OK) return s;
     }
     cudaError_t e = cudaMemsetAsync(flips, 0, 8, ctx->stream);
-    uint32_t tot[2] = {0, 0};
+    uint32_t tot[2] = {0, 0}, nfeat = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(tot, totals, 8, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&nfeat, nfeatures, 4, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "emc counts");
     const uint64_t nv = tot[0], nt = tot[1];
@@ -205,9 +230,21 @@ static iso_status emc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint32
     A.cap_t = nt;
     {
         StageTimer timer(ctx, ISO_STAGE_EMIT);
+        if (nfeat) {
+            // the feature points on a side stream, beside the other passes
+            // (none reads them): a few feature cells per warp, one warp for
+            // each of the SMs' four sub-partitions while there are enough
+            cudaStream_t side;
+            if ((s = fork_side(ctx, &side)) != ISO_OK) return s;
+            const uint64_t slots = 4ull * (uint64_t)std::max(ctx->sms, 1);
+            const uint32_t per = (uint32_t)std::min<uint64_t>(32, (nfeat + slots - 1) / slots);
+            emc_features<<<(unsigned)((nfeat + per - 1) / per), 32, 0, side>>>(A, features, nfeatures, per);
+            ctx->launches++;
+        }
         emc_vertices<<<grid_for(ctx, cells, 128, 32), 128, 0, ctx->stream>>>(A, active, nactive);
         emc_triangles<<<grid_for(ctx, cells, 256, 16), 256, 0, ctx->stream>>>(A, active, nactive);
         emc_flips<<<grid_for(ctx, cells, 256, 16), 256, 0, ctx->stream>>>(A, active, nactive, flips);
+        if (nfeat && (s = join_side(ctx)) != ISO_OK) return s;
     }
     ctx->launches += 3;
     if ((s = check_launch(ctx, "emc emit")) != ISO_OK) return s;

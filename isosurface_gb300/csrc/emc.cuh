@@ -417,8 +417,25 @@ __host__ __device__ inline void count_item(const Args& A, uint64_t c) {
     A.toff[c] = nt;
 }
 
-// the vertices cell `c` adds (offsets already scanned)
-__host__ __device__ inline void vertex_item(const Args& A, uint64_t c) {
+// the feature point of a feature cell (case `cube`, edge crossings `vtx`)
+// as vertex `id`: MinimiseQEF over the cell's tangent planes
+__host__ __device__ inline void put_feature(const Args& A, int cube, const V3* vtx, uint32_t id) {
+    PlanesN t;
+    cell_planes(A.prog, cube, vtx, &t);
+    bool ok;
+    const qef::F3 p = minimise_qef_n(t, &ok);
+    if (!ok) set_err(A.err, DERR_SVD_ITER);
+    if (id < A.cap_v) {
+        A.vertices[3 * (uint64_t)id] = p.x;
+        A.vertices[3 * (uint64_t)id + 1] = p.y;
+        A.vertices[3 * (uint64_t)id + 2] = p.z;
+    }
+}
+
+// the vertices cell `c` adds (offsets already scanned); with
+// feature_point = false a feature cell's first vertex (its feature point) is
+// left to feature_item
+__host__ __device__ inline void vertex_item(const Args& A, uint64_t c, bool feature_point = true) {
     const uint32_t info = A.cell[c];
     const int cube = (int)(info & 0xFF);
     if (cube == 0 || cube == 255) return;
@@ -430,16 +447,7 @@ __host__ __device__ inline void vertex_item(const Args& A, uint64_t c) {
     edge_crossings(cube, corners, values, vtx);
     uint32_t id = A.voff[c];
     if (feature) {
-        PlanesN t;
-        cell_planes(A.prog, cube, vtx, &t);
-        bool ok;
-        const qef::F3 p = minimise_qef_n(t, &ok);
-        if (!ok) set_err(A.err, DERR_SVD_ITER);
-        if (id < A.cap_v) {
-            A.vertices[3 * (uint64_t)id] = p.x;
-            A.vertices[3 * (uint64_t)id + 1] = p.y;
-            A.vertices[3 * (uint64_t)id + 2] = p.z;
-        }
+        if (feature_point) put_feature(A, cube, vtx, id);
         ++id;
     }
     const uint64_t order = feature ? iso_emc_fan_order[cube] : iso_edge_order[cube];
@@ -455,6 +463,17 @@ __host__ __device__ inline void vertex_item(const Args& A, uint64_t c) {
         A.edge_map[edge_key(A.g.n, x, y, z, e)] = id;
         ++id;
     }
+}
+
+// the feature point of feature cell `c` (its first vertex)
+__host__ __device__ inline void feature_item(const Args& A, uint64_t c) {
+    const int cube = (int)(A.cell[c] & 0xFF);
+    uint32_t x, y, z;
+    cell_xyz(A.g.n, c, &x, &y, &z);
+    V3 corners[8], values[8], vtx[12];
+    load_cell(A.field, A.g, x, y, z, corners, values);
+    edge_crossings(cube, corners, values, vtx);
+    put_feature(A, cube, vtx, A.voff[c]);
 }
 
 // the triangles of cell `c`, after every vertex_item

@@ -96,6 +96,10 @@ struct iso_ctx {
     // steady-state MarchingCubes: the whole extraction recorded as one CUDA
     // graph, replayed while the program, size, flags and buffers stay the same
     bool capturing = false;  // no allocation while a stream capture records
+    // a second stream for work that overlaps the context's stream (created on
+    // first use) and the events that fork it from and join it to that stream
+    cudaStream_t side = nullptr;
+    cudaEvent_t side_fork = nullptr, side_join = nullptr;
     // page-locked host buffers (device-side pointers) that the MarchingCubes
     // kernels fill alongside the device mesh (iso_mc_extract_host); `armed`
     // reports whether the last lattice pass could deliver there
@@ -192,6 +196,11 @@ iso_status ensure(iso_ctx* ctx, DevBuf& b, size_t bytes);
 iso_status check_launch(iso_ctx* ctx, const char* what);
 iso_status read_device_errors(iso_ctx* ctx);
 iso_status set_device(iso_ctx* ctx);
+// Work queued on *side after fork_side starts after the work queued on the
+// context's stream so far; join_side makes the context's stream wait for
+// the side stream's work so far.
+iso_status fork_side(iso_ctx* ctx, cudaStream_t* side);
+iso_status join_side(iso_ctx* ctx);
 
 // ctx.cu: the host side of a program from its bytes (no device work)
 iso_status parse_program(const uint8_t* bytes, size_t len, iso_program* p, std::string* err);
