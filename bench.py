@@ -593,6 +593,7 @@ def run_sharded(args, torch, dist, world, rank, ctx, stream, src):
                                                   SIZE, rank, world, dist)
         e2e_times.append(time.perf_counter() - t0)
     e2e_s = replicas.max_over_ranks(sum(e2e_times) / len(e2e_times), dist, "cuda")
+    batch_line = None if args.no_secondary else sharded_batch_workload(ctx, torch, dist, world, rank, stream)
     if rank == 0:
         out = {"metric": METRIC, "value": CELLS / (ms / 1e3), "unit": "cells/s", "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "strong",
@@ -602,9 +603,41 @@ def run_sharded(args, torch, dist, world, rank, ctx, stream, src):
                        "d2h_bytes_per_step": 12 * len(v) + 4 * len(i), "ms_per_step": 1e3 * e2e_s,
                        "note": "rank 0's slab bytes"},
                "gpu_launches": int(launches), "clocks": clk, "roofline": None, "cpu_baseline": None}
+        if batch_line:
+            out["secondary"] = {"batch_4096_chunks_sharded": batch_line}
         print(json.dumps(out))
     ctx.close()
     dist.destroy_process_group()
+
+
+def sharded_batch_workload(ctx, torch, dist, world, rank, stream):
+    """N > 1: the 4096-chunk batch sharded over the ranks
+    (isosurface_gb300/batch_shards.py: size-balanced round robin, each rank's
+    chunks as one CUDA graph, one all-gather of four counts per rank at the
+    end).  Strong scaling: the whole batch per step across the N GPUs, timed
+    with CUDA events (max over ranks)."""
+    from isosurface_gb300 import batch_shards, replicas, scenes
+    chunks = scenes.chunks(seed=7, count=4096)
+    mine, batch, info = batch_shards.run_shard(ctx, chunks, rank, world)
+    for _ in range(2):
+        batch.run(graph=True)
+    reps = 10
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    torch.cuda.synchronize()
+    dist.barrier()
+    for a, b in ev:
+        a.record(stream)
+        info = batch.run(graph=True)
+        b.record(stream)
+    torch.cuda.synchronize()
+    ms = replicas.max_over_ranks(sum(a.elapsed_time(b) for a, b in ev) / reps, dist, "cuda")
+    counts = batch_shards.gather_counts(len(mine), info.num_cells, info.num_vertices, info.num_triangles, dist,
+                                        "cuda")
+    batch.close()
+    cells = sum(c[1] for c in counts)
+    return {"ms": ms, "cells": cells, "cells_per_s": cells / (ms / 1e3), "scaling": "strong",
+            "chunks_per_rank": [c[0] for c in counts], "cells_per_rank": [c[1] for c in counts],
+            "vertices": sum(c[2] for c in counts), "triangles": sum(c[3] for c in counts)}
 
 
 def main():
