@@ -345,6 +345,19 @@ ISO_API iso_status iso_mc_cases(iso_ctx* ctx, const iso_program* prog, uint32_t 
  * lattice edge ids over the (size-1) x (size-1) x size dual vertices. */
 ISO_API iso_status iso_dc_extract(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t placer,
                                   uint32_t flags, iso_mesh_info* info);
+/* One slab of a z-partition of DualContouring::new(size, placer) across GPUs
+ * (no reference counterpart): the dual cube layers [z_begin, z_end),
+ * 0 <= z_begin < z_end <= size - 1, plus the halo cube layer below when
+ * z_begin > 0, sampled, placed and meshed on this GPU from the primal sample
+ * layers it needs (z_begin - halo .. z_end + 1), with positions and keys
+ * (ISO_FLAG_KEYS) in the whole dual lattice's frame; *halo_vertices and
+ * *halo_triangles count the halo layer's part, first in the mesh.  The
+ * slabs assemble exactly as iso_mc_extract_slab's do, with the dual lattice's
+ * size - 1 in place of the grid size (isosurface_gb300/slabs.py), into
+ * iso_dc_extract's buffers byte for byte.  Synchronous. */
+ISO_API iso_status iso_dc_extract_slab(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t placer,
+                                       uint32_t z_begin, uint32_t z_end, uint32_t flags, iso_mesh_info* info,
+                                       uint64_t* halo_vertices, uint64_t* halo_triangles);
 
 /* ------------------------------------------------------------------------ */
 /* LinearHashedMarchingCubes (src/linear_hashed_marching_cubes.rs:40-84)      */

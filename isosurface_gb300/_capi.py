@@ -100,6 +100,8 @@ SIGNATURES = {
     "iso_point_cloud_extract": (i32, [vp, vp, u32, u32, ctypes.POINTER(MeshInfo)]),
     "iso_emc_extract": (i32, [vp, vp, u32, u32, ctypes.POINTER(MeshInfo), ctypes.POINTER(ctypes.c_uint64)]),
     "iso_dc_extract": (i32, [vp, vp, u32, u32, u32, ctypes.POINTER(MeshInfo)]),
+    "iso_dc_extract_slab": (i32, [vp, vp, u32, u32, u32, u32, u32, ctypes.POINTER(MeshInfo), ctypes.POINTER(u64),
+                                  ctypes.POINTER(u64)]),
     "iso_lhmc_extract": (i32, [vp, vp, u32, u32, ctypes.POINTER(MeshInfo)]),
     "iso_lhmc_stale_corners": (u64, [vp]),
     "iso_batch_create": (i32, [vp, ctypes.POINTER(vp), u32, ctypes.POINTER(ChunkDesc), u32, ctypes.POINTER(vp)]),

@@ -171,6 +171,18 @@ class Context:
                                         ctypes.byref(info), ctypes.byref(hv), ctypes.byref(ht)), self.h)
         return info, int(hv.value), int(ht.value)
 
+    def dc_extract_slab(self, source, size, z_begin, z_end, placer=0, keys=False):
+        """One slab of a z-partition of DualContouring::new(size, placer):
+        dual cube layers [z_begin, z_end) of size - 1, plus the halo layer
+        below when z_begin > 0.  Returns (MeshInfo, halo vertices, halo
+        triangles); slabs.py assembles the slabs with size - 1 as the size."""
+        info = MeshInfo()
+        hv, ht = ctypes.c_uint64(), ctypes.c_uint64()
+        flags = self._flags(keys, False)
+        check(lib().iso_dc_extract_slab(self.h, self.program(source).h, size, placer, z_begin, z_end, flags,
+                                        ctypes.byref(info), ctypes.byref(hv), ctypes.byref(ht)), self.h)
+        return info, int(hv.value), int(ht.value)
+
     def mc_cases(self, source, size):
         out = np.empty((size, size - 1, size - 1), np.uint8)
         check(lib().iso_mc_cases(self.h, self.program(source).h, size,

@@ -32,6 +32,8 @@ struct DualArgs {
     uint32_t W;
     uint64_t pitch;       // primal row pitch
     uint32_t n;           // primal size: n x n x (n+1) samples
+    uint32_t nzd;         // dual layers here (primal cell layers zoff .. zoff + nzd - 1)
+    uint32_t zoff;        // primal cell layer of dual layer 0 (a slab of the whole lattice)
     float inv;
     float* dval;          // dual values, rows of dpitch
     uint64_t dpitch;
@@ -44,7 +46,7 @@ struct DualArgs {
 
 __global__ void __launch_bounds__(256) dc_dual(DualArgs A) {
     const uint32_t m = A.n - 1;
-    const uint64_t total = (uint64_t)m * m * A.n;
+    const uint64_t total = (uint64_t)m * m * A.nzd;
     const uint64_t id = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool active = false;
     if (id < total) {
@@ -62,8 +64,8 @@ __global__ void __launch_bounds__(256) dc_dual(DualArgs A) {
         const float* f0 = A.field + ((size_t)z * A.n + y) * A.pitch + x;
         const float v0 = __ldg(f0), v6 = __ldg(f0 + (size_t)A.n * A.pitch + A.pitch + 1);
         // Vec3::lerp / Signed::lerp with f = 0.5: (1 - f) * a + f * b
-        const float c0x = (float)x * A.inv, c0y = (float)y * A.inv, c0z = (float)z * A.inv;
-        const float c6x = (float)(x + 1) * A.inv, c6y = (float)(y + 1) * A.inv, c6z = (float)(z + 1) * A.inv;
+        const float c0x = (float)x * A.inv, c0y = (float)y * A.inv, c0z = (float)(z + A.zoff) * A.inv;
+        const float c6x = (float)(x + 1) * A.inv, c6y = (float)(y + 1) * A.inv, c6z = (float)(z + 1 + A.zoff) * A.inv;
         const float of = 1.0f - 0.5f;
         A.dpos[id] = make_float4(of * c0x + 0.5f * c6x, of * c0y + 0.5f * c6y, of * c0z + 0.5f * c6z, 0.0f);
         // a corner the sampler skipped lies more than 2.5 lattice steps' worth
@@ -93,6 +95,7 @@ __global__ void __launch_bounds__(256) dc_dual(DualArgs A) {
 struct PlaceArgs {
     ProgView pv;
     uint32_t n;
+    uint32_t zoff;  // as DualArgs::zoff
     float inv;
     const uint32_t* list;
     const uint32_t* count;
@@ -110,7 +113,7 @@ __device__ void place_one(const PlaceArgs& A, uint32_t i) {
     qef::F3 corners[8], normals[8];
     for (int k = 0; k < 8; ++k) {
         const float px = (float)(x + cornr[k][0]) * A.inv, py = (float)(y + cornr[k][1]) * A.inv,
-                    pz = (float)(z + cornr[k][2]) * A.inv;
+                    pz = (float)(z + A.zoff + cornr[k][2]) * A.inv;
         corners[k] = qef::f3(px, py, pz);
         V3 nn;
         eval_hermite(A.pv, v3(px, py, pz), &nn);
@@ -141,39 +144,44 @@ __global__ void __launch_bounds__(128) dc_place(PlaceArgs A) {
 
 using namespace iso;
 
-static iso_status dc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t placer,
-                                     uint32_t flags, iso_mesh_info* info) {
+static iso_status dc_check(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t placer, uint32_t flags) {
     if (!ctx || !prog) return ISO_ERR_INVALID_ARG;
     if (prog->ctx != ctx) return fail(ctx, ISO_ERR_INVALID_ARG, "program belongs to another context");
     if (size == 0 || size > 16384) return fail(ctx, ISO_ERR_INVALID_ARG, "size out of range");
     if (placer > 1) return fail(ctx, ISO_ERR_INVALID_ARG, "placer must be 0 (MinimiseQEF) or 1 (particles)");
     if (flags & ~(uint32_t)ISO_FLAG_KEYS) return fail(ctx, ISO_ERR_INVALID_ARG, "unsupported flags");
+    if ((uint64_t)(size - 1) * (size - 1) * size >= 0xFFFFFFFFull) return fail(ctx, ISO_ERR_TOO_LARGE, "grid too large");
     iso_status s = set_device(ctx);
     if (s != ISO_OK) return s;
     ctx->last = iso_mesh_info{};
     ctx->last_flags = flags;
     ctx->last_vertex_floats = 3;
-    if (size < 3) {  // the dual lattice has no cube
-        if (info) *info = ctx->last;
-        return ISO_OK;
-    }
-    const uint32_t n = size, m = size - 1;
+    return ISO_OK;
+}
+
+// The dual lattice's layers [zlo, zlo + nzd) of DualContouring::new(n) (dual
+// layer k: one vertex per primal cell of cell layer k), from the primal
+// sample layers [zlo, zlo + nzd]: values, signs and placed positions in the
+// whole lattice's frame.  The whole extraction is zlo = 0, nzd = n.
+static iso_status dc_lattice(iso_ctx* ctx, const iso_program* prog, uint32_t n, uint32_t placer, uint32_t zlo,
+                             uint32_t nzd, Lattice* L) {
+    const uint32_t m = n - 1, nzp = nzd + 1;  // primal sample layers
     const uint64_t pitch = default_pitch(n), W = words_per_row(n);
-    const uint64_t ndual = (uint64_t)m * m * n;
-    if (ndual >= 0xFFFFFFFFull) return fail(ctx, ISO_ERR_TOO_LARGE, "grid too large");
+    const uint64_t ndual = (uint64_t)m * m * nzd;
     const uint64_t dpitch = default_pitch(m), dW = words_per_row(m);
+    iso_status s;
     // primal field + bits | dual values | dual positions | dual bits | active list
-    if ((s = ensure(ctx, ctx->field, 4ull * pitch * n * (n + 1))) != ISO_OK) return s;
-    if ((s = ensure(ctx, ctx->bits, 4ull * W * n * (n + 1))) != ISO_OK) return s;
-    if ((s = ensure(ctx, ctx->aux, 4ull * dpitch * m * n)) != ISO_OK) return s;
+    if ((s = ensure(ctx, ctx->field, 4ull * pitch * n * nzp)) != ISO_OK) return s;
+    if ((s = ensure(ctx, ctx->bits, 4ull * W * n * nzp)) != ISO_OK) return s;
+    if ((s = ensure(ctx, ctx->aux, 4ull * dpitch * m * nzd)) != ISO_OK) return s;
     if ((s = ensure(ctx, ctx->aux2, 16ull * ndual)) != ISO_OK) return s;
-    if ((s = ensure(ctx, ctx->aux3, 4ull * dW * m * n + 4ull * ndual + 256)) != ISO_OK) return s;
+    if ((s = ensure(ctx, ctx->aux3, 4ull * dW * m * nzd + 4ull * ndual + 256)) != ISO_OK) return s;
     float* field = (float*)ctx->field.p;
     uint32_t* bits = (uint32_t*)ctx->bits.p;
     float* dval = (float*)ctx->aux.p;
     float4* dpos = (float4*)ctx->aux2.p;
     uint32_t* dbits = (uint32_t*)ctx->aux3.p;
-    uint32_t* count = dbits + dW * m * n;
+    uint32_t* count = dbits + dW * m * nzd;
     uint32_t* list = count + 64;
     const float inv = 1.0f / (float)(n - 1);
     // values only near the surface (programs with a Lipschitz bound): the
@@ -183,24 +191,60 @@ static iso_status dc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint32_
     // sampler keeps 2.5, and the others stay NaN for dc_dual to recognise
     const bool near = prog->lip > 0.0f;
     cudaError_t e = cudaSuccess;
-    if (near) e = cudaMemsetAsync(field, 0xFF, 4ull * pitch * n * (n + 1), ctx->stream);
+    if (near) e = cudaMemsetAsync(field, 0xFF, 4ull * pitch * n * nzp, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "clear field");
-    if ((s = launch_sample_grid(ctx, prog, n, n, n + 1, inv, field, pitch, bits, near, 0, 2.5f)) != ISO_OK) return s;
+    if ((s = launch_sample_grid(ctx, prog, n, n, nzp, inv, field, pitch, bits, near, zlo, 2.5f)) != ISO_OK) return s;
     e = cudaMemsetAsync(count, 0, 4, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "memset");
     {
         StageTimer timer(ctx, ISO_STAGE_PLACE);
-        DualArgs da{field, bits, (uint32_t)W, pitch, n, inv, dval, dpitch, dpos, list, count, (uint32_t)ndual, ctx->d_err};
+        DualArgs da{field, bits, (uint32_t)W, pitch, n, nzd, zlo, inv, dval, dpitch, dpos, list, count,
+                    (uint32_t)ndual, ctx->d_err};
         dc_dual<<<(unsigned)((ndual + 255) / 256), 256, 0, ctx->stream>>>(da);
-        PlaceArgs pa{prog->view(), n, inv, list, count, dpos, (int)placer, ctx->d_err};
+        PlaceArgs pa{prog->view(), n, zlo, inv, list, count, dpos, (int)placer, ctx->d_err};
         const uint64_t place_blocks = std::min<uint64_t>((ndual + 127) / 128, 152 * 64);
         dc_place<<<(unsigned)place_blocks, 128, 0, ctx->stream>>>(pa);
     }
     ctx->launches += 2;
     if ((s = check_launch(ctx, "dc passes")) != ISO_OK) return s;
-    if ((s = launch_sign_bits(ctx, dval, m, m, n, dpitch, dbits)) != ISO_OK) return s;
-    Lattice L{m, m, n, dpitch, dval, dbits, (uint32_t)dW, 0.0f, dpos};
+    if ((s = launch_sign_bits(ctx, dval, m, m, nzd, dpitch, dbits)) != ISO_OK) return s;
+    *L = Lattice{m, m, nzd, dpitch, dval, dbits, (uint32_t)dW, 0.0f, dpos, zlo};
+    return ISO_OK;
+}
+
+static iso_status dc_extract_impl(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t placer,
+                                     uint32_t flags, iso_mesh_info* info) {
+    iso_status s = dc_check(ctx, prog, size, placer, flags);
+    if (s != ISO_OK) return s;
+    if (size < 3) {  // the dual lattice has no cube
+        if (info) *info = ctx->last;
+        return ISO_OK;
+    }
+    Lattice L;
+    if ((s = dc_lattice(ctx, prog, size, placer, 0, size, &L)) != ISO_OK) return s;
     return mc_extract_lattice(ctx, L, flags, info);
+}
+
+// One slab of a z-partition of DualContouring::new(size): dual cube layers
+// [z_begin, z_end) of the size - 1, plus the halo cube layer below when
+// z_begin > 0, exactly as mc_extract_slab does for MarchingCubes.
+extern "C" iso_status iso_dc_extract_slab(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t placer,
+                                          uint32_t z_begin, uint32_t z_end, uint32_t flags, iso_mesh_info* info,
+                                          uint64_t* halo_vertices, uint64_t* halo_triangles) {
+    iso::NvtxRange nvtx_range("iso_dc_extract_slab");
+    iso_status s = dc_check(ctx, prog, size, placer, flags);
+    if (s != ISO_OK) return s;
+    if (size < 3 || z_begin >= z_end || z_end > size - 1)
+        return fail(ctx, ISO_ERR_INVALID_ARG, "need size >= 3 and 0 <= z_begin < z_end <= size - 1");
+    const uint32_t halo = z_begin > 0 ? 1u : 0u, zlo = z_begin - halo;
+    Lattice L;
+    if ((s = dc_lattice(ctx, prog, size, placer, zlo, z_end - zlo + 1, &L)) != ISO_OK) return s;
+    uint64_t hv = 0, ht = 0;
+    if (halo && (s = mc_first_layer_counts(ctx, L, &hv, &ht)) != ISO_OK) return s;
+    if ((s = mc_extract_lattice(ctx, L, flags, info)) != ISO_OK) return s;
+    if (halo_vertices) *halo_vertices = hv;
+    if (halo_triangles) *halo_triangles = ht;
+    return ISO_OK;
 }
 
 // ISO_FLAG_NORMALS: the *InterleavedNormals sinks, sample_normal at every vertex

@@ -237,6 +237,8 @@ struct Lattice {
 iso_status mc_extract_lattice(iso_ctx* ctx, const Lattice& L, uint32_t flags, iso_mesh_info* info);
 iso_status mc_extract_slab(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t z_begin, uint32_t z_end,
                            uint32_t flags, iso_mesh_info* info, uint64_t* halo_vertices, uint64_t* halo_triangles);
+// triangles and owned vertices of the lattice's first cell layer (synchronous)
+iso_status mc_first_layer_counts(iso_ctx* ctx, const Lattice& L, uint64_t* halo_vertices, uint64_t* halo_triangles);
 // iso_mc_extract without the normals sink: sampler + MarchingCubes, replaying
 // the context's recorded graph when it applies
 iso_status mc_extract_program(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t flags,

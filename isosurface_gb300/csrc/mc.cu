@@ -787,6 +787,31 @@ __global__ void __launch_bounds__(WARPS * 32) mc_layer_counts(const uint32_t* bi
 }
 }  // namespace
 
+// The triangles and owned vertices of a lattice's first cell layer (a slab's
+// halo layer), read back to the host.  The two counters live in the scan
+// buffer, which no lattice references and the passes after this reuse.
+iso_status mc_first_layer_counts(iso_ctx* ctx, const Lattice& L, uint64_t* hv, uint64_t* ht) {
+    iso_status s = ensure(ctx, ctx->scan, 64);
+    if (s != ISO_OK) return s;
+    unsigned long long* t = (unsigned long long*)ctx->scan.p;
+    cudaError_t e = cudaMemsetAsync(t, 0, 16, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "halo counts");
+    {
+        StageTimer timer(ctx, ISO_STAGE_CLASSIFY);
+        mc_layer_counts<<<(L.ny - 1 + WARPS - 1) / WARPS, WARPS * 32, 0, ctx->stream>>>(L.bits, L.words_per_row,
+                                                                                      L.nx, L.ny, t);
+    }
+    ctx->launches++;
+    uint64_t h[2] = {0, 0};
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, t, 16, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "halo counts");
+    *ht = h[0];
+    *hv = h[1];
+    return ISO_OK;
+}
+
 // MarchingCubes::new(size) restricted to the cell layers [z_begin, z_end),
 // for one slab of a z-partition across GPUs: see iso_mc_extract_slab.
 iso_status mc_extract_slab(iso_ctx* ctx, const iso_program* prog, uint32_t size, uint32_t z_begin, uint32_t z_end,
@@ -796,25 +821,7 @@ iso_status mc_extract_slab(iso_ctx* ctx, const iso_program* prog, uint32_t size,
     iso_status s = sample_lattice_slab(ctx, prog, size, zlo, z_end - zlo + 1, &L);
     if (s != ISO_OK) return s;
     uint64_t hv = 0, ht = 0;
-    if (halo) {
-        if ((s = ensure(ctx, ctx->aux, 64)) != ISO_OK) return s;
-        unsigned long long* t = (unsigned long long*)ctx->aux.p;
-        cudaError_t e = cudaMemsetAsync(t, 0, 16, ctx->stream);
-        if (e != cudaSuccess) return cuda_fail(ctx, e, "halo counts");
-        {
-            StageTimer timer(ctx, ISO_STAGE_CLASSIFY);
-            mc_layer_counts<<<(L.ny - 1 + WARPS - 1) / WARPS, WARPS * 32, 0, ctx->stream>>>(L.bits, L.words_per_row,
-                                                                                          L.nx, L.ny, t);
-        }
-        ctx->launches++;
-        uint64_t h[2] = {0, 0};
-        e = cudaGetLastError();
-        if (e == cudaSuccess) e = cudaMemcpyAsync(h, t, 16, cudaMemcpyDeviceToHost, ctx->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-        if (e != cudaSuccess) return cuda_fail(ctx, e, "halo counts");
-        ht = h[0];
-        hv = h[1];
-    }
+    if (halo && (s = mc_first_layer_counts(ctx, L, &hv, &ht)) != ISO_OK) return s;
     if ((s = mc_lattice_passes(ctx, L, flags, info, false)) != ISO_OK) return s;
     if (halo_vertices) *halo_vertices = hv;
     if (halo_triangles) *halo_triangles = ht;

@@ -19,6 +19,11 @@ the slabs below it own.  One GPU (rank) per slab of cell layers:
   in the same order, less those on the halo layer's bottom plane.
 
 The concatenated buffers are byte-identical to iso_mc_extract's.
+
+DualContouring shards the same way: its mesh is marching cubes over the
+dual lattice ((size-1) x (size-1) x size dual vertices, one per primal cell,
+in the same z-major order), so iso_dc_extract_slab's slabs of dual cube
+layers assemble with these functions given size - 1 as the size.
 """
 import numpy as np
 
@@ -100,6 +105,14 @@ def extract_slab_device(ctx, source, size, z_begin, z_end):
     """The slab on this rank's GPU: (vertices, indices, keys, halo vertices,
     halo triangles)."""
     info, hv, ht = ctx.mc_extract_slab(source, size, z_begin, z_end, keys=True)
+    m = ctx.download(info, keys=True)
+    return m.vertices, m.indices, m.keys, hv, ht
+
+
+def extract_dc_slab_device(ctx, source, size, z_begin, z_end, placer=0):
+    """A DualContouring slab on this rank's GPU, in the form extract_sharded
+    takes with the dual lattice's size - 1 as its size."""
+    info, hv, ht = ctx.dc_extract_slab(source, size, z_begin, z_end, placer, keys=True)
     m = ctx.download(info, keys=True)
     return m.vertices, m.indices, m.keys, hv, ht
 

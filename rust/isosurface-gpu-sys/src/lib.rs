@@ -219,6 +219,18 @@ extern "C" {
         flags: u32,
         info: *mut IsoMeshInfo,
     ) -> IsoStatus;
+    pub fn iso_dc_extract_slab(
+        ctx: *mut IsoCtx,
+        prog: *const IsoProgram,
+        size: u32,
+        placer: u32,
+        z_begin: u32,
+        z_end: u32,
+        flags: u32,
+        info: *mut IsoMeshInfo,
+        halo_vertices: *mut u64,
+        halo_triangles: *mut u64,
+    ) -> IsoStatus;
     pub fn iso_lhmc_extract(
         ctx: *mut IsoCtx,
         prog: *const IsoProgram,

@@ -6,7 +6,9 @@ device, and the partition logic under test -- slab bounds, the halo-layer
 drop, the renumbering, the one exchange of counts -- runs as written: in one
 process for several world sizes, and as two gloo ranks.  The concatenated
 per-rank buffers must equal the oracle's MarchingCubes of the whole grid byte
-for byte.  The GPU tests run the same logic on iso_mc_extract_slab."""
+for byte.  The GPU tests run the same logic on iso_mc_extract_slab, and on
+iso_dc_extract_slab (DualContouring's dual lattice, size - 1 as the size)
+against iso_dc_extract and the oracle."""
 import json
 import os
 import socket
@@ -157,3 +159,44 @@ def test_device_slabs_bench_grid(ctx):
     got_v, got_i = _concat(out)
     assert np.array_equal(got_v, whole.vertices)
     assert np.array_equal(got_i, whole.indices)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,size,worlds,placer", [("csg", 65, (2, 3, 7), 0), ("csg", 129, (2, 4), 0),
+                                                     ("sphere", 65, (3,), 1), ("torus", 97, (2, 5), 0),
+                                                     ("central_difference", 33, (2, 32), 1)])
+def test_device_dc_slabs_equal_the_whole_extraction(ctx, name, size, worlds, placer):
+    """iso_dc_extract_slab for every rank in turn (dual cube layers of the
+    (size-1) x (size-1) x size dual lattice), assembled by the same logic
+    with size - 1 as the size: iso_dc_extract's buffers byte for byte, and
+    the oracle's DualContouring."""
+    src = _dc_sources()[name]
+    whole = ctx.download(ctx.dc_extract(src, size, placer))
+    want = oracle.Program(S.lower(src)).dual_contouring(size, placer)
+    assert np.array_equal(whole.vertices, want.vertices) and np.array_equal(whole.indices, want.indices)
+    for world in worlds:
+        counts, raw = [], []
+        for z0, z1 in slabs.slab_bounds(size - 1, world):
+            v, i, k, hv, ht = slabs.extract_dc_slab_device(ctx, src, size, z0, z1, placer)
+            raw.append((v, i, k, hv, ht, z0))
+            counts.append(len(v) - hv)
+        bases = slabs.vertex_bases(counts)
+        out = [slabs.assemble(v, i, k, hv, ht, z0, size - 1, int(b)) for (v, i, k, hv, ht, z0), b in zip(raw, bases)]
+        got_v, got_i = _concat(out)
+        assert np.array_equal(got_v, whole.vertices), world
+        assert np.array_equal(got_i, whole.indices), world
+
+
+def _dc_sources():
+    return {"csg": scenes.csg(), "sphere": scenes.sphere(), "torus": S.unit_to_cube(S.Torus(0.5, 0.2)),
+            "central_difference": S.unit_to_cube(S.CentralDifference(
+                S.Intersection(S.Sphere(0.8), S.RectangularPrism((0.6, 0.6, 0.6)))))}
+
+
+@pytest.mark.gpu
+def test_device_dc_slab_arguments(ctx):
+    from isosurface_gb300._capi import IsoError
+    src = scenes.csg()
+    for z0, z1 in ((0, 0), (3, 2), (0, 65)):  # empty, reversed, past the 64 dual cube layers of new(65)
+        with pytest.raises(IsoError):
+            ctx.dc_extract_slab(src, 65, z0, z1)
