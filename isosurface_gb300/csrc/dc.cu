@@ -15,8 +15,10 @@
 // of every dual vertex, active primal cells appended to a list, (3) dc_place:
 // one thread per active cell -- eight normals from the program
 // (sample_normals_at_corners, marching_cubes_impl.rs:58-69), tangent planes,
-// QEF or particle placement, (4) sign bits of the dual values, (5)+(6) the
-// lattice marching-cubes passes.
+// the planar cells' centre of mass or particle placement, the non-planar
+// cells listed for (3b) dc_feature: their MinimiseQEF (f64 SVD) in full
+// warps, (4) sign bits of the dual values, (5)+(6) the lattice
+// marching-cubes passes.
 #include <cuda_runtime.h>
 
 #include "internal.h"
@@ -102,15 +104,17 @@ struct PlaceArgs {
     float4* dpos;
     int placer;  // 0 MinimiseQEF, 1 ParticleBasedMinimisation
     uint32_t* err;
+    uint32_t* features;   // MinimiseQEF: the non-planar cells, whose QEF dc_feature solves
+    uint32_t* nfeatures;
 };
 
-__device__ void place_one(const PlaceArgs& A, uint32_t i) {
+// the corners of dual vertex `id`'s primal cell and their normalised normals
+// (sample_normals_at_corners, marching_cubes_impl.rs:58-69)
+__device__ void cell_normals(const PlaceArgs& A, uint32_t id, qef::F3* corners, qef::F3* normals) {
     const uint32_t m = A.n - 1;
-    const uint32_t id = A.list[i];
     const uint32_t x = id % m, r = id / m;
     const uint32_t y = r % m, z = r / m;
     const uint8_t cornr[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
-    qef::F3 corners[8], normals[8];
     for (int k = 0; k < 8; ++k) {
         const float px = (float)(x + cornr[k][0]) * A.inv, py = (float)(y + cornr[k][1]) * A.inv,
                     pz = (float)(z + A.zoff + cornr[k][2]) * A.inv;
@@ -119,13 +123,23 @@ __device__ void place_one(const PlaceArgs& A, uint32_t i) {
         eval_hermite(A.pv, v3(px, py, pz), &nn);
         normals[k] = qef::normalised_or_zero(qef::f3(nn.x, nn.y, nn.z));
     }
+}
+
+__device__ void place_one(const PlaceArgs& A, uint32_t i) {
+    const uint32_t id = A.list[i];
+    qef::F3 corners[8], normals[8];
+    cell_normals(A, id, corners, normals);
     qef::F3 p;
     if (A.placer == 0) {
         qef::Planes t;
         qef::tangent_planes(corners, normals, &t);
-        bool ok;
-        p = qef::minimise_qef(t, &ok);
-        if (!ok) atomicOr(A.err, DERR_SVD_ITER);
+        if (t.feature != qef::PLANAR) {
+            // the f64 SVD: listed for dc_feature, which runs the non-planar
+            // cells (a few per warp here) in full warps
+            A.features[atomicAdd(A.nfeatures, 1u)] = id;
+            return;
+        }
+        p = t.com;  // minimise_qef of a planar cell
     } else {
         p = qef::particle_placement(corners, normals);
     }
@@ -137,6 +151,27 @@ __global__ void __launch_bounds__(128) dc_place(PlaceArgs A) {
     const uint32_t count = *A.count;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
         place_one(A, i);
+}
+
+// MinimiseQEF of the non-planar cells dc_place listed, one per thread over
+// one-warp blocks (grid-stride): each is a serial chain of f64 operations
+// (the SVD, in the reference's order), and a warp's f64 instruction holds
+// its sub-partition's f64 unit for many cycles however few of its lanes are
+// active, so packing the chains into full warps cuts the f64 instructions
+// the scattered cells of dc_place would have issued.
+__global__ void __launch_bounds__(32) dc_feature(PlaceArgs A) {
+    const uint32_t n = *A.nfeatures;
+    for (uint32_t i = blockIdx.x * 32 + threadIdx.x; i < n; i += gridDim.x * 32) {
+        const uint32_t id = A.features[i];
+        qef::F3 corners[8], normals[8];
+        cell_normals(A, id, corners, normals);
+        qef::Planes t;
+        qef::tangent_planes(corners, normals, &t);
+        bool ok;
+        const qef::F3 p = qef::minimise_qef(t, &ok);
+        if (!ok) atomicOr(A.err, DERR_SVD_ITER);
+        A.dpos[id] = make_float4(p.x, p.y, p.z, 0.0f);
+    }
 }
 
 }  // namespace
@@ -175,14 +210,16 @@ static iso_status dc_lattice(iso_ctx* ctx, const iso_program* prog, uint32_t n, 
     if ((s = ensure(ctx, ctx->bits, 4ull * W * n * nzp)) != ISO_OK) return s;
     if ((s = ensure(ctx, ctx->aux, 4ull * dpitch * m * nzd)) != ISO_OK) return s;
     if ((s = ensure(ctx, ctx->aux2, 16ull * ndual)) != ISO_OK) return s;
-    if ((s = ensure(ctx, ctx->aux3, 4ull * dW * m * nzd + 4ull * ndual + 256)) != ISO_OK) return s;
+    const uint64_t list_words = (ndual + 63) & ~(uint64_t)63;
+    if ((s = ensure(ctx, ctx->aux3, 4ull * dW * m * nzd + 8ull * list_words + 256)) != ISO_OK) return s;
     float* field = (float*)ctx->field.p;
     uint32_t* bits = (uint32_t*)ctx->bits.p;
     float* dval = (float*)ctx->aux.p;
     float4* dpos = (float4*)ctx->aux2.p;
     uint32_t* dbits = (uint32_t*)ctx->aux3.p;
-    uint32_t* count = dbits + dW * m * nzd;
+    uint32_t* count = dbits + dW * m * nzd;  // active cells, then (count + 1) non-planar ones
     uint32_t* list = count + 64;
+    uint32_t* features = list + list_words;
     const float inv = 1.0f / (float)(n - 1);
     // values only near the surface (programs with a Lipschitz bound): the
     // dual values read the primal ones up to 1 + sqrt(3)/2 lattice steps'
@@ -194,16 +231,21 @@ static iso_status dc_lattice(iso_ctx* ctx, const iso_program* prog, uint32_t n, 
     if (near) e = cudaMemsetAsync(field, 0xFF, 4ull * pitch * n * nzp, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "clear field");
     if ((s = launch_sample_grid(ctx, prog, n, n, nzp, inv, field, pitch, bits, near, zlo, 2.5f)) != ISO_OK) return s;
-    e = cudaMemsetAsync(count, 0, 4, ctx->stream);
+    e = cudaMemsetAsync(count, 0, 8, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "memset");
     {
         StageTimer timer(ctx, ISO_STAGE_PLACE);
         DualArgs da{field, bits, (uint32_t)W, pitch, n, nzd, zlo, inv, dval, dpitch, dpos, list, count,
                     (uint32_t)ndual, ctx->d_err};
         dc_dual<<<(unsigned)((ndual + 255) / 256), 256, 0, ctx->stream>>>(da);
-        PlaceArgs pa{prog->view(), n, zlo, inv, list, count, dpos, (int)placer, ctx->d_err};
+        PlaceArgs pa{prog->view(), n, zlo, inv, list, count, dpos, (int)placer, ctx->d_err, features, count + 1};
         const uint64_t place_blocks = std::min<uint64_t>((ndual + 127) / 128, 152 * 64);
         dc_place<<<(unsigned)place_blocks, 128, 0, ctx->stream>>>(pa);
+        if (placer == 0) {
+            // one warp for each of the SMs' four sub-partitions
+            dc_feature<<<(unsigned)(4 * std::max(ctx->sms, 1)), 32, 0, ctx->stream>>>(pa);
+            ctx->launches++;
+        }
     }
     ctx->launches += 2;
     if ((s = check_launch(ctx, "dc passes")) != ISO_OK) return s;
