@@ -11,14 +11,14 @@
 // the last two passes are mc_extract_lattice.
 //
 // Passes: (1) grid sampler (sign bits everywhere; for a program with a
-// Lipschitz bound, values only near the surface, NaN elsewhere), (2) dc_dual: value and centre
-// of every dual vertex, active primal cells appended to a list, (3) dc_place:
+// Lipschitz bound, values only near the surface, NaN elsewhere), (2) dc_dual:
+// sign bits of every dual vertex, value and centre of those marching cubes
+// can read, active primal cells appended to a list, (3) dc_place:
 // one thread per active cell -- eight normals from the program
 // (sample_normals_at_corners, marching_cubes_impl.rs:58-69), tangent planes,
 // the planar cells' centre of mass or particle placement, the non-planar
 // cells listed for (3b) dc_feature: their MinimiseQEF (f64 SVD) in full
-// warps, (4) sign bits of the dual values, (5)+(6) the lattice
-// marching-cubes passes.
+// warps, (4)+(5) the lattice marching-cubes passes.
 #include <cuda_runtime.h>
 
 #include "internal.h"
@@ -39,56 +39,73 @@ struct DualArgs {
     float inv;
     float* dval;          // dual values, rows of dpitch
     uint64_t dpitch;
-    float4* dpos;         // dual positions, dense (n-1) x (n-1) x n
+    float4* dpos;         // dual positions, dense (n-1) x (n-1) x nzd
+    uint32_t* dbits;      // dual sign bits (bit set iff !(value > 0)), dW words per row
+    uint32_t dW;
     uint32_t* list;       // active primal cells (linear dual index)
     uint32_t* count;
     uint32_t cap;
     uint32_t* err;
+    bool near;            // the sampler wrote values only near the surface (NaN elsewhere)
 };
 
+// One warp per 32 dual vertices of a dual row (x = 32 w + lane): value,
+// centre, sign word (by ballot) and the active primal cells.  A dual vertex
+// whose primal corners 0 or 6 the near-surface sampler skipped gets its sign
+// only: those corners lie more than 2.5 lattice steps' worth of value change
+// from zero, so (by the Lipschitz bound) v0 and v6 share the sign of corner 0
+// and the dual value lies more than 1.6 steps' worth from zero, while both
+// ends of a crossing dual edge lie within one step's worth; marching cubes
+// reads values and positions only at those ends.
 __global__ void __launch_bounds__(256) dc_dual(DualArgs A) {
-    const uint32_t m = A.n - 1;
-    const uint64_t total = (uint64_t)m * m * A.nzd;
-    const uint64_t id = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    bool active = false;
-    if (id < total) {
-        const uint32_t x = (uint32_t)(id % m);
-        const uint64_t r = id / m;
-        const uint32_t y = (uint32_t)(r % m), z = (uint32_t)(r / m);
-        // corners in CORNERS order (marching_cubes_tables.rs:16-25)
-        // corner signs from the sign bits, in CORNERS order
+    const uint32_t m = A.n - 1, lane = threadIdx.x & 31;
+    const uint64_t gw = (uint64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (gw >= (uint64_t)A.dW * m * A.nzd) return;  // warp-uniform
+    const uint32_t w = (uint32_t)(gw % A.dW);
+    const uint64_t row = gw / A.dW;
+    const uint32_t y = (uint32_t)(row % m), z = (uint32_t)(row / m);
+    const uint32_t x = 32 * w + lane;
+    bool active = false, inside = false;
+    if (x < m) {
+        // corner signs from the sign bits, in CORNERS order (marching_cubes_tables.rs:16-25)
         auto sign_bit = [&](uint32_t xx, uint32_t yy, uint32_t zz) {
             return (__ldg(A.bits + ((size_t)zz * A.n + yy) * A.W + (xx >> 5)) >> (xx & 31)) & 1u;
         };
-        uint32_t cs = sign_bit(x, y, z) | sign_bit(x + 1, y, z) << 1 | sign_bit(x + 1, y + 1, z) << 2 |
-                      sign_bit(x, y + 1, z) << 3 | sign_bit(x, y, z + 1) << 4 | sign_bit(x + 1, y, z + 1) << 5 |
-                      sign_bit(x + 1, y + 1, z + 1) << 6 | sign_bit(x, y + 1, z + 1) << 7;
+        const uint32_t cs = sign_bit(x, y, z) | sign_bit(x + 1, y, z) << 1 | sign_bit(x + 1, y + 1, z) << 2 |
+                            sign_bit(x, y + 1, z) << 3 | sign_bit(x, y, z + 1) << 4 |
+                            sign_bit(x + 1, y, z + 1) << 5 | sign_bit(x + 1, y + 1, z + 1) << 6 |
+                            sign_bit(x, y + 1, z + 1) << 7;
         const float* f0 = A.field + ((size_t)z * A.n + y) * A.pitch + x;
         const float v0 = __ldg(f0), v6 = __ldg(f0 + (size_t)A.n * A.pitch + A.pitch + 1);
-        // Vec3::lerp / Signed::lerp with f = 0.5: (1 - f) * a + f * b
-        const float c0x = (float)x * A.inv, c0y = (float)y * A.inv, c0z = (float)(z + A.zoff) * A.inv;
-        const float c6x = (float)(x + 1) * A.inv, c6y = (float)(y + 1) * A.inv, c6z = (float)(z + 1 + A.zoff) * A.inv;
-        const float of = 1.0f - 0.5f;
-        A.dpos[id] = make_float4(of * c0x + 0.5f * c6x, of * c0y + 0.5f * c6y, of * c0z + 0.5f * c6z, 0.0f);
-        // a corner the sampler skipped lies more than 2.5 lattice steps' worth
-        // of value change from zero, so (by the Lipschitz bound) v0 and v6
-        // share its sign and the dual value is more than 1.6 steps' worth
-        // from zero: never the end of a crossing dual edge, whose ends lie
-        // within one step's worth.  Only its sign is ever read.
-        const float dv = (v0 == v0 && v6 == v6) ? of * v0 + 0.5f * v6 : ((cs & 1u) ? -3.0e38f : 3.0e38f);
-        A.dval[((size_t)z * m + y) * A.dpitch + x] = dv;
+        const uint64_t id = ((uint64_t)z * m + y) * m + x;
+        const bool sampled = v0 == v0 && v6 == v6;
+        if (sampled || !A.near) {
+            // Vec3::lerp / Signed::lerp with f = 0.5: (1 - f) * a + f * b (a
+            // full field's own NaN gets a signed sentinel in its place)
+            const float of = 1.0f - 0.5f;
+            const float c0x = (float)x * A.inv, c0y = (float)y * A.inv, c0z = (float)(z + A.zoff) * A.inv;
+            const float c6x = (float)(x + 1) * A.inv, c6y = (float)(y + 1) * A.inv,
+                        c6z = (float)(z + 1 + A.zoff) * A.inv;
+            const float dv = sampled ? of * v0 + 0.5f * v6 : ((cs & 1u) ? -3.0e38f : 3.0e38f);
+            A.dpos[id] = make_float4(of * c0x + 0.5f * c6x, of * c0y + 0.5f * c6y, of * c0z + 0.5f * c6z, 0.0f);
+            A.dval[((size_t)z * m + y) * A.dpitch + x] = dv;
+            inside = !(dv > 0.0f);
+        } else {
+            inside = (cs & 1u) != 0;
+        }
         active = cs != 0 && cs != 255;
     }
+    const uint32_t word = __ballot_sync(0xFFFFFFFFu, inside);
+    if (lane == 0) A.dbits[row * A.dW + w] = word;
     // warp-aggregated append of the active cells (their order does not matter)
     const uint32_t mask = __ballot_sync(0xFFFFFFFFu, active);
     if (mask) {
-        const int lane = threadIdx.x & 31;
         uint32_t base = 0;
-        if (lane == __ffs(mask) - 1) base = atomicAdd(A.count, (uint32_t)__popc(mask));
+        if (lane == (uint32_t)__ffs(mask) - 1) base = atomicAdd(A.count, (uint32_t)__popc(mask));
         base = __shfl_sync(0xFFFFFFFFu, base, __ffs(mask) - 1);
         if (active) {
             const uint32_t at = base + __popc(mask & ((1u << lane) - 1u));
-            if (at < A.cap) A.list[at] = (uint32_t)id;
+            if (at < A.cap) A.list[at] = (uint32_t)(((uint64_t)z * m + y) * m + x);
             else atomicOr(A.err, DERR_CAPACITY);
         }
     }
@@ -235,9 +252,10 @@ static iso_status dc_lattice(iso_ctx* ctx, const iso_program* prog, uint32_t n, 
     if (e != cudaSuccess) return cuda_fail(ctx, e, "memset");
     {
         StageTimer timer(ctx, ISO_STAGE_PLACE);
-        DualArgs da{field, bits, (uint32_t)W, pitch, n, nzd, zlo, inv, dval, dpitch, dpos, list, count,
-                    (uint32_t)ndual, ctx->d_err};
-        dc_dual<<<(unsigned)((ndual + 255) / 256), 256, 0, ctx->stream>>>(da);
+        DualArgs da{field, bits, (uint32_t)W, pitch, n, nzd, zlo, inv, dval, dpitch, dpos, dbits, (uint32_t)dW,
+                    list, count, (uint32_t)ndual, ctx->d_err, near};
+        const uint64_t dual_warps = dW * m * nzd;
+        dc_dual<<<(unsigned)((dual_warps + 7) / 8), 256, 0, ctx->stream>>>(da);
         PlaceArgs pa{prog->view(), n, zlo, inv, list, count, dpos, (int)placer, ctx->d_err, features, count + 1};
         const uint64_t place_blocks = std::min<uint64_t>((ndual + 127) / 128, 152 * 64);
         dc_place<<<(unsigned)place_blocks, 128, 0, ctx->stream>>>(pa);
@@ -249,7 +267,6 @@ static iso_status dc_lattice(iso_ctx* ctx, const iso_program* prog, uint32_t n, 
     }
     ctx->launches += 2;
     if ((s = check_launch(ctx, "dc passes")) != ISO_OK) return s;
-    if ((s = launch_sign_bits(ctx, dval, m, m, nzd, dpitch, dbits)) != ISO_OK) return s;
     *L = Lattice{m, m, nzd, dpitch, dval, dbits, (uint32_t)dW, 0.0f, dpos, zlo};
     return ISO_OK;
 }
