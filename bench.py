@@ -110,8 +110,10 @@ class ClockSampler:
 
 # the kernels whose DRAM traffic profiles/traffic.json records; a capture
 # counts only for the sources it was taken from
+# every source of the translation units that hold the extraction's kernels
 TRAFFIC_SOURCES = ["isosurface_gb300/csrc/" + f for f in
-                   ("mc.cu", "mc_chunk.cuh", "mc_tables.h", "sample.cu", "vm.cuh", "internal.h")]
+                   ("mc.cu", "mc_chunk.cuh", "mc_tables.h", "sample.cu", "bricks.cuh", "bricks_core.cuh", "vm.cuh",
+                    "vm_math.cuh", "internal.h")] + ["include/isosurface_gpu.h"]
 
 
 def kernel_sources_sha256():

@@ -40,15 +40,16 @@ UNITS = {
     "jit.cu": ["-fmad=false"],
 }
 HEADERS = ["internal.h", "vm.cuh", "vm_math.cuh", "bricks.cuh", "bricks_core.cuh", "mc_tables.h", "mc_chunk.cuh",
-           "qef.cuh", "mlp.h", "emc.cuh", "emc_tables.h"]
+           "qef.cuh", "qef_planes.cuh", "dc_core.cuh", "mlp.h", "emc.cuh", "emc_tables.h"]
 # sources the library compiles again at run time, for one program at a time
 # (jit.cu): embedded as string literals in _build/jit_sources.inc
-JIT_SOURCES = (("kJitVmMath", "vm_math.cuh"), ("kJitBricksCore", "bricks_core.cuh"))
+JIT_SOURCES = (("kJitVmMath", "vm_math.cuh"), ("kJitBricksCore", "bricks_core.cuh"),
+               ("kJitQefPlanes", "qef_planes.cuh"), ("kJitDcCore", "dc_core.cuh"))
 JIT_INC = os.path.join(OUT_DIR, "jit_sources.inc")
 
 
 def _write_jit_sources():
-    parts = ["// written by isosurface_gb300/build.py from csrc/vm_math.cuh and csrc/bricks_core.cuh\n"]
+    parts = ["// written by isosurface_gb300/build.py from csrc/" + ", ".join(f for _, f in JIT_SOURCES) + "\n"]
     for name, fname in JIT_SOURCES:
         text = open(os.path.join(CSRC, fname)).read()
         text = "".join(l for l in text.splitlines(True) if l.strip() != "#pragma once")

@@ -24,8 +24,13 @@
 #include "internal.h"
 #include "qef.cuh"
 #include "vm.cuh"
+#include "dc_core.cuh"
 
 namespace iso {
+// jit.cu: dc_place with the program's compiled normals; false (nothing
+// launched) when the program has none
+bool jit_dc_place(iso_ctx* ctx, const iso_program* prog, const DcCells& cells, uint64_t blocks, cudaError_t* err);
+
 namespace {
 
 struct DualArgs {
@@ -111,64 +116,17 @@ __global__ void __launch_bounds__(256) dc_dual(DualArgs A) {
     }
 }
 
-struct PlaceArgs {
+// The interpreter's normals (eval_hermite) as a dc_core.cuh evaluator.
+struct VmHermite {
     ProgView pv;
-    uint32_t n;
-    uint32_t zoff;  // as DualArgs::zoff
-    float inv;
-    const uint32_t* list;
-    const uint32_t* count;
-    float4* dpos;
-    int placer;  // 0 MinimiseQEF, 1 ParticleBasedMinimisation
-    uint32_t* err;
-    uint32_t* features;   // MinimiseQEF: the non-planar cells, whose QEF dc_feature solves
-    uint32_t* nfeatures;
+    __device__ __forceinline__ V3 normal(V3 p) const {
+        V3 nn;
+        eval_hermite(pv, p, &nn);
+        return nn;
+    }
 };
 
-// the corners of dual vertex `id`'s primal cell and their normalised normals
-// (sample_normals_at_corners, marching_cubes_impl.rs:58-69)
-__device__ void cell_normals(const PlaceArgs& A, uint32_t id, qef::F3* corners, qef::F3* normals) {
-    const uint32_t m = A.n - 1;
-    const uint32_t x = id % m, r = id / m;
-    const uint32_t y = r % m, z = r / m;
-    const uint8_t cornr[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
-    for (int k = 0; k < 8; ++k) {
-        const float px = (float)(x + cornr[k][0]) * A.inv, py = (float)(y + cornr[k][1]) * A.inv,
-                    pz = (float)(z + A.zoff + cornr[k][2]) * A.inv;
-        corners[k] = qef::f3(px, py, pz);
-        V3 nn;
-        eval_hermite(A.pv, v3(px, py, pz), &nn);
-        normals[k] = qef::normalised_or_zero(qef::f3(nn.x, nn.y, nn.z));
-    }
-}
-
-__device__ void place_one(const PlaceArgs& A, uint32_t i) {
-    const uint32_t id = A.list[i];
-    qef::F3 corners[8], normals[8];
-    cell_normals(A, id, corners, normals);
-    qef::F3 p;
-    if (A.placer == 0) {
-        qef::Planes t;
-        qef::tangent_planes(corners, normals, &t);
-        if (t.feature != qef::PLANAR) {
-            // the f64 SVD: listed for dc_feature, which runs the non-planar
-            // cells (a few per warp here) in full warps
-            A.features[atomicAdd(A.nfeatures, 1u)] = id;
-            return;
-        }
-        p = t.com;  // minimise_qef of a planar cell
-    } else {
-        p = qef::particle_placement(corners, normals);
-    }
-    A.dpos[id] = make_float4(p.x, p.y, p.z, 0.0f);
-}
-
-// one thread per active cell, grid-stride over the list built by dc_dual
-__global__ void __launch_bounds__(128) dc_place(PlaceArgs A) {
-    const uint32_t count = *A.count;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
-        place_one(A, i);
-}
+__global__ void __launch_bounds__(128) dc_place(VmHermite ev, DcCells A) { dc_place_body(ev, A); }
 
 // MinimiseQEF of the non-planar cells dc_place listed, one per thread over
 // one-warp blocks (grid-stride): each is a serial chain of f64 operations
@@ -176,18 +134,18 @@ __global__ void __launch_bounds__(128) dc_place(PlaceArgs A) {
 // its sub-partition's f64 unit for many cycles however few of its lanes are
 // active, so packing the chains into full warps cuts the f64 instructions
 // the scattered cells of dc_place would have issued.
-__global__ void __launch_bounds__(32) dc_feature(PlaceArgs A) {
+__global__ void __launch_bounds__(32) dc_feature(VmHermite ev, DcCells A, uint32_t* err) {
     const uint32_t n = *A.nfeatures;
     for (uint32_t i = blockIdx.x * 32 + threadIdx.x; i < n; i += gridDim.x * 32) {
         const uint32_t id = A.features[i];
         qef::F3 corners[8], normals[8];
-        cell_normals(A, id, corners, normals);
+        dc_cell_normals(ev, A, id, corners, normals);
         qef::Planes t;
         qef::tangent_planes(corners, normals, &t);
         bool ok;
         const qef::F3 p = qef::minimise_qef(t, &ok);
-        if (!ok) atomicOr(A.err, DERR_SVD_ITER);
-        A.dpos[id] = make_float4(p.x, p.y, p.z, 0.0f);
+        if (!ok) atomicOr(err, DERR_SVD_ITER);
+        A.dpos[id] = DcPos{p.x, p.y, p.z, 0.0f};
     }
 }
 
@@ -256,12 +214,18 @@ static iso_status dc_lattice(iso_ctx* ctx, const iso_program* prog, uint32_t n, 
                     list, count, (uint32_t)ndual, ctx->d_err, near};
         const uint64_t dual_warps = dW * m * nzd;
         dc_dual<<<(unsigned)((dual_warps + 7) / 8), 256, 0, ctx->stream>>>(da);
-        PlaceArgs pa{prog->view(), n, zlo, inv, list, count, dpos, (int)placer, ctx->d_err, features, count + 1};
+        const DcCells cells{n, zlo, inv, list, count, reinterpret_cast<DcPos*>(dpos), (int)placer, features,
+                            count + 1};
+        const VmHermite ev{prog->view()};
         const uint64_t place_blocks = std::min<uint64_t>((ndual + 127) / 128, 152 * 64);
-        dc_place<<<(unsigned)place_blocks, 128, 0, ctx->stream>>>(pa);
+        cudaError_t je = cudaSuccess;
+        if (!jit_dc_place(ctx, prog, cells, place_blocks, &je))  // the program's compiled normals (jit.cu)
+            dc_place<<<(unsigned)place_blocks, 128, 0, ctx->stream>>>(ev, cells);
+        else if (je != cudaSuccess)
+            return cuda_fail(ctx, je, "compiled dc_place launch");
         if (placer == 0) {
             // one warp for each of the SMs' four sub-partitions
-            dc_feature<<<(unsigned)(4 * std::max(ctx->sms, 1)), 32, 0, ctx->stream>>>(pa);
+            dc_feature<<<(unsigned)(4 * std::max(ctx->sms, 1)), 32, 0, ctx->stream>>>(ev, cells, ctx->d_err);
             ctx->launches++;
         }
     }

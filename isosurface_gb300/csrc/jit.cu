@@ -9,8 +9,9 @@
 // time (--fmad=false, so nothing is contracted: values stay bit-identical to
 // the interpreter's), and launches the kernels from the loaded module: the
 // culled sampler's two (not for a flat union of translated primitives,
-// whose interpreted form prunes the primitives per sub-brick) and the full
-// field's one.  Modules are cached
+// whose interpreted form prunes the primitives per sub-brick), the full
+// field's one and, when the program's normals are written out too (no
+// central difference), DualContouring's placement pass (dc_core.cuh).  Modules are cached
 // per program contents for the life of the process.  NVRTC is loaded with
 // dlopen on first use; without it, or when a compilation fails, the
 // interpreter runs instead.
@@ -30,9 +31,12 @@
 
 #include "bricks.cuh"
 #include "internal.h"
+#include "qef.cuh"
 #include "vm.cuh"
+#include "dc_core.cuh"
 
-// the texts of vm_math.cuh and bricks_core.cuh (written by the build)
+// the texts of vm_math.cuh, bricks_core.cuh, qef_planes.cuh and dc_core.cuh
+// (written by the build)
 #include "jit_sources.inc"
 
 namespace iso {
@@ -160,11 +164,124 @@ bool emit_value(const iso_program* p, std::string* out) {
     return true;
 }
 
-std::string module_source(const std::string& value_body) {
+// The program's normal at p (the Hermite evaluation of vm.cuh's
+// eval_hermite: the same values, the same normal selections and rigid-map
+// rotations, in the same order) as straight-line code, or false for a
+// program the generator does not cover (sphere sets, central differences).
+bool emit_hermite(const iso_program* p, std::string* out) {
+    std::string& s = *out;
+    struct Pt {
+        std::string name;
+        uint32_t op;
+        const float* k;
+    };
+    std::vector<Pt> points{{"p", 0u, nullptr}};
+    std::vector<std::pair<std::string, std::string>> vals;  // (value, normal)
+    int np = 0, nv = 0;
+    const float* K = p->consts.data();
+    auto point = [&](const std::string& expr, uint32_t op, const float* k) {
+        const std::string name = "hpt" + std::to_string(++np);
+        s += "        const V3 " + name + " = " + expr + ";\n";
+        points.push_back({name, op, k});
+    };
+    auto push = [&](const std::string& value, const std::string& normal) {
+        const std::string id = std::to_string(++nv);
+        s += "        const float hval" + id + " = " + value + ";\n";
+        s += "        const V3 hnrm" + id + " = " + normal + ";\n";
+        vals.push_back({"hval" + id, "hnrm" + id});
+    };
+    for (uint32_t w : p->ops) {
+        const uint32_t op = w & 0xFFu;
+        const float* k = K + (w >> 8);
+        const std::string q = points.back().name;
+        switch (op) {
+        case OP_PT_DOMAIN:
+            point("v3(" + q + ".x * " + flit(k[0]) + " + " + flit(k[3]) + ", " + q + ".y * " + flit(k[1]) + " + " +
+                      flit(k[4]) + ", " + q + ".z * " + flit(k[2]) + " + " + flit(k[5]) + ")",
+                  op, k);
+            break;
+        case OP_PT_TRANSLATE:
+            point("v3(" + q + ".x - " + flit(k[0]) + ", " + q + ".y - " + flit(k[1]) + ", " + q + ".z - " +
+                      flit(k[2]) + ")",
+                  op, k);
+            break;
+        case OP_PT_RIGID: {
+            const std::string d = "hdif" + std::to_string(np + 1);
+            s += "        const V3 " + d + " = v3(" + q + ".x - " + flit(k[0]) + ", " + q + ".y - " + flit(k[1]) +
+                 ", " + q + ".z - " + flit(k[2]) + ");\n";
+            const float* m = k + 3;
+            auto row = [&](int r) {
+                return "(" + flit(m[3 * r]) + " * " + d + ".x + " + flit(m[3 * r + 1]) + " * " + d + ".y) + " +
+                       flit(m[3 * r + 2]) + " * " + d + ".z";
+            };
+            point("v3(" + row(0) + ", " + row(1) + ", " + row(2) + ")", op, k);
+            break;
+        }
+        case OP_PT_POP: {
+            if (points.size() < 2) return false;
+            const Pt top = points.back();
+            points.pop_back();
+            if (top.op == OP_PT_RIGID) {  // the normal rotated back: M^T n, column by column
+                if (vals.empty()) return false;
+                const float* m = top.k + 3;
+                const std::string n = vals.back().second, r = "hrot" + std::to_string(++np);
+                auto col = [&](int c) {
+                    return "(" + flit(m[c]) + " * " + n + ".x + " + flit(m[c + 3]) + " * " + n + ".y) + " +
+                           flit(m[c + 6]) + " * " + n + ".z";
+                };
+                s += "        const V3 " + r + " = v3(" + col(0) + ", " + col(1) + ", " + col(2) + ");\n";
+                vals.back().second = r;
+            }
+            break;
+        }
+        case OP_SPHERE: push("sd_sphere(" + q + ", " + flit(k[0]) + ")", q); break;
+        case OP_BOX:
+            push("sd_box(" + q + ", " + flit(k[0]) + ", " + flit(k[1]) + ", " + flit(k[2]) + ")", "n_box(" + q + ")");
+            break;
+        case OP_CYLINDER:
+            push("sd_cylinder(" + q + ", " + flit(k[0]) + ", " + flit(k[1]) + ")",
+                 "n_cylinder(" + q + ", " + flit(k[0]) + ", " + flit(k[1]) + ")");
+            break;
+        case OP_TORUS:
+            push("sd_torus(" + q + ", " + flit(k[0]) + ", " + flit(k[1]) + ")", "n_torus(" + q + ", " + flit(k[0]) + ")");
+            break;
+        case OP_UNION: case OP_INTERSECTION: case OP_DIFFERENCE: case OP_SMOOTH_UNION: {
+            if (vals.size() < 2) return false;
+            const auto b = vals.back();
+            vals.pop_back();
+            const auto a = vals.back();
+            vals.pop_back();
+            const std::string& va = a.first; const std::string& na = a.second;
+            const std::string& vb = b.first; const std::string& nb = b.second;
+            if (op == OP_UNION)
+                push("fminf(" + va + ", " + vb + ")", "vmin(" + na + ", " + nb + ")");
+            else if (op == OP_INTERSECTION)
+                push("fmaxf(" + va + ", " + vb + ")", "(!(" + va + " >= " + vb + ")) ? " + nb + " : " + na);
+            else if (op == OP_DIFFERENCE)
+                push("fmaxf(" + vb + ", -" + va + ")",
+                     "(" + vb + " >= -" + va + ") ? " + nb + " : v3(-" + na + ".x, -" + na + ".y, -" + na + ".z)");
+            else
+                push("smooth_min(" + va + ", " + vb + ", " + flit(k[0]) + ")",
+                     "(!(" + va + " <= " + vb + ")) ? " + nb + " : " + na);
+            break;
+        }
+        default: return false;  // sphere sets, central differences and anything new
+        }
+    }
+    if (vals.size() != 1) return false;
+    s += "        return " + vals.back().second + ";\n";
+    return true;
+}
+
+std::string module_source(const std::string& value_body, const std::string& hermite_body) {
     std::string s;
     s += "typedef unsigned char uint8_t;\ntypedef unsigned int uint32_t;\ntypedef unsigned long long uint64_t;\n";
     s += kJitVmMath;
     s += kJitBricksCore;
+    if (!hermite_body.empty()) {
+        s += kJitQefPlanes;
+        s += kJitDcCore;
+    }
     s += "namespace iso {\nstruct JitEval {\n"
          "    __device__ __forceinline__ float value(V3 p) const {\n";
     s += value_body;
@@ -183,6 +300,14 @@ std::string module_source(const std::string& value_body) {
          "    iso::brick_rows_body(iso::JitEval{}, tiles, list, count, cap);\n}\n"
          "extern \"C\" __global__ void __launch_bounds__(256) iso_jit_field(iso::BrickLattice g) {\n"
          "    iso::field_warp(iso::JitEval{}, g, (uint64_t)blockIdx.x * 8 + (threadIdx.x >> 5));\n}\n";
+    if (!hermite_body.empty()) {
+        s += "namespace iso {\nstruct JitHermite {\n"
+             "    __device__ __forceinline__ V3 normal(V3 p) const {\n";
+        s += hermite_body;
+        s += "    }\n};\n}  // namespace iso\n"
+             "extern \"C\" __global__ void __launch_bounds__(128) iso_jit_dc_place(iso::DcCells cells) {\n"
+             "    iso::dc_place_body(iso::JitHermite{}, cells);\n}\n";
+    }
     return s;
 }
 
@@ -193,6 +318,7 @@ struct Module {
     bool ok = false;
     cudaLibrary_t lib = nullptr;
     cudaKernel_t classify = nullptr, rows = nullptr, field = nullptr;
+    cudaKernel_t dc_place = nullptr;  // only for a program whose normals are compiled too
     std::atomic<int> rows_per_sm{0};
 };
 
@@ -212,7 +338,9 @@ Module* compile_module(const iso_program* p, std::string* why) {
         *why = n.why;
         return nullptr;
     }
-    const std::string src = module_source(body);
+    std::string hermite;
+    if (!emit_hermite(p, &hermite)) hermite.clear();
+    const std::string src = module_source(body, hermite);
     nvrtcProgram prog = nullptr;
     if (n.create(&prog, src.c_str(), "iso_program.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS) {
         *why = "nvrtcCreateProgram failed";
@@ -249,6 +377,7 @@ Module* compile_module(const iso_program* p, std::string* why) {
     if (e == cudaSuccess) e = cudaLibraryGetKernel(&m->classify, m->lib, "iso_jit_classify");
     if (e == cudaSuccess) e = cudaLibraryGetKernel(&m->rows, m->lib, "iso_jit_rows");
     if (e == cudaSuccess) e = cudaLibraryGetKernel(&m->field, m->lib, "iso_jit_field");
+    if (e == cudaSuccess && !hermite.empty()) e = cudaLibraryGetKernel(&m->dc_place, m->lib, "iso_jit_dc_place");
     if (e != cudaSuccess) {
         cudaGetLastError();
         if (m->lib) cudaLibraryUnload(m->lib);
@@ -308,6 +437,15 @@ bool jit_sample_bricks(iso_ctx* ctx, const iso_program* prog, const GridTiles& t
     return true;
 }
 
+bool jit_dc_place(iso_ctx* ctx, const iso_program* prog, const DcCells& cells, uint64_t blocks, cudaError_t* err) {
+    Module* m = module_for(prog);
+    if (!m || !m->dc_place) return false;
+    DcCells a = cells;
+    void* args[] = {&a};
+    *err = cudaLaunchKernel((const void*)m->dc_place, dim3((unsigned)blocks), dim3(128), args, 0, ctx->stream);
+    return true;
+}
+
 bool jit_sample_field(iso_ctx* ctx, const iso_program* prog, const BrickLattice& g, uint64_t blocks,
                       cudaError_t* err) {
     Module* m = module_for(prog);
@@ -342,7 +480,9 @@ extern "C" iso_status iso_program_source(const uint8_t* bytes, size_t len, char*
     if (s != ISO_OK) return s;
     std::string body;
     if (p.kind != iso::PK_GENERIC || !iso::emit_value(&p, &body)) return ISO_ERR_UNSUPPORTED;
-    const std::string src = iso::module_source(body);
+    std::string hermite;
+    if (!iso::emit_hermite(&p, &hermite)) hermite.clear();
+    const std::string src = iso::module_source(body, hermite);
     *needed = src.size() + 1;
     if (!out) return ISO_OK;
     if (cap < src.size() + 1) return ISO_ERR_CAPACITY;

@@ -41,26 +41,6 @@ __host__ __device__ __forceinline__ uint32_t float_bits(float f) {
 #endif
 }
 
-__host__ __device__ __forceinline__ V3 n_box(V3 p) {  // vector.rs:612-621
-    float ax = fabsf(p.x), ay = fabsf(p.y), az = fabsf(p.z);
-    if (ax > ay && ax > az) return v3(p.x, 0.0f, 0.0f);
-    if (ay > az) return v3(0.0f, p.y, 0.0f);
-    return v3(0.0f, 0.0f, p.z);
-}
-__host__ __device__ __forceinline__ V3 n_cylinder(V3 p, float r, float hl) {
-    float z = fabsf(p.z) / hl;
-    float rr = sqrtf(p.x * p.x + p.y * p.y) / r;
-    if (z > rr) return v3(0.0f, 0.0f, p.z);
-    return v3(p.x, p.y, 0.0f);
-}
-__host__ __device__ __forceinline__ V3 n_torus(V3 p, float R) {
-    float l = sqrtf((p.x * p.x + p.y * p.y) + 0.0f * 0.0f);
-    V3 ring;
-    if (fabsf(l) < 1.1920929e-07f) ring = v3(1.0f, 0.0f, 0.0f);
-    else ring = v3(p.x / l, p.y / l, 0.0f / l);
-    return p - ring * R;
-}
-
 __host__ __device__ __forceinline__ V3 pt_apply(uint32_t op, const float* k, V3 p) {
     if (op == OP_PT_DOMAIN) return v3(p.x * k[0] + k[3], p.y * k[1] + k[4], p.z * k[2] + k[5]);
     if (op == OP_PT_TRANSLATE) return v3(p.x - k[0], p.y - k[1], p.z - k[2]);

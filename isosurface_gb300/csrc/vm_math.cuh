@@ -42,6 +42,29 @@ __host__ __device__ __forceinline__ float sd_torus(V3 q, float R, float r) {
     float l = sqrtf(qx * qx + q.z * q.z);
     return l - r;
 }
+// the primitives' analytic normals, unnormalised (sample_normal:
+// rectangular_prism.rs:77 with vector.rs:612-621, cylinder.rs:75, torus.rs:99;
+// a sphere's is the point itself, sphere.rs:60)
+__host__ __device__ __forceinline__ V3 n_box(V3 p) {  // vector.rs:612-621
+    float ax = fabsf(p.x), ay = fabsf(p.y), az = fabsf(p.z);
+    if (ax > ay && ax > az) return v3(p.x, 0.0f, 0.0f);
+    if (ay > az) return v3(0.0f, p.y, 0.0f);
+    return v3(0.0f, 0.0f, p.z);
+}
+__host__ __device__ __forceinline__ V3 n_cylinder(V3 p, float r, float hl) {
+    float z = fabsf(p.z) / hl;
+    float rr = sqrtf(p.x * p.x + p.y * p.y) / r;
+    if (z > rr) return v3(0.0f, 0.0f, p.z);
+    return v3(p.x, p.y, 0.0f);
+}
+__host__ __device__ __forceinline__ V3 n_torus(V3 p, float R) {
+    float l = sqrtf((p.x * p.x + p.y * p.y) + 0.0f * 0.0f);
+    V3 ring;
+    if (fabsf(l) < 1.1920929e-07f) ring = v3(1.0f, 0.0f, 0.0f);
+    else ring = v3(p.x / l, p.y / l, 0.0f / l);
+    return p - ring * R;
+}
+
 // Polynomial smooth minimum (Quilez 2013)
 __host__ __device__ __forceinline__ float smooth_min(float a, float b, float k) {
     const float gap = k - fabsf(a - b);

@@ -13,7 +13,7 @@ CSRC = os.path.join(ROOT, "isosurface_gb300", "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libemc_host.so")
 DEPS = [os.path.join(HERE, "emc_host.cpp")] + [os.path.join(CSRC, f) for f in
-                                                ("emc.cuh", "emc_tables.h", "mc_tables.h", "qef.cuh", "vm.cuh",
+                                                ("emc.cuh", "emc_tables.h", "mc_tables.h", "qef.cuh", "qef_planes.cuh", "vm.cuh", "vm_math.cuh",
                                                  "internal.h")]
 CUDA_INCLUDE = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
 

@@ -93,3 +93,23 @@ def test_dc_interleaved_normals(ctx, placer):
     assert np.array_equal(got.vertices[:, :3], want.vertices)
     assert np.array_equal(got.vertices[:, 3:], o.sample_normal(want.vertices))
     assert np.array_equal(got.indices, want.indices)
+
+
+@pytest.mark.parametrize("placer", [0, 1])
+@pytest.mark.parametrize("name", ["csg", "torus", "cylinder", "box", "central_difference"])
+def test_dc_compiled_and_interpreted_normals(ctx, name, placer):
+    """DualContouring's placement runs the program's compiled normals when
+    compilation is on (iso_jit_dc_place; a central difference stays with the
+    interpreter), the interpreter's eval_hermite when it is off: both meshes
+    equal the oracle's byte for byte."""
+    from isosurface_gb300._capi import lib
+    src = _sources()[name]
+    size = 33
+    want = oracle.Program(S.lower(src)).dual_contouring(size, placer=placer)
+    for enable in (1, 0):
+        lib().iso_jit_enable(enable)
+        try:
+            got = ctx.download(ctx.dc_extract(src, size, placer=placer, keys=True), keys=True)
+        finally:
+            lib().iso_jit_enable(1)
+        _compare(got, want, size)

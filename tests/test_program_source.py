@@ -1,10 +1,11 @@
 """The CUDA C the library compiles per general program (csrc/jit.cu), on
 the CPU: iso_program_source needs no device, and NVRTC compiles for sm_103a
-without one.  Every general test program's module must compile (its three
-kernels: the culled sampler's two and the full field's), and the generated
-evaluator must walk the program's ops as the interpreter does (one
-statement per primitive, operator and point map); sphere sets are not
-compiled."""
+without one.  Every general test program's module must compile (the culled
+sampler's two kernels, the full field's, and DualContouring's placement
+with the program's normals written out unless it holds a central
+difference), and the generated evaluators must walk the program's ops as
+the interpreter does (one statement per primitive, operator and point map);
+sphere sets are not compiled."""
 import ctypes
 
 import numpy as np
@@ -106,6 +107,16 @@ def test_generated_module_compiles(name):
     assert body.count("const V3 pt") == maps
     for kernel in ("iso_jit_classify", "iso_jit_rows", "iso_jit_field"):
         assert 'extern "C" __global__ void __launch_bounds__(256) %s(' % kernel in text
+    # the normals are written out too (DualContouring's placement kernel),
+    # except through a central difference, which the interpreter keeps
+    has_cd = bool(np.isin(ops, [0x40]).any())
+    assert ("struct JitHermite" in text) == (not has_cd)
+    assert ("iso_jit_dc_place" in text) == (not has_cd)
+    if not has_cd:
+        h = text[text.index("struct JitHermite"):]
+        h = h[:h.index("iso_jit_dc_place")]
+        assert h.count("const float hval") == prims + binary
+        assert h.count("const V3 hnrm") == prims + binary
     rc, cubin, log = _compile(text)
     assert rc == 0 and cubin > 0, log
 
