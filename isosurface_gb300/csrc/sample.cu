@@ -391,8 +391,14 @@ __device__ __forceinline__ TileBox tile_box(const SetArgs& A, uint32_t wx, uint3
 }
 
 __global__ void __launch_bounds__(32 * TILE_WARPS) set_tiles(SetArgs A, uint32_t tiles_y, uint32_t tiles_z,
-                                                            TileRec* recs, uint32_t* mixed, uint32_t* nmixed) {
+                                                            TileRec* recs, uint32_t* mixed, uint32_t* nmixed,
+                                                            float4* thr) {
     const int lane = threadIdx.x & 31;
+    // near-only mode: the first block also writes every sphere's thresholds
+    // (they depend on r and the reach only), which set_rows reads after this
+    // grid in stream order
+    if (thr && blockIdx.x == 0)
+        for (uint32_t i = threadIdx.x; i < A.n; i += blockDim.x) thr[i] = sphere_thresholds(A.spheres[4 * i + 3], A.reach);
     const uint64_t t = (uint64_t)blockIdx.x * TILE_WARPS + (threadIdx.x >> 5);
     if (t >= (uint64_t)A.W * tiles_y * tiles_z) return;
     const uint32_t wx = (uint32_t)(t % A.W), rt = (uint32_t)(t / A.W);
@@ -452,12 +458,6 @@ __global__ void __launch_bounds__(32 * TILE_WARPS) set_tiles(SetArgs A, uint32_t
         rec->nk = (uint16_t)min(nk, 0xFFFFu);
         mixed[atomicAdd(nmixed, 1u)] = (uint32_t)t;
     }
-}
-
-// thresholds of every sphere (they depend on r and the reach only)
-__global__ void set_thresholds(SetArgs A, float4* thr) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < A.n) thr[i] = sphere_thresholds(A.spheres[4 * i + 3], A.reach);
 }
 
 // persistent: warps stride over (mixed tile, row) items.  A row is first
@@ -659,12 +659,8 @@ iso_status launch_sample_grid(iso_ctx* ctx, const iso_program* prog, uint32_t nx
             cudaError_t e = cudaMemsetAsync(nmixed, 0, 4, ctx->stream);
             if (e != cudaSuccess) return cuda_fail(ctx, e, "mixed-tile count");
             StageTimer timer(ctx, ISO_STAGE_SAMPLE);
-            if (near_only) {
-                set_thresholds<<<(prog->set_n + 127) / 128, 128, 0, ctx->stream>>>(a, thr);
-                ctx->launches++;
-            }
             set_tiles<<<(unsigned)((tiles + TILE_WARPS - 1) / TILE_WARPS), 32 * TILE_WARPS, 0, ctx->stream>>>(
-                a, ty, tz, recs, mixed, nmixed);
+                a, ty, tz, recs, mixed, nmixed, near_only ? thr : nullptr);
             set_rows<<<(unsigned)ctx->sms * SET_ROWS_BLOCKS, 256, 0, ctx->stream>>>(a, ty, recs, mixed, nmixed, thr);
             ctx->launches++;
         } else {
