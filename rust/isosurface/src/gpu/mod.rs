@@ -3,7 +3,8 @@
 //!
 //! Added to the crate under a `gpu` feature; each algorithm's `extract`
 //! keeps its signature, gains a `LowerToDevice` bound on the source, and
-//! forwards here (the one-line bodies are in INTEGRATION.md):
+//! forwards here in one line (`MarchingCubes::extract` becomes
+//! `crate::gpu::marching_cubes(self.size, source, extractor)`, and likewise):
 //!
 //! * `MarchingCubes::extract`            (src/marching_cubes.rs:59-82)
 //! * `DualContouring::extract`           (src/dual_contouring.rs:65-105)
