@@ -139,7 +139,19 @@ __global__ void __launch_bounds__(32) dc_feature(VmHermite ev, DcCells A, uint32
     for (uint32_t i = blockIdx.x * 32 + threadIdx.x; i < n; i += gridDim.x * 32) {
         const uint32_t id = A.features[i];
         qef::F3 corners[8], normals[8];
-        dc_cell_normals(ev, A, id, corners, normals);
+        if (i < A.fcap) {  // the normals dc_place computed when it listed the cell
+            const uint32_t m = A.n - 1;
+            const uint32_t x = id % m, r = id / m, y = r % m, z = r / m;
+            const uint8_t cornr[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                         {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+            for (int k = 0; k < 8; ++k) {
+                corners[k] = qef::f3((float)(x + cornr[k][0]) * A.inv, (float)(y + cornr[k][1]) * A.inv,
+                                     (float)(z + A.zoff + cornr[k][2]) * A.inv);
+                normals[k] = A.fnormals[8 * (uint64_t)i + k];
+            }
+        } else {
+            dc_cell_normals(ev, A, id, corners, normals);
+        }
         qef::Planes t;
         qef::tangent_planes(corners, normals, &t);
         bool ok;
@@ -186,7 +198,10 @@ static iso_status dc_lattice(iso_ctx* ctx, const iso_program* prog, uint32_t n, 
     if ((s = ensure(ctx, ctx->aux, 4ull * dpitch * m * nzd)) != ISO_OK) return s;
     if ((s = ensure(ctx, ctx->aux2, 16ull * ndual)) != ISO_OK) return s;
     const uint64_t list_words = (ndual + 63) & ~(uint64_t)63;
-    if ((s = ensure(ctx, ctx->aux3, 4ull * dW * m * nzd + 8ull * list_words + 256)) != ISO_OK) return s;
+    // normals kept for the first feature cells (96 bytes each, at most 96 MB)
+    const uint32_t fcap = (uint32_t)std::min<uint64_t>(list_words, 1u << 20);
+    if ((s = ensure(ctx, ctx->aux3, 4ull * dW * m * nzd + 8ull * list_words + 256 + 96ull * fcap)) != ISO_OK)
+        return s;
     float* field = (float*)ctx->field.p;
     uint32_t* bits = (uint32_t*)ctx->bits.p;
     float* dval = (float*)ctx->aux.p;
@@ -195,6 +210,7 @@ static iso_status dc_lattice(iso_ctx* ctx, const iso_program* prog, uint32_t n, 
     uint32_t* count = dbits + dW * m * nzd;  // active cells, then (count + 1) non-planar ones
     uint32_t* list = count + 64;
     uint32_t* features = list + list_words;
+    qef::F3* fnormals = reinterpret_cast<qef::F3*>(features + list_words);
     const float inv = 1.0f / (float)(n - 1);
     // values only near the surface (programs with a Lipschitz bound): the
     // dual values read the primal ones up to 1 + sqrt(3)/2 lattice steps'
@@ -215,7 +231,7 @@ static iso_status dc_lattice(iso_ctx* ctx, const iso_program* prog, uint32_t n, 
         const uint64_t dual_warps = dW * m * nzd;
         dc_dual<<<(unsigned)((dual_warps + 7) / 8), 256, 0, ctx->stream>>>(da);
         const DcCells cells{n, zlo, inv, list, count, reinterpret_cast<DcPos*>(dpos), (int)placer, features,
-                            count + 1};
+                            count + 1, fnormals, fcap};
         const VmHermite ev{prog->view()};
         const uint64_t place_blocks = std::min<uint64_t>((ndual + 127) / 128, 152 * 64);
         cudaError_t je = cudaSuccess;

@@ -26,6 +26,8 @@ struct DcCells {
     int placer;             // 0 MinimiseQEF, 1 ParticleBasedMinimisation
     uint32_t* features;     // MinimiseQEF: the non-planar cells, for the f64 QEF
     uint32_t* nfeatures;
+    qef::F3* fnormals;      // the first fcap listed cells' 8 normalised normals, in list order
+    uint32_t fcap;
 };
 
 // the corners of dual vertex `id`'s primal cell and their normalised normals
@@ -56,7 +58,10 @@ __device__ __forceinline__ void dc_place_one(const Ev& ev, const DcCells& A, uin
         qef::Planes t;
         qef::tangent_planes(corners, normals, &t);
         if (t.feature != qef::PLANAR) {
-            A.features[atomicAdd(A.nfeatures, 1u)] = id;
+            const uint32_t j = atomicAdd(A.nfeatures, 1u);
+            A.features[j] = id;
+            if (j < A.fcap)  // kept for the QEF kernel, which then need not evaluate them
+                for (int k = 0; k < 8; ++k) A.fnormals[8 * (uint64_t)j + k] = normals[k];
             return;
         }
         p = t.com;  // MinimiseQEF of a planar cell
